@@ -1,0 +1,113 @@
+"""Seeded synthetic cases for the pressure-correction hot path.
+
+No public dataset is involved: the cases are the shapes and value
+distributions of the workloads this library is measured on.
+
+* ``box``      -- hex box, velocity i.i.d. uniform[-1,1] per component
+                  (seed 1), one phase of density 1 and viscosity 1e-3, p = 0,
+                  dt = 1, no gravity.
+* ``vof``      -- jittered hex box with a water drop in air:
+                  alpha = 0.5*(1 - tanh((|x - c| - 0.25)/0.01)), c the cube
+                  centre; rho 1000 / 1.2, mu 1e-3 / 1.8e-5, g = (0,0,-9.81),
+                  velocity i.i.d. uniform[-1,1] (seed 1), dt = 1e-4.
+
+Boundary conditions in both: pressure fixedValue 0 on ``zmax`` and
+zeroGradient elsewhere; velocity and volume fraction zeroGradient.  Pressure
+and velocity under-relaxation are 0.3 (the reference's fvSolution defaults).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .meshgen import PolyMesh, hex_box
+
+# boundary-condition codes shared with the C-ABI (include/semo_gb300.h)
+BC_ZERO_GRADIENT = 0
+BC_FIXED_VALUE = 1
+BC_NO_SLIP = 2
+BC_SLIP = 3
+
+
+@dataclass
+class Case:
+    name: str
+    mesh: PolyMesh
+    P: np.ndarray
+    U: np.ndarray
+    V: np.ndarray
+    W: np.ndarray
+    VF: np.ndarray
+    # per patch: (type_p, type_u, type_vf), (val_p, val_u, val_v, val_w, val_vf)
+    bc_type: np.ndarray = None      # (n_patches, 3) int32
+    bc_value: np.ndarray = None     # (n_patches, 5) float64
+    dt: float = 1.0
+    rho: tuple = (1.0, 1.0)         # (phase 0 = VF[0], phase 1)
+    mu: tuple = (1e-3, 1e-3)
+    sigma: float = 0.0
+    gravity: tuple = (0.0, 0.0, 0.0)
+    use_gravity: bool = False
+    pre_p_urf: float = 0.3
+    pre_u_urf: float = 0.3
+    extra: dict = field(default_factory=dict)
+
+
+def approx_cell_centres(mesh: PolyMesh) -> np.ndarray:
+    """Mean of each cell's face-loop vertex means (used only to place fields)."""
+    nf = mesh.n_faces
+    cnt = np.diff(mesh.face_ptr).astype(np.int64)
+    fid = np.repeat(np.arange(nf), cnt)
+    fc = np.zeros((nf, 3))
+    np.add.at(fc, fid, mesh.points[mesh.face_pts])
+    fc /= cnt[:, None]
+    cc = np.zeros((mesh.n_cells, 3))
+    nc = np.zeros(mesh.n_cells)
+    np.add.at(cc, mesh.owner, fc)
+    np.add.at(nc, mesh.owner, 1.0)
+    ni = mesh.n_internal
+    np.add.at(cc, mesh.neighbour, fc[:ni])
+    np.add.at(nc, mesh.neighbour, 1.0)
+    return cc / nc[:, None]
+
+
+def _default_bcs(mesh: PolyMesh):
+    npatch = len(mesh.patch_names)
+    bt = np.zeros((npatch, 3), dtype=np.int32)
+    bv = np.zeros((npatch, 5), dtype=np.float64)
+    bt[mesh.patch_names.index("zmax"), 0] = BC_FIXED_VALUE
+    return bt, bv
+
+
+def _velocity(n_cells: int, seed: int = 1):
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-1.0, 1.0, size=(3, n_cells))
+    return u[0].copy(), u[1].copy(), u[2].copy()
+
+
+def box_case(n: int, jitter: float = 0.0, mesh_seed: int = 1234) -> Case:
+    mesh = hex_box(n, jitter=jitter, seed=mesh_seed)
+    U, V, W = _velocity(mesh.n_cells, 1)
+    bt, bv = _default_bcs(mesh)
+    nc = mesh.n_cells
+    return Case(name=f"box{n}" + ("j" if jitter else ""), mesh=mesh, P=np.zeros(nc), U=U, V=V, W=W,
+                VF=np.ones(nc), bc_type=bt, bc_value=bv, dt=1.0, rho=(1.0, 1.0), mu=(1e-3, 1e-3))
+
+
+def vof_case(n: int, jitter: float = 0.2, mesh_seed: int = 1234) -> Case:
+    mesh = hex_box(n, jitter=jitter, seed=mesh_seed)
+    U, V, W = _velocity(mesh.n_cells, 1)
+    cc = approx_cell_centres(mesh)
+    r = np.linalg.norm(cc - 0.5, axis=1)
+    alpha = 0.5 * (1.0 - np.tanh((r - 0.25) / 0.01))
+    bt, bv = _default_bcs(mesh)
+    return Case(name=f"vof{n}", mesh=mesh, P=np.zeros(mesh.n_cells), U=U, V=V, W=W, VF=alpha,
+                bc_type=bt, bc_value=bv, dt=1e-4, rho=(1000.0, 1.2), mu=(1e-3, 1.8e-5),
+                gravity=(0.0, 0.0, -9.81), use_gravity=True)
+
+
+def with_fields(case: Case, seed: int, p_scale: float = 1.0) -> Case:
+    """Same mesh, extra seeded randomness in P (exercises the pressure terms)."""
+    rng = np.random.default_rng(seed)
+    case.P = p_scale * rng.uniform(-1.0, 1.0, size=case.mesh.n_cells)
+    return case
