@@ -1,0 +1,142 @@
+"""ctypes binding of the CPU checker (oracle/semo_oracle.c).
+
+Test infrastructure: used by tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "semo_oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+               "-o", LIB, SRC, "-lm"]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        vp = C.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, vp, vp]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_len.restype = C.c_longlong
+        L.orc_len.argtypes = [vp, C.c_char_p]
+        L.orc_type.argtypes = [vp, C.c_char_p]
+        L.orc_get.argtypes = [vp, C.c_char_p, vp]
+        L.orc_set.argtypes = [vp, C.c_char_p, C.c_int, C.c_longlong, vp]
+        L.orc_set_case.argtypes = [vp, vp, vp, vp]
+        L.orc_assemble_pressure.argtypes = [vp]
+        L.orc_coo_to_csr.argtypes = [vp]
+        L.orc_permute_csr.argtypes = [vp]
+        L.orc_solve.restype = C.c_int
+        L.orc_solve.argtypes = [vp, C.c_int, C.c_double, C.c_int, vp]
+        L.orc_update.restype = C.c_double
+        L.orc_update.argtypes = [vp, vp]
+        L.orc_num_threads.restype = C.c_int
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """The reference's pressure pass restated on the CPU, for one mesh."""
+
+    def __init__(self, mesh):
+        L = lib()
+        self._keep = [np.ascontiguousarray(mesh.points, dtype=np.float64),
+                      np.ascontiguousarray(mesh.face_ptr, dtype=np.int32),
+                      np.ascontiguousarray(mesh.face_pts, dtype=np.int32),
+                      np.ascontiguousarray(mesh.owner, dtype=np.int32),
+                      np.ascontiguousarray(mesh.neighbour, dtype=np.int32),
+                      np.ascontiguousarray(mesh.patch_start, dtype=np.int32),
+                      np.ascontiguousarray(mesh.patch_size, dtype=np.int32)]
+        k = self._keep
+        self.mesh = mesh
+        self.h = L.orc_create(mesh.n_points, _p(k[0]), mesh.n_faces, mesh.n_internal, mesh.n_cells,
+                              _p(k[1]), _p(k[2]), _p(k[3]), _p(k[4]), len(mesh.patch_names), _p(k[5]), _p(k[6]))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def get(self, name: str) -> np.ndarray:
+        L = lib()
+        n = L.orc_len(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        t = L.orc_type(self.h, name.encode())
+        out = np.empty(n, dtype=np.float64 if t == 0 else np.int32)
+        L.orc_get(self.h, name.encode(), _p(out))
+        return out
+
+    def set(self, name: str, arr: np.ndarray) -> None:
+        if arr.dtype == np.int32:
+            a = np.ascontiguousarray(arr)
+            lib().orc_set(self.h, name.encode(), 1, a.size, _p(a))
+        else:
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            lib().orc_set(self.h, name.encode(), 0, a.size, _p(a))
+
+    def set_case(self, case) -> None:
+        bt = np.ascontiguousarray(case.bc_type, dtype=np.int32)
+        bv = np.ascontiguousarray(case.bc_value, dtype=np.float64)
+        prm = np.zeros(16)
+        prm[:12] = [case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
+                    case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf, case.pre_u_urf,
+                    1.0 if case.use_gravity else 0.0]
+        lib().orc_set_case(self.h, _p(bt), _p(bv), _p(prm))
+        for nm in ("P", "U", "V", "W", "VF"):
+            self.set(nm, getattr(case, nm))
+
+    def assemble(self) -> None:
+        lib().orc_assemble_pressure(self.h)
+        lib().orc_coo_to_csr(self.h)
+        lib().orc_permute_csr(self.h)
+
+    def solve(self, use_rcm: bool = False, tol: float = 1e-8, maxiter: int = 500) -> dict:
+        info = np.zeros(16)
+        it = lib().orc_solve(self.h, 1 if use_rcm else 0, tol, maxiter, _p(info))
+        if it < 0:
+            raise RuntimeError("oracle AMG setup failed")
+        x = self.get("rcm_x_orc" if use_rcm else "x_orc")
+        nlev = int(info[2])
+        return {"x": x, "iters": int(info[0]), "rel_res": float(info[1]), "levels": nlev,
+                "operator_complexity": float(info[3]), "coarse_n": int(info[4]),
+                "level_sizes": [int(v) for v in info[5:5 + min(nlev, 10)]]}
+
+    def update(self, x: np.ndarray) -> float:
+        xa = np.ascontiguousarray(x, dtype=np.float64)
+        return float(lib().orc_update(self.h, _p(xa)))
+
+    def pressure_pass(self, case, tol: float = 1e-8) -> dict:
+        """One full calcPressureEq: assemble, solve, Gauss-Green, update."""
+        self.set_case(case)
+        self.assemble()
+        sol = self.solve(False, tol)
+        norm = self.update(sol["x"])
+        sol["norm"] = norm
+        return sol
+
+    @staticmethod
+    def threads() -> int:
+        return int(lib().orc_num_threads())

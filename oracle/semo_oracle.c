@@ -1,0 +1,1204 @@
+/*
+ * semo_oracle.c -- CPU restatement of SEMO's pressure-correction pass.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared
+ * against (tests/, __graft_entry__.smoke) and the CPU baseline bench.py
+ * times.  Nothing in the shipped library links or calls it.
+ *
+ * Each stage restates the reference function cited beside it, with the same
+ * floating-point operation order, so that on the same inputs the results
+ * agree with the reference to the last bit (x86, no FMA contraction; it is
+ * built with -ffp-contract=off so it also stays FMA-free on other hosts).
+ * Parity of this restatement is pinned against the reference's own code,
+ * compiled from its sources into oracle/_ref (see tests/golden/).
+ *
+ * The linear solve is not AMGCL's IDR(s)/ILU0: it restates the GPU solver's
+ * algorithm (smoothed aggregation with MIS(2) aggregation, Chebyshev
+ * smoothing, dense Cholesky on the coarsest level, preconditioned CG), so the
+ * GPU hierarchy can be compared entry by entry.  Solutions are compared with
+ * the reference's AMGCL solution through the solution vector.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_ARR 96
+
+typedef struct {
+    char name[32];
+    int type;            /* 0 = double, 1 = int */
+    long long n;
+    void* p;
+} orc_arr;
+
+typedef struct {
+    /* mesh */
+    int np, nf, ni, nc, npatch;
+    double* pts; int *fptr, *fpts, *own, *nei, *pstart, *psize;
+    /* bc per patch: type p/u/vf and values p,u,v,w,vf */
+    int* bct; double* bcv;
+    /* parameters */
+    double dt, rho0, rho1, urf_p, urf_u, g[3];
+    int use_gravity;
+    double minP, maxP, minU, maxU, minV, maxV, minW, maxW;
+    /* registry of named arrays (owned) */
+    int narr;
+    orc_arr arr[ORC_MAX_ARR];
+} orc_ctx;
+
+static double* dget(orc_ctx* c, const char* name);
+static int* iget(orc_ctx* c, const char* name);
+
+static void* reg(orc_ctx* c, const char* name, int type, long long n) {
+    for (int i = 0; i < c->narr; ++i)
+        if (!strcmp(c->arr[i].name, name)) {
+            free(c->arr[i].p);
+            c->arr[i].p = calloc(n > 0 ? (size_t)n : 1, type ? sizeof(int) : sizeof(double));
+            c->arr[i].n = n; c->arr[i].type = type;
+            return c->arr[i].p;
+        }
+    if (c->narr >= ORC_MAX_ARR) { fprintf(stderr, "oracle: registry full\n"); abort(); }
+    orc_arr* a = &c->arr[c->narr++];
+    snprintf(a->name, sizeof a->name, "%s", name);
+    a->type = type; a->n = n;
+    a->p = calloc(n > 0 ? (size_t)n : 1, type ? sizeof(int) : sizeof(double));
+    return a->p;
+}
+static double* dreg(orc_ctx* c, const char* n, long long k) { return (double*)reg(c, n, 0, k); }
+static int* ireg(orc_ctx* c, const char* n, long long k) { return (int*)reg(c, n, 1, k); }
+static orc_arr* find(orc_ctx* c, const char* name) {
+    for (int i = 0; i < c->narr; ++i) if (!strcmp(c->arr[i].name, name)) return &c->arr[i];
+    return NULL;
+}
+static double* dget(orc_ctx* c, const char* name) { orc_arr* a = find(c, name); return a ? (double*)a->p : NULL; }
+static int* iget(orc_ctx* c, const char* name) { orc_arr* a = find(c, name); return a ? (int*)a->p : NULL; }
+
+long long orc_len(orc_ctx* c, const char* name) { orc_arr* a = find(c, name); return a ? a->n : -1; }
+int orc_type(orc_ctx* c, const char* name) { orc_arr* a = find(c, name); return a ? a->type : -1; }
+int orc_get(orc_ctx* c, const char* name, void* dst) {
+    orc_arr* a = find(c, name);
+    if (!a) return -1;
+    memcpy(dst, a->p, (size_t)a->n * (a->type ? sizeof(int) : sizeof(double)));
+    return 0;
+}
+int orc_set(orc_ctx* c, const char* name, int type, long long n, const void* src) {
+    void* p = reg(c, name, type, n);
+    memcpy(p, src, (size_t)n * (type ? sizeof(int) : sizeof(double)));
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* geometry: src/mesh/geometric.cpp:16-~370 (calcUnitNormals_Area3dPolygon), */
+/* :792-880 (volumes/centroids), :1206-1227 (distCells), :1297-1500 (weights) */
+/* ------------------------------------------------------------------------ */
+static void face_polygon(const double* pts, const int* idx, int n, double* nrm, double* area,
+                         double* cx, double* cy, double* cz, double* vsn, double* cen) {
+    double xa = 0.0, ya = 0.0, za = 0.0;
+    for (int i = 0; i < n; ++i) { xa += pts[3 * idx[i]]; ya += pts[3 * idx[i] + 1]; za += pts[3 * idx[i] + 2]; }
+    xa /= (double)n; ya /= (double)n; za /= (double)n;
+    double xt = 0, yt = 0, zt = 0, x0o = 0, y0o = 0, z0o = 0;
+    double un[3] = {0, 0, 0}, cc[3] = {0, 0, 0}, ar = 0, vs = 0;
+    for (int pass = 0; pass < 5; ++pass) {
+        un[0] = un[1] = un[2] = 0.0; cc[0] = cc[1] = cc[2] = 0.0; vs = 0.0;
+        double X0, Y0, Z0;
+        if (pass == 0) { X0 = xa; Y0 = ya; Z0 = za; }
+        else { X0 = x0o + 1.0 * (xt - x0o); Y0 = y0o + 1.0 * (yt - y0o); Z0 = z0o + 1.0 * (zt - z0o); }
+        x0o = X0; y0o = Y0; z0o = Z0;
+        xt = yt = zt = 0.0;
+        double tot = 0.0;
+        for (int i = 0; i < n; ++i) {
+            int b = idx[i], c = idx[(i == n - 1) ? 0 : i + 1];
+            double bx = pts[3 * b], by = pts[3 * b + 1], bz = pts[3 * b + 2];
+            double qx = pts[3 * c], qy = pts[3 * c + 1], qz = pts[3 * c + 2];
+            double A0 = bx - X0, A1 = by - Y0, A2 = bz - Z0;
+            double B0 = qx - X0, B1 = qy - Y0, B2 = qz - Z0;
+            double Nx = 0.5 * (A1 * B2 - A2 * B1);
+            double Ny = 0.5 * (A2 * B0 - A0 * B2);
+            double Nz = 0.5 * (A0 * B1 - A1 * B0);
+            un[0] += Nx; un[1] += Ny; un[2] += Nz;
+            double ta = (double)sqrtl((long double)(Nx * Nx + Ny * Ny + Nz * Nz));
+            double rx = (X0 + bx + qx) / 3.0, ry = (Y0 + by + qy) / 3.0, rz = (Z0 + bz + qz) / 3.0;
+            xt += rx * ta; yt += ry * ta; zt += rz * ta;
+            tot += ta;
+            vs += X0 * Nx; vs += Y0 * Ny; vs += Z0 * Nz;
+            cc[0] += 2.0 * Nx * ((X0 + bx) * (X0 + bx) + (bx + qx) * (bx + qx) + (qx + X0) * (qx + X0));
+            cc[1] += 2.0 * Ny * ((Y0 + by) * (Y0 + by) + (by + qy) * (by + qy) + (qy + Y0) * (qy + Y0));
+            cc[2] += 2.0 * Nz * ((Z0 + bz) * (Z0 + bz) + (bz + qz) * (bz + qz) + (qz + Z0) * (qz + Z0));
+        }
+        double mag = (double)sqrtl((long double)(un[0] * un[0] + un[1] * un[1] + un[2] * un[2]));
+        un[0] /= mag; un[1] /= mag; un[2] /= mag;
+        ar = mag;
+        xt /= tot; yt /= tot; zt /= tot;
+    }
+    nrm[0] = un[0]; nrm[1] = un[1]; nrm[2] = un[2];
+    *area = ar; *cx = xt; *cy = yt; *cz = zt; *vsn = vs;
+    cen[0] = cc[0]; cen[1] = cc[1]; cen[2] = cc[2];
+}
+
+static void build_geometry(orc_ctx* c) {
+    int nf = c->nf, nc = c->nc, ni = c->ni;
+    double* fa = dreg(c, "face_area", nf); double* fn = dreg(c, "face_n", 3LL * nf);
+    double* fc = dreg(c, "face_c", 3LL * nf); double* wc = dreg(c, "face_wC", nf);
+    double* mpn = dreg(c, "face_magPN", nf); double* al = dreg(c, "face_alphaF", nf);
+    double* epn = dreg(c, "face_ePN", 3LL * nf); double* sk = dreg(c, "face_skew", 3LL * nf);
+    double* pf = dreg(c, "face_vecPF", 3LL * nf); double* nfv = dreg(c, "face_vecNF", 3LL * nf);
+    double* dist = dreg(c, "face_dist", 3LL * nf);
+    double* vol = dreg(c, "cell_vol", nc); double* cc = dreg(c, "cell_c", 3LL * nc);
+    for (int f = 0; f < nf; ++f) {
+        double vsn, cen[3];
+        face_polygon(c->pts, c->fpts + c->fptr[f], c->fptr[f + 1] - c->fptr[f], fn + 3 * f, fa + f,
+                     fc + 3 * f, fc + 3 * f + 1, fc + 3 * f + 2, &vsn, cen);
+        int o = c->own[f];
+        vol[o] += vsn / 3.0; cc[3 * o] += cen[0]; cc[3 * o + 1] += cen[1]; cc[3 * o + 2] += cen[2];
+        if (f < ni) {
+            int q = c->nei[f];
+            vol[q] -= vsn / 3.0; cc[3 * q] -= cen[0]; cc[3 * q + 1] -= cen[1]; cc[3 * q + 2] -= cen[2];
+        }
+    }
+    for (int i = 0; i < nc; ++i) {
+        double s = 1.0 / (24.0 * 2.0 * vol[i]);
+        cc[3 * i] *= s; cc[3 * i + 1] *= s; cc[3 * i + 2] *= s;
+    }
+    for (int f = 0; f < nf; ++f) {
+        int o = c->own[f];
+        const double* n = fn + 3 * f;
+        double ox = cc[3 * o], oy = cc[3 * o + 1], oz = cc[3 * o + 2];
+        double fx = fc[3 * f], fy = fc[3 * f + 1], fz = fc[3 * f + 2];
+        if (f < ni) {
+            int q = c->nei[f];
+            double nx = cc[3 * q], ny = cc[3 * q + 1], nz = cc[3 * q + 2];
+            dist[3 * f] = nx - ox; dist[3 * f + 1] = ny - oy; dist[3 * f + 2] = nz - oz;
+            double dxFP = fx - ox, dyFP = fy - oy, dzFP = fz - oz;
+            double dxFN = fx - nx, dyFN = fy - ny, dzFN = fz - nz;
+            double dxPN = nx - ox, dyPN = ny - oy, dzPN = nz - oz;
+            double dPN = sqrt(dxPN * dxPN + dyPN * dyPN + dzPN * dzPN);
+            pf[3 * f] = dxFP; pf[3 * f + 1] = dyFP; pf[3 * f + 2] = dzFP;
+            nfv[3 * f] = dxFN; nfv[3 * f + 1] = dyFN; nfv[3 * f + 2] = dzFN;
+            double dFPo = fabs(dxFP * n[0] + dyFP * n[1] + dzFP * n[2]);
+            double dFNo = fabs(dxFN * n[0] + dyFN * n[1] + dzFN * n[2]);
+            double w = dFNo / (dFPo + dFNo);
+            wc[f] = (double)(float)(round(w * 10000000) / 10000000);
+            mpn[f] = dPN;
+            epn[3 * f] = dxPN / dPN; epn[3 * f + 1] = dyPN / dPN; epn[3 * f + 2] = dzPN / dPN;
+            double a = 0.0;
+            a += n[0] * epn[3 * f]; a += n[1] * epn[3 * f + 1]; a += n[2] * epn[3 * f + 2];
+            al[f] = 1.0 / fabs(a);
+            double Dp = -(n[0] * fx + n[1] * fy + n[2] * fz);
+            double u = (n[0] * ox + n[1] * oy + n[2] * oz + Dp) /
+                       (n[0] * (ox - nx) + n[1] * (oy - ny) + n[2] * (oz - nz));
+            double s0 = ox - u * (ox - nx), s1 = oy - u * (oy - ny), s2 = oz - u * (oz - nz);
+            sk[3 * f] = fx - s0; sk[3 * f + 1] = fy - s1; sk[3 * f + 2] = fz - s2;
+        } else {
+            dist[3 * f] = fx - ox; dist[3 * f + 1] = fy - oy; dist[3 * f + 2] = fz - oz;
+            wc[f] = (double)(float)(round(0.5 * 10000000) / 10000000);
+            double dxFP = fx - ox, dyFP = fy - oy, dzFP = fz - oz;
+            double dFP = sqrt(dxFP * dxFP + dyFP * dyFP + dzFP * dzFP);
+            pf[3 * f] = dxFP; pf[3 * f + 1] = dyFP; pf[3 * f + 2] = dzFP;
+            nfv[3 * f] = dxFP; nfv[3 * f + 1] = dyFP; nfv[3 * f + 2] = dzFP;
+            double dFPo = fabs(dxFP * n[0] + dyFP * n[1] + dzFP * n[2]);
+            mpn[f] = 2.0 * dFPo;
+            epn[3 * f] = dxFP / dFP; epn[3 * f + 1] = dyFP / dFP; epn[3 * f + 2] = dzFP / dFP;
+            double a = 0.0;
+            a += n[0] * epn[3 * f]; a += n[1] * epn[3 * f + 1]; a += n[2] * epn[3 * f + 2];
+            al[f] = 1.0 / fabs(a);
+            sk[3 * f] = sk[3 * f + 1] = sk[3 * f + 2] = 0.0;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* topology: src/mesh/build.cpp:587-608 (connectCelltoFaces), :613-690      */
+/* (connectCelltoPoints), src/mesh/geometric.cpp:1781-1845 (setStencil),     */
+/* src/mesh/build.cpp:1319-1424 (cellsGlobal CSR + face->slot maps)          */
+/* ------------------------------------------------------------------------ */
+typedef struct { int* p; int n, cap; } ivec;
+static void ivec_push(ivec* v, int x) {
+    if (v->n == v->cap) { v->cap = v->cap ? 2 * v->cap : 8; v->p = (int*)realloc(v->p, sizeof(int) * v->cap); }
+    v->p[v->n++] = x;
+}
+static int ivec_has(const ivec* v, int x) { for (int i = 0; i < v->n; ++i) if (v->p[i] == x) return 1; return 0; }
+
+static void flatten(orc_ctx* c, const char* pn, const char* in, ivec* v, int n) {
+    int* ptr = ireg(c, pn, n + 1);
+    for (int i = 0; i < n; ++i) ptr[i + 1] = ptr[i] + v[i].n;
+    int* idx = ireg(c, in, ptr[n]);
+    for (int i = 0; i < n; ++i) { memcpy(idx + ptr[i], v[i].p, sizeof(int) * v[i].n); free(v[i].p); }
+    free(v);
+}
+
+static void build_topology(orc_ctx* c) {
+    int nf = c->nf, nc = c->nc, ni = c->ni;
+    ivec* cf = (ivec*)calloc(nc, sizeof(ivec));
+    for (int f = 0; f < nf; ++f) { ivec_push(&cf[c->own[f]], f); if (f < ni) ivec_push(&cf[c->nei[f]], f); }
+    flatten(c, "cf_ptr", "cf_idx", cf, nc);
+    ivec* cp = (ivec*)calloc(nc, sizeof(ivec));
+    for (int f = 0; f < nf; ++f)
+        for (int k = c->fptr[f]; k < c->fptr[f + 1]; ++k) {
+            int p = c->fpts[k];
+            if (!ivec_has(&cp[c->own[f]], p)) ivec_push(&cp[c->own[f]], p);
+            if (f < ni && !ivec_has(&cp[c->nei[f]], p)) ivec_push(&cp[c->nei[f]], p);
+        }
+    flatten(c, "cp_ptr", "cp_idx", cp, nc);
+    int* cpp = iget(c, "cp_ptr"); int* cpi = iget(c, "cp_idx");
+    ivec* pc = (ivec*)calloc(c->np, sizeof(ivec));
+    for (int i = 0; i < nc; ++i) for (int k = cpp[i]; k < cpp[i + 1]; ++k) ivec_push(&pc[cpi[k]], i);
+    ivec* st = (ivec*)calloc(nc, sizeof(ivec));
+    for (int i = 0; i < nc; ++i)
+        for (int k = cpp[i]; k < cpp[i + 1]; ++k) {
+            ivec* pl = &pc[cpi[k]];
+            for (int q = 0; q < pl->n; ++q) {
+                int j = pl->p[q];
+                if (j == i) continue;
+                if (!ivec_has(&st[i], j)) ivec_push(&st[i], j);
+            }
+        }
+    for (int p = 0; p < c->np; ++p) free(pc[p].p);
+    free(pc);
+    flatten(c, "stencil_ptr", "stencil_idx", st, nc);
+    /* CSR pattern: COO = N diagonals, then per internal face (LR, RL) */
+    int nnz = nc + 2 * ni;
+    int* ptr = ireg(c, "CRS_ptr", nc + 1);
+    int* col = ireg(c, "CRS_col", nnz);
+    int* dig = ireg(c, "CRS_dig", nc);
+    int* lr = ireg(c, "CRS_LR", nf); int* rl = ireg(c, "CRS_RL", nf);
+    for (int f = 0; f < nf; ++f) { lr[f] = -1; rl[f] = -1; }
+    int* cnt = (int*)calloc(nc + 1, sizeof(int));
+    for (int i = 0; i < nc; ++i) cnt[i]++;
+    for (int f = 0; f < ni; ++f) { cnt[c->own[f]]++; cnt[c->nei[f]]++; }
+    for (int i = 0, s = 0; i < nc; ++i) { ptr[i] = s; s += cnt[i]; }
+    ptr[nc] = nnz;
+    int* fill = (int*)malloc(sizeof(int) * nc);
+    for (int i = 0; i < nc; ++i) fill[i] = ptr[i];
+    for (int i = 0; i < nc; ++i) { int d = fill[i]++; col[d] = i; dig[i] = d; }
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        int d = fill[o]++; col[d] = q; lr[f] = d;
+        d = fill[q]++; col[d] = o; rl[f] = d;
+    }
+    free(cnt); free(fill);
+}
+
+/* ------------------------------------------------------------------------ */
+/* LSQ setup: src/math/gradient.cpp:246-453 (initLeastSquare, cellVertex,    */
+/* first-order block of the normal matrix, cofactor inverse)                 */
+/* ------------------------------------------------------------------------ */
+static void build_lsq(orc_ctx* c) {
+    int nc = c->nc;
+    double* cc = dget(c, "cell_c"); double* fc = dget(c, "face_c");
+    int* sp = iget(c, "stencil_ptr"); int* si = iget(c, "stencil_idx");
+    double* minv = dreg(c, "lsq_minv", 6LL * nc);
+    double* vs = (double*)calloc(6 * (size_t)nc, sizeof(double)); /* v0 v1 v2 v9 v10 v17 */
+    for (int i = 0; i < nc; ++i)
+        for (int k = sp[i]; k < sp[i + 1]; ++k) {
+            int j = si[k];
+            double dx = cc[3 * j] - cc[3 * i], dy = cc[3 * j + 1] - cc[3 * i + 1], dz = cc[3 * j + 2] - cc[3 * i + 2];
+            double wk = 1.0 / (dx * dx + dy * dy + dz * dz);
+            double* v = vs + 6 * i;
+            v[0] += wk * dx * dx; v[1] += wk * dx * dy; v[2] += wk * dx * dz;
+            v[3] += wk * dy * dy; v[4] += wk * dy * dz; v[5] += wk * dz * dz;
+        }
+    for (int f = c->ni; f < c->nf; ++f) {
+        int i = c->own[f];
+        double dx = fc[3 * f] - cc[3 * i], dy = fc[3 * f + 1] - cc[3 * i + 1], dz = fc[3 * f + 2] - cc[3 * i + 2];
+        double wk = 1.0 / (dx * dx + dy * dy + dz * dz);
+        double* v = vs + 6 * i;
+        v[0] += wk * dx * dx; v[1] += wk * dx * dy; v[2] += wk * dx * dz;
+        v[3] += wk * dy * dy; v[4] += wk * dy * dz; v[5] += wk * dz * dz;
+    }
+    for (int i = 0; i < nc; ++i) {
+        double a0 = vs[6 * i], a1 = vs[6 * i + 1], a2 = vs[6 * i + 2], a9 = vs[6 * i + 3], a10 = vs[6 * i + 4], a17 = vs[6 * i + 5];
+        double det = a0 * a9 * a17 + a1 * a10 * a2 + a2 * a1 * a10 - a0 * a10 * a10 - a2 * a9 * a2 - a1 * a1 * a17;
+        double* m = minv + 6 * i;
+        m[0] = (a9 * a17 - a10 * a10) / det;
+        m[1] = (a2 * a10 - a1 * a17) / det;
+        m[2] = (a1 * a10 - a2 * a9) / det;
+        m[3] = (a0 * a17 - a2 * a2) / det;
+        m[4] = (a2 * a1 - a0 * a10) / det;
+        m[5] = (a0 * a9 - a1 * a1) / det;
+    }
+    free(vs);
+}
+
+/* ------------------------------------------------------------------------ */
+/* RCM: src/math/RCM.cpp:34-218 (lib_RCM) over SPARSEPAK genrcm / rcm /      */
+/* root_find / level_set / degree (George & Liu), 1-based adjacency built    */
+/* from each cell's internal faces in cell.faces order                       */
+/* ------------------------------------------------------------------------ */
+static void rcm_degree(int root, int* xadj, const int* adj, const int* mask, int* deg, int* ccsize, int* ls) {
+    ls[0] = root; xadj[root - 1] = -xadj[root - 1];
+    int lvlend = 0; *ccsize = 1;
+    for (;;) {
+        int lbegin = lvlend + 1; lvlend = *ccsize;
+        for (int i = lbegin; i <= lvlend; ++i) {
+            int node = ls[i - 1];
+            int jstrt = -xadj[node - 1], jstop = abs(xadj[node]) - 1, ideg = 0;
+            for (int j = jstrt; j <= jstop; ++j) {
+                int nbr = adj[j - 1];
+                if (mask[nbr - 1] != 0) {
+                    ideg++;
+                    if (xadj[nbr - 1] >= 0) { xadj[nbr - 1] = -xadj[nbr - 1]; (*ccsize)++; ls[*ccsize - 1] = nbr; }
+                }
+            }
+            deg[node - 1] = ideg;
+        }
+        if (*ccsize - lvlend == 0) break;
+    }
+    for (int i = 0; i < *ccsize; ++i) { int node = ls[i] - 1; xadj[node] = -xadj[node]; }
+}
+static void rcm_level_set(int root, const int* xadj, const int* adj, int* mask, int* nlvl, int* xls, int* ls) {
+    mask[root - 1] = 0; ls[0] = root; *nlvl = 0;
+    int lvlend = 0, ccsize = 1;
+    for (;;) {
+        int lbegin = lvlend + 1; lvlend = ccsize; (*nlvl)++;
+        xls[*nlvl - 1] = lbegin;
+        for (int i = lbegin; i <= lvlend; ++i) {
+            int node = ls[i - 1];
+            for (int j = xadj[node - 1]; j <= xadj[node] - 1; ++j) {
+                int nbr = adj[j - 1];
+                if (mask[nbr - 1] != 0) { ccsize++; ls[ccsize - 1] = nbr; mask[nbr - 1] = 0; }
+            }
+        }
+        if (ccsize - lvlend <= 0) break;
+    }
+    xls[*nlvl] = lvlend + 1;
+    for (int i = 0; i < ccsize; ++i) mask[ls[i] - 1] = 1;
+}
+static void rcm_root_find(int* root, const int* xadj, const int* adj, int* mask, int* nlvl, int* xls, int* ls) {
+    rcm_level_set(*root, xadj, adj, mask, nlvl, xls, ls);
+    int ccsize = xls[*nlvl] - 1;
+    if (*nlvl == 1 || *nlvl == ccsize) return;
+    for (;;) {
+        int mindeg = ccsize, jstrt = xls[*nlvl - 1];
+        *root = ls[jstrt - 1];
+        if (jstrt < ccsize)
+            for (int j = jstrt; j <= ccsize; ++j) {
+                int node = ls[j - 1], ndeg = 0;
+                for (int k = xadj[node - 1]; k <= xadj[node] - 1; ++k) if (mask[adj[k - 1] - 1] > 0) ndeg++;
+                if (ndeg < mindeg) { *root = node; mindeg = ndeg; }
+            }
+        int nlvl2;
+        rcm_level_set(*root, xadj, adj, mask, &nlvl2, xls, ls);
+        if (nlvl2 <= *nlvl) break;
+        *nlvl = nlvl2;
+        if (ccsize <= *nlvl) break;
+    }
+}
+static void rcm_one(int root, int* xadj, const int* adj, int* mask, int* perm, int* ccsize, int n) {
+    int* deg = (int*)malloc(sizeof(int) * n);
+    rcm_degree(root, xadj, adj, mask, deg, ccsize, perm);
+    mask[root - 1] = 0;
+    if (*ccsize == 1) { free(deg); return; }
+    int lvlend = 0, lnbr = 1;
+    while (lvlend < lnbr) {
+        int lbegin = lvlend + 1; lvlend = lnbr;
+        for (int i = lbegin; i <= lvlend; ++i) {
+            int node = perm[i - 1];
+            int fnbr = lnbr + 1;
+            for (int j = xadj[node - 1]; j <= xadj[node] - 1; ++j) {
+                int nbr = adj[j - 1];
+                if (mask[nbr - 1] != 0) { lnbr++; mask[nbr - 1] = 0; perm[lnbr - 1] = nbr; }
+            }
+            if (lnbr <= fnbr) continue;
+            int k = fnbr;
+            while (k < lnbr) {
+                int l = k; k++;
+                int nbr = perm[k - 1];
+                while (fnbr < l) {
+                    int lperm = perm[l - 1];
+                    if (deg[lperm - 1] <= deg[nbr - 1]) break;
+                    perm[l] = lperm; l--;
+                }
+                perm[l] = nbr;
+            }
+        }
+    }
+    for (int i = 0, j = *ccsize - 1; i < j; ++i, --j) { int t = perm[i]; perm[i] = perm[j]; perm[j] = t; }
+    free(deg);
+}
+static void build_rcm(orc_ctx* c) {
+    int n = c->nc;
+    int* cfp = iget(c, "cf_ptr"); int* cfi = iget(c, "cf_idx");
+    int* xadj = (int*)malloc(sizeof(int) * (n + 1));
+    int* adj = (int*)malloc(sizeof(int) * (2 * (size_t)c->ni + 1));
+    int m = 0; xadj[0] = 1;
+    for (int i = 0; i < n; ++i) {
+        for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+            int f = cfi[k];
+            if (f >= c->ni) continue;
+            adj[m++] = (c->own[f] == i ? c->nei[f] : c->own[f]) + 1;
+        }
+        xadj[i + 1] = m + 1;
+    }
+    int* perm1 = (int*)malloc(sizeof(int) * n);
+    int* mask = (int*)malloc(sizeof(int) * n);
+    int* xls = (int*)malloc(sizeof(int) * (n + 1));
+    for (int i = 0; i < n; ++i) mask[i] = 1;
+    int num = 1;
+    for (int i = 0; i < n; ++i) {
+        if (mask[i] == 0) continue;
+        int root = i + 1, nlvl, cs;
+        rcm_root_find(&root, xadj, adj, mask, &nlvl, xls, perm1 + num - 1);
+        rcm_one(root, xadj, adj, mask, perm1 + num - 1, &cs, n);
+        num += cs;
+        if (num > n) break;
+    }
+    int* perm = ireg(c, "rcm_perm", n); int* iperm = ireg(c, "rcm_iperm", n);
+    for (int i = 0; i < n; ++i) perm[i] = perm1[i] - 1;
+    for (int i = 0; i < n; ++i) iperm[perm[i]] = i;
+    free(xadj); free(adj); free(perm1); free(mask); free(xls);
+}
+
+/* ------------------------------------------------------------------------ */
+/* public: mesh                                                             */
+/* ------------------------------------------------------------------------ */
+orc_ctx* orc_create(int np, const double* pts, int nf, int ni, int nc, const int* fptr, const int* fpts,
+                    const int* own, const int* nei, int npatch, const int* pstart, const int* psize) {
+    orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
+    c->np = np; c->nf = nf; c->ni = ni; c->nc = nc; c->npatch = npatch;
+    c->pts = dreg(c, "points", 3LL * np); memcpy(c->pts, pts, sizeof(double) * 3 * (size_t)np);
+    c->fptr = ireg(c, "face_ptr", nf + 1); memcpy(c->fptr, fptr, sizeof(int) * (nf + 1));
+    c->fpts = ireg(c, "face_pts", fptr[nf]); memcpy(c->fpts, fpts, sizeof(int) * fptr[nf]);
+    c->own = ireg(c, "owner", nf); memcpy(c->own, own, sizeof(int) * nf);
+    c->nei = ireg(c, "neighbour", ni > 0 ? ni : 1); if (ni) memcpy(c->nei, nei, sizeof(int) * ni);
+    c->pstart = ireg(c, "patch_start", npatch); memcpy(c->pstart, pstart, sizeof(int) * npatch);
+    c->psize = ireg(c, "patch_size", npatch); memcpy(c->psize, psize, sizeof(int) * npatch);
+    c->bct = ireg(c, "bc_type", 3LL * npatch);
+    c->bcv = dreg(c, "bc_value", 5LL * npatch);
+    c->minP = c->minU = c->minV = c->minW = -1e300;
+    c->maxP = c->maxU = c->maxV = c->maxW = 1e300;
+    build_geometry(c);
+    build_topology(c);
+    build_lsq(c);
+    build_rcm(c);
+    return c;
+}
+
+void orc_destroy(orc_ctx* c) {
+    if (!c) return;
+    for (int i = 0; i < c->narr; ++i) free(c->arr[i].p);
+    free(c);
+}
+
+void orc_set_case(orc_ctx* c, const int* bct, const double* bcv, const double* prm) {
+    memcpy(c->bct, bct, sizeof(int) * 3 * c->npatch);
+    memcpy(c->bcv, bcv, sizeof(double) * 5 * c->npatch);
+    c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2];
+    c->g[0] = prm[6]; c->g[1] = prm[7]; c->g[2] = prm[8];
+    c->urf_p = prm[9]; c->urf_u = prm[10]; c->use_gravity = prm[11] != 0.0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* face values + EOS: src/solvers/eos.cpp:10-151 (calcIncomCellEOSVF),       */
+/* :439-520 (getValuesFromEOSVF), src/solvers/reconIncom.cpp:501-1035        */
+/* (reconIncomZeroOrder), :440-496 (calcOtherDataIncomFromEOS)               */
+/* ------------------------------------------------------------------------ */
+/* std::max / std::min semantics: max(a,b) = (a<b)?b:a, min(a,b) = (b<a)?b:a */
+static double smax(double a, double b) { return (a < b) ? b : a; }
+static double smin(double a, double b) { return (b < a) ? b : a; }
+static double clamp01(double x) { return smax(0.0, smin(1.0, x)); }
+static double eos_face(double vf, double r0, double r1) {
+    double v0 = clamp01(vf), v1 = clamp01(1.0 - vf);
+    double rho = 0.0; rho += v0 * r0; rho += v1 * r1;
+    return rho;
+}
+static int patch_of(orc_ctx* c, int f) {
+    for (int p = 0; p < c->npatch; ++p) if (f >= c->pstart[p] && f < c->pstart[p] + c->psize[p]) return p;
+    return -1;
+}
+static void face_values(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    double *P = dget(c, "P"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *VF = dget(c, "VF");
+    double* rho = dreg(c, "rho", nc);
+    for (int i = 0; i < nc; ++i) {
+        double mf = clamp01(VF[i]);
+        double v0 = clamp01(mf);
+        double v1 = clamp01(1.0 - mf);
+        double r = 0.0; r += v0 * c->rho0; r += v1 * c->rho1;
+        rho[i] = r; VF[i] = v0;
+    }
+    double* fn = dget(c, "face_n");
+    double *pl = dreg(c, "face_pL", nf), *pr = dreg(c, "face_pR", nf);
+    double *ul = dreg(c, "face_uL", 3LL * nf), *ur = dreg(c, "face_uR", 3LL * nf);
+    double *vl = dreg(c, "face_vfL", nf), *vr = dreg(c, "face_vfR", nf);
+    double *rl = dreg(c, "face_rhoL", nf), *rr = dreg(c, "face_rhoR", nf);
+    for (int f = 0; f < nf; ++f) {
+        int o = c->own[f];
+        if (f < ni) {
+            int q = c->nei[f];
+            pl[f] = P[o]; ul[3 * f] = U[o]; ul[3 * f + 1] = V[o]; ul[3 * f + 2] = W[o]; vl[f] = VF[o];
+            pr[f] = P[q]; ur[3 * f] = U[q]; ur[3 * f + 1] = V[q]; ur[3 * f + 2] = W[q]; vr[f] = VF[q];
+        } else {
+            int p = patch_of(c, f);
+            const int* t = c->bct + 3 * p; const double* bv = c->bcv + 5 * p;
+            pl[f] = (t[0] == 1) ? bv[0] : P[o]; pr[f] = pl[f];
+            const double* n = fn + 3 * f;
+            if (t[1] == 1) { ul[3 * f] = bv[1]; ul[3 * f + 1] = bv[2]; ul[3 * f + 2] = bv[3]; }
+            else if (t[1] == 2) { ul[3 * f] = 0.0; ul[3 * f + 1] = 0.0; ul[3 * f + 2] = 0.0; }
+            else if (t[1] == 3) {
+                double un = U[o] * n[0] + V[o] * n[1] + W[o] * n[2];
+                ul[3 * f] = U[o] - un * n[0]; ul[3 * f + 1] = V[o] - un * n[1]; ul[3 * f + 2] = W[o] - un * n[2];
+            } else { ul[3 * f] = U[o]; ul[3 * f + 1] = V[o]; ul[3 * f + 2] = W[o]; }
+            /* fixedValue velocity keeps the boundary value on the right only; the
+               left carries it too except for the reference's orifice special case */
+            ur[3 * f] = ul[3 * f]; ur[3 * f + 1] = ul[3 * f + 1]; ur[3 * f + 2] = ul[3 * f + 2];
+            vl[f] = (t[2] == 1) ? bv[4] : VF[o]; vr[f] = vl[f];
+        }
+        rl[f] = eos_face(vl[f], c->rho0, c->rho1);
+        rr[f] = eos_face(vr[f], c->rho0, c->rho1);
+    }
+}
+
+/* gravity source: src/solvers/source/gravity.cpp:7-75 (calcSourceGravity) */
+static void gravity_source(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    double* sg = dreg(c, "src_grav", 4LL * nc);
+    if (!c->use_gravity) return;
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *pf = dget(c, "face_vecPF"), *nfv = dget(c, "face_vecNF"), *vol = dget(c, "cell_vol");
+    double *ul = dget(c, "face_uL"), *ur = dget(c, "face_uR"), *rl = dget(c, "face_rhoL"), *rr = dget(c, "face_rhoR");
+    for (int f = 0; f < nf; ++f) {
+        double wL = wc[f], wR = 1.0 - wL;
+        const double* n = fn + 3 * f;
+        double UnL = ul[3 * f] * n[0] + ul[3 * f + 1] * n[1] + ul[3 * f + 2] * n[2];
+        double UnR = ur[3 * f] * n[0] + ur[3 * f + 1] * n[1] + ur[3 * f + 2] * n[2];
+        double UnF = wL * UnL + wR * UnR;
+        double RhoF = 1.0 / (wL / rl[f] + wR / rr[f]);
+        double gL = 0.0, gR = 0.0;
+        for (int k = 0; k < 3; ++k) { gL += c->g[k] * pf[3 * f + k]; gR += c->g[k] * nfv[3 * f + k]; }
+        int o = c->own[f];
+        for (int k = 0; k < 3; ++k) sg[4 * o + k] += ((RhoF * gL * n[k]) * fa[f] / vol[o]);
+        sg[4 * o + 3] += ((RhoF * gL * UnF) * fa[f] / vol[o]);
+        if (f < ni) {
+            int q = c->nei[f];
+            for (int k = 0; k < 3; ++k) sg[4 * q + k] -= ((RhoF * gR * n[k]) * fa[f] / vol[q]);
+            sg[4 * q + 3] -= ((RhoF * gR * UnF) * fa[f] / vol[q]);
+        }
+    }
+}
+
+/* stencil min/max: src/solvers/cellVarMinMax.cpp:8-23 (setCellVarMinMax) */
+static void minmax(orc_ctx* c, const double* phi, double* mx, double* mn) {
+    int* sp = iget(c, "stencil_ptr"); int* si = iget(c, "stencil_idx");
+    for (int i = 0; i < c->nc; ++i) {
+        double a = phi[i], b = phi[i];
+        for (int k = sp[i]; k < sp[i + 1]; ++k) {
+            double v = phi[si[k]];
+            a = (a < v) ? v : a;       /* std::max(a, v) */
+            b = (v < b) ? v : b;       /* std::min(b, v) */
+        }
+        mx[i] = a; mn[i] = b;
+    }
+}
+
+/* LSQ gradient: src/math/gradient.cpp:761-816 (cellVertex stencil), :997-1050
+   (boundary faces, phi_f = face varR), :1136-1159 (M^-1 apply) */
+static void lsq_grad(orc_ctx* c, const double* phi, const double* phiR, double* grad) {
+    int* sp = iget(c, "stencil_ptr"); int* si = iget(c, "stencil_idx");
+    double *cc = dget(c, "cell_c"), *fc = dget(c, "face_c"), *minv = dget(c, "lsq_minv");
+    int nc = c->nc;
+    double* gt = (double*)calloc(3 * (size_t)nc, sizeof(double));
+    for (int i = 0; i < nc; ++i)
+        for (int k = sp[i]; k < sp[i + 1]; ++k) {
+            int j = si[k];
+            double dx = cc[3 * j] - cc[3 * i], dy = cc[3 * j + 1] - cc[3 * i + 1], dz = cc[3 * j + 2] - cc[3 * i + 2];
+            double wk = 1.0 / (dx * dx + dy * dy + dz * dz);
+            double dv = phi[j] - phi[i];
+            gt[3 * i] += wk * dx * dv; gt[3 * i + 1] += wk * dy * dv; gt[3 * i + 2] += wk * dz * dv;
+        }
+    for (int f = c->ni; f < c->nf; ++f) {
+        int i = c->own[f];
+        double dv = phiR[f] - phi[i];
+        double dx = fc[3 * f] - cc[3 * i], dy = fc[3 * f + 1] - cc[3 * i + 1], dz = fc[3 * f + 2] - cc[3 * i + 2];
+        double wk = 1.0 / (dx * dx + dy * dy + dz * dz);
+        gt[3 * i] += wk * dx * dv; gt[3 * i + 1] += wk * dy * dv; gt[3 * i + 2] += wk * dz * dv;
+    }
+    for (int i = 0; i < nc; ++i) {
+        const double* m = minv + 6 * i; const double* g = gt + 3 * i;
+        double t0 = 0.0; t0 += m[0] * g[0]; t0 += m[1] * g[1]; t0 += m[2] * g[2];
+        double t1 = 0.0; t1 += m[1] * g[0]; t1 += m[3] * g[1]; t1 += m[4] * g[2];
+        double t2 = 0.0; t2 += m[2] * g[0]; t2 += m[4] * g[1]; t2 += m[5] * g[2];
+        grad[3 * i] = t0; grad[3 * i + 1] = t1; grad[3 * i + 2] = t2;
+    }
+    free(gt);
+}
+
+/* ------------------------------------------------------------------------ */
+/* pressure equation assembly: src/solvers/eqPressure.cpp:40-105 (min/max,   */
+/* gradients), :217-564 (diagonal COO + internal face loop, with             */
+/* src/solvers/surfaceNormalVelocity.cpp:125-221 Rhie-Chow terms), :570-673  */
+/* (boundary loop).  COO order: N diagonals, then (LR, RL) per internal face */
+/* ------------------------------------------------------------------------ */
+void orc_assemble_pressure(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    face_values(c);
+    double* mxvf = dreg(c, "max_vf", nc); double* mnvf = dreg(c, "min_vf", nc);
+    minmax(c, dget(c, "VF"), mxvf, mnvf);
+    gravity_source(c);
+    double *P = dget(c, "P"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *VF = dget(c, "VF");
+    double *rho = dget(c, "rho"), *sg = dget(c, "src_grav");
+    double* mm = dreg(c, "minmax_uvw", 6LL * nc);
+    double *t1 = (double*)malloc(sizeof(double) * nc), *t2 = (double*)malloc(sizeof(double) * nc);
+    minmax(c, U, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i] = t1[i]; mm[6 * i + 1] = t2[i]; }
+    minmax(c, V, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 2] = t1[i]; mm[6 * i + 3] = t2[i]; }
+    minmax(c, W, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 4] = t1[i]; mm[6 * i + 5] = t2[i]; }
+    free(t1); free(t2);
+    double *pr = dget(c, "face_pR"), *ur = dget(c, "face_uR"), *vr = dget(c, "face_vfR");
+    double* tmp = (double*)malloc(sizeof(double) * nf);
+    double* gP = dreg(c, "grad_P", 3LL * nc); lsq_grad(c, P, pr, gP);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f];
+    double* gU = dreg(c, "grad_U", 3LL * nc); lsq_grad(c, U, tmp, gU);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 1];
+    double* gV = dreg(c, "grad_V", 3LL * nc); lsq_grad(c, V, tmp, gV);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 2];
+    double* gW = dreg(c, "grad_W", 3LL * nc); lsq_grad(c, W, tmp, gW);
+    double* gVF = dreg(c, "grad_VF", 3LL * nc); lsq_grad(c, VF, vr, gVF);
+    free(tmp);
+
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *mpn = dget(c, "face_magPN"), *al = dget(c, "face_alphaF"), *epn = dget(c, "face_ePN");
+    double *sk = dget(c, "face_skew"), *ul = dget(c, "face_uL"), *rl = dget(c, "face_rhoL");
+    int nnz = nc + 2 * ni;
+    int* ar = ireg(c, "A_rows", nnz); int* acl = ireg(c, "A_cols", nnz);
+    double* av = dreg(c, "A_vals", nnz); double* B = dreg(c, "B", nc);
+    double* unf = dreg(c, "face_UnF", nf);
+    for (int i = 0; i < nc; ++i) { ar[i] = i; acl[i] = i; }
+    const double dt = c->dt;
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f; const double* s = sk + 3 * f;
+        double area = fa[f], wCL = wc[f], wCR = 1.0 - wCL;
+        double RhoL = rho[o], RhoR = rho[q], PL = P[o], PR = P[q];
+        double Rho_star = 1.0 / (wCR / RhoL + wCR / RhoR);    /* eqPressure.cpp:396 (wCR twice) */
+        double tmp1 = dt / Rho_star;
+        double dPN = mpn[f], alpha = al[f];
+        double ULs = U[o], VLs = V[o], WLs = W[o], URs = U[q], VRs = V[q], WRs = W[q];
+        for (int k = 0; k < 3; ++k) {
+            ULs += gU[3 * o + k] * s[k]; URs += gU[3 * q + k] * s[k];
+            VLs += gV[3 * o + k] * s[k]; VRs += gV[3 * q + k] * s[k];
+            WLs += gW[3 * o + k] * s[k]; WRs += gW[3 * q + k] * s[k];
+        }
+        ULs = smax(mm[6 * o + 1], smin(mm[6 * o + 0], ULs)); URs = smax(mm[6 * q + 1], smin(mm[6 * q + 0], URs));
+        VLs = smax(mm[6 * o + 3], smin(mm[6 * o + 2], VLs)); VRs = smax(mm[6 * q + 3], smin(mm[6 * q + 2], VRs));
+        WLs = smax(mm[6 * o + 5], smin(mm[6 * o + 4], WLs)); WRs = smax(mm[6 * q + 5], smin(mm[6 * q + 4], WRs));
+        double UnL = ULs * n[0] + VLs * n[1] + WLs * n[2];
+        double UnR = URs * n[0] + VRs * n[1] + WRs * n[2];
+        double UnF = wCL * UnL + wCR * UnR;
+        /* surfaceNormalVelocity.cpp:125-155 (pressure) */
+        double rs = 1.0 / (wCL / RhoL + wCR / RhoR);
+        double tt = dt / rs;
+        UnF -= alpha * tt * (PR - PL) / dPN;
+        for (int k = 0; k < 3; ++k) {
+            UnF -= tt * rs * wCL / RhoL * gP[3 * o + k] * (n[k] - alpha * e[k]);
+            UnF -= tt * rs * wCR / RhoR * gP[3 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * gP[3 * o + k] * n[k];
+            UnF += tt * rs * wCR / RhoR * gP[3 * q + k] * n[k];
+        }
+        /* surfaceNormalVelocity.cpp:156-187 (gravity) */
+        for (int k = 0; k < 3; ++k) UnF += alpha * tt * rs * c->g[k] * alpha * e[k];
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * sg[4 * o + k] * (n[k] - alpha * e[k]);
+            UnF += tt * rs * wCR / RhoR * sg[4 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
+            UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
+        }
+        unf[f] = UnF;
+        double coef = alpha * tmp1 / dPN * area;
+        av[o] += (+coef);
+        ar[nc + 2 * f] = o; acl[nc + 2 * f] = q; av[nc + 2 * f] = (-coef);
+        av[q] -= (-coef);
+        ar[nc + 2 * f + 1] = q; acl[nc + 2 * f + 1] = o; av[nc + 2 * f + 1] = -(+coef);
+        B[o] -= (UnF * area);
+        B[q] += (UnF * area);
+    }
+    double* pRf = dget(c, "face_pR");
+    for (int f = ni; f < nf; ++f) {
+        int p = patch_of(c, f), o = c->own[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f;
+        double area = fa[f];
+        double UnL = ul[3 * f] * n[0] + ul[3 * f + 1] * n[1] + ul[3 * f + 2] * n[2];
+        double UnR = ur[3 * f] * n[0] + ur[3 * f + 1] * n[1] + ur[3 * f + 2] * n[2];
+        double UnF = 0.5 * UnL + 0.5 * UnR;
+        double RhoL = rl[f];
+        double tmp1 = 1.0 / RhoL * dt;
+        double diff = (c->bct[3 * p] == 1) ? 1.0 : 0.0;
+        double dPN = 0.5 * mpn[f], alpha = al[f];
+        double PL = P[o], PR = pRf[f];
+        if (c->bct[3 * p] == 1) {
+            UnF -= alpha * tmp1 * (PR - PL) / dPN;
+            for (int k = 0; k < 3; ++k) UnF += alpha * tmp1 * gP[3 * o + k] * e[k];
+        }
+        unf[f] = UnF;
+        av[o] += diff * (alpha * tmp1 / dPN * area);
+        B[o] -= (UnF * area);
+    }
+}
+
+/* COO -> CSR, src/solvers/solveAMGCL.cpp:206-251 (in-row order = COO order) */
+void orc_coo_to_csr(orc_ctx* c) {
+    int n = c->nc, nnz = c->nc + 2 * c->ni;
+    int *r = iget(c, "A_rows"), *cl = iget(c, "A_cols"); double* v = dget(c, "A_vals");
+    int* ptr = ireg(c, "csr_ptr", n + 1); int* col = ireg(c, "csr_col", nnz); double* val = dreg(c, "csr_val", nnz);
+    for (int k = 0; k < nnz; ++k) ptr[r[k]]++;
+    for (int i = 0, s = 0; i < n; ++i) { int t = ptr[i]; ptr[i] = s; s += t; }
+    ptr[n] = nnz;
+    for (int k = 0; k < nnz; ++k) { int d = ptr[r[k]]++; col[d] = cl[k]; val[d] = v[k]; }
+    for (int i = 0, last = 0; i <= n; ++i) { int t = ptr[i]; ptr[i] = last; last = t; }
+}
+
+/* Symmetric RCM permutation of the CSR system (rows in RCM order, in-row
+   order kept, column indices renumbered through the inverse permutation). */
+void orc_permute_csr(orc_ctx* c) {
+    int n = c->nc;
+    int *ptr = iget(c, "csr_ptr"), *col = iget(c, "csr_col"); double* val = dget(c, "csr_val");
+    int *perm = iget(c, "rcm_perm"), *iperm = iget(c, "rcm_iperm");
+    double* B = dget(c, "B");
+    int nnz = ptr[n];
+    int* pp = ireg(c, "rcm_csr_ptr", n + 1); int* pc = ireg(c, "rcm_csr_col", nnz);
+    double* pv = dreg(c, "rcm_csr_val", nnz); double* pb = dreg(c, "rcm_B", n);
+    for (int r = 0; r < n; ++r) {
+        int o = perm[r];
+        pp[r + 1] = pp[r] + (ptr[o + 1] - ptr[o]);
+        for (int k = ptr[o], d = pp[r]; k < ptr[o + 1]; ++k, ++d) { pc[d] = iperm[col[k]]; pv[d] = val[k]; }
+        pb[r] = B[o];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Solver: smoothed-aggregation AMG (AMGCL coarsening/smoothed_aggregation   */
+/* .hpp:130-215 semantics: strength eps^2 d_i d_j < a_ij^2 with eps 0.08      */
+/* halved per level, filtered diagonal, omega 2/3) with MIS(2) aggregation,  */
+/* Chebyshev smoothing, dense Cholesky on the coarsest level, inside CG.     */
+/* ------------------------------------------------------------------------ */
+typedef struct { int n, nnz; int *ptr, *col; double* val; } csr_t;
+typedef struct {
+    csr_t A, P, R;
+    double *dinv, lam_max;
+    double *r, *x, *b, *t1, *t2;   /* work vectors */
+    int nagg;
+} level_t;
+typedef struct {
+    int nlev;
+    level_t lev[32];
+    int nc; double* chol;  /* coarsest dense Cholesky factor (lower, row-major) */
+    int cheb_degree;
+    long long total_nnz;
+} amg_t;
+
+static void csr_free(csr_t* a) { free(a->ptr); free(a->col); free(a->val); memset(a, 0, sizeof *a); }
+
+static uint32_t hash_u32(uint32_t x) {
+    /* integer avalanche mixer (public-domain "lowbias32" constants) */
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+/* MIS(2) aggregation over the strong graph, as the GPU does it: synchronous
+   rounds of two max-propagations of the tuple (state, hash, index). */
+static int aggregate(const csr_t* A, const char* strong, int* agg) {
+    int n = A->n;
+    /* state: 2 root, 1 undecided, 0 out; tuple key packed into 64 bits */
+    uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
+    uint64_t* m1 = (uint64_t*)malloc(sizeof(uint64_t) * n);
+    uint64_t* m2 = (uint64_t*)malloc(sizeof(uint64_t) * n);
+    int* st = (int*)malloc(sizeof(int) * n);
+    for (int i = 0; i < n; ++i) {
+        int has = 0;
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) if (strong[k]) { has = 1; break; }
+        st[i] = has ? 1 : -1;    /* -1: isolated, never aggregated */
+    }
+#define MKKEY(s, i) ((((uint64_t)(s)) << 62) | (((uint64_t)hash_u32((uint32_t)(i))) << 30) | (uint64_t)(i))
+    for (int round = 0; round < 1000; ++round) {
+        int und = 0;
+        for (int i = 0; i < n; ++i) { int s = st[i] < 0 ? 0 : st[i]; key[i] = MKKEY(s, i); if (st[i] == 1) und++; }
+        if (!und) break;
+        for (int i = 0; i < n; ++i) {
+            uint64_t m = key[i];
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) if (strong[k] && key[A->col[k]] > m) m = key[A->col[k]];
+            m1[i] = m;
+        }
+        for (int i = 0; i < n; ++i) {
+            uint64_t m = m1[i];
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) if (strong[k] && m1[A->col[k]] > m) m = m1[A->col[k]];
+            m2[i] = m;
+        }
+        for (int i = 0; i < n; ++i) {
+            if (st[i] != 1) continue;
+            if (m2[i] == key[i]) st[i] = 2;
+            else if ((m2[i] >> 62) == 2) st[i] = 0;
+        }
+    }
+#undef MKKEY
+    int nagg = 0;
+    for (int i = 0; i < n; ++i) agg[i] = (st[i] == 2) ? nagg++ : -1;
+    /* pass 1: join the strongest-keyed root neighbour; pass 2: join through
+       a neighbour assigned in pass 1 (synchronous, so order-independent) */
+    int* a1 = (int*)malloc(sizeof(int) * n);
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int i = 0; i < n; ++i) {
+            a1[i] = agg[i];
+            if (agg[i] >= 0 || st[i] < 0) continue;
+            uint64_t best = 0; int ba = -1;
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+                int j = A->col[k];
+                if (!strong[k] || agg[j] < 0) continue;
+                uint64_t kj = (((uint64_t)hash_u32((uint32_t)j)) << 32) | (uint64_t)j;
+                if (ba < 0 || kj > best) { best = kj; ba = agg[j]; }
+            }
+            a1[i] = ba;
+        }
+        memcpy(agg, a1, sizeof(int) * n);
+    }
+    free(a1); free(key); free(m1); free(m2); free(st);
+    return nagg;
+}
+
+/* C = A * B, rows of C sorted by column; accumulation in product order */
+static void spgemm(const csr_t* A, const csr_t* B, int ncolB, csr_t* C) {
+    int n = A->n;
+    C->n = n; C->ptr = (int*)calloc(n + 1, sizeof(int));
+    int* mark = (int*)malloc(sizeof(int) * ncolB);
+    for (int j = 0; j < ncolB; ++j) mark[j] = -1;
+    for (int i = 0; i < n; ++i) {
+        int cnt = 0;
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+            int a = A->col[k];
+            for (int q = B->ptr[a]; q < B->ptr[a + 1]; ++q) if (mark[B->col[q]] != i) { mark[B->col[q]] = i; cnt++; }
+        }
+        C->ptr[i + 1] = C->ptr[i] + cnt;
+    }
+    C->nnz = C->ptr[n];
+    C->col = (int*)malloc(sizeof(int) * (C->nnz + 1)); C->val = (double*)malloc(sizeof(double) * (C->nnz + 1));
+    double* acc = (double*)calloc(ncolB, sizeof(double));
+    for (int j = 0; j < ncolB; ++j) mark[j] = -1;
+    int* tmp = (int*)malloc(sizeof(int) * (ncolB + 1));
+    for (int i = 0; i < n; ++i) {
+        int cnt = 0;
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+            int a = A->col[k]; double va = A->val[k];
+            for (int q = B->ptr[a]; q < B->ptr[a + 1]; ++q) {
+                int j = B->col[q];
+                if (mark[j] != i) { mark[j] = i; acc[j] = 0.0; tmp[cnt++] = j; }
+                acc[j] += va * B->val[q];
+            }
+        }
+        /* insertion sort of the (short) column list */
+        for (int s = 1; s < cnt; ++s) { int v = tmp[s], t = s - 1; while (t >= 0 && tmp[t] > v) { tmp[t + 1] = tmp[t]; --t; } tmp[t + 1] = v; }
+        for (int s = 0; s < cnt; ++s) { C->col[C->ptr[i] + s] = tmp[s]; C->val[C->ptr[i] + s] = acc[tmp[s]]; }
+    }
+    free(mark); free(acc); free(tmp);
+}
+
+static void transpose(const csr_t* A, int ncol, csr_t* T) {
+    T->n = ncol; T->nnz = A->nnz;
+    T->ptr = (int*)calloc(ncol + 1, sizeof(int));
+    T->col = (int*)malloc(sizeof(int) * (A->nnz + 1)); T->val = (double*)malloc(sizeof(double) * (A->nnz + 1));
+    for (int k = 0; k < A->nnz; ++k) T->ptr[A->col[k] + 1]++;
+    for (int j = 0; j < ncol; ++j) T->ptr[j + 1] += T->ptr[j];
+    int* fill = (int*)malloc(sizeof(int) * (ncol + 1));
+    memcpy(fill, T->ptr, sizeof(int) * (ncol + 1));
+    for (int i = 0; i < A->n; ++i)
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) { int d = fill[A->col[k]]++; T->col[d] = i; T->val[d] = A->val[k]; }
+    free(fill);
+}
+
+static void spmv(const csr_t* A, const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < A->n; ++i) {
+        double s = 0.0;
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) s += A->val[k] * x[A->col[k]];
+        y[i] = s;
+    }
+}
+
+typedef struct { double eps_strong; int coarse_enough; int max_levels; int cheb_degree; } amg_prm;
+
+static void amg_free(amg_t* h) {
+    for (int l = 0; l < h->nlev; ++l) {
+        level_t* L = &h->lev[l];
+        if (l > 0) csr_free(&L->A);
+        csr_free(&L->P); csr_free(&L->R);
+        free(L->dinv); free(L->r); free(L->x); free(L->b); free(L->t1); free(L->t2);
+    }
+    free(h->chol);
+    memset(h, 0, sizeof *h);
+}
+
+static int dense_cholesky(int n, double* a) {
+    for (int j = 0; j < n; ++j) {
+        double d = a[j * n + j];
+        for (int k = 0; k < j; ++k) d -= a[j * n + k] * a[j * n + k];
+        if (!(d > 0.0)) return -1;
+        d = sqrt(d); a[j * n + j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double s = a[i * n + j];
+            for (int k = 0; k < j; ++k) s -= a[i * n + k] * a[j * n + k];
+            a[i * n + j] = s / d;
+        }
+        for (int i = 0; i < j; ++i) a[i * n + j] = 0.0;
+    }
+    return 0;
+}
+
+static int amg_setup(amg_t* h, const csr_t* A0, const amg_prm* prm) {
+    memset(h, 0, sizeof *h);
+    h->cheb_degree = prm->cheb_degree;
+    float eps = (float)prm->eps_strong;
+    h->lev[0].A = *A0;
+    int l = 0;
+    for (;;) {
+        level_t* L = &h->lev[l];
+        csr_t* A = &L->A;
+        int n = A->n;
+        h->total_nnz += A->nnz;
+        L->dinv = (double*)malloc(sizeof(double) * n);
+        double lam = 0.0;
+        for (int i = 0; i < n; ++i) {
+            double d = 0.0, rs = 0.0;
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) { if (A->col[k] == i) d = A->val[k]; rs += fabs(A->val[k]); }
+            L->dinv[i] = 1.0 / d;
+            double r = rs / fabs(d);
+            if (r > lam) lam = r;
+        }
+        L->lam_max = lam;   /* Gershgorin bound on rho(D^-1 A) */
+        L->r = (double*)calloc(n, sizeof(double)); L->x = (double*)calloc(n, sizeof(double));
+        L->b = (double*)calloc(n, sizeof(double)); L->t1 = (double*)calloc(n, sizeof(double));
+        L->t2 = (double*)calloc(n, sizeof(double));
+        if (n <= prm->coarse_enough || l == prm->max_levels - 1) break;
+        /* strength */
+        double eps2 = (double)(eps * eps);
+        char* strong = (char*)malloc(A->nnz + 1);
+        double* dia = (double*)malloc(sizeof(double) * n);
+        for (int i = 0; i < n; ++i) { dia[i] = 0.0; for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) if (A->col[k] == i) dia[i] = A->val[k]; }
+        for (int i = 0; i < n; ++i) {
+            double ed = eps2 * dia[i];
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+                int j = A->col[k]; double v = A->val[k];
+                strong[k] = (j != i) && (ed * dia[j] < v * v);
+            }
+        }
+        eps *= 0.5f;
+        int* agg = (int*)malloc(sizeof(int) * n);
+        int nagg = aggregate(A, strong, agg);
+        if (nagg == 0 || nagg >= n) { free(strong); free(dia); free(agg); break; }
+        L->nagg = nagg;
+        /* smoothed prolongation: row i = (1-w) e_agg(i) + sum_strong (-w/df_i) a_ij e_agg(j) */
+        const double omega = 2.0 / 3.0;
+        csr_t* P = &L->P;
+        P->n = n; P->ptr = (int*)calloc(n + 1, sizeof(int));
+        int cap = A->nnz + 1;
+        P->col = (int*)malloc(sizeof(int) * cap); P->val = (double*)malloc(sizeof(double) * cap);
+        int* mark = (int*)malloc(sizeof(int) * nagg); for (int j = 0; j < nagg; ++j) mark[j] = -1;
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            double df = 0.0;
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) if (A->col[k] == i || !strong[k]) df += A->val[k];
+            df = -omega * (1.0 / df);
+            int rb = m;
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+                int j = A->col[k];
+                if (j != i && !strong[k]) continue;
+                int g = agg[j];
+                if (g < 0) continue;
+                double v = (j == i) ? (1.0 - omega) : df * A->val[k];
+                if (mark[g] >= rb) P->val[mark[g]] += v;
+                else { mark[g] = m; P->col[m] = g; P->val[m] = v; m++; }
+            }
+            /* sort row by column */
+            for (int s = rb + 1; s < m; ++s) {
+                int cv = P->col[s]; double vv = P->val[s]; int t = s - 1;
+                while (t >= rb && P->col[t] > cv) { P->col[t + 1] = P->col[t]; P->val[t + 1] = P->val[t]; --t; }
+                P->col[t + 1] = cv; P->val[t + 1] = vv;
+            }
+            for (int s = rb; s < m; ++s) mark[P->col[s]] = -1;
+            P->ptr[i + 1] = m;
+        }
+        P->nnz = m;
+        free(mark); free(strong); free(dia); free(agg);
+        transpose(P, nagg, &L->R);
+        csr_t AP, Ac;
+        spgemm(A, P, nagg, &AP);
+        spgemm(&L->R, &AP, nagg, &Ac);
+        csr_free(&AP);
+        l++;
+        h->lev[l].A = Ac;
+    }
+    h->nlev = l + 1;
+    /* coarsest: dense Cholesky */
+    csr_t* Ac = &h->lev[l].A;
+    h->nc = Ac->n;
+    h->chol = (double*)calloc((size_t)h->nc * h->nc, sizeof(double));
+    for (int i = 0; i < Ac->n; ++i) for (int k = Ac->ptr[i]; k < Ac->ptr[i + 1]; ++k) h->chol[(size_t)i * h->nc + Ac->col[k]] = Ac->val[k];
+    return dense_cholesky(h->nc, h->chol);
+}
+
+/* Chebyshev smoother on D^-1 A over [lam/30, lam]; x updated in place */
+static void cheb_smooth(const level_t* L, const double* b, double* x, int degree) {
+    int n = L->A.n;
+    double hi = L->lam_max, lo = hi / 30.0;
+    double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+    double sigma = theta / delta, rho = 1.0 / sigma;
+    double* r = L->t1; double* d = L->t2;
+    spmv(&L->A, x, r);
+    for (int i = 0; i < n; ++i) { r[i] = L->dinv[i] * (b[i] - r[i]); d[i] = r[i] / theta; }
+    for (int k = 0; k < degree; ++k) {
+        for (int i = 0; i < n; ++i) x[i] += d[i];
+        if (k == degree - 1) break;
+        spmv(&L->A, x, r);
+        double rho_new = 1.0 / (2.0 * sigma - rho);
+        for (int i = 0; i < n; ++i) {
+            double z = L->dinv[i] * (b[i] - r[i]);
+            d[i] = rho_new * rho * d[i] + 2.0 * rho_new / delta * z;
+        }
+        rho = rho_new;
+    }
+}
+
+static void vcycle(amg_t* h, int l, const double* b, double* x) {
+    level_t* L = &h->lev[l];
+    int n = L->A.n;
+    if (l == h->nlev - 1) {
+        int m = h->nc; const double* c = h->chol;
+        double* y = L->t1;
+        for (int i = 0; i < m; ++i) { double s = b[i]; for (int k = 0; k < i; ++k) s -= c[(size_t)i * m + k] * y[k]; y[i] = s / c[(size_t)i * m + i]; }
+        for (int i = m - 1; i >= 0; --i) { double s = y[i]; for (int k = i + 1; k < m; ++k) s -= c[(size_t)k * m + i] * x[k]; x[i] = s / c[(size_t)i * m + i]; }
+        return;
+    }
+    for (int i = 0; i < n; ++i) x[i] = 0.0;
+    cheb_smooth(L, b, x, h->cheb_degree);
+    spmv(&L->A, x, L->r);
+    for (int i = 0; i < n; ++i) L->r[i] = b[i] - L->r[i];
+    level_t* C = &h->lev[l + 1];
+    spmv(&L->R, L->r, C->b);
+    vcycle(h, l + 1, C->b, C->x);
+    for (int i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int k = L->P.ptr[i]; k < L->P.ptr[i + 1]; ++k) s += L->P.val[k] * C->x[L->P.col[k]];
+        x[i] += s;
+    }
+    cheb_smooth(L, b, x, h->cheb_degree);
+}
+
+static double dot(const double* a, const double* b, int n) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+:s) schedule(static)
+    for (int i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+/* preconditioned CG on the system in csr_ptr/col/val (or its RCM form) */
+int orc_solve(orc_ctx* c, int use_rcm, double tol, int maxiter, double* out_info) {
+    csr_t A;
+    A.n = c->nc;
+    A.ptr = iget(c, use_rcm ? "rcm_csr_ptr" : "csr_ptr");
+    A.col = iget(c, use_rcm ? "rcm_csr_col" : "csr_col");
+    A.val = dget(c, use_rcm ? "rcm_csr_val" : "csr_val");
+    A.nnz = A.ptr[A.n];
+    double* b = dget(c, use_rcm ? "rcm_B" : "B");
+    int n = A.n;
+    amg_t h; amg_prm prm = {0.08, 64, 24, 2};
+    if (amg_setup(&h, &A, &prm) != 0) { amg_free(&h); return -2; }
+    double* x = dreg(c, use_rcm ? "rcm_x_orc" : "x_orc", n);
+    double *r = (double*)malloc(sizeof(double) * n), *z = (double*)malloc(sizeof(double) * n);
+    double *p = (double*)malloc(sizeof(double) * n), *q = (double*)malloc(sizeof(double) * n);
+    memcpy(r, b, sizeof(double) * n);
+    double bn = sqrt(dot(b, b, n));
+    double rn = bn;
+    int it = 0;
+    double rz = 0.0;
+    if (bn == 0.0) { bn = 1.0; rn = 0.0; }
+    while (it < maxiter && rn > tol * bn) {
+        vcycle(&h, 0, r, z);
+        double rz_new = dot(r, z, n);
+        if (it == 0) memcpy(p, z, sizeof(double) * n);
+        else { double beta = rz_new / rz; for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i]; }
+        rz = rz_new;
+        spmv(&A, p, q);
+        double alpha = rz / dot(p, q, n);
+        for (int i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+        rn = sqrt(dot(r, r, n));
+        it++;
+    }
+    /* true residual */
+    spmv(&A, x, q);
+    double tr = 0.0;
+    for (int i = 0; i < n; ++i) { double d = b[i] - q[i]; tr += d * d; }
+    if (out_info) {
+        out_info[0] = it; out_info[1] = sqrt(tr) / bn; out_info[2] = h.nlev;
+        out_info[3] = (double)h.total_nnz / (double)A.nnz;
+        out_info[4] = h.nc;
+        for (int l = 0; l < h.nlev && l < 10; ++l) out_info[5 + l] = h.lev[l].A.n;
+    }
+    /* the finest level's A is borrowed */
+    memset(&h.lev[0].A, 0, sizeof(csr_t));
+    amg_free(&h);
+    free(r); free(z); free(p); free(q);
+    return it;
+}
+
+/* ------------------------------------------------------------------------ */
+/* post-solve: src/solvers/eqPressure.cpp:686-809 (Gauss-Green grad p', two */
+/* sweeps with skewness correction), :823-883 (update + norms)               */
+/* ------------------------------------------------------------------------ */
+double orc_update(orc_ctx* c, const double* x) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *sk = dget(c, "face_skew"), *vol = dget(c, "cell_vol");
+    double *P = dget(c, "P"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *rho = dget(c, "rho");
+    double* g = dreg(c, "grad_x", 3LL * nc);
+    double* gt = (double*)malloc(sizeof(double) * 3 * nc);
+    for (int it = 0; it < 2; ++it) {
+        memset(gt, 0, sizeof(double) * 3 * nc);
+        for (int f = 0; f < ni; ++f) {
+            int o = c->own[f], q = c->nei[f];
+            double wL = wc[f], wR = 1.0 - wL;
+            double vF = wL * x[o] + wR * x[q];
+            for (int k = 0; k < 3; ++k) { vF += wL * g[3 * o + k] * sk[3 * f + k]; vF += wR * g[3 * q + k] * sk[3 * f + k]; }
+            for (int k = 0; k < 3; ++k) gt[3 * o + k] += vF * fn[3 * f + k] * fa[f] / vol[o];
+            for (int k = 0; k < 3; ++k) gt[3 * q + k] -= vF * fn[3 * f + k] * fa[f] / vol[q];
+        }
+        /* the reference tests the type of variable 0 (pressure) per patch */
+        for (int f = ni; f < nf; ++f) {
+            int o = c->own[f], p = patch_of(c, f);
+            double vF = x[o];
+            if (c->bct[3 * p] == 1) vF = 0.0;
+            for (int k = 0; k < 3; ++k) gt[3 * o + k] += vF * fn[3 * f + k] * fa[f] / vol[o];
+        }
+        memcpy(g, gt, sizeof(double) * 3 * nc);
+    }
+    free(gt);
+    double nd = 0.0, npn = 0.0;
+    for (int i = 0; i < nc; ++i) {
+        P[i] += c->urf_p * x[i];
+        double t = c->dt / rho[i];
+        double ru = c->urf_u * t * g[3 * i], rv = c->urf_u * t * g[3 * i + 1], rw = c->urf_u * t * g[3 * i + 2];
+        U[i] -= ru; V[i] -= rv; W[i] -= rw;
+        if (P[i] <= c->minP) P[i] = c->minP;
+        if (P[i] >= c->maxP) P[i] = c->maxP;
+        if (U[i] <= c->minU) U[i] = c->minU;
+        if (U[i] >= c->maxU) U[i] = c->maxU;
+        if (V[i] <= c->minV) V[i] = c->minV;
+        if (V[i] >= c->maxV) V[i] = c->maxV;
+        if (W[i] <= c->minW) W[i] = c->minW;
+        if (W[i] >= c->maxW) W[i] = c->maxW;
+        nd += x[i] * x[i]; nd += ru * ru; nd += rv * rv; nd += rw * rw;
+        npn += P[i] * P[i]; npn += U[i] * U[i]; npn += V[i] * V[i]; npn += W[i] * W[i];
+    }
+    return sqrt(nd) / sqrt(npn);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

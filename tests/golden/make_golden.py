@@ -1,0 +1,68 @@
+"""Generate the golden fixtures in this folder from the reference's own code.
+
+Builds oracle/_ref/semo_ref from the reference sources (oracle/ref/Makefile),
+runs it on small seeded cases and stores inputs and every dumped intermediate
+as .npz.  The fixtures are committed so the parity tests need neither the
+reference tree nor its build.
+
+    python tests/golden/make_golden.py [REF_DIR]
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from semo_mesh_gb300.cases import box_case, vof_case, with_fields, BC_FIXED_VALUE  # noqa: E402
+from oracle.refcase import run_reference  # noqa: E402
+
+
+def golden_cases():
+    cs = []
+    cs.append(("box4", box_case(4)))
+    cs.append(("box5j", box_case(5, jitter=0.2)))
+    cs.append(("vof6", vof_case(6)))
+    c = with_fields(vof_case(5), seed=7, p_scale=50.0)
+    c.name = "vof5p"
+    # a second Dirichlet patch with a non-zero value exercises the boundary terms
+    c.bc_type[c.mesh.patch_names.index("xmin"), 0] = BC_FIXED_VALUE
+    c.bc_value[c.mesh.patch_names.index("xmin"), 0] = 3.0
+    cs.append(("vof5p", c))
+    c = box_case(7, jitter=0.3, mesh_seed=99)
+    c.name = "box7j"
+    c.P = np.random.default_rng(5).uniform(-2, 2, c.mesh.n_cells)
+    cs.append(("box7j", c))
+    return cs
+
+
+def save(name: str, case, ref: dict) -> None:
+    m = case.mesh
+    out = {f"ref_{k}": v for k, v in ref.items()}
+    out.update(points=m.points, face_ptr=m.face_ptr, face_pts=m.face_pts, owner=m.owner,
+               neighbour=m.neighbour, patch_start=m.patch_start, patch_size=m.patch_size,
+               n_cells=np.int64(m.n_cells), P=case.P, U=case.U, V=case.V, W=case.W, VF=case.VF,
+               bc_type=case.bc_type, bc_value=case.bc_value,
+               params=np.array([case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
+                                case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf,
+                                case.pre_u_urf, 1.0 if case.use_gravity else 0.0]))
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
+def main():
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref_dir}", "-j8"],
+                   check=True, stdout=subprocess.DEVNULL)
+    for name, case in golden_cases():
+        ref = run_reference(case, threads=1)
+        save(name, case, ref)
+        print(name, case.mesh.n_cells, "cells")
+
+
+if __name__ == "__main__":
+    main()
