@@ -1,0 +1,181 @@
+/*
+ * semo_gb300.h -- C-ABI of the GB300 (sm_103a) pressure-correction hot path.
+ *
+ * Drop-in for SEMO's per-outer-iteration pressure path: owner/neighbour face
+ * lists go in (OpenFOAM polyMesh order, as SEMO loads them), the assembled
+ * pressure-correction system comes out as an RCM-reordered CSR matrix plus
+ * right-hand side, and the solution vector of the AMG-preconditioned Krylov
+ * solve comes out in the caller's cell order.
+ *
+ * Conventions
+ *  - plain pointers and sizes; no CUDA or torch types.  Host pointers unless a
+ *    function says otherwise.  The caller owns every array it passes; the
+ *    context owns all device memory.
+ *  - every call returns a semo_status; semo_last_error() gives the message.
+ *  - calls on one context are synchronous at return and not re-entrant; one
+ *    context drives one GPU through one CUDA stream.
+ *  - cell indices at the boundary are the caller's (original) numbering;
+ *    only the *_rcm getters expose the reordered numbering.
+ */
+#ifndef SEMO_GB300_H
+#define SEMO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SEMO_OK = 0,
+    SEMO_ERR_ARGUMENT = 1,       /* null pointer, bad size, bad enum */
+    SEMO_ERR_MESH = 2,           /* malformed face lists, non-positive volume, singular LSQ */
+    SEMO_ERR_CUDA = 3,           /* CUDA runtime failure (message has the CUDA error) */
+    SEMO_ERR_OUT_OF_MEMORY = 4,
+    SEMO_ERR_NOT_CONVERGED = 5,  /* Krylov hit max_iter above tol (solution still returned) */
+    SEMO_ERR_NAN = 6,            /* NaN/Inf in inputs or in a residual */
+    SEMO_ERR_BREAKDOWN = 7,      /* Krylov breakdown (p.Ap <= 0 or rho == 0) */
+    SEMO_ERR_STATE = 8,          /* call out of order (e.g. solve before assemble) */
+    SEMO_ERR_NO_DEVICE = 9       /* no CUDA device / extension built for another arch */
+} semo_status;
+
+typedef enum {
+    SEMO_PREC_FP64 = 0,          /* AMG hierarchy, V-cycle and Krylov all FP64 */
+    SEMO_PREC_MIXED = 1          /* FP32 AMG hierarchy + V-cycle inside FP64 CG */
+} semo_precision;
+
+typedef enum {
+    SEMO_BC_ZERO_GRADIENT = 0,
+    SEMO_BC_FIXED_VALUE = 1,
+    SEMO_BC_NO_SLIP = 2,         /* velocity only */
+    SEMO_BC_SLIP = 3             /* velocity only */
+} semo_bc;
+
+typedef struct semo_ctx semo_ctx;
+
+typedef struct {
+    int device;                  /* CUDA ordinal */
+    int precision;               /* semo_precision */
+    double tol;                  /* relative residual ||b-Ax||/||b|| (FP64), default 1e-8 */
+    int max_iter;                /* Krylov iteration cap, default 500 */
+    /* smoothed aggregation (AMGCL smoothed_aggregation semantics) */
+    double eps_strong;           /* strength threshold, halved per level; default 0.08 */
+    int coarse_enough;           /* direct solve at or below this size; default 64 */
+    int max_levels;              /* default 24 */
+    int cheb_degree;             /* Chebyshev pre/post smoothing degree; default 2 */
+} semo_params;
+
+/* Physics of one pressure-correction pass (calcPressureEq inputs). */
+typedef struct {
+    double dt;                   /* controls.timeStep */
+    double rho[2];               /* phase densities; phase 0 is the volume fraction VF */
+    double gravity[3];           /* controls.gravityAcceleration */
+    int use_gravity;             /* compute the gravity body-force source */
+    double urf_p;                /* controls.prePreURF */
+    double urf_u;                /* controls.preVelURF */
+    double p_min, p_max, u_min, u_max, v_min, v_max, w_min, w_max;  /* controls.min/max clamps */
+} semo_physics;
+
+typedef struct {
+    int iterations;
+    double rel_residual;         /* FP64 ||b-Ax||/||b|| of the returned solution */
+    int levels;
+    int coarse_size;
+    double operator_complexity;
+    double setup_ms, solve_ms;   /* device time of AMG setup and Krylov iterations */
+} semo_solve_info;
+
+/* Fill *p with defaults. */
+void semo_params_default(semo_params* p);
+void semo_physics_default(semo_physics* p);
+
+/* Context lifetime.  Replaces: nothing (SEMO has no solver handle; its
+   solveAMGCL builds everything per call, src/solvers/solveAMGCL.cpp:179). */
+semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm);
+semo_status semo_ctx_destroy(semo_ctx* ctx);
+const char* semo_last_error(const semo_ctx* ctx);
+/* The cudaStream_t the context launches on, as an opaque pointer (for timing). */
+void* semo_stream(semo_ctx* ctx);
+
+/* Mesh ingestion, OpenFOAM polyMesh arrays.  Computes the geometry on the
+   GPU (src/mesh/geometric.cpp:792-1500 semantics), the vertex stencil
+   (geometric.cpp:1781-1845), the LSQ normal-matrix inverses
+   (src/math/gradient.cpp:246-453), the RCM order (src/math/RCM.cpp:34-218)
+   and the CSR pattern with face->slot maps (src/mesh/build.cpp:1319-1424).
+   Replaces: SEMO_Mesh_Load::OpenFoam post-load sequence
+   (src/load/loadOpenFoam.cpp:356-374) + SEMO_Mesh_Geometric::init +
+   SEMO_Utility_Math::initLeastSquare. */
+semo_status semo_mesh_upload(semo_ctx* ctx, int n_points, const double* points /*3*n_points*/,
+                             int n_faces, int n_internal, int n_cells,
+                             const int32_t* face_ptr /*n_faces+1*/, const int32_t* face_pts,
+                             const int32_t* owner /*n_faces*/, const int32_t* neighbour /*n_internal*/,
+                             int n_patches, const int32_t* patch_start, const int32_t* patch_size);
+
+/* RCM permutation, bit-exact with SEMO_Utility_Math::lib_RCM
+   (src/math/RCM.cpp:199-201): perm[r] = original cell at RCM position r
+   (cells[r].RCM), iperm[c] = RCM position of original cell c (cells[c].invRCM). */
+semo_status semo_rcm(semo_ctx* ctx, int32_t* perm, int32_t* iperm);
+
+/* Boundary conditions and physics.  bc_type is n_patches x 3 (pressure,
+   velocity, volume fraction: semo_bc); bc_value is n_patches x 5 (p, u, v, w,
+   vf).  Replaces: boundary.type / boundary.var and controls fields read by
+   src/solvers/reconIncom.cpp:501-1035 and src/solvers/eqPressure.cpp. */
+semo_status semo_set_physics(semo_ctx* ctx, const semo_physics* phys,
+                             const int32_t* bc_type, const double* bc_value);
+
+/* Cell fields in the caller's cell order (host pointers, n_cells each). */
+semo_status semo_set_fields(semo_ctx* ctx, const double* P, const double* U, const double* V,
+                            const double* W, const double* VF);
+semo_status semo_get_fields(semo_ctx* ctx, double* P, double* U, double* V, double* W);
+
+/* One pressure-correction pass: EOS, face values, gravity source, stencil
+   min/max, five LSQ gradients, face-loop assembly, AMG-Krylov solve, two
+   Gauss-Green sweeps of grad p' and the P/U/V/W update.  Returns SEMO's
+   ||dprim||/||prim|| in *norm.  Replaces: SEMO_Solvers_Builder::calcPressureEq
+   (src/solvers/build.h:150-154, src/solvers/eqPressure.cpp:8-942) together
+   with the setIncomValuesLeftRightFace / calcSourceGravity calls before it
+   (src/solvers/pressureBased.cpp:139-141, :211). */
+semo_status semo_pressure_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
+
+/* Assembly only (steps up to the face loop of calcPressureEq).  After it, the
+   system can be read out or solved. */
+semo_status semo_assemble_pressure(semo_ctx* ctx);
+
+/* The assembled system in RCM order: ptr (n_cells+1), col (nnz), val (nnz),
+   b (n_cells).  In-row order is SEMO's (diagonal first, then faces in face
+   order, src/solvers/solveAMGCL.cpp:206-251).  nnz = n_cells + 2*n_internal. */
+semo_status semo_get_system_rcm(semo_ctx* ctx, int32_t* ptr, int32_t* col, double* val, double* b);
+
+/* Intermediates of the last assembly, in the caller's cell order, for
+   checking: name is one of "grad_P","grad_U","grad_V","grad_W","grad_VF"
+   (3*n_cells, xyz interleaved), "minmax_uvw" (6*n_cells), "rho" (n_cells),
+   "src_grav" (4*n_cells), "face_UnF" (n_faces, face order), "geometry:<name>". */
+semo_status semo_get_array(semo_ctx* ctx, const char* name, double* out, int64_t count);
+
+/* Solve the assembled pressure system; x in the caller's cell order. */
+semo_status semo_solve_pressure(semo_ctx* ctx, double* x, semo_solve_info* info);
+
+/* Solve a caller-supplied scalar system given as SEMO's COO triple (first
+   n entries are the diagonals, as calcPressureEq builds them).  x is in/out
+   (initial guess in, solution out).  Replaces: SEMO_Solvers_Builder::solveAMGCL
+   for B_n = 1 (src/solvers/build.h:225-231, src/solvers/solveAMGCL.cpp:179-1108),
+   with smoothed-aggregation AMG + CG instead of AMGCL's IDR(s). */
+semo_status semo_solve_coo(semo_ctx* ctx, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,
+                           const double* vals, const double* b, double* x, semo_solve_info* info);
+
+/* Optional per-cell source s (caller's order) added to the pressure RHS as
+   b_i += s_i * V_i after assembly; NULL clears it.  No reference counterpart
+   (used by the adjoint check of the pressure solve). */
+semo_status semo_set_source(semo_ctx* ctx, const double* s);
+
+/* Discrete adjoint of the pressure solve + face-flux residual: given
+   dJ/dx (caller's order), returns lambda = A^-T dJ/dx and dJ/ds for a per-cell
+   source s entering as b_i += s_i * V_i.  No reference counterpart (SEMO has
+   no adjoint). */
+semo_status semo_vjp_source(semo_ctx* ctx, const double* dJ_dx, double* lambda, double* dJ_ds,
+                            semo_solve_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,281 @@
+"""GB300 (sm_103a) drop-in for SEMO's per-outer-iteration pressure path.
+
+Python mirror of the reference's interface for this path, over the C-ABI of
+include/semo_gb300.h (libsemo_gb300.so, built in-tree by
+``semo_mesh_gb300.build``):
+
+* ``Context.calc_pressure_eq()``   -- SEMO_Solvers_Builder::calcPressureEq
+  (src/solvers/eqPressure.cpp:8-942), returning SEMO's ||dprim||/||prim||;
+* ``Context.solve_amgcl(...)``     -- SEMO_Solvers_Builder::solveAMGCL for the
+  scalar "pressure" equation (src/solvers/solveAMGCL.cpp:179-1108): SEMO's
+  COO triple in, solution vector out;
+* ``Context.lib_rcm()``            -- SEMO_Utility_Math::lib_RCM
+  (src/math/RCM.cpp:34-218): (cells[i].RCM, cells[i].invRCM).
+
+There is no CPU fallback: without the built library (or without a GB300) the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsemo_gb300.so")
+
+SEMO_OK = 0
+STATUS = {0: "SEMO_OK", 1: "SEMO_ERR_ARGUMENT", 2: "SEMO_ERR_MESH", 3: "SEMO_ERR_CUDA",
+          4: "SEMO_ERR_OUT_OF_MEMORY", 5: "SEMO_ERR_NOT_CONVERGED", 6: "SEMO_ERR_NAN",
+          7: "SEMO_ERR_BREAKDOWN", 8: "SEMO_ERR_STATE", 9: "SEMO_ERR_NO_DEVICE"}
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+
+class SemoError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
+                ("eps_strong", C.c_double), ("coarse_enough", C.c_int), ("max_levels", C.c_int),
+                ("cheb_degree", C.c_int)]
+
+
+class Physics(C.Structure):
+    _fields_ = [("dt", C.c_double), ("rho", C.c_double * 2), ("gravity", C.c_double * 3),
+                ("use_gravity", C.c_int), ("urf_p", C.c_double), ("urf_u", C.c_double),
+                ("p_min", C.c_double), ("p_max", C.c_double), ("u_min", C.c_double), ("u_max", C.c_double),
+                ("v_min", C.c_double), ("v_max", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("levels", C.c_int),
+                ("coarse_size", C.c_int), ("operator_complexity", C.c_double),
+                ("setup_ms", C.c_double), ("solve_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load the C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m semo_mesh_gb300.build` "
+                          "(there is no CPU fallback)")
+    L = C.CDLL(path)
+    vp, i32p, f64p = C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)
+    L.semo_params_default.argtypes = [C.POINTER(Params)]
+    L.semo_physics_default.argtypes = [C.POINTER(Physics)]
+    L.semo_ctx_create.argtypes = [C.POINTER(vp), C.POINTER(Params)]
+    L.semo_ctx_destroy.argtypes = [vp]
+    L.semo_last_error.restype = C.c_char_p
+    L.semo_last_error.argtypes = [vp]
+    L.semo_stream.restype = vp
+    L.semo_stream.argtypes = [vp]
+    L.semo_mesh_upload.argtypes = [vp, C.c_int, f64p, C.c_int, C.c_int, C.c_int, i32p, i32p, i32p, i32p,
+                                   C.c_int, i32p, i32p]
+    L.semo_rcm.argtypes = [vp, i32p, i32p]
+    L.semo_set_physics.argtypes = [vp, C.POINTER(Physics), i32p, f64p]
+    L.semo_set_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p]
+    L.semo_get_fields.argtypes = [vp, f64p, f64p, f64p, f64p]
+    L.semo_pressure_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_assemble_pressure.argtypes = [vp]
+    L.semo_get_system_rcm.argtypes = [vp, i32p, i32p, f64p, f64p]
+    L.semo_get_array.argtypes = [vp, C.c_char_p, f64p, C.c_int64]
+    L.semo_solve_pressure.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_solve_coo.argtypes = [vp, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, f64p, C.POINTER(SolveInfo)]
+    L.semo_set_source.argtypes = [vp, f64p]
+    L.semo_vjp_source.argtypes = [vp, f64p, f64p, f64p, C.POINTER(SolveInfo)]
+    _lib = L
+    return L
+
+
+def _i32(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@dataclass
+class SolveResult:
+    x: np.ndarray
+    info: dict
+
+
+class Context:
+    """One GPU context (semo_ctx) holding a mesh, its fields and the solver."""
+
+    def __init__(self, precision: str = "mixed", tol: float = 1e-8, max_iter: int = 500, device: int = 0,
+                 eps_strong: float = 0.08, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24):
+        self.L = load_library()
+        p = Params()
+        self.L.semo_params_default(C.byref(p))
+        p.device = device
+        p.precision = PREC_MIXED if precision == "mixed" else PREC_FP64
+        p.tol = tol
+        p.max_iter = max_iter
+        p.eps_strong = eps_strong
+        p.coarse_enough = coarse_enough
+        p.cheb_degree = cheb_degree
+        p.max_levels = max_levels
+        h = C.c_void_p()
+        st = self.L.semo_ctx_create(C.byref(h), C.byref(p))
+        if st != SEMO_OK:
+            raise SemoError(st, "semo_ctx_create failed (no GB300 / CUDA device?)")
+        self.h = h
+        self.mesh = None
+        self.n_cells = 0
+
+    def _check(self, st: int, allow=()):
+        if st != SEMO_OK and st not in allow:
+            raise SemoError(st, self.L.semo_last_error(self.h).decode(errors="replace"))
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.semo_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.semo_stream(self.h) or 0)
+
+    # ---- mesh / case -----------------------------------------------------
+    def upload_mesh(self, mesh) -> None:
+        pts, pp = _f64(mesh.points.reshape(-1))
+        keep = [_i32(mesh.face_ptr), _i32(mesh.face_pts), _i32(mesh.owner), _i32(mesh.neighbour),
+                _i32(mesh.patch_start), _i32(mesh.patch_size)]
+        self._check(self.L.semo_mesh_upload(self.h, mesh.n_points, pp, mesh.n_faces, mesh.n_internal, mesh.n_cells,
+                                            keep[0][1], keep[1][1], keep[2][1], keep[3][1],
+                                            len(mesh.patch_names), keep[4][1], keep[5][1]))
+        self.mesh = mesh
+        self.n_cells = mesh.n_cells
+
+    def set_physics(self, case) -> None:
+        ph = Physics()
+        self.L.semo_physics_default(C.byref(ph))
+        ph.dt = case.dt
+        ph.rho[0], ph.rho[1] = case.rho
+        ph.gravity[0], ph.gravity[1], ph.gravity[2] = case.gravity
+        ph.use_gravity = 1 if case.use_gravity else 0
+        ph.urf_p = case.pre_p_urf
+        ph.urf_u = case.pre_u_urf
+        bt, btp = _i32(case.bc_type.reshape(-1))
+        bv, bvp = _f64(case.bc_value.reshape(-1))
+        self._check(self.L.semo_set_physics(self.h, C.byref(ph), btp, bvp))
+
+    def set_fields(self, P, U, V, W, VF) -> None:
+        arrs = [_f64(a) for a in (P, U, V, W, VF)]
+        self._check(self.L.semo_set_fields(self.h, *[a[1] for a in arrs]))
+
+    def set_case(self, case) -> None:
+        if self.mesh is not case.mesh:
+            self.upload_mesh(case.mesh)
+        self.set_physics(case)
+        self.set_fields(case.P, case.U, case.V, case.W, case.VF)
+
+    def fields(self) -> dict:
+        n = self.n_cells
+        out = {k: np.empty(n) for k in ("P", "U", "V", "W")}
+        ptrs = [out[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("P", "U", "V", "W")]
+        self._check(self.L.semo_get_fields(self.h, *ptrs))
+        return out
+
+    def set_source(self, s) -> None:
+        if s is None:
+            self._check(self.L.semo_set_source(self.h, None))
+        else:
+            a, ap = _f64(s)
+            self._check(self.L.semo_set_source(self.h, ap))
+
+    # ---- the reference's entry points -------------------------------------
+    def calc_pressure_eq(self) -> tuple:
+        """calcPressureEq: one pressure-correction pass; returns (norm, info)."""
+        norm = C.c_double()
+        info = SolveInfo()
+        self._check(self.L.semo_pressure_pass(self.h, C.byref(norm), C.byref(info)))
+        return norm.value, info.as_dict()
+
+    def lib_rcm(self) -> tuple:
+        """lib_RCM: (perm, iperm) = (cells[i].RCM, cells[i].invRCM)."""
+        perm = np.empty(self.n_cells, dtype=np.int32)
+        iperm = np.empty(self.n_cells, dtype=np.int32)
+        self._check(self.L.semo_rcm(self.h, perm.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    iperm.ctypes.data_as(C.POINTER(C.c_int32))))
+        return perm, iperm
+
+    def solve_amgcl(self, equation: str, B_n: int, A_rows, A_cols, A_vals, B, resiVar=None) -> SolveResult:
+        """solveAMGCL(equation, mesh, B_n, A_rows, A_cols, A_vals, B, resiVar) for B_n == 1."""
+        if B_n != 1:
+            raise SemoError(1, "only scalar systems (B_n == 1) are supported")
+        if equation != "pressure":
+            raise SemoError(1, f"equation '{equation}' is not on this path (only 'pressure')")
+        n = len(B)
+        x = np.zeros(n) if resiVar is None else np.array(resiVar, dtype=np.float64)
+        r, rp = _i32(A_rows)
+        c, cp = _i32(A_cols)
+        v, vp = _f64(A_vals)
+        b, bp = _f64(B)
+        info = SolveInfo()
+        self._check(self.L.semo_solve_coo(self.h, n, len(r), rp, cp, vp, bp,
+                                          x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+        return SolveResult(x=x, info=info.as_dict())
+
+    # ---- pieces ----------------------------------------------------------
+    def assemble(self) -> None:
+        self._check(self.L.semo_assemble_pressure(self.h))
+
+    def system_rcm(self) -> dict:
+        n = self.n_cells
+        nnz = n + 2 * self.mesh.n_internal
+        ptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz, dtype=np.int32)
+        val = np.empty(nnz)
+        b = np.empty(n)
+        self._check(self.L.semo_get_system_rcm(self.h, ptr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               col.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               val.ctypes.data_as(C.POINTER(C.c_double)),
+                                               b.ctypes.data_as(C.POINTER(C.c_double))))
+        return {"ptr": ptr, "col": col, "val": val, "b": b}
+
+    def solve(self) -> SolveResult:
+        x = np.empty(self.n_cells)
+        info = SolveInfo()
+        self._check(self.L.semo_solve_pressure(self.h, x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+        return SolveResult(x=x, info=info.as_dict())
+
+    def get_array(self, name: str, count: int) -> np.ndarray:
+        out = np.empty(count)
+        self._check(self.L.semo_get_array(self.h, name.encode(), out.ctypes.data_as(C.POINTER(C.c_double)), count))
+        return out
+
+    def vjp_source(self, dJ_dx) -> tuple:
+        """lambda = A^-T dJ/dx and dJ/ds (s entering as b_i += s_i V_i)."""
+        g, gp = _f64(dJ_dx)
+        lam = np.empty(self.n_cells)
+        djds = np.empty(self.n_cells)
+        info = SolveInfo()
+        self._check(self.L.semo_vjp_source(self.h, gp, lam.ctypes.data_as(C.POINTER(C.c_double)),
+                                           djds.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+        return lam, djds, info.as_dict()

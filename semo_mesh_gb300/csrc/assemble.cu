@@ -1,0 +1,517 @@
+// Per-outer-iteration pressure-correction assembly on the GPU.
+//
+// Stages (reference function, file:line):
+//   k_cell_eos        calcIncomCellEOSVF            src/solvers/eos.cpp:10-151
+//   k_bface_values    reconIncomZeroOrder + face EOS src/solvers/reconIncom.cpp:501-1035, :440-496
+//   k_grav_face/cell  calcSourceGravity             src/solvers/source/gravity.cpp:7-75
+//   k_stencil         setCellVarMinMax x4 + calcLeastSquare("cellVertex","1st") x5
+//                                                   src/solvers/cellVarMinMax.cpp:8-23,
+//                                                   src/math/gradient.cpp:761-816, :997-1050, :1136-1159
+//   k_pface           calcPressureEq face loop      src/solvers/eqPressure.cpp:246-564
+//                     + Rhie-Chow helpers           src/solvers/surfaceNormalVelocity.cpp:125-187
+//   k_pbface          calcPressureEq boundary loop  src/solvers/eqPressure.cpp:570-673
+//   k_pcell           diagonal and RHS gather       (the += into A_vals[diag] / B of the two loops)
+//   k_gg_face/cell    Gauss-Green grad p', 2 sweeps src/solvers/eqPressure.cpp:686-809
+//   k_update          P/U/V/W update + norms        src/solvers/eqPressure.cpp:823-883
+//
+// Everything is atomic-free: faces write per-face results, cells gather them
+// through the cell->face list in ascending face order (the order SEMO's face
+// loop accumulates them), so results are deterministic run to run.  Cells are
+// in RCM order, faces in the caller's order; all arrays are SoA planes.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "semo_internal.h"
+
+namespace {
+
+constexpr int kFaceMask = 0x3FFFFFFF;
+inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+// Order-preserving int64 image of a double (for min/max on the integer
+// pipes instead of the FP64 unit); the map is its own inverse.
+__device__ __forceinline__ long long okey(double x) {
+    long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ double ounkey(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
+}
+// std::max(a,b) = (a<b)?b:a ; std::min(a,b) = (b<a)?b:a
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double clamp01(double x) { return smax(0.0, smin(1.0, x)); }
+
+__global__ void k_cell_eos(int nc, double r0, double r1, double* __restrict__ VF, double* __restrict__ rho,
+                           double* __restrict__ irho) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double mf = clamp01(VF[i]);
+    const double v0 = clamp01(mf), v1 = clamp01(1.0 - mf);
+    double r = 0.0;
+    r += v0 * r0;
+    r += v1 * r1;
+    rho[i] = r;
+    irho[i] = 1.0 / r;
+    VF[i] = v0;
+}
+
+// boundary-face values (left == right for every supported condition);
+// planes of nb: 0 p, 1 u, 2 v, 3 w, 4 vf, 5 rho
+__global__ void k_bface_values(int nb, int ni, int nf, const int* __restrict__ own, const int* __restrict__ bpatch,
+                               const int* __restrict__ bct, const double* __restrict__ bcv,
+                               const double* __restrict__ fn, const double* __restrict__ P,
+                               const double* __restrict__ U, const double* __restrict__ V,
+                               const double* __restrict__ W, const double* __restrict__ VF, double r0, double r1,
+                               double* __restrict__ bf) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int f = ni + b, o = own[f], p = bpatch[b];
+    const int tp = bct[3 * p], tu = bct[3 * p + 1], tv = bct[3 * p + 2];
+    bf[b] = (tp == SEMO_BC_FIXED_VALUE) ? bcv[5 * p] : P[o];
+    double u, v, w;
+    if (tu == SEMO_BC_FIXED_VALUE) { u = bcv[5 * p + 1]; v = bcv[5 * p + 2]; w = bcv[5 * p + 3]; }
+    else if (tu == SEMO_BC_NO_SLIP) { u = 0.0; v = 0.0; w = 0.0; }
+    else if (tu == SEMO_BC_SLIP) {
+        const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f];
+        const double un = U[o] * n0 + V[o] * n1 + W[o] * n2;
+        u = U[o] - un * n0; v = V[o] - un * n1; w = W[o] - un * n2;
+    } else { u = U[o]; v = V[o]; w = W[o]; }
+    bf[nb + b] = u; bf[2 * nb + b] = v; bf[3 * nb + b] = w;
+    const double vf = (tv == SEMO_BC_FIXED_VALUE) ? bcv[5 * p + 4] : VF[o];
+    bf[4 * nb + b] = vf;
+    const double a0 = clamp01(vf), a1 = clamp01(1.0 - vf);
+    double r = 0.0;
+    r += a0 * r0;
+    r += a1 * r1;
+    bf[5 * nb + b] = r;
+}
+
+// gravity source, face part: (RhoF*g.PF, RhoF*g.NF, UnF) per face
+__global__ void k_grav_face(int nf, int ni, int nc, int nb, const int* __restrict__ own, const int* __restrict__ nei,
+                            const double* __restrict__ fn, const double* __restrict__ wc,
+                            const double* __restrict__ pf, const double* __restrict__ nfv,
+                            const double* __restrict__ U, const double* __restrict__ V,
+                            const double* __restrict__ W, const double* __restrict__ rho,
+                            const double* __restrict__ bf, double g0, double g1, double g2,
+                            double* __restrict__ out) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int o = own[f];
+    const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f];
+    const double wL = wc[f], wR = 1.0 - wL;
+    double uL, vL, wwL, uR, vR, wwR, rL, rR;
+    if (f < ni) {
+        const int q = nei[f];
+        uL = U[o]; vL = V[o]; wwL = W[o]; uR = U[q]; vR = V[q]; wwR = W[q];
+        rL = rho[o]; rR = rho[q];
+    } else {
+        const int b = f - ni;
+        uL = uR = bf[nb + b]; vL = vR = bf[2 * nb + b]; wwL = wwR = bf[3 * nb + b];
+        rL = rR = bf[5 * nb + b];
+    }
+    const double UnL = uL * n0 + vL * n1 + wwL * n2;
+    const double UnR = uR * n0 + vR * n1 + wwR * n2;
+    const double UnF = wL * UnL + wR * UnR;
+    const double RhoF = 1.0 / (wL / rL + wR / rR);
+    double gL = 0.0, gR = 0.0;
+    gL += g0 * pf[f]; gL += g1 * pf[nf + f]; gL += g2 * pf[2 * nf + f];
+    gR += g0 * nfv[f]; gR += g1 * nfv[nf + f]; gR += g2 * nfv[2 * nf + f];
+    out[f] = RhoF * gL;
+    out[nf + f] = RhoF * gR;
+    out[2 * nf + f] = UnF;
+}
+
+__global__ void k_grav_cell(int nc, int nf, const int* __restrict__ cfp, const int* __restrict__ cfi,
+                            const double* __restrict__ fn, const double* __restrict__ fa,
+                            const double* __restrict__ vol, const double* __restrict__ gf, double* __restrict__ sg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double v = vol[i];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+        const int e = cfi[k], f = e & kFaceMask;
+        const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f], a = fa[f];
+        if (e >> 30) {
+            const double t = gf[nf + f];
+            s0 -= ((t * n0) * a / v); s1 -= ((t * n1) * a / v); s2 -= ((t * n2) * a / v);
+            s3 -= ((t * gf[2 * nf + f]) * a / v);
+        } else {
+            const double t = gf[f];
+            s0 += ((t * n0) * a / v); s1 += ((t * n1) * a / v); s2 += ((t * n2) * a / v);
+            s3 += ((t * gf[2 * nf + f]) * a / v);
+        }
+    }
+    sg[i] = s0; sg[nc + i] = s1; sg[2 * nc + i] = s2; sg[3 * nc + i] = s3;
+}
+
+// One pass over each cell's vertex stencil: LSQ gradients of P,U,V,W,VF and
+// stencil min/max of U,V,W,VF.  Stencil weights w_k*d_k are precomputed.
+__global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb, const int* __restrict__ stp,
+                                                 const int* __restrict__ sti, const double* __restrict__ stw,
+                                                 int64_t stn, const int* __restrict__ cfp,
+                                                 const int* __restrict__ cfi, const double* __restrict__ bfw,
+                                                 const double* __restrict__ minv, const double* __restrict__ P,
+                                                 const double* __restrict__ U, const double* __restrict__ V,
+                                                 const double* __restrict__ W, const double* __restrict__ VF,
+                                                 const double* __restrict__ bf, double* __restrict__ grad,
+                                                 double* __restrict__ mm) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double pi = P[i], ui = U[i], vi = V[i], wi = W[i], fi = VF[i];
+    double g[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    long long kmaxu = okey(ui), kminu = kmaxu, kmaxv = okey(vi), kminv = kmaxv;
+    long long kmaxw = okey(wi), kminw = kmaxw, kmaxf = okey(fi), kminf = kmaxf;
+    const int kb = stp[i], ke = stp[i + 1];
+    for (int k = kb; k < ke; ++k) {
+        const int j = __ldg(sti + k);
+        const double wx = __ldg(stw + k), wy = __ldg(stw + stn + k), wz = __ldg(stw + 2 * stn + k);
+        const double pj = __ldg(P + j), uj = __ldg(U + j), vj = __ldg(V + j), wj = __ldg(W + j), fj = __ldg(VF + j);
+        double d;
+        d = pj - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
+        d = uj - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
+        d = vj - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
+        d = wj - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
+        d = fj - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
+        long long t;
+        t = okey(uj); kmaxu = (kmaxu < t) ? t : kmaxu; kminu = (t < kminu) ? t : kminu;
+        t = okey(vj); kmaxv = (kmaxv < t) ? t : kmaxv; kminv = (t < kminv) ? t : kminv;
+        t = okey(wj); kmaxw = (kmaxw < t) ? t : kmaxw; kminw = (t < kminw) ? t : kminw;
+        t = okey(fj); kmaxf = (kmaxf < t) ? t : kmaxf; kminf = (t < kminf) ? t : kminf;
+    }
+    // boundary faces (face index >= ni) come last in the ascending list
+    {
+        int kfirst = cfp[i + 1];
+        while (kfirst > cfp[i] && (cfi[kfirst - 1] & kFaceMask) >= ni) --kfirst;
+        for (int k = kfirst; k < cfp[i + 1]; ++k) {
+            const int b = (cfi[k] & kFaceMask) - ni;
+            const double wx = bfw[b], wy = bfw[nb + b], wz = bfw[2 * nb + b];
+            double d;
+            d = bf[b] - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
+            d = bf[nb + b] - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
+            d = bf[2 * nb + b] - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
+            d = bf[3 * nb + b] - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
+            d = bf[4 * nb + b] - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
+        }
+    }
+    const double m0 = minv[i], m1 = minv[nc + i], m2 = minv[2 * nc + i];
+    const double m3 = minv[3 * nc + i], m4 = minv[4 * nc + i], m5 = minv[5 * nc + i];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        double t0 = 0.0; t0 += m0 * g[q][0]; t0 += m1 * g[q][1]; t0 += m2 * g[q][2];
+        double t1 = 0.0; t1 += m1 * g[q][0]; t1 += m3 * g[q][1]; t1 += m4 * g[q][2];
+        double t2 = 0.0; t2 += m2 * g[q][0]; t2 += m4 * g[q][1]; t2 += m5 * g[q][2];
+        grad[(3 * q + 0) * (size_t)nc + i] = t0;
+        grad[(3 * q + 1) * (size_t)nc + i] = t1;
+        grad[(3 * q + 2) * (size_t)nc + i] = t2;
+    }
+    mm[i] = ounkey(kmaxu); mm[nc + i] = ounkey(kminu);
+    mm[2 * (size_t)nc + i] = ounkey(kmaxv); mm[3 * (size_t)nc + i] = ounkey(kminv);
+    mm[4 * (size_t)nc + i] = ounkey(kmaxw); mm[5 * (size_t)nc + i] = ounkey(kminw);
+    mm[6 * (size_t)nc + i] = ounkey(kmaxf); mm[7 * (size_t)nc + i] = ounkey(kminf);
+}
+
+struct FaceArgs {
+    int ni, nf, nc;
+    const int *own, *nei, *lr, *rl;
+    const double *fn, *epn, *skew, *alf, *fk;
+    const double *P, *U, *V, *W, *irho, *grad, *mm, *sg;
+    double dt, g0, g1, g2;
+    int use_gravity;
+    double *val, *coef, *flux, *unf;
+};
+
+// Internal faces of calcPressureEq.  The Rhie-Chow terms are evaluated in
+// reduced form: (dt/rho*)*rho* = dt, and the (n - alpha e) and n pieces of
+// the non-orthogonal correction combine to alpha e; agreement with SEMO's
+// operation order is to rounding (a few ulp), not bit-for-bit.
+__global__ void __launch_bounds__(256) k_pface(FaceArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.ni) return;
+    const int nf = a.nf, nc = a.nc, ni = a.ni;
+    const int o = a.own[f], q = a.nei[f];
+    const double n0 = a.fn[f], n1 = a.fn[nf + f], n2 = a.fn[2 * nf + f];
+    const double s0 = a.skew[f], s1 = a.skew[nf + f], s2 = a.skew[2 * nf + f];
+    const double alpha = a.alf[f];
+    const double ae0 = alpha * a.epn[f], ae1 = alpha * a.epn[nf + f], ae2 = alpha * a.epn[2 * nf + f];
+    const double kA = a.fk[f], kP = a.fk[ni + f], area = a.fk[2 * ni + f], wL = a.fk[3 * ni + f];
+    const double wR = 1.0 - wL;
+    const double iRL = __ldg(a.irho + o), iRR = __ldg(a.irho + q);
+    const double* G = a.grad;
+    const size_t N = nc;
+    // skew-corrected, stencil-limited velocities (eqPressure.cpp:416-451)
+    double ul = __ldg(a.U + o) + __ldg(G + 3 * N + o) * s0 + __ldg(G + 4 * N + o) * s1 + __ldg(G + 5 * N + o) * s2;
+    double vl = __ldg(a.V + o) + __ldg(G + 6 * N + o) * s0 + __ldg(G + 7 * N + o) * s1 + __ldg(G + 8 * N + o) * s2;
+    double wl = __ldg(a.W + o) + __ldg(G + 9 * N + o) * s0 + __ldg(G + 10 * N + o) * s1 + __ldg(G + 11 * N + o) * s2;
+    double ur = __ldg(a.U + q) + __ldg(G + 3 * N + q) * s0 + __ldg(G + 4 * N + q) * s1 + __ldg(G + 5 * N + q) * s2;
+    double vr = __ldg(a.V + q) + __ldg(G + 6 * N + q) * s0 + __ldg(G + 7 * N + q) * s1 + __ldg(G + 8 * N + q) * s2;
+    double wr = __ldg(a.W + q) + __ldg(G + 9 * N + q) * s0 + __ldg(G + 10 * N + q) * s1 + __ldg(G + 11 * N + q) * s2;
+    const double* M = a.mm;
+    ul = smax(__ldg(M + N + o), smin(__ldg(M + o), ul));
+    ur = smax(__ldg(M + N + q), smin(__ldg(M + q), ur));
+    vl = smax(__ldg(M + 3 * N + o), smin(__ldg(M + 2 * N + o), vl));
+    vr = smax(__ldg(M + 3 * N + q), smin(__ldg(M + 2 * N + q), vr));
+    wl = smax(__ldg(M + 5 * N + o), smin(__ldg(M + 4 * N + o), wl));
+    wr = smax(__ldg(M + 5 * N + q), smin(__ldg(M + 4 * N + q), wr));
+    const double UnL = ul * n0 + vl * n1 + wl * n2;
+    const double UnR = ur * n0 + vr * n1 + wr * n2;
+    double UnF = wL * UnL + wR * UnR;
+    // pressure Rhie-Chow (surfaceNormalVelocity.cpp:125-155)
+    const double tt = a.dt * (wL * iRL + wR * iRR);
+    UnF -= tt * kP * (__ldg(a.P + q) - __ldg(a.P + o));
+    const double aL = a.dt * wL * iRL, aR = a.dt * wR * iRR;
+    UnF += aL * (__ldg(G + o) * ae0 + __ldg(G + N + o) * ae1 + __ldg(G + 2 * N + o) * ae2);
+    UnF += aR * (__ldg(G + q) * ae0 + __ldg(G + N + q) * ae1 + __ldg(G + 2 * N + q) * ae2);
+    if (a.use_gravity) {
+        // gravity Rhie-Chow (surfaceNormalVelocity.cpp:156-187)
+        UnF += a.dt * alpha * (a.g0 * ae0 + a.g1 * ae1 + a.g2 * ae2);
+        const double t0 = n0 - ae0 - alpha * n0, t1 = n1 - ae1 - alpha * n1, t2 = n2 - ae2 - alpha * n2;
+        const double* S = a.sg;
+        UnF += aL * (__ldg(S + o) * t0 + __ldg(S + N + o) * t1 + __ldg(S + 2 * N + o) * t2);
+        UnF += aR * (__ldg(S + q) * t0 + __ldg(S + N + q) * t1 + __ldg(S + 2 * N + q) * t2);
+    }
+    // off-diagonal coefficient, with SEMO's rho* = 1/(wCR/rhoL + wCR/rhoR) (eqPressure.cpp:396)
+    const double coef = kA * (a.dt * (wR * iRL + wR * iRR));
+    a.val[a.lr[f]] = -coef;
+    a.val[a.rl[f]] = -coef;
+    a.coef[f] = coef;
+    a.flux[f] = UnF * area;
+    a.unf[f] = UnF;
+}
+
+__global__ void k_pbface(int nb, int ni, int nf, int nc, const int* __restrict__ own, const int* __restrict__ bpatch,
+                         const int* __restrict__ bct, const double* __restrict__ fn, const double* __restrict__ fa,
+                         const double* __restrict__ mpn, const double* __restrict__ alf,
+                         const double* __restrict__ epn, const double* __restrict__ P,
+                         const double* __restrict__ grad, const double* __restrict__ bf, double dt,
+                         double* __restrict__ coef, double* __restrict__ flux, double* __restrict__ unf) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int f = ni + b, o = own[f];
+    const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f], area = fa[f];
+    const double u = bf[nb + b], v = bf[2 * nb + b], w = bf[3 * nb + b];
+    const double UnL = u * n0 + v * n1 + w * n2;
+    double UnF = 0.5 * UnL + 0.5 * UnL;
+    const double tmp1 = 1.0 / bf[5 * nb + b] * dt;
+    const bool fixed = bct[3 * bpatch[b]] == SEMO_BC_FIXED_VALUE;
+    const double dPN = 0.5 * mpn[f], alpha = alf[f];
+    double d = 0.0;
+    if (fixed) {
+        UnF -= alpha * tmp1 * (bf[b] - P[o]) / dPN;
+        UnF += alpha * tmp1 * grad[o] * epn[f];
+        UnF += alpha * tmp1 * grad[nc + o] * epn[nf + f];
+        UnF += alpha * tmp1 * grad[2 * (size_t)nc + o] * epn[2 * nf + f];
+        d = 1.0 * (alpha * tmp1 / dPN * area);
+    } else {
+        d = 0.0 * (alpha * tmp1 / dPN * area);
+    }
+    coef[f] = d;
+    flux[f] = UnF * area;
+    unf[f] = UnF;
+}
+
+__global__ void k_pcell(int nc, int ni, const int* __restrict__ cfp, const int* __restrict__ cfi,
+                        const int* __restrict__ dig, const double* __restrict__ coef,
+                        const double* __restrict__ flux, const double* __restrict__ src,
+                        const double* __restrict__ vol, double* __restrict__ val, double* __restrict__ b) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double d = 0.0, s = 0.0;
+    for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+        const int e = cfi[k], f = e & kFaceMask;
+        d += coef[f];
+        if (e >> 30) s += flux[f]; else s -= flux[f];
+    }
+    if (src) s += src[i] * vol[i];
+    val[dig[i]] = d;
+    b[i] = s;
+}
+
+// Gauss-Green sweep, face part: interpolated p' with skewness correction
+__global__ void k_gg_face(int nf, int ni, int nc, int nb, const int* __restrict__ own, const int* __restrict__ nei,
+                          const int* __restrict__ bpatch, const int* __restrict__ bct,
+                          const double* __restrict__ wc, const double* __restrict__ skew,
+                          const double* __restrict__ x, const double* __restrict__ g, double* __restrict__ vF) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int o = own[f];
+    if (f < ni) {
+        const int q = nei[f];
+        const double wL = wc[f], wR = 1.0 - wL;
+        double v = wL * x[o] + wR * x[q];
+        for (int k = 0; k < 3; ++k) {
+            const double s = skew[(size_t)k * nf + f];
+            v += wL * g[(size_t)k * nc + o] * s;
+            v += wR * g[(size_t)k * nc + q] * s;
+        }
+        vF[f] = v;
+    } else {
+        vF[f] = (bct[3 * bpatch[f - ni]] == SEMO_BC_FIXED_VALUE) ? 0.0 : x[o];
+    }
+}
+
+__global__ void k_gg_cell(int nc, int nf, const int* __restrict__ cfp, const int* __restrict__ cfi,
+                          const double* __restrict__ fn, const double* __restrict__ fa,
+                          const double* __restrict__ vol, const double* __restrict__ vF, double* __restrict__ g) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const double v = vol[i];
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+        const int e = cfi[k], f = e & kFaceMask;
+        const double t = vF[f], a = fa[f];
+        const double c0 = t * fn[f] * a / v, c1 = t * fn[nf + f] * a / v, c2 = t * fn[2 * nf + f] * a / v;
+        if (e >> 30) { g0 -= c0; g1 -= c1; g2 -= c2; }
+        else { g0 += c0; g1 += c1; g2 += c2; }
+    }
+    g[i] = g0; g[nc + i] = g1; g[2 * (size_t)nc + i] = g2;
+}
+
+constexpr int kRedBlocks = 608;   // 4 x 152 SMs; fixed so reductions are deterministic
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = 0.0;
+    if (threadIdx.x < 32) {
+        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_update(int nc, double urf_p, double urf_u, double dt,
+                                                        const double* __restrict__ x,
+                                                        const double* __restrict__ g,
+                                                        const double* __restrict__ rho, double* __restrict__ P,
+                                                        double* __restrict__ U, double* __restrict__ V,
+                                                        double* __restrict__ W, double pmin, double pmax,
+                                                        double umin, double umax, double vmin, double vmax,
+                                                        double wmin, double wmax, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double nd = 0.0, np = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        double p = P[i] + urf_p * xi;
+        const double t = dt / rho[i];
+        const double ru = urf_u * t * g[i], rv = urf_u * t * g[nc + i], rw = urf_u * t * g[2 * (size_t)nc + i];
+        double u = U[i] - ru, v = V[i] - rv, w = W[i] - rw;
+        if (p <= pmin) p = pmin;
+        if (p >= pmax) p = pmax;
+        if (u <= umin) u = umin;
+        if (u >= umax) u = umax;
+        if (v <= vmin) v = vmin;
+        if (v >= vmax) v = vmax;
+        if (w <= wmin) w = wmin;
+        if (w >= wmax) w = wmax;
+        P[i] = p; U[i] = u; V[i] = v; W[i] = w;
+        nd += xi * xi + ru * ru + rv * rv + rw * rw;
+        np += p * p + u * u + v * v + w * w;
+    }
+    nd = block_sum(nd, sh);
+    np = block_sum(np, sh);
+    if (threadIdx.x == 0) { part[blockIdx.x] = nd; part[kRedBlocks + blockIdx.x] = np; }
+}
+
+__global__ void k_finish2(const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) { a += part[i]; b += part[kRedBlocks + i]; }
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) { out[0] = a; out[1] = b; }
+}
+
+}  // namespace
+
+namespace semo {
+
+void assemble_face_values(semo_ctx* c) {
+    const int T = 256;
+    cudaStream_t s = c->stream;
+    k_cell_eos<<<blocks(c->nc, T), T, 0, s>>>(c->nc, c->phys.rho[0], c->phys.rho[1], c->VF, c->rho, c->irho);
+    SEMO_CHECK_LAUNCH();
+    if (c->nb > 0) {
+        k_bface_values<<<blocks(c->nb, T), T, 0, s>>>(c->nb, c->ni, c->nf, c->own, c->bpatch, c->bc_type, c->bc_value,
+                                                       c->fn, c->P, c->U, c->V, c->W, c->VF, c->phys.rho[0],
+                                                       c->phys.rho[1], c->bface);
+        SEMO_CHECK_LAUNCH();
+    }
+}
+
+void assemble_pressure(semo_ctx* c) {
+    const int T = 256;
+    cudaStream_t s = c->stream;
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    assemble_face_values(c);
+    if (c->phys.use_gravity) {
+        k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
+                                                 c->W, c->rho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
+                                                 c->phys.gravity[2], c->fscr);
+        SEMO_CHECK_LAUNCH();
+        k_grav_cell<<<blocks(nc, T), T, 0, s>>>(nc, nf, c->cf_ptr, c->cf_idx, c->fn, c->fa, c->vol, c->fscr, c->sg);
+        SEMO_CHECK_LAUNCH();
+    } else {
+        c->sg.zero();
+    }
+    k_stencil<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
+                                               c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
+                                               c->grad, c->mm);
+    SEMO_CHECK_LAUNCH();
+    double* coef = c->fscr.p;
+    double* flux = c->fscr.p + nf;
+    if (ni > 0) {
+        FaceArgs a;
+        a.ni = ni; a.nf = nf; a.nc = nc;
+        a.own = c->own; a.nei = c->nei; a.lr = c->A_lr; a.rl = c->A_rl;
+        a.fn = c->fn; a.epn = c->epn; a.skew = c->skew; a.alf = c->alf; a.fk = c->fk;
+        a.P = c->P; a.U = c->U; a.V = c->V; a.W = c->W; a.irho = c->irho; a.grad = c->grad; a.mm = c->mm; a.sg = c->sg;
+        a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
+        a.use_gravity = c->phys.use_gravity;
+        a.val = c->A_val; a.coef = coef; a.flux = flux; a.unf = c->unf;
+        k_pface<<<blocks(ni, 256), 256, 0, s>>>(a);
+        SEMO_CHECK_LAUNCH();
+    }
+    if (nb > 0) {
+        k_pbface<<<blocks(nb, T), T, 0, s>>>(nb, ni, nf, nc, c->own, c->bpatch, c->bc_type, c->fn, c->fa, c->mpn,
+                                              c->alf, c->epn, c->P, c->grad, c->bface, c->phys.dt, coef, flux, c->unf);
+        SEMO_CHECK_LAUNCH();
+    }
+    k_pcell<<<blocks(nc, T), T, 0, s>>>(nc, ni, c->cf_ptr, c->cf_idx, c->A_dig, coef, flux,
+                                         c->has_src ? c->src.p : nullptr, c->vol, c->A_val, c->b);
+    SEMO_CHECK_LAUNCH();
+}
+
+double pressure_update(semo_ctx* c) {
+    const int T = 256;
+    cudaStream_t s = c->stream;
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    c->gx.zero();
+    double* vF = c->fscr.p;
+    for (int it = 0; it < 2; ++it) {
+        k_gg_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->bpatch, c->bc_type, c->wc, c->skew,
+                                               c->x, c->gx, vF);
+        SEMO_CHECK_LAUNCH();
+        k_gg_cell<<<blocks(nc, T), T, 0, s>>>(nc, nf, c->cf_ptr, c->cf_idx, c->fn, c->fa, c->vol, vF, c->gx);
+        SEMO_CHECK_LAUNCH();
+    }
+    c->red.alloc(2 * kRedBlocks + 8, s);
+    const semo_physics& p = c->phys;
+    k_update<<<kRedBlocks, kRedThreads, 0, s>>>(nc, p.urf_p, p.urf_u, p.dt, c->x, c->gx, c->rho, c->P, c->U, c->V,
+                                                c->W, p.p_min, p.p_max, p.u_min, p.u_max, p.v_min, p.v_max, p.w_min,
+                                                p.w_max, c->red);
+    SEMO_CHECK_LAUNCH();
+    k_finish2<<<1, 256, 0, s>>>(c->red, c->red.p + 2 * kRedBlocks);
+    SEMO_CHECK_LAUNCH();
+    double h[2];
+    SEMO_CUDA(cudaMemcpyAsync(h, c->red.p + 2 * kRedBlocks, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    return std::sqrt(h[0]) / std::sqrt(h[1]);
+}
+
+}  // namespace semo

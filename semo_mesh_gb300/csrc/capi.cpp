@@ -1,0 +1,632 @@
+// C-ABI entry points (include/semo_gb300.h) and host-side mesh preprocessing.
+//
+// Host work is limited to what SEMO also does once per mesh on the host:
+// topology lists, the vertex stencil, RCM and the CSR pattern.  Everything per
+// outer iteration runs on the GPU.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "semo_internal.h"
+
+using semo::Error;
+
+namespace {
+
+template <class F>
+semo_status guarded(semo_ctx* c, F&& f) {
+    if (!c) return SEMO_ERR_ARGUMENT;
+    try {
+        c->err.clear();
+        f();
+        return SEMO_OK;
+    } catch (const Error& e) {
+        c->err = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        c->err = "host allocation failed";
+        return SEMO_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return SEMO_ERR_CUDA;
+    }
+}
+
+void need(bool ok, semo_status s, const std::string& msg) {
+    if (!ok) throw Error(s, msg);
+}
+
+}  // namespace
+
+extern "C" {
+
+void semo_params_default(semo_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->device = 0;
+    p->precision = SEMO_PREC_MIXED;
+    p->tol = 1e-8;
+    p->max_iter = 500;
+    p->eps_strong = 0.08;
+    p->coarse_enough = 64;
+    p->max_levels = 24;
+    p->cheb_degree = 2;
+}
+
+void semo_physics_default(semo_physics* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->dt = 1.0;
+    p->rho[0] = p->rho[1] = 1.0;
+    p->urf_p = 0.3;
+    p->urf_u = 0.3;
+    p->p_min = p->u_min = p->v_min = p->w_min = -1e300;
+    p->p_max = p->u_max = p->v_max = p->w_max = 1e300;
+}
+
+semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
+    if (!out) return SEMO_ERR_ARGUMENT;
+    *out = nullptr;
+    semo_ctx* c = new (std::nothrow) semo_ctx();
+    if (!c) return SEMO_ERR_OUT_OF_MEMORY;
+    if (prm) c->prm = *prm; else semo_params_default(&c->prm);
+    semo_physics_default(&c->phys);
+    semo_status st = guarded(c, [&] {
+        need(c->prm.tol > 0.0 && c->prm.max_iter > 0 && c->prm.coarse_enough > 0 && c->prm.max_levels > 0 &&
+                 c->prm.cheb_degree > 0 && c->prm.cheb_degree <= 16 &&
+                 (c->prm.precision == SEMO_PREC_FP64 || c->prm.precision == SEMO_PREC_MIXED),
+             SEMO_ERR_ARGUMENT, "invalid semo_params");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(SEMO_ERR_NO_DEVICE, "no CUDA device");
+        need(c->prm.device >= 0 && c->prm.device < ndev, SEMO_ERR_ARGUMENT, "device ordinal out of range");
+        c->device = c->prm.device;
+        SEMO_CUDA(cudaSetDevice(c->device));
+        cudaDeviceProp dp;
+        SEMO_CUDA(cudaGetDeviceProperties(&dp, c->device));
+        if (dp.major * 10 + dp.minor != 103)
+            throw Error(SEMO_ERR_NO_DEVICE, "library built for sm_103a, device is sm_" +
+                                                std::to_string(dp.major) + std::to_string(dp.minor));
+        SEMO_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        // keep freed blocks in the stream-ordered pool instead of returning them
+        cudaMemPool_t pool;
+        SEMO_CUDA(cudaDeviceGetDefaultMemPool(&pool, c->device));
+        uint64_t thr = UINT64_MAX;
+        SEMO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        for (auto& e : c->ev) SEMO_CUDA(cudaEventCreate(&e));
+        c->flag.alloc(16, c->stream);
+        c->flag.zero();
+    });
+    if (st != SEMO_OK) {
+        semo_ctx_destroy(c);
+        return st;
+    }
+    *out = c;
+    return SEMO_OK;
+}
+
+semo_status semo_ctx_destroy(semo_ctx* c) {
+    if (!c) return SEMO_ERR_ARGUMENT;
+    if (c->stream) {
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->stream);
+    }
+    c->amg64.clear();
+    c->amg32.clear();
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    cudaStream_t s = c->stream;
+    delete c;  // DBuf destructors enqueue frees on the (still valid) stream
+    if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+    return SEMO_OK;
+}
+
+const char* semo_last_error(const semo_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+void* semo_stream(semo_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, int n_faces, int n_internal,
+                             int n_cells, const int32_t* face_ptr, const int32_t* face_pts, const int32_t* owner,
+                             const int32_t* neighbour, int n_patches, const int32_t* patch_start,
+                             const int32_t* patch_size) {
+    return guarded(c, [&] {
+        need(points && face_ptr && face_pts && owner && (neighbour || n_internal == 0) && patch_start &&
+                 patch_size,
+             SEMO_ERR_ARGUMENT, "null mesh array");
+        need(n_points > 0 && n_cells > 0 && n_faces > 0 && n_internal >= 0 && n_internal <= n_faces &&
+                 n_patches >= 0,
+             SEMO_ERR_ARGUMENT, "bad mesh sizes");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        const int nf = n_faces, ni = n_internal, nc = n_cells;
+        // ---- validation (reference: SEMO_Mesh_Builder::check, build.cpp:8-450) ----
+        need(face_ptr[0] == 0, SEMO_ERR_MESH, "face_ptr[0] != 0");
+        for (int f = 0; f < nf; ++f) {
+            need(face_ptr[f + 1] - face_ptr[f] >= 3, SEMO_ERR_MESH, "face with fewer than 3 points: " + std::to_string(f));
+            need(owner[f] >= 0 && owner[f] < nc, SEMO_ERR_MESH, "owner out of range at face " + std::to_string(f));
+        }
+        for (int k = 0; k < face_ptr[nf]; ++k)
+            need(face_pts[k] >= 0 && face_pts[k] < n_points, SEMO_ERR_MESH, "face point out of range");
+        for (int f = 0; f < ni; ++f) {
+            need(neighbour[f] >= 0 && neighbour[f] < nc, SEMO_ERR_MESH, "neighbour out of range at face " + std::to_string(f));
+            need(neighbour[f] != owner[f], SEMO_ERR_MESH, "face " + std::to_string(f) + " has neighbour == owner");
+        }
+        {
+            int expect = ni;
+            for (int p = 0; p < n_patches; ++p) {
+                need(patch_start[p] == expect && patch_size[p] >= 0, SEMO_ERR_MESH,
+                     "patches must tile the boundary faces contiguously");
+                expect += patch_size[p];
+            }
+            need(expect == nf, SEMO_ERR_MESH, "patches do not cover all boundary faces");
+        }
+        c->np = n_points; c->nf = nf; c->ni = ni; c->nc = nc; c->nb = nf - ni; c->npatch = n_patches;
+        c->patch_start.assign(patch_start, patch_start + n_patches);
+        c->patch_size.assign(patch_size, patch_size + n_patches);
+        c->mesh_ready = c->phys_ready = c->fields_ready = c->assembled = false;
+
+        // ---- cell -> faces, ascending face index (connectCelltoFaces, build.cpp:587-608) ----
+        std::vector<int> cfp(nc + 1, 0), cfi;
+        for (int f = 0; f < nf; ++f) { cfp[owner[f] + 1]++; if (f < ni) cfp[neighbour[f] + 1]++; }
+        for (int i = 0; i < nc; ++i) cfp[i + 1] += cfp[i];
+        cfi.resize(cfp[nc]);
+        {
+            std::vector<int> fill(cfp.begin(), cfp.end() - 1);
+            for (int f = 0; f < nf; ++f) {
+                cfi[fill[owner[f]]++] = f;
+                if (f < ni) cfi[fill[neighbour[f]]++] = f | (1 << 30);  // bit 30 marks the neighbour side
+            }
+        }
+        // ---- cell -> points, first-touch over the cell's faces (connectCelltoPoints, build.cpp:613-690) ----
+        std::vector<int> cpp(nc + 1, 0), cpi;
+        {
+            std::vector<int> cnt(nc, 0);
+#pragma omp parallel for schedule(dynamic, 4096)
+            for (int i = 0; i < nc; ++i) {
+                int buf[256]; int m = 0; bool over = false;
+                for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+                    int f = cfi[k] & 0x3FFFFFFF;
+                    for (int q = face_ptr[f]; q < face_ptr[f + 1]; ++q) {
+                        int p = face_pts[q];
+                        bool seen = false;
+                        for (int t = 0; t < m; ++t) if (buf[t] == p) { seen = true; break; }
+                        if (!seen) { if (m < 256) buf[m++] = p; else over = true; }
+                    }
+                }
+                cnt[i] = over ? -1 : m;
+            }
+            for (int i = 0; i < nc; ++i) need(cnt[i] >= 0, SEMO_ERR_MESH, "cell with more than 256 points");
+            for (int i = 0; i < nc; ++i) cpp[i + 1] = cpp[i] + cnt[i];
+            cpi.resize(cpp[nc]);
+#pragma omp parallel for schedule(dynamic, 4096)
+            for (int i = 0; i < nc; ++i) {
+                int m = cpp[i];
+                for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+                    int f = cfi[k] & 0x3FFFFFFF;
+                    for (int q = face_ptr[f]; q < face_ptr[f + 1]; ++q) {
+                        int p = face_pts[q];
+                        bool seen = false;
+                        for (int t = cpp[i]; t < m; ++t) if (cpi[t] == p) { seen = true; break; }
+                        if (!seen) cpi[m++] = p;
+                    }
+                }
+            }
+        }
+        // ---- point -> cells (ascending cell), vertex stencil (setStencil, geometric.cpp:1781-1845) ----
+        std::vector<int> pcp(n_points + 1, 0), pci;
+        for (int k = 0; k < cpp[nc]; ++k) pcp[cpi[k] + 1]++;
+        for (int p = 0; p < n_points; ++p) pcp[p + 1] += pcp[p];
+        pci.resize(pcp[n_points]);
+        {
+            std::vector<int> fill(pcp.begin(), pcp.end() - 1);
+            for (int i = 0; i < nc; ++i)
+                for (int k = cpp[i]; k < cpp[i + 1]; ++k) pci[fill[cpi[k]]++] = i;
+        }
+        std::vector<int> stp(nc + 1, 0), sti;
+        {
+            std::vector<int> cnt(nc, 0);
+#pragma omp parallel
+            {
+                std::vector<int> mark;
+#pragma omp for schedule(dynamic, 4096)
+                for (int i = 0; i < nc; ++i) {
+                    int m = 0;
+                    int local[1024]; bool over = false;
+                    for (int k = cpp[i]; k < cpp[i + 1]; ++k) {
+                        int p = cpi[k];
+                        for (int q = pcp[p]; q < pcp[p + 1]; ++q) {
+                            int j = pci[q];
+                            if (j == i) continue;
+                            bool seen = false;
+                            for (int t = 0; t < m; ++t) if (local[t] == j) { seen = true; break; }
+                            if (!seen) { if (m < 1024) local[m++] = j; else over = true; }
+                        }
+                    }
+                    cnt[i] = over ? -1 : m;
+                }
+            }
+            for (int i = 0; i < nc; ++i) need(cnt[i] >= 0, SEMO_ERR_MESH, "vertex stencil larger than 1024");
+            for (int i = 0; i < nc; ++i) stp[i + 1] = stp[i] + cnt[i];
+            sti.resize(stp[nc]);
+#pragma omp parallel for schedule(dynamic, 4096)
+            for (int i = 0; i < nc; ++i) {
+                int m = stp[i];
+                for (int k = cpp[i]; k < cpp[i + 1]; ++k) {
+                    int p = cpi[k];
+                    for (int q = pcp[p]; q < pcp[p + 1]; ++q) {
+                        int j = pci[q];
+                        if (j == i) continue;
+                        bool seen = false;
+                        for (int t = stp[i]; t < m; ++t) if (sti[t] == j) { seen = true; break; }
+                        if (!seen) sti[m++] = j;
+                    }
+                }
+            }
+        }
+        // ---- RCM over the internal-face graph, adjacency in cell.faces order (RCM.cpp:83-118) ----
+        {
+            std::vector<int> xadj(nc + 1), adj;
+            adj.reserve(2 * (size_t)ni + 1);
+            xadj[0] = 1;
+            for (int i = 0; i < nc; ++i) {
+                for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
+                    int f = cfi[k] & 0x3FFFFFFF;
+                    if (f >= ni) continue;
+                    adj.push_back((owner[f] == i ? neighbour[f] : owner[f]) + 1);
+                }
+                xadj[i + 1] = (int)adj.size() + 1;
+            }
+            if (adj.empty()) adj.push_back(0);
+            semo::genrcm_perm(nc, xadj, adj, c->perm);
+            c->iperm.assign(nc, 0);
+            for (int r = 0; r < nc; ++r) c->iperm[c->perm[r]] = r;
+        }
+        const std::vector<int>& perm = c->perm;
+        const std::vector<int>& iperm = c->iperm;
+        // ---- renumbered lists ----
+        std::vector<int> own_r(nf), nei_r(std::max(ni, 1));
+        for (int f = 0; f < nf; ++f) own_r[f] = iperm[owner[f]];
+        for (int f = 0; f < ni; ++f) nei_r[f] = iperm[neighbour[f]];
+        std::vector<int> rcfp(nc + 1, 0), rcfi(cfi.size()), rstp(nc + 1, 0), rsti(sti.size());
+        for (int r = 0; r < nc; ++r) {
+            int o = perm[r];
+            rcfp[r + 1] = rcfp[r] + (cfp[o + 1] - cfp[o]);
+            rstp[r + 1] = rstp[r] + (stp[o + 1] - stp[o]);
+        }
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < nc; ++r) {
+            int o = perm[r];
+            std::copy(cfi.begin() + cfp[o], cfi.begin() + cfp[o + 1], rcfi.begin() + rcfp[r]);
+            for (int k = stp[o], d = rstp[r]; k < stp[o + 1]; ++k, ++d) rsti[d] = iperm[sti[k]];
+        }
+        // ---- CSR pattern in RCM order, SEMO in-row order (cellsGlobal, build.cpp:1319-1424) ----
+        c->nnz = (int64_t)nc + 2 * (int64_t)ni;
+        need(c->nnz < INT32_MAX, SEMO_ERR_ARGUMENT, "matrix too large for 32-bit indices");
+        std::vector<int> aptr(nc + 1), acol(c->nnz), adig(nc), alr(std::max(ni, 1)), arl(std::max(ni, 1));
+        for (int r = 0; r < nc; ++r) {
+            int o = perm[r];
+            int row_len = 1;
+            for (int k = cfp[o]; k < cfp[o + 1]; ++k) if ((cfi[k] & 0x3FFFFFFF) < ni) ++row_len;
+            aptr[r + 1] = aptr[r] + row_len;
+        }
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < nc; ++r) {
+            int o = perm[r];
+            int d = aptr[r];
+            acol[d] = r; adig[r] = d; ++d;
+            for (int k = cfp[o]; k < cfp[o + 1]; ++k) {
+                int fe = cfi[k];
+                int f = fe & 0x3FFFFFFF;
+                if (f >= ni) continue;
+                bool nb_side = (fe >> 30) & 1;
+                acol[d] = nb_side ? own_r[f] : nei_r[f];
+                if (nb_side) arl[f] = d; else alr[f] = d;
+                ++d;
+            }
+        }
+        // boundary face -> patch
+        std::vector<int> bp(std::max(c->nb, 1), 0);
+        for (int p = 0; p < n_patches; ++p)
+            for (int f = patch_start[p]; f < patch_start[p] + patch_size[p]; ++f) bp[f - ni] = p;
+
+        // ---- upload ----
+        cudaStream_t s = c->stream;
+        c->own.upload(own_r.data(), nf, s);
+        c->nei.upload(nei_r.data(), std::max(ni, 1), s);
+        c->cf_ptr.upload(rcfp.data(), nc + 1, s);
+        c->cf_idx.upload(rcfi.data(), rcfi.size(), s);
+        c->st_ptr.upload(rstp.data(), nc + 1, s);
+        c->st_idx.upload(rsti.data(), std::max<size_t>(rsti.size(), 1), s);
+        c->st_nnz = (int64_t)rsti.size();
+        c->cf_nnz = (int64_t)rcfi.size();
+        c->bpatch.upload(bp.data(), bp.size(), s);
+        c->A_ptr.upload(aptr.data(), nc + 1, s);
+        c->A_col.upload(acol.data(), acol.size(), s);
+        c->A_dig.upload(adig.data(), nc, s);
+        c->A_lr.upload(alr.data(), alr.size(), s);
+        c->A_rl.upload(arl.data(), arl.size(), s);
+        c->A_val.alloc(c->nnz, s);
+        c->b.alloc(nc, s);
+        semo::DBuf<double> d_pts;
+        semo::DBuf<int> d_fptr, d_fpts;
+        d_pts.upload(points, 3 * (size_t)n_points, s);
+        d_fptr.upload(face_ptr, nf + 1, s);
+        d_fpts.upload(face_pts, face_ptr[nf], s);
+        semo::geometry_build(c, d_pts.p, d_fptr.p, d_fpts.p, own_r);
+        // field storage
+        for (auto* b : {&c->P, &c->U, &c->V, &c->W, &c->VF, &c->rho, &c->irho, &c->x}) b->alloc(nc, s);
+        c->grad.alloc(15 * (size_t)nc, s);
+        c->mm.alloc(8 * (size_t)nc, s);
+        c->sg.alloc(4 * (size_t)nc, s);
+        c->gx.alloc(3 * (size_t)nc, s);
+        c->bface.alloc(10 * (size_t)std::max(c->nb, 1), s);
+        c->fscr.alloc(3 * (size_t)nf, s);
+        c->unf.alloc(nf, s);
+        c->x.zero();
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        c->mesh_ready = true;
+    });
+}
+
+semo_status semo_rcm(semo_ctx* c, int32_t* perm, int32_t* iperm) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        if (perm) std::copy(c->perm.begin(), c->perm.end(), perm);
+        if (iperm) std::copy(c->iperm.begin(), c->iperm.end(), iperm);
+    });
+}
+
+semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_t* bc_type, const double* bc_value) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(phys && (bc_type || c->npatch == 0) && (bc_value || c->npatch == 0), SEMO_ERR_ARGUMENT, "null argument");
+        need(std::isfinite(phys->dt) && phys->dt > 0.0, SEMO_ERR_ARGUMENT, "dt must be positive");
+        need(phys->rho[0] > 0.0 && phys->rho[1] > 0.0, SEMO_ERR_ARGUMENT, "densities must be positive");
+        for (int p = 0; p < c->npatch; ++p) {
+            need(bc_type[3 * p] == SEMO_BC_ZERO_GRADIENT || bc_type[3 * p] == SEMO_BC_FIXED_VALUE, SEMO_ERR_ARGUMENT,
+                 "pressure BC must be zeroGradient or fixedValue");
+            need(bc_type[3 * p + 1] >= 0 && bc_type[3 * p + 1] <= 3, SEMO_ERR_ARGUMENT, "bad velocity BC");
+            need(bc_type[3 * p + 2] == SEMO_BC_ZERO_GRADIENT || bc_type[3 * p + 2] == SEMO_BC_FIXED_VALUE,
+                 SEMO_ERR_ARGUMENT, "volume-fraction BC must be zeroGradient or fixedValue");
+        }
+        c->phys = *phys;
+        c->h_bc_type.assign(bc_type, bc_type + 3 * c->npatch);
+        c->h_bc_value.assign(bc_value, bc_value + 5 * c->npatch);
+        c->bc_type.upload(c->h_bc_type.data(), std::max<size_t>(c->h_bc_type.size(), 1), c->stream);
+        c->bc_value.upload(c->h_bc_value.data(), std::max<size_t>(c->h_bc_value.size(), 1), c->stream);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->phys_ready = true;
+        c->assembled = false;
+    });
+}
+
+static void upload_permuted(semo_ctx* c, const double* h, semo::DBuf<double>& d, std::vector<double>& tmp) {
+    const int n = c->nc;
+    tmp.resize(n);
+    for (int r = 0; r < n; ++r) tmp[r] = h[c->perm[r]];
+    SEMO_CUDA(cudaMemcpyAsync(d.p, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    SEMO_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+static void download_permuted(semo_ctx* c, const double* d, double* h, int planes = 1, bool interleave = false) {
+    const int n = c->nc;
+    std::vector<double> tmp((size_t)n * planes);
+    SEMO_CUDA(cudaMemcpyAsync(tmp.data(), d, sizeof(double) * n * planes, cudaMemcpyDeviceToHost, c->stream));
+    SEMO_CUDA(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < n; ++r)
+        for (int q = 0; q < planes; ++q) {
+            size_t dst = interleave ? (size_t)c->perm[r] * planes + q : (size_t)q * n + c->perm[r];
+            h[dst] = tmp[(size_t)q * n + r];
+        }
+}
+
+semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const double* V, const double* W,
+                            const double* VF) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(P && U && V && W && VF, SEMO_ERR_ARGUMENT, "null field");
+        for (const double* a : {P, U, V, W, VF})
+            for (int i = 0; i < c->nc; ++i) need(std::isfinite(a[i]), SEMO_ERR_NAN, "non-finite input field value");
+        std::vector<double> tmp;
+        upload_permuted(c, P, c->P, tmp);
+        upload_permuted(c, U, c->U, tmp);
+        upload_permuted(c, V, c->V, tmp);
+        upload_permuted(c, W, c->W, tmp);
+        upload_permuted(c, VF, c->VF, tmp);
+        c->fields_ready = true;
+        c->assembled = false;
+    });
+}
+
+semo_status semo_get_fields(semo_ctx* c, double* P, double* U, double* V, double* W) {
+    return guarded(c, [&] {
+        need(c->fields_ready, SEMO_ERR_STATE, "no fields set");
+        if (P) download_permuted(c, c->P, P);
+        if (U) download_permuted(c, c->U, U);
+        if (V) download_permuted(c, c->V, V);
+        if (W) download_permuted(c, c->W, W);
+    });
+}
+
+semo_status semo_assemble_pressure(semo_ctx* c) {
+    return guarded(c, [&] {
+        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+             "mesh, physics and fields must be set before assembly");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::assemble_pressure(c);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->assembled = true;
+    });
+}
+
+semo_status semo_get_system_rcm(semo_ctx* c, int32_t* ptr, int32_t* col, double* val, double* b) {
+    return guarded(c, [&] {
+        need(c->assembled, SEMO_ERR_STATE, "system not assembled");
+        cudaStream_t s = c->stream;
+        if (ptr) SEMO_CUDA(cudaMemcpyAsync(ptr, c->A_ptr.p, sizeof(int) * (c->nc + 1), cudaMemcpyDeviceToHost, s));
+        if (col) SEMO_CUDA(cudaMemcpyAsync(col, c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
+        if (val) SEMO_CUDA(cudaMemcpyAsync(val, c->A_val.p, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, s));
+        if (b) SEMO_CUDA(cudaMemcpyAsync(b, c->b.p, sizeof(double) * c->nc, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t count) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(name && out, SEMO_ERR_ARGUMENT, "null argument");
+        std::string nm(name);
+        const int n = c->nc, nf = c->nf;
+        auto cell_planes = [&](const double* d, int planes, bool inter) {
+            need(count == (int64_t)n * planes, SEMO_ERR_ARGUMENT, "count mismatch for " + nm);
+            download_permuted(c, d, out, planes, inter);
+        };
+        auto face_planes = [&](const double* d, int planes, int64_t len) {
+            need(count == len * planes, SEMO_ERR_ARGUMENT, "count mismatch for " + nm);
+            std::vector<double> tmp((size_t)len * planes);
+            SEMO_CUDA(cudaMemcpyAsync(tmp.data(), d, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaStreamSynchronize(c->stream));
+            for (int64_t f = 0; f < len; ++f)
+                for (int q = 0; q < planes; ++q) out[f * planes + q] = tmp[(size_t)q * len + f];
+        };
+        const char* grads[5] = {"grad_P", "grad_U", "grad_V", "grad_W", "grad_VF"};
+        for (int g = 0; g < 5; ++g)
+            if (nm == grads[g]) { need(c->assembled, SEMO_ERR_STATE, "not assembled"); cell_planes(c->grad.p + (size_t)3 * g * n, 3, true); return; }
+        if (nm == "minmax_uvw") { cell_planes(c->mm.p, 6, true); return; }
+        if (nm == "minmax_vf") { cell_planes(c->mm.p + (size_t)6 * n, 2, true); return; }
+        if (nm == "rho") { cell_planes(c->rho.p, 1, false); return; }
+        if (nm == "src_grav") { cell_planes(c->sg.p, 4, true); return; }
+        if (nm == "grad_x") { cell_planes(c->gx.p, 3, true); return; }
+        if (nm == "face_UnF") { face_planes(c->unf.p, 1, nf); return; }
+        if (nm == "geometry:cell_vol") { cell_planes(c->vol.p, 1, false); return; }
+        if (nm == "geometry:cell_c") { cell_planes(c->cc.p, 3, true); return; }
+        if (nm == "geometry:lsq_minv") { cell_planes(c->minv.p, 6, true); return; }
+        if (nm == "geometry:face_n") { face_planes(c->fn.p, 3, nf); return; }
+        if (nm == "geometry:face_area") { face_planes(c->fa.p, 1, nf); return; }
+        if (nm == "geometry:face_c") { face_planes(c->fc.p, 3, nf); return; }
+        if (nm == "geometry:face_wC") { face_planes(c->wc.p, 1, nf); return; }
+        if (nm == "geometry:face_magPN") { face_planes(c->mpn.p, 1, nf); return; }
+        if (nm == "geometry:face_alphaF") { face_planes(c->alf.p, 1, nf); return; }
+        if (nm == "geometry:face_ePN") { face_planes(c->epn.p, 3, nf); return; }
+        if (nm == "geometry:face_skew") { face_planes(c->skew.p, 3, nf); return; }
+        if (nm == "geometry:face_vecPF") { face_planes(c->pf.p, 3, nf); return; }
+        if (nm == "geometry:face_vecNF") { face_planes(c->nfv.p, 3, nf); return; }
+        throw Error(SEMO_ERR_ARGUMENT, "unknown array " + nm);
+    });
+}
+
+semo_status semo_solve_pressure(semo_ctx* c, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->assembled, SEMO_ERR_STATE, "system not assembled");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo_solve_info inf{};
+        semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
+        if (info) *info = inf;
+        if (x) download_permuted(c, c->x.p, x);
+        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
+semo_status semo_pressure_pass(semo_ctx* c, double* norm, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+             "mesh, physics and fields must be set before a pass");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::assemble_pressure(c);
+        c->assembled = true;
+        semo_solve_info inf{};
+        semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
+        double nrm = semo::pressure_update(c);
+        if (norm) *norm = nrm;
+        if (info) *info = inf;
+        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
+semo_status semo_solve_coo(semo_ctx* c, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,
+                           const double* vals, const double* b, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(n > 0 && nnz >= n && rows && cols && vals && b && x, SEMO_ERR_ARGUMENT, "bad COO system");
+        need(nnz < INT32_MAX, SEMO_ERR_ARGUMENT, "nnz too large");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        // COO -> CSR exactly as solveAMGCL.cpp:206-251 (in-row order = COO order)
+        std::vector<int> ptr(n + 1, 0), col(nnz);
+        std::vector<double> val(nnz);
+        for (int64_t k = 0; k < nnz; ++k) {
+            need(rows[k] >= 0 && rows[k] < n && cols[k] >= 0 && cols[k] < n, SEMO_ERR_ARGUMENT, "COO index out of range");
+            need(std::isfinite(vals[k]), SEMO_ERR_NAN, "non-finite matrix value");
+            ptr[rows[k]]++;
+        }
+        for (int i = 0, s = 0; i < n; ++i) { int t = ptr[i]; ptr[i] = s; s += t; }
+        ptr[n] = (int)nnz;
+        for (int64_t k = 0; k < nnz; ++k) { int d = ptr[rows[k]]++; col[d] = cols[k]; val[d] = vals[k]; }
+        for (int i = 0, last = 0; i <= n; ++i) { int t = ptr[i]; ptr[i] = last; last = t; }
+        for (int i = 0; i < n; ++i) need(std::isfinite(b[i]) && std::isfinite(x[i]), SEMO_ERR_NAN, "non-finite rhs/guess");
+        cudaStream_t s = c->stream;
+        semo::DBuf<int> dp, dc;
+        semo::DBuf<double> dv, db, dx;
+        dp.upload(ptr.data(), n + 1, s);
+        dc.upload(col.data(), nnz, s);
+        dv.upload(val.data(), nnz, s);
+        db.upload(b, n, s);
+        dx.upload(x, n, s);
+        semo_solve_info inf{};
+        semo::solve_system(c, dp.p, dc.p, dv.p, n, nnz, db.p, dx.p, &inf, false);
+        SEMO_CUDA(cudaMemcpyAsync(x, dx.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (info) *info = inf;
+        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
+semo_status semo_set_source(semo_ctx* c, const double* src) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        if (!src) { c->has_src = false; c->assembled = false; return; }
+        for (int i = 0; i < c->nc; ++i) need(std::isfinite(src[i]), SEMO_ERR_NAN, "non-finite source");
+        c->src.alloc(c->nc, c->stream);
+        std::vector<double> tmp;
+        upload_permuted(c, src, c->src, tmp);
+        c->has_src = true;
+        c->assembled = false;
+    });
+}
+
+semo_status semo_vjp_source(semo_ctx* c, const double* dJ_dx, double* lambda, double* dJ_ds, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->assembled, SEMO_ERR_STATE, "no assembled system: run a forward pass first");
+        need(dJ_dx != nullptr, SEMO_ERR_ARGUMENT, "null dJ/dx");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        const int n = c->nc;
+        semo::DBuf<double> g, lam, out;
+        g.alloc(n, c->stream);
+        lam.alloc(n, c->stream);
+        std::vector<double> tmp;
+        upload_permuted(c, dJ_dx, g, tmp);
+        semo_solve_info inf{};
+        semo::solve_transpose_reuse(c, g.p, lam.p, &inf);
+        if (info) *info = inf;
+        if (lambda) download_permuted(c, lam.p, lambda);
+        if (dJ_ds) {
+            std::vector<double> l(n), v(n);
+            download_permuted(c, lam.p, l.data());
+            download_permuted(c, c->vol.p, v.data());
+            for (int i = 0; i < n; ++i) dJ_ds[i] = l[i] * v[i];
+        }
+        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "adjoint solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
+}  // extern "C"

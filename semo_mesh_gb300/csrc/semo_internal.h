@@ -1,0 +1,180 @@
+// Internal declarations shared by the host C-ABI layer and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/semo_gb300.h"
+
+namespace semo {
+
+struct Error : std::runtime_error {
+    semo_status status;
+    Error(semo_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define SEMO_CUDA(call)                                                                      \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            throw ::semo::Error(e_ == cudaErrorMemoryAllocation ? SEMO_ERR_OUT_OF_MEMORY     \
+                                                                : SEMO_ERR_CUDA,             \
+                                std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    } while (0)
+
+#define SEMO_CHECK_LAUNCH() SEMO_CUDA(cudaGetLastError())
+
+// Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void alloc(size_t count, cudaStream_t st) {
+        if (count == n && p) return;
+        release();
+        s = st;
+        n = count;
+        if (count) SEMO_CUDA(cudaMallocAsync((void**)&p, sizeof(T) * count, st));
+    }
+    void zero() { if (n) SEMO_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * n, s)); }
+    void upload(const T* h, size_t count, cudaStream_t st) {
+        alloc(count, st);
+        if (count) SEMO_CUDA(cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, st));
+    }
+    void release() {
+        if (p) { cudaFreeAsync(p, s); p = nullptr; }
+        n = 0;
+    }
+    operator T*() const { return p; }
+};
+
+// Scalar CSR matrix on the device.
+template <class V>
+struct DCsr {
+    int n = 0, m = 0;      // rows, cols
+    int64_t nnz = 0;
+    DBuf<int> ptr, col;
+    DBuf<V> val;
+};
+
+// One level of the smoothed-aggregation hierarchy, value type V.
+template <class V>
+struct AmgLevel {
+    DCsr<V> A, P, R;
+    DBuf<V> dinv;          // 1 / a_ii
+    double lam_max = 0.0;  // Gershgorin bound on rho(D^-1 A)
+    DBuf<V> x, b, r, t;    // work vectors
+    int nagg = 0;
+};
+
+template <class V>
+struct Amg {
+    std::vector<AmgLevel<V>> lev;
+    int coarse_n = 0;
+    DBuf<double> cinv;     // explicit FP64 inverse of the coarsest matrix (row-major)
+    int64_t total_nnz = 0;
+    bool ready = false;
+    void clear() { lev.clear(); cinv.release(); coarse_n = 0; total_nnz = 0; ready = false; }
+};
+
+struct Timer {
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+
+}  // namespace semo
+
+struct semo_ctx {
+    semo_params prm{};
+    semo_physics phys{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // mesh sizes
+    int np = 0, nf = 0, ni = 0, nc = 0, nb = 0, npatch = 0;
+    int64_t nnz = 0, st_nnz = 0, cf_nnz = 0;
+    std::vector<int> perm, iperm;                 // RCM
+    std::vector<int> patch_start, patch_size;
+    std::vector<int> h_bc_type;                   // npatch*3
+    std::vector<double> h_bc_value;               // npatch*5
+
+    // ---- device mesh (cells in RCM numbering, faces in caller order) ----
+    semo::DBuf<int> own, nei;                     // face -> cell (RCM numbering)
+    semo::DBuf<int> cf_ptr, cf_idx;               // cell -> faces, ascending face, bit 30 = neighbour side
+    semo::DBuf<int> st_ptr, st_idx;               // vertex stencil (reference order)
+    semo::DBuf<int> bpatch;                       // boundary face -> patch
+    semo::DBuf<int> bc_type;                      // npatch*3
+    semo::DBuf<double> bc_value;                  // npatch*5
+    // geometry (SoA, 3-vectors stored as 3 planes of length nf or nc)
+    semo::DBuf<double> fn, fa, fc, wc, mpn, alf, epn, skew, pf, nfv;
+    semo::DBuf<double> vol, cc, minv;             // cc: 3 planes; minv: 6 planes
+    semo::DBuf<double> stw;                       // 3 planes of st_nnz: w_k * d_k (LSQ weight vectors)
+    semo::DBuf<double> bfw;                       // 3 planes of nb: boundary-face LSQ weight vectors
+    // derived per-face constants for the hot face kernel
+    semo::DBuf<double> fk;                        // 4 planes of ni: kA = alpha*area/magPN, kP = alpha/magPN, area, wC
+
+    // ---- CSR pattern (RCM order) ----
+    semo::DBuf<int> A_ptr, A_col, A_dig, A_lr, A_rl;
+    semo::DBuf<double> A_val, b;
+
+    // ---- fields (RCM order) ----
+    semo::DBuf<double> P, U, V, W, VF, rho, irho;
+    semo::DBuf<double> grad;                      // 15 planes: P,U,V,W,VF x (x,y,z)
+    semo::DBuf<double> mm;                        // 8 planes: maxU,minU,maxV,minV,maxW,minW,maxVF,minVF
+    semo::DBuf<double> sg;                        // 4 planes gravity source
+    semo::DBuf<double> bface;                     // boundary face values: 10 planes of nb
+    semo::DBuf<double> fscr;                      // face scratch: 3 planes of nf
+    semo::DBuf<double> unf;                       // UnF per face
+    semo::DBuf<double> x, gx;                     // solution and its Gauss-Green gradient (3 planes)
+    semo::DBuf<double> src;                       // optional per-cell source s (b_i += s_i V_i)
+    bool has_src = false;
+    semo::DBuf<double> red;                       // reduction partials
+    semo::DBuf<int> flag;                         // device error flags
+
+    // solver state
+    semo::Amg<double> amg64;
+    semo::Amg<float> amg32;
+    semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
+    semo::DBuf<float> kz32, kr32;
+
+    bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace semo {
+
+// host-side mesh preprocessing (topology.cpp, rcm.cpp)
+void genrcm_perm(int n, const std::vector<int>& xadj, const std::vector<int>& adj, std::vector<int>& perm);
+
+// geometry.cu
+void geometry_build(semo_ctx* c, const double* d_points, const int* d_fptr, const int* d_fpts,
+                    const std::vector<int>& h_own_rcm);
+
+// assemble.cu
+void assemble_pressure(semo_ctx* c);
+double pressure_update(semo_ctx* c);
+void assemble_face_values(semo_ctx* c);
+
+// solve.cu
+void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double* d_val, int n, int64_t nnz,
+                  const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess);
+
+void solve_transpose_reuse(semo_ctx* c, const double* d_g, double* d_lam, semo_solve_info* info);
+
+int sm_count(int device);
+
+}  // namespace semo
