@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark: SEMO's per-outer-iteration pressure-correction pass on one GB300.
+
+Workload: jittered hex box 128^3 (2,097,152 cells, 6,340,608 faces), two-phase
+VOF fields (water drop in air, gravity), seeded synthetic inputs.  One step is
+one full pass: EOS and face values, gravity source, stencil min/max, five LSQ
+gradients, face-loop assembly of the pressure-correction system, smoothed-
+aggregation AMG setup, CG to a 1e-8 FP64 relative residual, two Gauss-Green
+sweeps and the P/U/V/W update -- what calcPressureEq does per outer
+iteration.  Mesh data (several GB) is far larger than the 129 MB L2, so no
+flush is needed between steps.
+
+  value    Mcells/s per pass, inputs resident in HBM, FP32 AMG inside FP64 CG
+  e2e      the same through the public C-ABI with host buffers: fields copied in,
+           the pass, fields copied out, every step (wall clock)
+  fp64     the same pass with an all-FP64 hierarchy and V-cycle
+  adjoint  A^T lambda = dJ/dx on the forward hierarchy, time vs the forward solve
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 128]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcells/s per outer iter to 1e-8 rel. residual: FP32-mixed vs FP64 GPU; adj/fwd"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "dram_traffic.json")
+UNIT = "Mcells/s"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(r[1]) for r in self.rows if len(r) > 2) if v is not None]
+        mx = [v for v in (num(r[2]) for r in self.rows if len(r) > 2) if v is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({nm for r in self.rows for k, nm in enumerate(names)
+                          if len(r) > 5 + k and r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def hbm_peak() -> tuple:
+    if os.path.exists(PEAKS):
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def stencil_bytes(m: dict) -> float:
+    """Algorithmic bytes of one k_stencil launch (every array touched once).
+
+    per cell: P,U,V,W,VF (40) + stencil row pointer (4) + M^-1 (48) read, 15
+    gradient components (120) + 8 min/max (64) written; per stencil entry:
+    cell index (4) + precomputed LSQ weight vector w*d (24); per boundary face:
+    weight vector (24) + 5 face values (40).
+    """
+    return m["cells"] * (40 + 4 + 48 + 120 + 64) + m["stencil_nnz"] * (4 + 24) + m["boundary_faces"] * (24 + 40)
+
+
+def pface_bytes(m: dict) -> float:
+    """Algorithmic bytes of one k_pface launch.
+
+    per internal face: owner/neighbour (8), normal, e_PN, skew (72), alpha (8),
+    4 face constants (32), 2 CSR slots (8) read; 2 off-diagonals (16) and coef,
+    flux, UnF (24) written; per cell, read once: 1/rho, P, U, V, W, 12 gradient
+    components, 6 min/max, 3 gravity sources (216).
+    """
+    return m["internal_faces"] * (8 + 72 + 8 + 32 + 8 + 16 + 24) + m["cells"] * 216
+
+
+KERNEL_OF_STAGE = {"stencil": ("k_stencil", stencil_bytes), "pface": ("k_pface", pface_bytes)}
+
+
+def cpu_baseline(case, passes: int = 1) -> dict:
+    """The oracle (restated reference pass) timed on this host's cores."""
+    from oracle.oracle import Oracle, build
+    build()
+    o = Oracle(case.mesh)
+    t_total = 0.0
+    for _ in range(passes):
+        o.set_case(case)
+        t0 = time.perf_counter()
+        o.assemble()
+        s = o.solve(False, 1e-8)
+        o.update(s["x"])
+        t_total += time.perf_counter() - t0
+    n = case.mesh.n_cells
+    return {"value": round(n * passes / t_total / 1e6, 4), "unit": UNIT, "cores": Oracle.threads(),
+            "kind": "port", "seconds": round(t_total, 2),
+            "sample": f"{passes} full pass(es) of the same {n}-cell workload: serial assembly as in SEMO, "
+                      f"OpenMP SA-AMG + CG solve ({s['iters']} iterations)"}
+
+
+def run_gpu_arm(args, rank, world, local) -> None:
+    import torch
+    import semo_mesh_gb300 as S
+    from semo_mesh_gb300.build import build
+    from semo_mesh_gb300.cases import vof_case
+
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    case = vof_case(args.n)
+    mesh = case.mesh
+    nc = mesh.n_cells
+    inputs = tuple(a.copy() for a in (case.P, case.U, case.V, case.W, case.VF))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def passes(ctx, strm, k):
+        infos = []
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(strm)
+        for _ in range(k):
+            infos.append(ctx.calc_pressure_eq()[1])
+        e1.record(strm)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / k, infos
+
+    ctx = S.Context(precision="mixed", tol=1e-8, device=local)
+    ctx.set_case(case)
+    minfo = ctx.mesh_info()
+    strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
+
+    # ---- mixed precision, inputs resident in HBM (the headline value) ------
+    for _ in range(args.warmup):
+        ctx.calc_pressure_eq()
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    l0 = ctx.kernel_launches()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms_mixed, infos = passes(ctx, strm, args.steps)
+    torch.cuda.synchronize()
+    barrier()
+    launches = ctx.kernel_launches() - l0
+    stages = ctx.stage_times()
+    ctx.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([ms_mixed], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_mixed = float(t.item())
+
+    # ---- end to end through the C-ABI, host buffers ------------------------
+    for _ in range(2):
+        ctx.set_fields(*inputs)
+        ctx.calc_pressure_eq()
+        ctx.fields()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.set_fields(*inputs)
+        ctx.calc_pressure_eq()
+        out = ctx.fields()
+    torch.cuda.synchronize()
+    ms_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+    if not np.isfinite(out["P"]).all():
+        raise RuntimeError("non-finite pressure after the e2e passes")
+
+    # ---- adjoint: A^T lambda = dJ/dx, J = sum of p'^2 over the z=1 cells -----
+    zc = mesh.patch_cells("zmax")
+    ctx.set_fields(*inputs)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ctx.assemble()
+    e0.record(strm)
+    fwd = ctx.solve()
+    e1.record(strm)
+    e1.synchronize()
+    ms_fwd = e0.elapsed_time(e1)
+    g = np.zeros(nc)
+    np.add.at(g, zc, 2.0 * fwd.x[zc])
+    e0.record(strm)
+    _, _, ainfo = ctx.vjp_source(g)
+    e1.record(strm)
+    e1.synchronize()
+    ms_adj = e0.elapsed_time(e1)
+    ctx.close()
+
+    # ---- all-FP64 hierarchy and V-cycle ------------------------------------
+    ctx64 = S.Context(precision="fp64", tol=1e-8, device=local)
+    ctx64.set_case(case)
+    strm64 = torch.cuda.ExternalStream(ctx64.stream, device=torch.device(f"cuda:{local}"))
+    for _ in range(args.warmup):
+        ctx64.calc_pressure_eq()
+    ms_fp64, infos64 = passes(ctx64, strm64, args.steps)
+    ctx64.close()
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline for the dominant single-kernel stage ----------------------
+    peak, peak_src = hbm_peak()
+    single = {k: v for k, v in stages.items() if k in KERNEL_OF_STAGE and v[1] > 0}
+    dom = max(single, key=lambda k: single[k][0])
+    kname, fbytes = KERNEL_OF_STAGE[dom]
+    per_launch_ms = single[dom][0] / single[dom][1]
+    algo = fbytes(minfo)
+    achieved = algo / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    if os.path.exists(TRAFFIC):
+        with open(TRAFFIC) as f:
+            tr = json.load(f)
+        if kname in tr:
+            traffic = tr[kname]["dram_bytes_per_cell"] * nc
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "algorithmic_bytes": algo,
+                "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src}
+
+    cells_all = nc * world
+    value = cells_all / (ms_mixed * 1e-3) / 1e6
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_mixed, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 assembly + f32 AMG in f64 CG",
+        "data": "synthetic (seeded jittered hex mesh and VOF fields)",
+        "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF pressure-correction pass "
+                               f"(assembly + SA-AMG setup + CG to 1e-8 + update)",
+                   "cells": nc, "faces": minfo["faces"], "nnz": minfo["nnz"],
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (mesh + fields several GB), no flush"},
+        "iterations": [i["iterations"] for i in infos][:3], "rel_residual": max(i["rel_residual"] for i in infos),
+        "amg_levels": infos[-1]["levels"], "operator_complexity": round(infos[-1]["operator_complexity"], 3),
+        "fp64": {"value": round(cells_all / (ms_fp64 * 1e-3) / 1e6, 3), "ms_per_step": round(ms_fp64, 3),
+                 "iterations": infos64[-1]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3)},
+        "adjoint": {"ms_adjoint_solve": round(ms_adj, 3), "ms_forward_solve": round(ms_fwd, 3),
+                    "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
+                    "adj_over_fwd_pass": round(ms_adj / ms_mixed, 3), "iterations": ainfo["iterations"]},
+        "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1] > 0},
+        "e2e": {"value": round(cells_all / (ms_e2e * 1e-3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms_e2e, 3),
+                "h2d_bytes_per_step": 5 * 8 * nc, "d2h_bytes_per_step": 4 * 8 * nc},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(case, passes=1)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference_arm(args, rank, world) -> None:
+    """The reference's CPU implementation of the path (oracle port), same workload."""
+    if rank != 0:
+        return
+    from semo_mesh_gb300.cases import vof_case
+    from oracle.oracle import Oracle, build
+    build()
+    case = vof_case(args.n)
+    o = Oracle(case.mesh)
+    times, iters = [], []
+    for k in range(args.warmup + args.steps):
+        o.set_case(case)
+        t0 = time.perf_counter()
+        o.assemble()
+        s = o.solve(False, 1e-8)
+        o.update(s["x"])
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            iters.append(s["iters"])
+    nc = case.mesh.n_cells
+    ms = 1e3 * sum(times) / len(times)
+    value = nc / (ms * 1e-3) / 1e6
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered hex mesh and VOF fields)",
+            "impl": "reference",
+            "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF pressure-correction pass "
+                                   f"(assembly + SA-AMG setup + CG to 1e-8 + update)", "cells": nc},
+            "iterations": iters[:3],
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
+                             "sample": f"each step one full pass over all {nc} cells on the host cores"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="hex cells per edge")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+    else:
+        run_gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -175,6 +175,20 @@ semo_status semo_set_source(semo_ctx* ctx, const double* s);
 semo_status semo_vjp_source(semo_ctx* ctx, const double* dJ_dx, double* lambda, double* dJ_ds,
                             semo_solve_info* info);
 
+/* Measurement hooks (no reference counterpart).  With profiling on, the
+   named stages are bracketed by CUDA events on the context's stream:
+   "face_values","gravity","stencil","pface","pbface","pcell","amg_setup",
+   "pcg","gauss_green","update","vcycle".  semo_stage_time returns the summed
+   device time and number of timed calls since the last semo_reset_stats. */
+void semo_set_profiling(semo_ctx* ctx, int on);
+semo_status semo_stage_time(semo_ctx* ctx, const char* stage, double* total_ms, int64_t* calls);
+semo_status semo_reset_stats(semo_ctx* ctx);
+/* Kernel launches made by this library in this process so far. */
+int64_t semo_kernel_launches(void);
+/* Mesh counts: out[0..6) = cells, faces, internal faces, boundary faces,
+   vertex-stencil entries, matrix nonzeros. */
+semo_status semo_mesh_info(semo_ctx* ctx, int64_t* out6);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,26 @@ int orc_set(orc_ctx* c, const char* name, int type, long long n, const void* src
 /* geometry: src/mesh/geometric.cpp:16-~370 (calcUnitNormals_Area3dPolygon), */
 /* :792-880 (volumes/centroids), :1206-1227 (distCells), :1297-1500 (weights) */
 /* ------------------------------------------------------------------------ */
+/* The reference takes sqrtl of a double (x87: root rounded to a 64-bit
+   significand, then to double).  Restated portably so the checker gives the
+   same bits on hosts whose long double is not x87: IEEE sqrt, corrected when
+   the root lies within 2^-12 ulp of a midpoint (exact residual via fma). */
+static double sqrt_ext_rounded(double x) {
+    double y = sqrt(x);
+    if (!(y > 0.0) || !isfinite(y)) return y;
+    uint64_t yb; memcpy(&yb, &y, 8);
+    if (!(yb & 1)) return y;
+    double t = fma(-y, y, x);
+    uint64_t ub = yb + 1, db = yb - 1;
+    double up, dn; memcpy(&up, &ub, 8); memcpy(&dn, &db, 8);
+    double half = 0.5 * (up - y);
+    double z = t / (2.0 * y);
+    double edge = half - half * (1.0 / 2048.0);
+    if (z > edge) return up;
+    if (z < -edge) return dn;
+    return y;
+}
+
 static void face_polygon(const double* pts, const int* idx, int n, double* nrm, double* area,
                          double* cx, double* cy, double* cz, double* vsn, double* cen) {
     double xa = 0.0, ya = 0.0, za = 0.0;
@@ -121,7 +141,7 @@ static void face_polygon(const double* pts, const int* idx, int n, double* nrm, 
             double Ny = 0.5 * (A2 * B0 - A0 * B2);
             double Nz = 0.5 * (A0 * B1 - A1 * B0);
             un[0] += Nx; un[1] += Ny; un[2] += Nz;
-            double ta = (double)sqrtl((long double)(Nx * Nx + Ny * Ny + Nz * Nz));
+            double ta = sqrt_ext_rounded(Nx * Nx + Ny * Ny + Nz * Nz);
             double rx = (X0 + bx + qx) / 3.0, ry = (Y0 + by + qy) / 3.0, rz = (Z0 + bz + qz) / 3.0;
             xt += rx * ta; yt += ry * ta; zt += rz * ta;
             tot += ta;
@@ -130,7 +150,7 @@ static void face_polygon(const double* pts, const int* idx, int n, double* nrm, 
             cc[1] += 2.0 * Ny * ((Y0 + by) * (Y0 + by) + (by + qy) * (by + qy) + (qy + Y0) * (qy + Y0));
             cc[2] += 2.0 * Nz * ((Z0 + bz) * (Z0 + bz) + (bz + qz) * (bz + qz) + (qz + Z0) * (qz + Z0));
         }
-        double mag = (double)sqrtl((long double)(un[0] * un[0] + un[1] * un[1] + un[2] * un[2]));
+        double mag = sqrt_ext_rounded(un[0] * un[0] + un[1] * un[1] + un[2] * un[2]);
         un[0] /= mag; un[1] /= mag; un[2] /= mag;
         ar = mag;
         xt /= tot; yt /= tot; zt /= tot;

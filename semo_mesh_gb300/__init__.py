@@ -97,6 +97,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_solve_coo.argtypes = [vp, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, f64p, C.POINTER(SolveInfo)]
     L.semo_set_source.argtypes = [vp, f64p]
     L.semo_vjp_source.argtypes = [vp, f64p, f64p, f64p, C.POINTER(SolveInfo)]
+    L.semo_set_profiling.argtypes = [vp, C.c_int]
+    L.semo_stage_time.argtypes = [vp, C.c_char_p, f64p, C.POINTER(C.c_int64)]
+    L.semo_reset_stats.argtypes = [vp]
+    L.semo_kernel_launches.restype = C.c_int64
+    L.semo_mesh_info.argtypes = [vp, C.POINTER(C.c_int64)]
     _lib = L
     return L
 
@@ -269,6 +274,34 @@ class Context:
         out = np.empty(count)
         self._check(self.L.semo_get_array(self.h, name.encode(), out.ctypes.data_as(C.POINTER(C.c_double)), count))
         return out
+
+    # ---- measurement hooks -------------------------------------------------
+    STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
+              "gauss_green", "update", "vcycle")
+
+    def set_profiling(self, on: bool) -> None:
+        self.L.semo_set_profiling(self.h, 1 if on else 0)
+
+    def reset_stats(self) -> None:
+        self._check(self.L.semo_reset_stats(self.h))
+
+    def stage_times(self) -> dict:
+        out = {}
+        for st in self.STAGES:
+            ms = C.c_double()
+            n = C.c_int64()
+            self._check(self.L.semo_stage_time(self.h, st.encode(), C.byref(ms), C.byref(n)))
+            out[st] = (ms.value, n.value)
+        return out
+
+    def kernel_launches(self) -> int:
+        return int(self.L.semo_kernel_launches())
+
+    def mesh_info(self) -> dict:
+        out = (C.c_int64 * 6)()
+        self._check(self.L.semo_mesh_info(self.h, out))
+        keys = ("cells", "faces", "internal_faces", "boundary_faces", "stencil_nnz", "nnz")
+        return {k: int(v) for k, v in zip(keys, out)}
 
     def vjp_source(self, dJ_dx) -> tuple:
         """lambda = A^-T dJ/dx and dJ/ds (s entering as b_i += s_i V_i)."""

@@ -49,9 +49,10 @@ __global__ void k_cell_eos(int nc, double r0, double r1, double* __restrict__ VF
     if (i >= nc) return;
     const double mf = clamp01(VF[i]);
     const double v0 = clamp01(mf), v1 = clamp01(1.0 - mf);
+    // unfused, as the reference rounds it (rho feeds every coefficient)
     double r = 0.0;
-    r += v0 * r0;
-    r += v1 * r1;
+    r = __dadd_rn(r, __dmul_rn(v0, r0));
+    r = __dadd_rn(r, __dmul_rn(v1, r1));
     rho[i] = r;
     irho[i] = 1.0 / r;
     VF[i] = v0;
@@ -83,8 +84,8 @@ __global__ void k_bface_values(int nb, int ni, int nf, const int* __restrict__ o
     bf[4 * nb + b] = vf;
     const double a0 = clamp01(vf), a1 = clamp01(1.0 - vf);
     double r = 0.0;
-    r += a0 * r0;
-    r += a1 * r1;
+    r = __dadd_rn(r, __dmul_rn(a0, r0));
+    r = __dadd_rn(r, __dmul_rn(a1, r1));
     bf[5 * nb + b] = r;
 }
 
@@ -434,6 +435,7 @@ namespace semo {
 void assemble_face_values(semo_ctx* c) {
     const int T = 256;
     cudaStream_t s = c->stream;
+    StageScope sc(c, ST_FACE_VALUES);
     k_cell_eos<<<blocks(c->nc, T), T, 0, s>>>(c->nc, c->phys.rho[0], c->phys.rho[1], c->VF, c->rho, c->irho);
     SEMO_CHECK_LAUNCH();
     if (c->nb > 0) {
@@ -450,6 +452,7 @@ void assemble_pressure(semo_ctx* c) {
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
     assemble_face_values(c);
     if (c->phys.use_gravity) {
+        StageScope sc(c, ST_GRAVITY);
         k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
                                                  c->W, c->rho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
                                                  c->phys.gravity[2], c->fscr);
@@ -459,10 +462,13 @@ void assemble_pressure(semo_ctx* c) {
     } else {
         c->sg.zero();
     }
+    {
+    StageScope sc(c, ST_STENCIL);
     k_stencil<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
                                                c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
                                                c->grad, c->mm);
     SEMO_CHECK_LAUNCH();
+    }
     double* coef = c->fscr.p;
     double* flux = c->fscr.p + nf;
     if (ni > 0) {
@@ -474,14 +480,17 @@ void assemble_pressure(semo_ctx* c) {
         a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
         a.use_gravity = c->phys.use_gravity;
         a.val = c->A_val; a.coef = coef; a.flux = flux; a.unf = c->unf;
+        StageScope sc(c, ST_PFACE);
         k_pface<<<blocks(ni, 256), 256, 0, s>>>(a);
         SEMO_CHECK_LAUNCH();
     }
     if (nb > 0) {
+        StageScope sc(c, ST_PBFACE);
         k_pbface<<<blocks(nb, T), T, 0, s>>>(nb, ni, nf, nc, c->own, c->bpatch, c->bc_type, c->fn, c->fa, c->mpn,
                                               c->alf, c->epn, c->P, c->grad, c->bface, c->phys.dt, coef, flux, c->unf);
         SEMO_CHECK_LAUNCH();
     }
+    StageScope sc(c, ST_PCELL);
     k_pcell<<<blocks(nc, T), T, 0, s>>>(nc, ni, c->cf_ptr, c->cf_idx, c->A_dig, coef, flux,
                                          c->has_src ? c->src.p : nullptr, c->vol, c->A_val, c->b);
     SEMO_CHECK_LAUNCH();
@@ -494,14 +503,16 @@ double pressure_update(semo_ctx* c) {
     c->gx.zero();
     double* vF = c->fscr.p;
     for (int it = 0; it < 2; ++it) {
+        StageScope sg(c, ST_GG);
         k_gg_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->bpatch, c->bc_type, c->wc, c->skew,
                                                c->x, c->gx, vF);
         SEMO_CHECK_LAUNCH();
         k_gg_cell<<<blocks(nc, T), T, 0, s>>>(nc, nf, c->cf_ptr, c->cf_idx, c->fn, c->fa, c->vol, vF, c->gx);
         SEMO_CHECK_LAUNCH();
     }
-    c->red.alloc(2 * kRedBlocks + 8, s);
+    c->red.alloc(4 * kRedBlocks + 32, s);
     const semo_physics& p = c->phys;
+    StageScope su(c, ST_UPDATE);
     k_update<<<kRedBlocks, kRedThreads, 0, s>>>(nc, p.urf_p, p.urf_u, p.dt, c->x, c->gx, c->rho, c->P, c->U, c->V,
                                                 c->W, p.p_min, p.p_max, p.u_min, p.u_max, p.v_min, p.v_max, p.w_min,
                                                 p.w_max, c->red);

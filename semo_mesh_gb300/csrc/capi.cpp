@@ -14,6 +14,10 @@
 
 using semo::Error;
 
+namespace semo {
+long long g_kernel_launches = 0;
+}
+
 namespace {
 
 template <class F>
@@ -116,6 +120,8 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     c->amg64.clear();
     c->amg32.clear();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    semo::resolve_stage_timers(c);
+    for (auto e : c->ev_pool) cudaEventDestroy(e);
     cudaStream_t s = c->stream;
     delete c;  // DBuf destructors enqueue frees on the (still valid) stream
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
@@ -586,6 +592,44 @@ semo_status semo_solve_coo(semo_ctx* c, int n, int64_t nnz, const int32_t* rows,
     });
     if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
     return st != SEMO_OK ? st : conv;
+}
+
+void semo_set_profiling(semo_ctx* c, int on) {
+    if (c) c->profiling = on != 0;
+}
+
+semo_status semo_stage_time(semo_ctx* c, const char* stage, double* total_ms, int64_t* calls) {
+    return guarded(c, [&] {
+        need(stage != nullptr, SEMO_ERR_ARGUMENT, "null stage name");
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        semo::resolve_stage_timers(c);
+        for (int k = 0; k < semo::ST_COUNT; ++k)
+            if (std::string(stage) == semo::kStageNames[k]) {
+                if (total_ms) *total_ms = c->stage_ms[k];
+                if (calls) *calls = c->stage_calls[k];
+                return;
+            }
+        throw Error(SEMO_ERR_ARGUMENT, std::string("unknown stage ") + stage);
+    });
+}
+
+semo_status semo_reset_stats(semo_ctx* c) {
+    return guarded(c, [&] {
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        semo::resolve_stage_timers(c);
+        for (int k = 0; k < semo::ST_COUNT; ++k) { c->stage_ms[k] = 0.0; c->stage_calls[k] = 0; }
+    });
+}
+
+int64_t semo_kernel_launches(void) { return __atomic_load_n(&semo::g_kernel_launches, __ATOMIC_RELAXED); }
+
+semo_status semo_mesh_info(semo_ctx* c, int64_t* out6) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(out6 != nullptr, SEMO_ERR_ARGUMENT, "null output");
+        out6[0] = c->nc; out6[1] = c->nf; out6[2] = c->ni; out6[3] = c->nb;
+        out6[4] = c->st_nnz; out6[5] = c->nnz;
+    });
 }
 
 semo_status semo_set_source(semo_ctx* c, const double* src) {

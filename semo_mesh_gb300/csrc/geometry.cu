@@ -22,6 +22,27 @@ namespace {
 
 constexpr int kFaceMask = 0x3FFFFFFF;
 
+// sqrt as the reference computes it: SEMO calls sqrtl on a double argument
+// (geometric.cpp, calcUnitNormals_Area3dPolygon), i.e. the root rounded to
+// the x87 64-bit significand and then to double.  That double rounding
+// differs from IEEE sqrt only when the root lies within 2^-12 ulp of a
+// midpoint between doubles; the exact residual x - y*y (representable for
+// y = RN(sqrt x)) tells which side and how close.
+__device__ __forceinline__ double sqrt_ext_rounded(double x) {
+    double y = sqrt(x);
+    if (!(y > 0.0) || !isfinite(y)) return y;
+    const long long yb = __double_as_longlong(y);
+    if (!(yb & 1)) return y;                      // ties at 53 bits resolve to y itself
+    const double t = fma(-y, y, x);               // exact residual
+    const double up = __longlong_as_double(yb + 1), dn = __longlong_as_double(yb - 1);
+    const double half = 0.5 * (up - y);
+    const double z = t / (2.0 * y);               // sqrt(x) - y, to ~2^-53 relative
+    const double edge = half - half * (1.0 / 2048.0);
+    if (z > edge) return up;
+    if (z < -edge) return dn;
+    return y;
+}
+
 __global__ void k_face_polygon(int nf, const double* __restrict__ pts, const int* __restrict__ fptr,
                                const int* __restrict__ fpts, double* __restrict__ fn, double* __restrict__ fa,
                                double* __restrict__ fc, double* __restrict__ vsn3, double* __restrict__ cen) {
@@ -54,7 +75,7 @@ __global__ void k_face_polygon(int nf, const double* __restrict__ pts, const int
             const double Ny = 0.5 * (A2 * B0 - A0 * B2);
             const double Nz = 0.5 * (A0 * B1 - A1 * B0);
             u0 += Nx; u1 += Ny; u2 += Nz;
-            const double ta = sqrt(Nx * Nx + Ny * Ny + Nz * Nz);
+            const double ta = sqrt_ext_rounded(Nx * Nx + Ny * Ny + Nz * Nz);
             const double rx = (X0 + bx + qx) / 3.0, ry = (Y0 + by + qy) / 3.0, rz = (Z0 + bz + qz) / 3.0;
             xt += rx * ta; yt += ry * ta; zt += rz * ta;
             tot += ta;
@@ -63,7 +84,7 @@ __global__ void k_face_polygon(int nf, const double* __restrict__ pts, const int
             c1 += 2.0 * Ny * ((Y0 + by) * (Y0 + by) + (by + qy) * (by + qy) + (qy + Y0) * (qy + Y0));
             c2 += 2.0 * Nz * ((Z0 + bz) * (Z0 + bz) + (bz + qz) * (bz + qz) + (qz + Z0) * (qz + Z0));
         }
-        const double mag = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
+        const double mag = sqrt_ext_rounded(u0 * u0 + u1 * u1 + u2 * u2);
         u0 /= mag; u1 /= mag; u2 /= mag;
         area = mag;
         xt /= tot; yt /= tot; zt /= tot;

@@ -26,7 +26,19 @@ struct Error : std::runtime_error {
                                 std::string(#call) + ": " + cudaGetErrorString(e_));         \
     } while (0)
 
-#define SEMO_CHECK_LAUNCH() SEMO_CUDA(cudaGetLastError())
+// Every kernel launch is followed by this check, which also counts launches.
+extern long long g_kernel_launches;
+#define SEMO_CHECK_LAUNCH()                         \
+    do {                                            \
+        __atomic_add_fetch(&::semo::g_kernel_launches, 1, __ATOMIC_RELAXED); \
+        SEMO_CUDA(cudaGetLastError());              \
+    } while (0)
+
+// Named stages timed with CUDA events on the context's stream when profiling is on.
+enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
+             ST_GG, ST_UPDATE, ST_VCYCLE, ST_COUNT };
+static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
+                                                  "amg_setup", "pcg", "gauss_green", "update", "vcycle"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -153,7 +165,57 @@ struct semo_ctx {
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    // profiling: per-stage device time from event pairs, resolved after each call
+    bool profiling = false;
+    double stage_ms[semo::ST_COUNT] = {0};
+    long long stage_calls[semo::ST_COUNT] = {0};
+    std::vector<cudaEvent_t> ev_pool;
+    struct Pending { int stage; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
 };
+
+namespace semo {
+
+inline cudaEvent_t take_event(semo_ctx* c) {
+    if (!c->ev_pool.empty()) { cudaEvent_t e = c->ev_pool.back(); c->ev_pool.pop_back(); return e; }
+    cudaEvent_t e;
+    SEMO_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+// RAII: times the enclosed launches of one stage when profiling is enabled.
+struct StageScope {
+    semo_ctx* c;
+    int stage;
+    cudaEvent_t a = nullptr;
+    StageScope(semo_ctx* ctx, int st) : c(ctx), stage(st) {
+        if (c->profiling) { a = take_event(c); cudaEventRecord(a, c->stream); }
+    }
+    ~StageScope() {
+        if (a) {
+            cudaEvent_t b = take_event(c);
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({stage, a, b});
+        }
+    }
+};
+
+// Accumulate finished stage timings (call after the stream is synchronized).
+inline void resolve_stage_timers(semo_ctx* c) {
+    for (auto& p : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            c->stage_ms[p.stage] += ms;
+            c->stage_calls[p.stage] += 1;
+        }
+        c->ev_pool.push_back(p.a);
+        c->ev_pool.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
+}  // namespace semo
 
 namespace semo {
 

@@ -1023,6 +1023,7 @@ void precondition(semo_ctx* c, Amg<V>& h, const double* r) {
     cudaStream_t s = c->stream;
     AmgLevel<V>& L0 = h.lev[0];
     const int n = L0.A.n;
+    StageScope sc(c, ST_VCYCLE);
     k_convert<double, V><<<blocks(n, 256), 256, 0, s>>>(n, r, L0.b.p);
     SEMO_CHECK_LAUNCH();
     vcycle(s, h, 0, c->prm.cheb_degree);
@@ -1117,20 +1118,26 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
     cudaStream_t s = c->stream;
     c->flag.zero();
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
-    if (c->prm.precision == SEMO_PREC_MIXED) {
-        c->amg64.clear();
-        amg_setup<float>(c, c->amg32, ptr, col, val, n, nnz);
-    } else {
-        c->amg32.clear();
-        amg_setup<double>(c, c->amg64, ptr, col, val, n, nnz);
+    {
+        StageScope sc(c, ST_AMG_SETUP);
+        if (c->prm.precision == SEMO_PREC_MIXED) {
+            c->amg64.clear();
+            amg_setup<float>(c, c->amg32, ptr, col, val, n, nnz);
+        } else {
+            c->amg32.clear();
+            amg_setup<double>(c, c->amg64, ptr, col, val, n, nnz);
+        }
     }
     SEMO_CUDA(cudaEventRecord(c->ev[1], s));
-    if (c->prm.precision == SEMO_PREC_MIXED) {
-        pcg<float>(c, c->amg32, ptr, col, val, n, b, x, zero_guess, info);
-        fill_info(c->amg32, nnz, info);
-    } else {
-        pcg<double>(c, c->amg64, ptr, col, val, n, b, x, zero_guess, info);
-        fill_info(c->amg64, nnz, info);
+    {
+        StageScope sc(c, ST_PCG);
+        if (c->prm.precision == SEMO_PREC_MIXED) {
+            pcg<float>(c, c->amg32, ptr, col, val, n, b, x, zero_guess, info);
+            fill_info(c->amg32, nnz, info);
+        } else {
+            pcg<double>(c, c->amg64, ptr, col, val, n, b, x, zero_guess, info);
+            fill_info(c->amg64, nnz, info);
+        }
     }
     SEMO_CUDA(cudaEventRecord(c->ev[2], s));
     SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
