@@ -122,6 +122,7 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     semo::resolve_stage_timers(c);
     for (auto e : c->ev_pool) cudaEventDestroy(e);
+    if (c->hpin) cudaFreeHost(c->hpin);
     cudaStream_t s = c->stream;
     delete c;  // DBuf destructors enqueue frees on the (still valid) stream
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }

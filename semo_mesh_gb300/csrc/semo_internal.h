@@ -162,6 +162,7 @@ struct semo_ctx {
     semo::Amg<float> amg32;
     semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
     semo::DBuf<float> kz32, kr32;
+    double* hpin = nullptr;                       // pinned host scalars for convergence checks
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -157,19 +157,33 @@ int scan_exclusive(cudaStream_t s, int* d, int n) {
 }
 
 // ------------------------------------------------------------------ SpMV etc.
-// y = A x with VS lanes per row (rows are short: ~7 on the finest level)
+// Sub-warp CSR row dot product: VS lanes per row (rows are short, ~7 entries
+// on the finest level).  Accumulates in the matrix's own type, so the FP32
+// V-cycle runs on the FP32 pipes; every lane takes part in the shuffles,
+// rows past n contribute zero.
+template <class V, class X, int VS>
+__device__ __forceinline__ V row_dot(int row, int n, int lane, const int* __restrict__ ptr,
+                                     const int* __restrict__ col, const V* __restrict__ val,
+                                     const X* __restrict__ x) {
+    V s = V(0);
+    if (row < n) {
+        const int e = ptr[row + 1];
+        for (int k = ptr[row] + lane; k < e; k += VS) s += val[k] * (V)__ldg(x + col[k]);
+    }
+#pragma unroll
+    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
+    return s;
+}
+
+// y = A x
 template <class V, class X, int VS>
 __global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                               const V* __restrict__ val, const X* __restrict__ x,
                                               X* __restrict__ y) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / VS, lane = g % VS;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += (double)val[k] * (double)__ldg(x + col[k]);
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    if (lane == 0) y[row] = (X)s;
+    const V s = row_dot<V, X, VS>(row, n, lane, ptr, col, val, x);
+    if (row < n && lane == 0) y[row] = (X)s;
 }
 
 // q = A p (FP64) and part = p.q
@@ -183,11 +197,7 @@ __global__ void __launch_bounds__(256) k_spmv_dot(int n, const int* __restrict__
     const int lane = threadIdx.x % VS;
     for (int row0 = blockIdx.x * rows_per_block; row0 < n; row0 += gridDim.x * rows_per_block) {
         const int row = row0 + threadIdx.x / VS;
-        double s = 0.0;
-        if (row < n)
-            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += val[k] * __ldg(p + col[k]);
-#pragma unroll
-        for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
+        const double s = row_dot<double, double, VS>(row, n, lane, ptr, col, val, p);
         if (lane == 0 && row < n) { q[row] = s; acc += s * p[row]; }
     }
     acc = block_sum(acc, sh);
@@ -201,65 +211,47 @@ __global__ void __launch_bounds__(256) k_residual(int n, const int* __restrict__
                                                   const V* __restrict__ b, V* __restrict__ r) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / VS, lane = g % VS;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += (double)val[k] * (double)__ldg(x + col[k]);
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    if (lane == 0) r[row] = (V)((double)b[row] - s);
+    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
+    if (row < n && lane == 0) r[row] = b[row] - s;
 }
 
 // Chebyshev first step from x = 0: d = D^-1 b / theta ; x = d
 template <class V>
-__global__ void k_cheb_first(int n, const V* __restrict__ dinv, const V* __restrict__ b, double inv_theta,
+__global__ void k_cheb_first(int n, const V* __restrict__ dinv, const V* __restrict__ b, V inv_theta,
                              V* __restrict__ x, V* __restrict__ d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const V v = (V)((double)dinv[i] * (double)b[i] * inv_theta);
+    const V v = dinv[i] * b[i] * inv_theta;
     d[i] = v;
     x[i] = v;
 }
-// Chebyshev first step from a given x: d = D^-1 (b - A x) / theta ; x += d
+// Chebyshev first step from a given x: d = D^-1 (b - A x) / theta (x += d by k_add:
+// other rows of this launch still read x)
 template <class V, int VS>
 __global__ void __launch_bounds__(256) k_cheb_start(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                                     const V* __restrict__ val, const V* __restrict__ dinv,
-                                                    const V* __restrict__ b, double inv_theta, V* __restrict__ x,
+                                                    const V* __restrict__ b, V inv_theta, const V* __restrict__ x,
                                                     V* __restrict__ d) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / VS, lane = g % VS;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += (double)val[k] * (double)__ldg(x + col[k]);
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    if (lane == 0) {
-        const double dv = (double)dinv[row] * ((double)b[row] - s) * inv_theta;
-        d[row] = (V)dv;
-        // x is read by other rows in this launch: write the update to d only; x += d in k_axpy_inplace
-    }
+    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
+    if (row < n && lane == 0) d[row] = dinv[row] * (b[row] - s) * inv_theta;
 }
 template <class V>
 __global__ void k_add(int n, const V* __restrict__ d, V* __restrict__ x) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] = (V)((double)x[i] + (double)d[i]);
+    if (i < n) x[i] += d[i];
 }
-// Chebyshev recurrence step: z = D^-1 (b - A x); d = c1 d + c2 z  (x updated by k_add afterwards)
+// Chebyshev recurrence step: z = D^-1 (b - A x); d = c1 d + c2 z  (x += d by k_add)
 template <class V, int VS>
 __global__ void __launch_bounds__(256) k_cheb_step(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                                    const V* __restrict__ val, const V* __restrict__ dinv,
-                                                   const V* __restrict__ b, const V* __restrict__ x, double c1,
-                                                   double c2, V* __restrict__ d) {
+                                                   const V* __restrict__ b, const V* __restrict__ x, V c1, V c2,
+                                                   V* __restrict__ d) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / VS, lane = g % VS;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += (double)val[k] * (double)__ldg(x + col[k]);
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    if (lane == 0) {
-        const double z = (double)dinv[row] * ((double)b[row] - s);
-        d[row] = (V)(c1 * (double)d[row] + c2 * z);
-    }
+    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
+    if (row < n && lane == 0) d[row] = c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
 }
 // x += P xc (prolongation and correction)
 template <class V, int VS>
@@ -268,12 +260,8 @@ __global__ void __launch_bounds__(256) k_prolong(int n, const int* __restrict__ 
                                                  V* __restrict__ x) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / VS, lane = g % VS;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int k = ptr[row] + lane; k < ptr[row + 1]; k += VS) s += (double)val[k] * (double)__ldg(xc + col[k]);
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    if (lane == 0) x[row] = (V)((double)x[row] + s);
+    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, xc);
+    if (row < n && lane == 0) x[row] += s;
 }
 
 // coarse solve x = Ainv b (dense FP64 inverse), one block
@@ -294,11 +282,14 @@ __global__ void k_convert(int n, const A* __restrict__ a, B* __restrict__ b) {
 
 // ----------------------------------------------------------- Krylov updates
 // scal[0..] live on the device: 0 rz, 1 zq, 2 pq, 3 rr, 4 alpha_prev, 5 beta, 6 alpha, 7 rz_prev
-__global__ void k_cg_beta(double* scal, int first) {
+// scal[10] counts iterations (0 on the first), so one captured iteration
+// serves every iteration of the loop
+__global__ void k_cg_beta(double* scal) {
     if (threadIdx.x != 0) return;
     // Polak-Ribiere: beta = z.(r_k - r_{k-1}) / (z_{k-1}.r_{k-1}) = -alpha_{k-1} z.q_{k-1} / rz_prev
-    scal[5] = first ? 0.0 : (-scal[4] * scal[1] / scal[7]);
+    scal[5] = (scal[10] == 0.0) ? 0.0 : (-scal[4] * scal[1] / scal[7]);
     scal[7] = scal[0];
+    scal[10] += 1.0;
 }
 __global__ void k_p_update(int n, const double* __restrict__ z, double* __restrict__ p, const double* scal) {
     const double beta = scal[5];
@@ -528,30 +519,23 @@ __global__ void k_transpose_fill(int n, const int* __restrict__ ptr, const int* 
         tval[d] = val[k];
     }
 }
+// Sort each row by column into a second buffer, one warp per row: an entry's
+// place is the number of smaller columns in its row (columns are unique).
 template <class V>
-__global__ void k_sort_rows(int n, const int* __restrict__ ptr, int* __restrict__ col, V* __restrict__ val) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int rb = ptr[i], re = ptr[i + 1];
-    for (int s = rb + 1; s < re; ++s) {
-        const int cv = col[s];
-        const V vv = val[s];
-        int t = s - 1;
-        while (t >= rb && col[t] > cv) { col[t + 1] = col[t]; val[t + 1] = val[t]; --t; }
-        col[t + 1] = cv;
-        val[t + 1] = vv;
+__global__ void k_sort_rows(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                            const V* __restrict__ val, int* __restrict__ ocol, V* __restrict__ oval) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int rb = ptr[warp], re = ptr[warp + 1];
+    for (int e = rb + lane; e < re; e += 32) {
+        const int ce = col[e];
+        int rank = 0;
+        for (int u = rb; u < re; ++u) rank += (__ldg(col + u) < ce);
+        ocol[rb + rank] = ce;
+        oval[rb + rank] = val[e];
     }
 }
 
-// upper bound of products per row of A*B
-__global__ void k_prod_bound(int n, const int* __restrict__ aptr, const int* __restrict__ acol,
-                             const int* __restrict__ bptr, int* __restrict__ bound) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int s = 0;
-    for (int k = aptr[i]; k < aptr[i + 1]; ++k) s += bptr[acol[k] + 1] - bptr[acol[k]];
-    bound[i] = s;
-}
 __global__ void k_max_int(int n, const int* __restrict__ a, int* __restrict__ out) {
     __shared__ int sh[32];
     int m = 0;
@@ -567,10 +551,12 @@ __global__ void k_max_int(int n, const int* __restrict__ a, int* __restrict__ ou
 }
 
 // Row-wise SpGEMM C = A * B, one warp per row, open-addressing hash table in
-// shared memory.  Pass 0 counts distinct columns; pass 1 fills.  Products are
-// consumed in a fixed order (A entries in row order, B entries in chunks of
-// 32); lanes that hit the same column are combined in lane order by the
-// lowest lane, so every sum has a fixed association.  Output rows are sorted.
+// shared memory.  Pass 0 counts distinct columns (flagging rows that fill
+// more than 3/4 of the table); pass 1 fills.  Products are consumed in a fixed
+// order (A entries in row order, B entries in chunks of 32); lanes that hit
+// the same column are combined in lane order by the lowest lane, so every sum
+// has a fixed association.  Occupied slots are compacted and ranked by
+// column, so output rows are sorted.
 constexpr int kGemmWarps = 4;
 template <class V, int HT>
 __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __restrict__ aptr,
@@ -582,20 +568,24 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                                                             int* __restrict__ overflow) {
     extern __shared__ unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int* keys = reinterpret_cast<int*>(smem) + wid * HT;
-    double* vals = reinterpret_cast<double*>(smem + sizeof(int) * HT * kGemmWarps) + wid * HT;
+    // per warp: keys[HT] int, ckeys[HT] int, vals[HT] double, cvals[HT] double
+    int* keys = reinterpret_cast<int*>(smem) + wid * 2 * HT;
+    int* ckeys = keys + HT;
+    double* vals = reinterpret_cast<double*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
+    double* cvals = vals + HT;
     for (int row = blockIdx.x * kGemmWarps + wid; row < n; row += gridDim.x * kGemmWarps) {
         for (int t = lane; t < HT; t += 32) { keys[t] = -1; vals[t] = 0.0; }
         __syncwarp();
         int distinct = 0;
-        for (int ka = aptr[row]; ka < aptr[row + 1]; ++ka) {
+        bool full = false;
+        for (int ka = aptr[row]; ka < aptr[row + 1] && !full; ++ka) {
             const int a = acol[ka];
             const double av = (double)aval[ka];
             const int bb = bptr[a], be = bptr[a + 1];
             for (int q0 = bb; q0 < be; q0 += 32) {
                 const int q = q0 + lane;
                 const bool act = q < be;
-                int c = act ? bcol[q] : -1;
+                const int c = act ? bcol[q] : -1;
                 int slot = -1;
                 bool fresh = false;
                 if (act) {
@@ -607,40 +597,45 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                         h = (h + 1) & (HT - 1);
                     }
                 }
-                const unsigned freshmask = __ballot_sync(0xffffffffu, fresh);
-                distinct += __popc(freshmask);
-                if (pass == 1) {
-                    const double pv = act ? av * (double)bval[q] : 0.0;
-                    const unsigned grp = __match_any_sync(0xffffffffu, slot);
-                    const int leader = __ffs(grp) - 1;
-                    double s = 0.0;
-                    unsigned m = grp;
-                    while (m) {            // sum the group in lane order
-                        const int l = __ffs(m) - 1;
-                        s += __shfl_sync(grp, pv, l);
-                        m &= m - 1;
-                    }
-                    if (act && lane == leader) vals[slot] += s;
-                }
+                distinct += __popc(__ballot_sync(0xffffffffu, fresh));
+                const bool lost = __any_sync(0xffffffffu, act && slot < 0);
+                // the lanes of one chunk hold distinct columns of one B row, so
+                // no two lanes share a slot; chunks are applied in order
+                if (pass == 1 && !lost && act) vals[slot] += av * (double)bval[q];
                 __syncwarp();
+                if (lost || distinct > (HT * 3) / 4) { full = true; break; }
             }
         }
-        if (distinct > (HT * 3) / 4 && lane == 0) atomicExch(overflow, 1);
+        if (full) {
+            if (lane == 0) atomicExch(overflow, 1);
+            if (pass == 0 && lane == 0) cnt[row] = 0;
+            __syncwarp();
+            continue;
+        }
         if (pass == 0) {
             if (lane == 0) cnt[row] = distinct;
         } else {
-            // rank occupied slots by column and write the sorted row
-            const int base = cptr[row];
-            for (int t = lane; t < HT; t += 32) {
-                const int c = keys[t];
-                if (c < 0) continue;
-                int rank = 0;
-                for (int u = 0; u < HT; ++u) {
-                    const int cu = keys[u];
-                    rank += (cu >= 0 && cu < c);
+            // compact occupied slots (slot order), then rank by column
+            int base_c = 0;
+            for (int t0 = 0; t0 < HT; t0 += 32) {
+                const int t = t0 + lane;
+                const bool occ = keys[t] >= 0;
+                const unsigned bal = __ballot_sync(0xffffffffu, occ);
+                if (occ) {
+                    const int pos = base_c + __popc(bal & ((1u << lane) - 1u));
+                    ckeys[pos] = keys[t];
+                    cvals[pos] = vals[t];
                 }
-                ccol[base + rank] = c;
-                cval[base + rank] = (V)vals[t];
+                base_c += __popc(bal);
+            }
+            __syncwarp();
+            const int out = cptr[row];
+            for (int e = lane; e < base_c; e += 32) {
+                const int ce = ckeys[e];
+                int rank = 0;
+                for (int u = 0; u < base_c; ++u) rank += (ckeys[u] < ce);
+                ccol[out + rank] = ce;
+                cval[out + rank] = (V)cvals[e];
             }
         }
         __syncwarp();
@@ -727,63 +722,70 @@ void spmv(cudaStream_t s, const DCsr<V>& A, const V* x, V* y) {
 
 // C = A * B (rows of A, cols of B = m)
 template <class V>
+void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C, int* cnt,
+                 int* overflow) {
+    const int n = A.n;
+    const size_t shm = (size_t)kGemmWarps * ht * 2 * (sizeof(int) + sizeof(double));
+    const int grid = std::max(1, std::min(blocks(n, kGemmWarps), 152 * 32));
+#define SEMO_GEMM_CASE(H)                                                                                        \
+    case H:                                                                                                      \
+        if (shm > 48 * 1024)                                                                                     \
+            SEMO_CUDA(cudaFuncSetAttribute(k_spgemm<V, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm)); \
+        k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, pass, cnt,  \
+                                                           C.ptr, C.col.p, C.val.p, overflow);                   \
+        break;
+    switch (ht) {
+        SEMO_GEMM_CASE(64)
+        SEMO_GEMM_CASE(128)
+        SEMO_GEMM_CASE(256)
+        SEMO_GEMM_CASE(512)
+        SEMO_GEMM_CASE(1024)
+        default:
+        SEMO_GEMM_CASE(2048)
+    }
+#undef SEMO_GEMM_CASE
+    SEMO_CHECK_LAUNCH();
+}
+
+template <class V>
 void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C) {
     const int n = A.n;
     C.n = n;
     C.m = B.m;
     C.ptr.alloc(n + 1, s);
-    DBuf<int> bound, mx;
-    bound.alloc(std::max(n, 1), s);
+    DBuf<int> flags;
+    flags.alloc(2, s);
+    // pass 0 with a growing table until no row overflows; counts land in C.ptr
+    int ht = 256, of = 0;
+    for (;;) {
+        flags.zero();
+        SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
+        spgemm_pass(s, ht, 0, A, B, C, C.ptr.p, flags.p);
+        SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (!of) break;
+        if (ht >= 2048) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
+        ht <<= 1;
+    }
+    // pass 1 with the smallest table that holds the densest row at <= 3/4 load
+    DBuf<int> mx;
     mx.alloc(1, s);
     mx.zero();
-    k_prod_bound<<<blocks(n, 256), 256, 0, s>>>(n, A.ptr, A.col, B.ptr, bound);
+    k_max_int<<<std::min(blocks(n, 256), 1024), 256, 0, s>>>(n, C.ptr, mx);
     SEMO_CHECK_LAUNCH();
-    k_max_int<<<std::min(blocks(n, 256), 1024), 256, 0, s>>>(n, bound, mx);
-    SEMO_CHECK_LAUNCH();
-    int maxprod = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&maxprod, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    const int need_slots = std::min(2 * std::max(maxprod, 1), 2 * std::max(B.m, 1));
-    int ht = 64;
-    while (ht < need_slots && ht < 4096) ht <<= 1;
-    DBuf<int> overflow;
-    overflow.alloc(1, s);
-    overflow.zero();
-    auto run = [&](int pass) {
-        const size_t shm = (size_t)kGemmWarps * ht * (sizeof(int) + sizeof(double));
-        const int grid = std::max(1, std::min(blocks(n, kGemmWarps), 152 * 16));
-#define SEMO_GEMM_CASE(H)                                                                                    \
-    case H:                                                                                                  \
-        if (shm > 48 * 1024)                                                                                 \
-            SEMO_CUDA(cudaFuncSetAttribute(k_spgemm<V, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm)); \
-        k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, pass, C.ptr, \
-                                                           C.ptr, C.col.p, C.val.p, overflow);               \
-        break;
-        switch (ht) {
-            SEMO_GEMM_CASE(64)
-            SEMO_GEMM_CASE(128)
-            SEMO_GEMM_CASE(256)
-            SEMO_GEMM_CASE(512)
-            SEMO_GEMM_CASE(1024)
-            SEMO_GEMM_CASE(2048)
-            default:
-            SEMO_GEMM_CASE(4096)
-        }
-#undef SEMO_GEMM_CASE
-        SEMO_CHECK_LAUNCH();
-    };
-    // pass 0: counts land in C.ptr[0..n)
-    SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
-    run(0);
-    const int nnz = scan_exclusive(s, C.ptr.p, n + 1);
+    int maxd = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&maxd, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    const int nnz = scan_exclusive(s, C.ptr.p, n + 1);   // syncs
+    int ht1 = 64;
+    while (ht1 * 3 / 4 < maxd + 32 && ht1 < ht) ht1 <<= 1;
     C.nnz = nnz;
     C.col.alloc(std::max(nnz, 1), s);
     C.val.alloc(std::max(nnz, 1), s);
-    run(1);
-    int of = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&of, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    flags.zero();
+    spgemm_pass(s, ht1, 1, A, B, C, nullptr, flags.p);
+    SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
-    if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM hash table overflow (row too dense)");
+    if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM numeric pass overflowed its table");
     (void)c;
 }
 
@@ -794,6 +796,10 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
     T.nnz = A.nnz;
     T.ptr.alloc(T.n + 1, s);
     T.ptr.zero();
+    DBuf<int> tcol;
+    DBuf<V> tval;
+    tcol.alloc(std::max<int64_t>(A.nnz, 1), s);
+    tval.alloc(std::max<int64_t>(A.nnz, 1), s);
     T.col.alloc(std::max<int64_t>(A.nnz, 1), s);
     T.val.alloc(std::max<int64_t>(A.nnz, 1), s);
     if (A.nnz) {
@@ -804,9 +810,9 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
     DBuf<int> fill;
     fill.alloc(T.n + 1, s);
     SEMO_CUDA(cudaMemcpyAsync(fill.p, T.ptr.p, sizeof(int) * (T.n + 1), cudaMemcpyDeviceToDevice, s));
-    k_transpose_fill<V><<<blocks(A.n, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, fill, T.col, T.val);
+    k_transpose_fill<V><<<blocks(A.n, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, fill, tcol, tval);
     SEMO_CHECK_LAUNCH();
-    k_sort_rows<V><<<blocks(T.n, 128), 128, 0, s>>>(T.n, T.ptr, T.col, T.val);
+    k_sort_rows<V><<<blocks((int64_t)T.n * 32, 256), 256, 0, s>>>(T.n, T.ptr, tcol, tval, T.col, T.val);
     SEMO_CHECK_LAUNCH();
 }
 
@@ -947,14 +953,14 @@ void chebyshev(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_start) {
     V* x = L.x.p;
     V* d = L.t.p;
     if (zero_start) {
-        k_cheb_first<V><<<blocks(n, 256), 256, 0, s>>>(n, L.dinv, L.b, 1.0 / theta, x, d);
+        k_cheb_first<V><<<blocks(n, 256), 256, 0, s>>>(n, L.dinv, L.b, (V)(1.0 / theta), x, d);
         SEMO_CHECK_LAUNCH();
     } else {
         switch (vs) {
-            case 4: k_cheb_start<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, 1.0 / theta, x, d); break;
-            case 8: k_cheb_start<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, 1.0 / theta, x, d); break;
-            case 16: k_cheb_start<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, 1.0 / theta, x, d); break;
-            default: k_cheb_start<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, 1.0 / theta, x, d); break;
+            case 4: k_cheb_start<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
+            case 8: k_cheb_start<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
+            case 16: k_cheb_start<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
+            default: k_cheb_start<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
         }
         SEMO_CHECK_LAUNCH();
         k_add<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
@@ -964,10 +970,10 @@ void chebyshev(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_start) {
         const double rho_new = 1.0 / (2.0 * sigma - rho);
         const double c1 = rho_new * rho, c2 = 2.0 * rho_new / delta;
         switch (vs) {
-            case 4: k_cheb_step<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, c1, c2, d); break;
-            case 8: k_cheb_step<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, c1, c2, d); break;
-            case 16: k_cheb_step<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, c1, c2, d); break;
-            default: k_cheb_step<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, c1, c2, d); break;
+            case 4: k_cheb_step<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
+            case 8: k_cheb_step<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
+            case 16: k_cheb_step<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
+            default: k_cheb_step<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
         }
         SEMO_CHECK_LAUNCH();
         k_add<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
@@ -1023,11 +1029,49 @@ void precondition(semo_ctx* c, Amg<V>& h, const double* r) {
     cudaStream_t s = c->stream;
     AmgLevel<V>& L0 = h.lev[0];
     const int n = L0.A.n;
-    StageScope sc(c, ST_VCYCLE);
     k_convert<double, V><<<blocks(n, 256), 256, 0, s>>>(n, r, L0.b.p);
     SEMO_CHECK_LAUNCH();
     vcycle(s, h, 0, c->prm.cheb_degree);
 }
+
+// One flexible-CG iteration, every scalar kept on the device.
+template <class V>
+void cg_iteration(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n, double* x,
+                  const Red& R) {
+    cudaStream_t s = c->stream;
+    double* r = c->kr.p;
+    double* p = c->kp.p;
+    double* q = c->kq.p;
+    AmgLevel<V>& L0 = h.lev[0];
+    precondition(c, h, r);
+    k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L0.x.p, r, q, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_finish<<<1, 256, 0, s>>>(R.part, 2, R.scal + 0);
+    SEMO_CHECK_LAUNCH();
+    k_cg_beta<<<1, 32, 0, s>>>(R.scal);
+    SEMO_CHECK_LAUNCH();
+    k_p_update_t<V><<<blocks(n, 256), 256, 0, s>>>(n, L0.x.p, p, R.scal);
+    SEMO_CHECK_LAUNCH();
+    k_spmv_dot<8><<<kRedBlocks, 256, 0, s>>>(n, ptr, col, val, p, q, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 2);
+    SEMO_CHECK_LAUNCH();
+    k_cg_alpha<<<1, 32, 0, s>>>(R.scal);
+    SEMO_CHECK_LAUNCH();
+    k_xr_update<<<kRedBlocks, kRedThreads, 0, s>>>(n, x, r, p, q, R.scal, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 3);
+    SEMO_CHECK_LAUNCH();
+}
+
+struct GraphGuard {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    ~GraphGuard() {
+        if (e) cudaGraphExecDestroy(e);
+        if (g) cudaGraphDestroy(g);
+    }
+};
 
 template <class V>
 void pcg(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n, const double* b,
@@ -1035,10 +1079,9 @@ void pcg(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* v
     cudaStream_t s = c->stream;
     Red R = red_area(c);
     c->kr.alloc(n, s); c->kp.alloc(n, s); c->kq.alloc(n, s);
+    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
+    double* h2 = c->hpin;
     double* r = c->kr.p;
-    double* p = c->kp.p;
-    double* q = c->kq.p;
-    double h2[4];
     // r = b - A x
     if (zero_guess) {
         SEMO_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
@@ -1047,8 +1090,9 @@ void pcg(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* v
         k_residual<double, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, ptr, col, val, x, b, r);
         SEMO_CHECK_LAUNCH();
     }
-    SEMO_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, s));
-    SEMO_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, s));
+    SEMO_CUDA(cudaMemsetAsync(c->kq.p, 0, sizeof(double) * n, s));
+    SEMO_CUDA(cudaMemsetAsync(c->kp.p, 0, sizeof(double) * n, s));
+    SEMO_CUDA(cudaMemsetAsync(R.scal, 0, sizeof(double) * 16, s));
     k_dot<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(n, b, b, R.part);
     SEMO_CHECK_LAUNCH();
     k_dot<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part + kRedBlocks);
@@ -1062,28 +1106,31 @@ void pcg(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* v
     if (!std::isfinite(bn) || !std::isfinite(rn)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
     const double bnorm = (bn > 0.0) ? bn : 1.0;
     int it = 0;
-    const int vsA = 8;
-    AmgLevel<V>& L0 = h.lev[0];
+    // The iteration body is captured once per hierarchy and replayed: the
+    // coarse levels are launch-latency bound, the graph removes the per-kernel
+    // host overhead.  Convergence is read back after every iteration.
+    GraphGuard gg;
+    size_t graph_nodes = 0;
+    if (rn > c->prm.tol * bnorm && c->prm.max_iter > 0) {
+        // launches recorded during capture do not run; replays are counted below
+        const long long launches_before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        SEMO_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+            cg_iteration(c, h, ptr, col, val, n, x, R);
+        } catch (...) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(s, &junk);
+            if (junk) cudaGraphDestroy(junk);
+            throw;
+        }
+        SEMO_CUDA(cudaStreamEndCapture(s, &gg.g));
+        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
+        SEMO_CUDA(cudaGraphGetNodes(gg.g, nullptr, &graph_nodes));
+        __atomic_store_n(&g_kernel_launches, launches_before, __ATOMIC_RELAXED);
+    }
     while (it < c->prm.max_iter && rn > c->prm.tol * bnorm) {
-        precondition(c, h, r);
-        k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L0.x.p, r, q, R.part);
-        SEMO_CHECK_LAUNCH();
-        k_finish<<<1, 256, 0, s>>>(R.part, 2, R.scal + 0);
-        SEMO_CHECK_LAUNCH();
-        k_cg_beta<<<1, 32, 0, s>>>(R.scal, it == 0 ? 1 : 0);
-        SEMO_CHECK_LAUNCH();
-        k_p_update_t<V><<<blocks(n, 256), 256, 0, s>>>(n, L0.x.p, p, R.scal);
-        SEMO_CHECK_LAUNCH();
-        k_spmv_dot<vsA><<<kRedBlocks, 256, 0, s>>>(n, ptr, col, val, p, q, R.part);
-        SEMO_CHECK_LAUNCH();
-        k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 2);
-        SEMO_CHECK_LAUNCH();
-        k_cg_alpha<<<1, 32, 0, s>>>(R.scal);
-        SEMO_CHECK_LAUNCH();
-        k_xr_update<<<kRedBlocks, kRedThreads, 0, s>>>(n, x, r, p, q, R.scal, R.part);
-        SEMO_CHECK_LAUNCH();
-        k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 3);
-        SEMO_CHECK_LAUNCH();
+        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
+        __atomic_add_fetch(&g_kernel_launches, (long long)graph_nodes, __ATOMIC_RELAXED);
         SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
         ++it;
