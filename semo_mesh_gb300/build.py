@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("geometry.cu", ["--fmad=false"]),
     ("assemble.cu", []),
-    ("solve.cu", []),
+    ("amg_setup.cu", []),
+    ("cycle.cu", []),
     ("capi.cpp", []),
     ("rcm.cpp", []),
 ]

@@ -1,8 +1,8 @@
-// AMG-preconditioned Krylov solve on the GPU.
+// Smoothed-aggregation AMG setup on the GPU (the hierarchy; cycle.cu applies it).
 //
-// Replaces SEMO's solveAMGCL (src/solvers/solveAMGCL.cpp:179-1108), which
-// builds AMGCL's smoothed-aggregation hierarchy and runs an OpenMP Krylov
-// solver.  The coarsening keeps AMGCL's smoothed-aggregation semantics
+// Replaces the setup half of SEMO's solveAMGCL (src/solvers/solveAMGCL.cpp:
+// 974-976), which builds AMGCL's smoothed-aggregation hierarchy on the CPU
+// every call.  The coarsening keeps AMGCL's smoothed-aggregation semantics
 // (lib/amgcl/coarsening/smoothed_aggregation.hpp:130-215,
 // lib/amgcl/coarsening/plain_aggregates.hpp:120-140):
 //   strong(i,j)  <=>  j != i  and  eps^2 * a_ii * a_jj < a_ij^2,  eps = 0.08 halved per level
@@ -156,177 +156,10 @@ int scan_exclusive(cudaStream_t s, int* d, int n) {
     return total;
 }
 
-// ------------------------------------------------------------------ SpMV etc.
-// Sub-warp CSR row dot product: VS lanes per row (rows are short, ~7 entries
-// on the finest level).  Accumulates in the matrix's own type, so the FP32
-// V-cycle runs on the FP32 pipes; every lane takes part in the shuffles,
-// rows past n contribute zero.
-template <class V, class X, int VS>
-__device__ __forceinline__ V row_dot(int row, int n, int lane, const int* __restrict__ ptr,
-                                     const int* __restrict__ col, const V* __restrict__ val,
-                                     const X* __restrict__ x) {
-    V s = V(0);
-    if (row < n) {
-        const int e = ptr[row + 1];
-        for (int k = ptr[row] + lane; k < e; k += VS) s += val[k] * (V)__ldg(x + col[k]);
-    }
-#pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
-    return s;
-}
-
-// y = A x
-template <class V, class X, int VS>
-__global__ void __launch_bounds__(256) k_spmv(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                              const V* __restrict__ val, const X* __restrict__ x,
-                                              X* __restrict__ y) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = g / VS, lane = g % VS;
-    const V s = row_dot<V, X, VS>(row, n, lane, ptr, col, val, x);
-    if (row < n && lane == 0) y[row] = (X)s;
-}
-
-// q = A p (FP64) and part = p.q
-template <int VS>
-__global__ void __launch_bounds__(256) k_spmv_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                  const double* __restrict__ val, const double* __restrict__ p,
-                                                  double* __restrict__ q, double* __restrict__ part) {
-    __shared__ double sh[32];
-    double acc = 0.0;
-    const int rows_per_block = blockDim.x / VS;
-    const int lane = threadIdx.x % VS;
-    for (int row0 = blockIdx.x * rows_per_block; row0 < n; row0 += gridDim.x * rows_per_block) {
-        const int row = row0 + threadIdx.x / VS;
-        const double s = row_dot<double, double, VS>(row, n, lane, ptr, col, val, p);
-        if (lane == 0 && row < n) { q[row] = s; acc += s * p[row]; }
-    }
-    acc = block_sum(acc, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = acc;
-}
-
-// r = b - A x
-template <class V, int VS>
-__global__ void __launch_bounds__(256) k_residual(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                  const V* __restrict__ val, const V* __restrict__ x,
-                                                  const V* __restrict__ b, V* __restrict__ r) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = g / VS, lane = g % VS;
-    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
-    if (row < n && lane == 0) r[row] = b[row] - s;
-}
-
-// Chebyshev first step from x = 0: d = D^-1 b / theta ; x = d
-template <class V>
-__global__ void k_cheb_first(int n, const V* __restrict__ dinv, const V* __restrict__ b, V inv_theta,
-                             V* __restrict__ x, V* __restrict__ d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const V v = dinv[i] * b[i] * inv_theta;
-    d[i] = v;
-    x[i] = v;
-}
-// Chebyshev first step from a given x: d = D^-1 (b - A x) / theta (x += d by k_add:
-// other rows of this launch still read x)
-template <class V, int VS>
-__global__ void __launch_bounds__(256) k_cheb_start(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                    const V* __restrict__ val, const V* __restrict__ dinv,
-                                                    const V* __restrict__ b, V inv_theta, const V* __restrict__ x,
-                                                    V* __restrict__ d) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = g / VS, lane = g % VS;
-    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
-    if (row < n && lane == 0) d[row] = dinv[row] * (b[row] - s) * inv_theta;
-}
-template <class V>
-__global__ void k_add(int n, const V* __restrict__ d, V* __restrict__ x) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += d[i];
-}
-// Chebyshev recurrence step: z = D^-1 (b - A x); d = c1 d + c2 z  (x += d by k_add)
-template <class V, int VS>
-__global__ void __launch_bounds__(256) k_cheb_step(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                   const V* __restrict__ val, const V* __restrict__ dinv,
-                                                   const V* __restrict__ b, const V* __restrict__ x, V c1, V c2,
-                                                   V* __restrict__ d) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = g / VS, lane = g % VS;
-    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, x);
-    if (row < n && lane == 0) d[row] = c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
-}
-// x += P xc (prolongation and correction)
-template <class V, int VS>
-__global__ void __launch_bounds__(256) k_prolong(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                 const V* __restrict__ val, const V* __restrict__ xc,
-                                                 V* __restrict__ x) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = g / VS, lane = g % VS;
-    const V s = row_dot<V, V, VS>(row, n, lane, ptr, col, val, xc);
-    if (row < n && lane == 0) x[row] += s;
-}
-
-// coarse solve x = Ainv b (dense FP64 inverse), one block
-template <class V>
-__global__ void k_coarse_solve(int n, const double* __restrict__ inv, const V* __restrict__ b, V* __restrict__ x) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double s = 0.0;
-        for (int k = 0; k < n; ++k) s += inv[(size_t)i * n + k] * (double)b[k];
-        x[i] = (V)s;
-    }
-}
-
 template <class A, class B>
 __global__ void k_convert(int n, const A* __restrict__ a, B* __restrict__ b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (B)a[i];
-}
-
-// ----------------------------------------------------------- Krylov updates
-// scal[0..] live on the device: 0 rz, 1 zq, 2 pq, 3 rr, 4 alpha_prev, 5 beta, 6 alpha, 7 rz_prev
-// scal[10] counts iterations (0 on the first), so one captured iteration
-// serves every iteration of the loop
-__global__ void k_cg_beta(double* scal) {
-    if (threadIdx.x != 0) return;
-    // Polak-Ribiere: beta = z.(r_k - r_{k-1}) / (z_{k-1}.r_{k-1}) = -alpha_{k-1} z.q_{k-1} / rz_prev
-    scal[5] = (scal[10] == 0.0) ? 0.0 : (-scal[4] * scal[1] / scal[7]);
-    scal[7] = scal[0];
-    scal[10] += 1.0;
-}
-__global__ void k_p_update(int n, const double* __restrict__ z, double* __restrict__ p, const double* scal) {
-    const double beta = scal[5];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = z[i] + beta * p[i];
-}
-template <class Z>
-__global__ void k_p_update_t(int n, const Z* __restrict__ z, double* __restrict__ p, const double* scal) {
-    const double beta = scal[5];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = (double)z[i] + beta * p[i];
-}
-__global__ void k_cg_alpha(double* scal) {
-    if (threadIdx.x != 0) return;
-    scal[6] = scal[7] / scal[2];
-    scal[4] = scal[6];
-}
-__global__ void __launch_bounds__(kRedThreads) k_xr_update(int n, double* __restrict__ x, double* __restrict__ r,
-                                                           const double* __restrict__ p,
-                                                           const double* __restrict__ q, const double* scal,
-                                                           double* __restrict__ part) {
-    __shared__ double sh[32];
-    const double alpha = scal[6];
-    double s = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += alpha * p[i];
-        const double ri = r[i] - alpha * q[i];
-        r[i] = ri;
-        s += ri * ri;
-    }
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-template <class R>
-__global__ void k_copy_residual(int n, const double* __restrict__ r, R* __restrict__ rr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rr[i] = (R)r[i];
 }
 
 // --------------------------------------------------------------- AMG setup
@@ -574,7 +407,21 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
     double* vals = reinterpret_cast<double*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
     double* cvals = vals + HT;
     for (int row = blockIdx.x * kGemmWarps + wid; row < n; row += gridDim.x * kGemmWarps) {
-        for (int t = lane; t < HT; t += 32) { keys[t] = -1; vals[t] = 0.0; }
+        // table size for this row (power of two, 32..HT): from the product
+        // count in the counting pass, from the known column count when filling
+        int need;
+        if (pass == 0) {
+            int prod = 0;
+            for (int ka = aptr[row] + lane; ka < aptr[row + 1]; ka += 32) prod += bptr[acol[ka] + 1] - bptr[acol[ka]];
+            for (int o = 16; o > 0; o >>= 1) prod += __shfl_xor_sync(0xffffffffu, prod, o);
+            need = 2 * prod;
+        } else {
+            need = (4 * (cptr[row + 1] - cptr[row])) / 3 + 2;
+        }
+        int ht = 32;
+        while (ht < need && ht < HT) ht <<= 1;
+        const int hmask = ht - 1;
+        for (int t = lane; t < ht; t += 32) { keys[t] = -1; vals[t] = 0.0; }
         __syncwarp();
         int distinct = 0;
         bool full = false;
@@ -589,12 +436,12 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 int slot = -1;
                 bool fresh = false;
                 if (act) {
-                    uint32_t h = hash_u32((uint32_t)c) & (HT - 1);
-                    for (int probe = 0; probe < HT; ++probe) {
+                    uint32_t h = hash_u32((uint32_t)c) & hmask;
+                    for (int probe = 0; probe < ht; ++probe) {
                         const int prev = atomicCAS(keys + h, -1, c);
                         if (prev == -1) { slot = (int)h; fresh = true; break; }
                         if (prev == c) { slot = (int)h; break; }
-                        h = (h + 1) & (HT - 1);
+                        h = (h + 1) & hmask;
                     }
                 }
                 distinct += __popc(__ballot_sync(0xffffffffu, fresh));
@@ -603,7 +450,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 // no two lanes share a slot; chunks are applied in order
                 if (pass == 1 && !lost && act) vals[slot] += av * (double)bval[q];
                 __syncwarp();
-                if (lost || distinct > (HT * 3) / 4) { full = true; break; }
+                if (lost || distinct > (ht * 3) / 4) { full = true; break; }
             }
         }
         if (full) {
@@ -617,7 +464,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
         } else {
             // compact occupied slots (slot order), then rank by column
             int base_c = 0;
-            for (int t0 = 0; t0 < HT; t0 += 32) {
+            for (int t0 = 0; t0 < ht; t0 += 32) {
                 const int t = t0 + lane;
                 const bool occ = keys[t] >= 0;
                 const unsigned bal = __ballot_sync(0xffffffffu, occ);
@@ -694,33 +541,12 @@ __global__ void k_gauss_jordan(int n, double* __restrict__ a, double* __restrict
 }
 
 // ------------------------------------------------------------- host helpers
-double finish_dot(semo_ctx* c, double* part, int count, double* out_host) {
-    cudaStream_t s = c->stream;
-    k_finish<<<1, 256, 0, s>>>(part, count, part + 4 * kRedBlocks);
-    SEMO_CHECK_LAUNCH();
-    SEMO_CUDA(cudaMemcpyAsync(out_host, part + 4 * kRedBlocks, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    return out_host[0];
-}
-
 template <class V>
 int pick_vs(const DCsr<V>& A) {
     const double avg = A.n ? (double)A.nnz / A.n : 1.0;
     return avg <= 6 ? 4 : (avg <= 12 ? 8 : (avg <= 24 ? 16 : 32));
 }
 
-template <class V>
-void spmv(cudaStream_t s, const DCsr<V>& A, const V* x, V* y) {
-    switch (pick_vs(A)) {
-        case 4: k_spmv<V, V, 4><<<blocks((int64_t)A.n * 4, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y); break;
-        case 8: k_spmv<V, V, 8><<<blocks((int64_t)A.n * 8, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y); break;
-        case 16: k_spmv<V, V, 16><<<blocks((int64_t)A.n * 16, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y); break;
-        default: k_spmv<V, V, 32><<<blocks((int64_t)A.n * 32, 256), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y); break;
-    }
-    SEMO_CHECK_LAUNCH();
-}
-
-// C = A * B (rows of A, cols of B = m)
 template <class V>
 void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C, int* cnt,
                  int* overflow) {
@@ -941,280 +767,16 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     h.ready = true;
 }
 
-// ------------------------------------------------------------------ V-cycle
-template <class V>
-void chebyshev(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_start) {
-    const int n = L.A.n;
-    const double hi = L.lam_max, lo = hi / 30.0;
-    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
-    const double sigma = theta / delta;
-    double rho = 1.0 / sigma;
-    const int vs = pick_vs(L.A);
-    V* x = L.x.p;
-    V* d = L.t.p;
-    if (zero_start) {
-        k_cheb_first<V><<<blocks(n, 256), 256, 0, s>>>(n, L.dinv, L.b, (V)(1.0 / theta), x, d);
-        SEMO_CHECK_LAUNCH();
-    } else {
-        switch (vs) {
-            case 4: k_cheb_start<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
-            case 8: k_cheb_start<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
-            case 16: k_cheb_start<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
-            default: k_cheb_start<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, (V)(1.0 / theta), x, d); break;
-        }
-        SEMO_CHECK_LAUNCH();
-        k_add<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
-        SEMO_CHECK_LAUNCH();
-    }
-    for (int k = 1; k < degree; ++k) {
-        const double rho_new = 1.0 / (2.0 * sigma - rho);
-        const double c1 = rho_new * rho, c2 = 2.0 * rho_new / delta;
-        switch (vs) {
-            case 4: k_cheb_step<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
-            case 8: k_cheb_step<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
-            case 16: k_cheb_step<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
-            default: k_cheb_step<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.dinv, L.b, x, (V)c1, (V)c2, d); break;
-        }
-        SEMO_CHECK_LAUNCH();
-        k_add<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
-        SEMO_CHECK_LAUNCH();
-        rho = rho_new;
-    }
-}
-
-template <class V>
-void vcycle(cudaStream_t s, Amg<V>& h, int l, int degree) {
-    AmgLevel<V>& L = h.lev[l];
-    const int n = L.A.n;
-    if (l == (int)h.lev.size() - 1) {
-        k_coarse_solve<V><<<1, 256, 0, s>>>(h.coarse_n, h.cinv, L.b, L.x);
-        SEMO_CHECK_LAUNCH();
-        return;
-    }
-    chebyshev(s, L, degree, true);
-    const int vs = pick_vs(L.A);
-    switch (vs) {
-        case 4: k_residual<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.x, L.b, L.r); break;
-        case 8: k_residual<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.x, L.b, L.r); break;
-        case 16: k_residual<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.x, L.b, L.r); break;
-        default: k_residual<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.x, L.b, L.r); break;
-    }
-    SEMO_CHECK_LAUNCH();
-    AmgLevel<V>& C = h.lev[l + 1];
-    spmv(s, L.R, L.r.p, C.b.p);
-    vcycle(s, h, l + 1, degree);
-    const int pvs = pick_vs(L.P);
-    switch (pvs) {
-        case 4: k_prolong<V, 4><<<blocks((int64_t)n * 4, 256), 256, 0, s>>>(n, L.P.ptr, L.P.col, L.P.val, C.x, L.x); break;
-        case 8: k_prolong<V, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, L.P.ptr, L.P.col, L.P.val, C.x, L.x); break;
-        case 16: k_prolong<V, 16><<<blocks((int64_t)n * 16, 256), 256, 0, s>>>(n, L.P.ptr, L.P.col, L.P.val, C.x, L.x); break;
-        default: k_prolong<V, 32><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, L.P.ptr, L.P.col, L.P.val, C.x, L.x); break;
-    }
-    SEMO_CHECK_LAUNCH();
-    chebyshev(s, L, degree, false);
-}
-
-// scalars on the device, inside c->red: [0,4R) partials, [4R, 4R+16) scalars
-struct Red {
-    double* part;
-    double* scal;
-};
-Red red_area(semo_ctx* c) {
-    c->red.alloc(4 * kRedBlocks + 32, c->stream);
-    return Red{c->red.p, c->red.p + 4 * kRedBlocks + 8};
-}
-
-template <class V>
-void precondition(semo_ctx* c, Amg<V>& h, const double* r) {
-    cudaStream_t s = c->stream;
-    AmgLevel<V>& L0 = h.lev[0];
-    const int n = L0.A.n;
-    k_convert<double, V><<<blocks(n, 256), 256, 0, s>>>(n, r, L0.b.p);
-    SEMO_CHECK_LAUNCH();
-    vcycle(s, h, 0, c->prm.cheb_degree);
-}
-
-// One flexible-CG iteration, every scalar kept on the device.
-template <class V>
-void cg_iteration(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n, double* x,
-                  const Red& R) {
-    cudaStream_t s = c->stream;
-    double* r = c->kr.p;
-    double* p = c->kp.p;
-    double* q = c->kq.p;
-    AmgLevel<V>& L0 = h.lev[0];
-    precondition(c, h, r);
-    k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L0.x.p, r, q, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_finish<<<1, 256, 0, s>>>(R.part, 2, R.scal + 0);
-    SEMO_CHECK_LAUNCH();
-    k_cg_beta<<<1, 32, 0, s>>>(R.scal);
-    SEMO_CHECK_LAUNCH();
-    k_p_update_t<V><<<blocks(n, 256), 256, 0, s>>>(n, L0.x.p, p, R.scal);
-    SEMO_CHECK_LAUNCH();
-    k_spmv_dot<8><<<kRedBlocks, 256, 0, s>>>(n, ptr, col, val, p, q, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 2);
-    SEMO_CHECK_LAUNCH();
-    k_cg_alpha<<<1, 32, 0, s>>>(R.scal);
-    SEMO_CHECK_LAUNCH();
-    k_xr_update<<<kRedBlocks, kRedThreads, 0, s>>>(n, x, r, p, q, R.scal, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 3);
-    SEMO_CHECK_LAUNCH();
-}
-
-struct GraphGuard {
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t e = nullptr;
-    ~GraphGuard() {
-        if (e) cudaGraphExecDestroy(e);
-        if (g) cudaGraphDestroy(g);
-    }
-};
-
-template <class V>
-void pcg(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n, const double* b,
-         double* x, bool zero_guess, semo_solve_info* info) {
-    cudaStream_t s = c->stream;
-    Red R = red_area(c);
-    c->kr.alloc(n, s); c->kp.alloc(n, s); c->kq.alloc(n, s);
-    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
-    double* h2 = c->hpin;
-    double* r = c->kr.p;
-    // r = b - A x
-    if (zero_guess) {
-        SEMO_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-        SEMO_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    } else {
-        k_residual<double, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, ptr, col, val, x, b, r);
-        SEMO_CHECK_LAUNCH();
-    }
-    SEMO_CUDA(cudaMemsetAsync(c->kq.p, 0, sizeof(double) * n, s));
-    SEMO_CUDA(cudaMemsetAsync(c->kp.p, 0, sizeof(double) * n, s));
-    SEMO_CUDA(cudaMemsetAsync(R.scal, 0, sizeof(double) * 16, s));
-    k_dot<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(n, b, b, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_dot<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part + kRedBlocks);
-    SEMO_CHECK_LAUNCH();
-    k_finish<<<1, 256, 0, s>>>(R.part, 2, R.scal + 8);
-    SEMO_CHECK_LAUNCH();
-    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 8, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    const double bn = std::sqrt(h2[0]);
-    double rn = std::sqrt(h2[1]);
-    if (!std::isfinite(bn) || !std::isfinite(rn)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
-    const double bnorm = (bn > 0.0) ? bn : 1.0;
-    int it = 0;
-    // The iteration body is captured once per hierarchy and replayed: the
-    // coarse levels are launch-latency bound, the graph removes the per-kernel
-    // host overhead.  Convergence is read back after every iteration.
-    GraphGuard gg;
-    size_t graph_nodes = 0;
-    if (rn > c->prm.tol * bnorm && c->prm.max_iter > 0) {
-        // launches recorded during capture do not run; replays are counted below
-        const long long launches_before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        try {
-            cg_iteration(c, h, ptr, col, val, n, x, R);
-        } catch (...) {
-            cudaGraph_t junk = nullptr;
-            cudaStreamEndCapture(s, &junk);
-            if (junk) cudaGraphDestroy(junk);
-            throw;
-        }
-        SEMO_CUDA(cudaStreamEndCapture(s, &gg.g));
-        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
-        SEMO_CUDA(cudaGraphGetNodes(gg.g, nullptr, &graph_nodes));
-        __atomic_store_n(&g_kernel_launches, launches_before, __ATOMIC_RELAXED);
-    }
-    while (it < c->prm.max_iter && rn > c->prm.tol * bnorm) {
-        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
-        __atomic_add_fetch(&g_kernel_launches, (long long)graph_nodes, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        ++it;
-        if (!std::isfinite(h2[3]) || !std::isfinite(h2[2])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
-        if (!(h2[2] > 0.0)) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
-        rn = std::sqrt(h2[3]);
-    }
-    // true FP64 residual of the returned solution
-    k_residual<double, 8><<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(n, ptr, col, val, x, b, r);
-    SEMO_CHECK_LAUNCH();
-    k_dot<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_finish<<<1, 256, 0, s>>>(R.part, 1, R.scal + 8);
-    SEMO_CHECK_LAUNCH();
-    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    info->iterations = it;
-    info->rel_residual = (bn > 0.0) ? std::sqrt(h2[0]) / bn : 0.0;
-}
-
-template <class V>
-void fill_info(const Amg<V>& h, int64_t nnz, semo_solve_info* info) {
-    info->levels = (int)h.lev.size();
-    info->coarse_size = h.coarse_n;
-    info->operator_complexity = (double)h.total_nnz / (double)std::max<int64_t>(nnz, 1);
-}
-
 }  // namespace
 
-void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
-                  const double* b, double* x, semo_solve_info* info, bool zero_guess) {
-    cudaStream_t s = c->stream;
-    c->flag.zero();
-    SEMO_CUDA(cudaEventRecord(c->ev[0], s));
-    {
-        StageScope sc(c, ST_AMG_SETUP);
-        if (c->prm.precision == SEMO_PREC_MIXED) {
-            c->amg64.clear();
-            amg_setup<float>(c, c->amg32, ptr, col, val, n, nnz);
-        } else {
-            c->amg32.clear();
-            amg_setup<double>(c, c->amg64, ptr, col, val, n, nnz);
-        }
-    }
-    SEMO_CUDA(cudaEventRecord(c->ev[1], s));
-    {
-        StageScope sc(c, ST_PCG);
-        if (c->prm.precision == SEMO_PREC_MIXED) {
-            pcg<float>(c, c->amg32, ptr, col, val, n, b, x, zero_guess, info);
-            fill_info(c->amg32, nnz, info);
-        } else {
-            pcg<double>(c, c->amg64, ptr, col, val, n, b, x, zero_guess, info);
-            fill_info(c->amg64, nnz, info);
-        }
-    }
-    SEMO_CUDA(cudaEventRecord(c->ev[2], s));
-    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
-    float t0 = 0, t1 = 0;
-    SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
-    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
-    info->setup_ms = t0;
-    info->solve_ms = t1;
+template <class V>
+void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n,
+                     int64_t nnz) {
+    amg_setup<V>(c, h, ptr, col, val, n, nnz);
 }
+template void build_hierarchy<float>(semo_ctx*, Amg<float>&, const int*, const int*, const double*, int, int64_t);
+template void build_hierarchy<double>(semo_ctx*, Amg<double>&, const int*, const int*, const double*, int, int64_t);
 
-// Adjoint solve on the hierarchy of the last forward solve (the pressure
-// matrix is symmetric, so A^T = A and the same preconditioner applies).
-void solve_transpose_reuse(semo_ctx* c, const double* g, double* lam, semo_solve_info* info) {
-    const int n = c->nc;
-    SEMO_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    if (c->prm.precision == SEMO_PREC_MIXED) {
-        if (!c->amg32.ready) throw Error(SEMO_ERR_STATE, "no hierarchy: run a forward solve first");
-        pcg<float>(c, c->amg32, c->A_ptr, c->A_col, c->A_val, n, g, lam, true, info);
-        fill_info(c->amg32, c->nnz, info);
-    } else {
-        if (!c->amg64.ready) throw Error(SEMO_ERR_STATE, "no hierarchy: run a forward solve first");
-        pcg<double>(c, c->amg64, c->A_ptr, c->A_col, c->A_val, n, g, lam, true, info);
-        fill_info(c->amg64, c->nnz, info);
-    }
-    SEMO_CUDA(cudaEventRecord(c->ev[2], c->stream));
-    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
-    float t1 = 0;
-    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
-    info->setup_ms = 0.0;
-    info->solve_ms = t1;
-}
+int device_scan(cudaStream_t s, int* d, int n) { return scan_exclusive(s, d, n); }
 
 }  // namespace semo

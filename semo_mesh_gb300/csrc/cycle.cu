@@ -1,0 +1,755 @@
+// Applying the AMG hierarchy: V-cycle and the outer flexible CG.
+//
+// Replaces the solve half of SEMO's solveAMGCL (src/solvers/solveAMGCL.cpp:
+// 974-980, AMGCL's V-cycle lib/amgcl/mpi/amg.hpp:343-380 and its Krylov
+// loop).  The hierarchy is built by amg_setup.cu.
+//
+// Layout and kernels, GB300-first:
+//  * the finest level and the FP64 outer operator are stored SELL-32 (slices
+//    of 32 rows, column-major inside a slice, padded to the slice's longest
+//    row): one thread per row, every load coalesced.  Rows there have ~7
+//    entries, so a warp-per-row or sub-warp CSR kernel is latency-bound;
+//    coarse levels (27-60 entries a row) stay CSR with 4-32 lanes a row;
+//  * degree-2 Chebyshev smoothing is fused: pre-smoothing from a zero guess
+//    is one kernel (the first iterate D^-1 b / theta is formed on the fly
+//    for the neighbours), post-smoothing is two, with no separate x += d;
+//  * the CG update uses q = A z + beta q (so p and q update in place) and
+//    the dot products are folded into the kernels that produce their
+//    operands; one CG iteration is ~30 launches, captured as a CUDA graph.
+// FP32 V-cycle arithmetic stays on the FP32 pipes (FP64 is 1/58 of FP32
+// on GB300); dot products and the outer residual are FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "semo_internal.h"
+
+namespace semo {
+namespace {
+
+constexpr int kRedBlocks = 608;   // 4 x 152 SMs; fixed so every sum has a fixed order
+constexpr int kRedThreads = 256;
+inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = 0.0;
+    if (threadIdx.x < 32) {
+        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+        v = warp_sum(v);
+    }
+    __syncthreads();
+    return v;
+}
+
+// ------------------------------------------------------------ matrix views
+// CSR with VS lanes per row.
+template <class V, int VS>
+struct CsrView {
+    static constexpr int kVS = VS;
+    const int* __restrict__ ptr;
+    const int* __restrict__ col;
+    const V* __restrict__ val;
+    int n;
+    template <class F>
+    __device__ __forceinline__ V dot(int row, int lane, const F& x) const {
+        V s = V(0);
+        if (row < n) {
+            const int e = ptr[row + 1];
+            for (int k = ptr[row] + lane; k < e; k += VS) s += val[k] * x(col[k]);
+        }
+#pragma unroll
+        for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, VS);
+        return s;
+    }
+};
+
+// SELL-32: slice s holds rows 32s..32s+31; entry j of row 32s+l at
+// sptr[s] + 32j + l; padding entries point at the row itself with value 0.
+template <class V>
+struct SellView {
+    static constexpr int kVS = 1;
+    const int* __restrict__ sptr;
+    const int* __restrict__ col;
+    const V* __restrict__ val;
+    int n;
+    template <class F>
+    __device__ __forceinline__ V dot(int row, int, const F& x) const {
+        V s = V(0);
+        if (row < n) {
+            const int sl = row >> 5, l = row & 31;
+            const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+            int k = b + l;
+            int j = 0;
+            for (; j + 1 < w; j += 2, k += 64) {   // two independent loads in flight
+                const int c0 = col[k], c1 = col[k + 32];
+                const V v0 = val[k], v1 = val[k + 32];
+                s += v0 * x(c0);
+                s += v1 * x(c1);
+            }
+            if (j < w) s += val[k] * x(col[k]);
+        }
+        return s;
+    }
+};
+
+template <class V, class X>
+struct Vec {
+    const X* __restrict__ p;
+    __device__ __forceinline__ V operator()(int j) const { return (V)__ldg(p + j); }
+};
+// the first Chebyshev iterate from zero, D^-1 b / theta, formed on the fly
+template <class V>
+struct FirstIterate {
+    const V* __restrict__ dinv;
+    const V* __restrict__ b;
+    V inv_theta;
+    __device__ __forceinline__ V operator()(int j) const { return __ldg(dinv + j) * __ldg(b + j) * inv_theta; }
+};
+
+// ------------------------------------------------------- V-cycle kernels
+// pre-smoothing, degree 2 from x = 0:  x = d0 + c1 d0 + c2 D^-1 (b - A d0),  d0 = D^-1 b / theta
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_pre2(M A, const V* __restrict__ dinv, const V* __restrict__ b,
+                                              V inv_theta, V c1, V c2, V* __restrict__ x) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, FirstIterate<V>{dinv, b, inv_theta});
+    if (row < A.n && lane == 0) {
+        const V di = dinv[row], bi = b[row];
+        const V d0 = di * bi * inv_theta;
+        x[row] = d0 + c1 * d0 + c2 * (di * (bi - s));
+    }
+}
+// r = b - A x
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_res(M A, const V* __restrict__ x, const V* __restrict__ b,
+                                             V* __restrict__ r) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, Vec<V, V>{x});
+    if (row < A.n && lane == 0) r[row] = b[row] - s;
+}
+// y = A x (restriction with R, or any plain product)
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_mv(M A, const V* __restrict__ x, V* __restrict__ y) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, Vec<V, V>{x});
+    if (row < A.n && lane == 0) y[row] = s;
+}
+// x += P xc
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_prolong_add(M P, const V* __restrict__ xc, V* __restrict__ x) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = P.dot(row, lane, Vec<V, V>{xc});
+    if (row < P.n && lane == 0) x[row] += s;
+}
+// post-smoothing step 0 from x:  d = D^-1 (b - A x) / theta ;  y = x + d
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_post0(M A, const V* __restrict__ dinv, const V* __restrict__ b,
+                                               V inv_theta, const V* __restrict__ x, V* __restrict__ d,
+                                               V* __restrict__ y) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, Vec<V, V>{x});
+    if (row < A.n && lane == 0) {
+        const V dv = dinv[row] * (b[row] - s) * inv_theta;
+        d[row] = dv;
+        y[row] = x[row] + dv;
+    }
+}
+// post-smoothing step 1:  x = y + c1 d + c2 D^-1 (b - A y)
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_post1(M A, const V* __restrict__ dinv, const V* __restrict__ b, V c1, V c2,
+                                               const V* __restrict__ y, const V* __restrict__ d,
+                                               V* __restrict__ x) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, Vec<V, V>{y});
+    if (row < A.n && lane == 0) x[row] = y[row] + c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
+}
+// finest-level post-smoothing step 1 (SELL), also folding in the CG dots
+// z.r and z.q (q = A p of the previous iteration); grid-stride, fixed grid
+template <class V>
+__global__ void __launch_bounds__(kRedThreads) k_post1_dots(SellView<V> A, const V* __restrict__ dinv,
+                                                            const V* __restrict__ b, V c1, V c2,
+                                                            const V* __restrict__ y, const V* __restrict__ d,
+                                                            V* __restrict__ z, const double* __restrict__ r,
+                                                            const double* __restrict__ q,
+                                                            double* __restrict__ part) {
+    __shared__ double sh[32];
+    double zr = 0.0, zq = 0.0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += stride) {
+        const V s = A.dot(row, 0, Vec<V, V>{y});
+        const V zi = y[row] + c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
+        z[row] = zi;
+        zr += (double)zi * r[row];
+        zq += (double)zi * q[row];
+    }
+    zr = block_sum(zr, sh);
+    zq = block_sum(zq, sh);
+    if (threadIdx.x == 0) { part[blockIdx.x] = zr; part[kRedBlocks + blockIdx.x] = zq; }
+}
+
+// generic Chebyshev pieces for degrees other than 2 (CSR)
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_cheb_d(M A, const V* __restrict__ dinv, const V* __restrict__ b,
+                                                const V* __restrict__ x, V c1, V c2, V* __restrict__ d) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / M::kVS, lane = g % M::kVS;
+    const V s = A.dot(row, lane, Vec<V, V>{x});
+    if (row < A.n && lane == 0) d[row] = c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
+}
+template <class V>
+__global__ void k_axpy1(int n, const V* __restrict__ d, V* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += d[i];
+}
+template <class V>
+__global__ void k_zero(int n, V* __restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = V(0);
+}
+template <class V>
+__global__ void k_copy_t(int n, const V* __restrict__ a, V* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
+// coarsest level: x = A^-1 b with the explicit FP64 inverse, one block
+template <class V>
+__global__ void k_coarse_solve(int n, const double* __restrict__ inv, const V* __restrict__ b, V* __restrict__ x) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < n; ++k) s += inv[(size_t)i * n + k] * (double)b[k];
+        x[i] = (V)s;
+    }
+}
+
+// ---------------------------------------------------------- CG kernels
+// device scalars: 0 rz, 1 zq, 2 pq, 3 rr, 4 alpha_prev, 5 beta, 6 alpha,
+// 7 rz_prev, 8/9 scratch, 10 iteration count
+__device__ __forceinline__ double sum_parts(const double* part, double* sh) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) s += part[i];
+    return block_sum(s, sh);
+}
+__global__ void k_fin_beta(const double* __restrict__ part, double* __restrict__ scal) {
+    __shared__ double sh[32];
+    const double rz = sum_parts(part, sh);
+    const double zq = sum_parts(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+        scal[0] = rz;
+        scal[1] = zq;
+        // Polak-Ribiere: beta = z.(r_k - r_{k-1}) / (z_{k-1}.r_{k-1}) = -alpha_{k-1} z.q_{k-1} / rz_prev
+        scal[5] = (scal[10] == 0.0) ? 0.0 : (-scal[4] * zq / scal[7]);
+        scal[7] = rz;
+        scal[10] += 1.0;
+    }
+}
+// w = A z;  q = w + beta q;  p = z + beta p;  part = p.q   (FP64 SELL operator)
+template <class Z>
+__global__ void __launch_bounds__(kRedThreads) k_outer_mv(SellView<double> A, const Z* __restrict__ z,
+                                                          double* __restrict__ p, double* __restrict__ q,
+                                                          const double* __restrict__ scal,
+                                                          double* __restrict__ part) {
+    __shared__ double sh[32];
+    const double beta = scal[5];
+    double pq = 0.0;
+    const int stride = gridDim.x * blockDim.x;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += stride) {
+        const double w = A.dot(row, 0, Vec<double, Z>{z});
+        const double qi = w + beta * q[row];
+        const double pi = (double)z[row] + beta * p[row];
+        q[row] = qi;
+        p[row] = pi;
+        pq += pi * qi;
+    }
+    pq = block_sum(pq, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = pq;
+}
+__global__ void k_fin_alpha(const double* __restrict__ part, double* __restrict__ scal) {
+    __shared__ double sh[32];
+    const double pq = sum_parts(part, sh);
+    if (threadIdx.x == 0) {
+        scal[2] = pq;
+        scal[6] = scal[7] / pq;
+        scal[4] = scal[6];
+    }
+}
+// x += alpha p;  r -= alpha q;  rv = r in the V-cycle's type;  part = r.r
+template <class V>
+__global__ void __launch_bounds__(kRedThreads) k_xr(int n, double* __restrict__ x, double* __restrict__ r,
+                                                    V* __restrict__ rv, const double* __restrict__ p,
+                                                    const double* __restrict__ q, const double* __restrict__ scal,
+                                                    double* __restrict__ part) {
+    __shared__ double sh[32];
+    const double alpha = scal[6];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        rv[i] = (V)ri;
+        s += ri * ri;
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_fin_rr(const double* __restrict__ part, double* __restrict__ scal) {
+    __shared__ double sh[32];
+    const double rr = sum_parts(part, sh);
+    if (threadIdx.x == 0) scal[3] = rr;
+}
+// generic dots for the non-fused path: part = a.b, part+R = a.c
+template <class A>
+__global__ void __launch_bounds__(kRedThreads) k_dot2(int n, const A* __restrict__ a, const double* __restrict__ b,
+                                                      const double* __restrict__ c, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double s = 0.0, t = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double ai = (double)a[i];
+        s += ai * b[i];
+        t += ai * c[i];
+    }
+    s = block_sum(s, sh);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) { part[blockIdx.x] = s; part[kRedBlocks + blockIdx.x] = t; }
+}
+__global__ void __launch_bounds__(kRedThreads) k_dot(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                                     double* __restrict__ part) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * b[i];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+template <class A, class B>
+__global__ void k_conv(int n, const A* __restrict__ a, B* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (B)a[i];
+}
+// r = b - A x in FP64 (CSR, 8 lanes a row)
+__global__ void __launch_bounds__(256) k_res64(CsrView<double, 8> A, const double* __restrict__ x,
+                                               const double* __restrict__ b, double* __restrict__ r) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = g / 8, lane = g % 8;
+    const double s = A.dot(row, lane, Vec<double, double>{x});
+    if (row < A.n && lane == 0) r[row] = b[row] - s;
+}
+
+// --------------------------------------------------------------- SELL build
+__global__ void k_sell_width(int n, const int* __restrict__ ptr, int* __restrict__ slice_len) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int len = (row < n) ? ptr[row + 1] - ptr[row] : 0;
+    const int w = __reduce_max_sync(0xffffffffu, len);
+    if ((threadIdx.x & 31) == 0 && row < ((n + 31) & ~31)) slice_len[row >> 5] = 32 * w;
+}
+template <class V, class W>
+__global__ void k_sell_fill(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                            const V* __restrict__ val, const int* __restrict__ sptr, int* __restrict__ scol,
+                            W* __restrict__ sval) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= ((n + 31) & ~31)) return;
+    const int sl = row >> 5, l = row & 31;
+    const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+    const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
+    const int self = (row < n) ? row : 0;
+    for (int j = 0; j < w; ++j) {
+        const int k = b + 32 * j + l;
+        if (j < len) { scol[k] = col[rb + j]; sval[k] = (W)val[rb + j]; }
+        else { scol[k] = self; sval[k] = W(0); }
+    }
+}
+
+// ------------------------------------------------------------ host side
+template <class V>
+struct Sell {
+    int n = 0, nslices = 0;
+    DBuf<int> sptr, col;
+    DBuf<V> val;
+    SellView<V> view() const { return SellView<V>{sptr.p, col.p, val.p, n}; }
+};
+
+template <class V>
+CsrView<V, 4> csr4(const DCsr<V>& A) { return CsrView<V, 4>{A.ptr.p, A.col.p, A.val.p, A.n}; }
+
+template <class V>
+int pick_vs(const DCsr<V>& A) {
+    const double avg = A.n ? (double)A.nnz / A.n : 1.0;
+    return avg <= 6 ? 4 : (avg <= 12 ? 8 : (avg <= 24 ? 16 : 32));
+}
+
+// launch a row kernel on a CSR matrix with the lanes-per-row that suits it
+template <class V, class F>
+void with_csr(const DCsr<V>& A, F&& f) {
+    switch (pick_vs(A)) {
+        case 4: f(CsrView<V, 4>{A.ptr.p, A.col.p, A.val.p, A.n}); break;
+        case 8: f(CsrView<V, 8>{A.ptr.p, A.col.p, A.val.p, A.n}); break;
+        case 16: f(CsrView<V, 16>{A.ptr.p, A.col.p, A.val.p, A.n}); break;
+        default: f(CsrView<V, 32>{A.ptr.p, A.col.p, A.val.p, A.n}); break;
+    }
+}
+template <class M>
+int grid_for(const M& A) { return blocks((int64_t)A.n * M::kVS, 256); }
+
+// SELL-32 copy of a CSR matrix's structure and values (value type W)
+template <class V, class W>
+void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell<W>& S) {
+    S.n = n;
+    S.nslices = (n + 31) / 32;
+    S.sptr.alloc(S.nslices + 1, s);
+    SEMO_CUDA(cudaMemsetAsync(S.sptr.p + S.nslices, 0, sizeof(int), s));
+    const int rows_pad = S.nslices * 32;
+    k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
+    SEMO_CHECK_LAUNCH();
+    const int total = device_scan(s, S.sptr.p, S.nslices + 1);
+    S.col.alloc(std::max(total, 1), s);
+    S.val.alloc(std::max(total, 1), s);
+    k_sell_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.col.p, S.val.p);
+    SEMO_CHECK_LAUNCH();
+}
+
+struct ChebCoef {
+    double inv_theta, c1, c2;
+};
+ChebCoef cheb2(double lam) {
+    const double hi = lam, lo = lam / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+    const double sigma = theta / delta, rho0 = 1.0 / sigma;
+    const double rho1 = 1.0 / (2.0 * sigma - rho0);
+    return ChebCoef{1.0 / theta, rho1 * rho0, 2.0 * rho1 / delta};
+}
+
+// Everything the V-cycle needs beyond the hierarchy: the finest level in SELL.
+template <class V>
+struct Cycle {
+    Sell<V> fine;
+};
+
+template <class V>
+void chebyshev_generic(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_start) {
+    const int n = L.A.n;
+    const double hi = L.lam_max, lo = hi / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+    const double sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    V* x = L.x.p;
+    V* d = L.t.p;
+    if (zero_start) {
+        k_zero<V><<<blocks(n, 256), 256, 0, s>>>(n, x);
+        SEMO_CHECK_LAUNCH();
+    }
+    k_zero<V><<<blocks(n, 256), 256, 0, s>>>(n, d);
+    SEMO_CHECK_LAUNCH();
+    // d = D^-1 (b - A x) / theta ; x += d
+    with_csr(L.A, [&](auto M) {
+        k_cheb_d<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, x, V(0), (V)(1.0 / theta), d);
+    });
+    SEMO_CHECK_LAUNCH();
+    k_axpy1<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
+    SEMO_CHECK_LAUNCH();
+    for (int k = 1; k < degree; ++k) {
+        const double rho_new = 1.0 / (2.0 * sigma - rho);
+        const V c1 = (V)(rho_new * rho), c2 = (V)(2.0 * rho_new / delta);
+        with_csr(L.A, [&](auto M) { k_cheb_d<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, x, c1, c2, d); });
+        SEMO_CHECK_LAUNCH();
+        k_axpy1<V><<<blocks(n, 256), 256, 0, s>>>(n, d, x);
+        SEMO_CHECK_LAUNCH();
+        rho = rho_new;
+    }
+}
+
+// V-cycle below the finest level (CSR levels), input L.b, output L.x
+template <class V>
+void vcycle_csr(semo_ctx* c, Amg<V>& h, int l) {
+    cudaStream_t s = c->stream;
+    AmgLevel<V>& L = h.lev[l];
+    if (l == (int)h.lev.size() - 1) {
+        k_coarse_solve<V><<<1, 256, 0, s>>>(h.coarse_n, h.cinv, L.b, L.x);
+        SEMO_CHECK_LAUNCH();
+        return;
+    }
+    const int degree = c->prm.cheb_degree;
+    const ChebCoef cc = cheb2(L.lam_max);
+    if (degree == 2) {
+        with_csr(L.A, [&](auto M) {
+            k_pre2<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
+        });
+    } else {
+        chebyshev_generic(s, L, degree, true);
+    }
+    SEMO_CHECK_LAUNCH();
+    with_csr(L.A, [&](auto M) { k_res<<<grid_for(M), 256, 0, s>>>(M, L.x.p, L.b.p, L.r.p); });
+    SEMO_CHECK_LAUNCH();
+    AmgLevel<V>& C = h.lev[l + 1];
+    with_csr(L.R, [&](auto M) { k_mv<<<grid_for(M), 256, 0, s>>>(M, L.r.p, C.b.p); });
+    SEMO_CHECK_LAUNCH();
+    vcycle_csr(c, h, l + 1);
+    with_csr(L.P, [&](auto M) { k_prolong_add<<<grid_for(M), 256, 0, s>>>(M, C.x.p, L.x.p); });
+    SEMO_CHECK_LAUNCH();
+    if (degree == 2) {
+        with_csr(L.A, [&](auto M) {
+            k_post0<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
+        });
+        SEMO_CHECK_LAUNCH();
+        with_csr(L.A, [&](auto M) {
+            k_post1<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
+        });
+        SEMO_CHECK_LAUNCH();
+    } else {
+        chebyshev_generic(s, L, degree, false);
+    }
+}
+
+struct Red {
+    double* part;
+    double* scal;
+};
+Red red_area(semo_ctx* c) {
+    c->red.alloc(4 * kRedBlocks + 32, c->stream);
+    return Red{c->red.p, c->red.p + 4 * kRedBlocks + 8};
+}
+
+// One preconditioned CG iteration.  In: r (FP64) and its copy L0.b in V; out: x, r, L0.b updated.
+template <class V>
+void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, double* x, const Red& R) {
+    cudaStream_t s = c->stream;
+    AmgLevel<V>& L = h.lev[0];
+    const int n = L.A.n;
+    double* r = c->kr.p;
+    double* p = c->kp.p;
+    double* q = c->kq.p;
+    const int degree = c->prm.cheb_degree;
+    const bool single = h.lev.size() == 1;
+    if (single) {
+        k_coarse_solve<V><<<1, 256, 0, s>>>(h.coarse_n, h.cinv, L.b, L.x);
+        SEMO_CHECK_LAUNCH();
+        k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L.x.p, r, q, R.part);
+        SEMO_CHECK_LAUNCH();
+    } else if (degree == 2) {
+        const ChebCoef cc = cheb2(L.lam_max);
+        const SellView<V> A = cy.fine.view();
+        k_pre2<<<blocks(n, 256), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
+        SEMO_CHECK_LAUNCH();
+        k_res<<<blocks(n, 256), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p);
+        SEMO_CHECK_LAUNCH();
+        AmgLevel<V>& C = h.lev[1];
+        with_csr(L.R, [&](auto M) { k_mv<<<grid_for(M), 256, 0, s>>>(M, L.r.p, C.b.p); });
+        SEMO_CHECK_LAUNCH();
+        vcycle_csr(c, h, 1);
+        with_csr(L.P, [&](auto M) { k_prolong_add<<<grid_for(M), 256, 0, s>>>(M, C.x.p, L.x.p); });
+        SEMO_CHECK_LAUNCH();
+        k_post0<<<blocks(n, 256), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
+        SEMO_CHECK_LAUNCH();
+        // z lands in L.x; z.r and z.q folded in
+        k_post1_dots<V><<<kRedBlocks, kRedThreads, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p,
+                                                           L.x.p, r, q, R.part);
+        SEMO_CHECK_LAUNCH();
+    } else {
+        vcycle_csr(c, h, 0);
+        k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L.x.p, r, q, R.part);
+        SEMO_CHECK_LAUNCH();
+    }
+    k_fin_beta<<<1, 256, 0, s>>>(R.part, R.scal);
+    SEMO_CHECK_LAUNCH();
+    k_outer_mv<V><<<kRedBlocks, kRedThreads, 0, s>>>(outer.view(), L.x.p, p, q, R.scal, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_fin_alpha<<<1, 256, 0, s>>>(R.part, R.scal);
+    SEMO_CHECK_LAUNCH();
+    k_xr<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, x, r, L.b.p, p, q, R.scal, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal);
+    SEMO_CHECK_LAUNCH();
+}
+
+struct GraphGuard {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    ~GraphGuard() {
+        if (e) cudaGraphExecDestroy(e);
+        if (g) cudaGraphDestroy(g);
+    }
+};
+
+template <class V>
+void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, const int* ptr, const int* col,
+         const double* val, int n, const double* b, double* x, bool zero_guess, semo_solve_info* info) {
+    cudaStream_t s = c->stream;
+    Red R = red_area(c);
+    c->kr.alloc(n, s); c->kp.alloc(n, s); c->kq.alloc(n, s);
+    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
+    double* h2 = c->hpin;
+    double* r = c->kr.p;
+    const CsrView<double, 8> A8{ptr, col, val, n};
+    if (zero_guess) {
+        SEMO_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+        SEMO_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+        k_res64<<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(A8, x, b, r);
+        SEMO_CHECK_LAUNCH();
+    }
+    k_conv<double, V><<<blocks(n, 256), 256, 0, s>>>(n, r, h.lev[0].b.p);
+    SEMO_CHECK_LAUNCH();
+    SEMO_CUDA(cudaMemsetAsync(c->kq.p, 0, sizeof(double) * n, s));
+    SEMO_CUDA(cudaMemsetAsync(c->kp.p, 0, sizeof(double) * n, s));
+    SEMO_CUDA(cudaMemsetAsync(R.scal, 0, sizeof(double) * 16, s));
+    k_dot<<<kRedBlocks, kRedThreads, 0, s>>>(n, b, b, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_dot<<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part + kRedBlocks);
+    SEMO_CHECK_LAUNCH();
+    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal + 8);   // ||b||^2 -> scal[11]
+    SEMO_CHECK_LAUNCH();
+    k_fin_rr<<<1, 256, 0, s>>>(R.part + kRedBlocks, R.scal + 9);   // ||r0||^2 -> scal[12]
+    SEMO_CHECK_LAUNCH();
+    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 11, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    const double bn = std::sqrt(h2[0]);
+    double rn = std::sqrt(h2[1]);
+    if (!std::isfinite(bn) || !std::isfinite(rn)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
+    const double bnorm = (bn > 0.0) ? bn : 1.0;
+    int it = 0;
+    // One iteration is captured once per hierarchy and replayed; the
+    // residual norm is read back after every iteration.
+    GraphGuard gg;
+    size_t graph_nodes = 0;
+    if (rn > c->prm.tol * bnorm && c->prm.max_iter > 0) {
+        const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        SEMO_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+            cg_iteration(c, h, cy, outer, x, R);
+        } catch (...) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(s, &junk);
+            if (junk) cudaGraphDestroy(junk);
+            throw;
+        }
+        SEMO_CUDA(cudaStreamEndCapture(s, &gg.g));
+        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
+        SEMO_CUDA(cudaGraphGetNodes(gg.g, nullptr, &graph_nodes));
+        __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
+    }
+    while (it < c->prm.max_iter && rn > c->prm.tol * bnorm) {
+        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
+        __atomic_add_fetch(&g_kernel_launches, (long long)graph_nodes, __ATOMIC_RELAXED);
+        SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        ++it;
+        if (!std::isfinite(h2[3]) || !std::isfinite(h2[2])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
+        if (!(h2[2] > 0.0)) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
+        rn = std::sqrt(h2[3]);
+    }
+    // true FP64 residual of the returned solution
+    k_res64<<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(A8, x, b, r);
+    SEMO_CHECK_LAUNCH();
+    k_dot<<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part);
+    SEMO_CHECK_LAUNCH();
+    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal + 8);
+    SEMO_CHECK_LAUNCH();
+    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 11, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    info->iterations = it;
+    info->rel_residual = (bn > 0.0) ? std::sqrt(h2[0]) / bn : 0.0;
+}
+
+template <class V>
+void fill_info(const Amg<V>& h, int64_t nnz, semo_solve_info* info) {
+    info->levels = (int)h.lev.size();
+    info->coarse_size = h.coarse_n;
+    info->operator_complexity = (double)h.total_nnz / (double)std::max<int64_t>(nnz, 1);
+}
+
+// per-context apply state (kept for the adjoint solve on the same hierarchy)
+struct ApplyState {
+    Cycle<float> cy32;
+    Cycle<double> cy64;
+    Sell<double> outer;
+};
+ApplyState& apply_state(semo_ctx* c) {
+    if (!c->apply) c->apply = std::shared_ptr<void>(new ApplyState(), [](void* p) { delete (ApplyState*)p; });
+    return *(ApplyState*)c->apply.get();
+}
+
+template <class V>
+void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
+    AmgLevel<V>& L = h.lev[0];
+    build_sell<V, V>(c->stream, L.A.ptr, L.A.col, L.A.val, L.A.n, cy.fine);
+}
+
+}  // namespace
+
+void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
+                  const double* b, double* x, semo_solve_info* info, bool zero_guess) {
+    cudaStream_t s = c->stream;
+    ApplyState& st = apply_state(c);
+    c->flag.zero();
+    SEMO_CUDA(cudaEventRecord(c->ev[0], s));
+    {
+        StageScope sc(c, ST_AMG_SETUP);
+        if (c->prm.precision == SEMO_PREC_MIXED) {
+            c->amg64.clear();
+            build_hierarchy<float>(c, c->amg32, ptr, col, val, n, nnz);
+            prepare_cycle(c, c->amg32, st.cy32);
+        } else {
+            c->amg32.clear();
+            build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
+            prepare_cycle(c, c->amg64, st.cy64);
+        }
+        build_sell<double, double>(s, ptr, col, val, n, st.outer);
+    }
+    SEMO_CUDA(cudaEventRecord(c->ev[1], s));
+    {
+        StageScope sc(c, ST_PCG);
+        if (c->prm.precision == SEMO_PREC_MIXED) {
+            pcg<float>(c, c->amg32, st.cy32, st.outer, ptr, col, val, n, b, x, zero_guess, info);
+            fill_info(c->amg32, nnz, info);
+        } else {
+            pcg<double>(c, c->amg64, st.cy64, st.outer, ptr, col, val, n, b, x, zero_guess, info);
+            fill_info(c->amg64, nnz, info);
+        }
+    }
+    SEMO_CUDA(cudaEventRecord(c->ev[2], s));
+    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
+    float t0 = 0, t1 = 0;
+    SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
+    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
+    info->setup_ms = t0;
+    info->solve_ms = t1;
+}
+
+// Adjoint solve on the hierarchy of the last forward solve (the pressure
+// matrix is symmetric, so A^T = A and the same preconditioner applies).
+void solve_transpose_reuse(semo_ctx* c, const double* g, double* lam, semo_solve_info* info) {
+    const int n = c->nc;
+    ApplyState& st = apply_state(c);
+    SEMO_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    if (c->prm.precision == SEMO_PREC_MIXED) {
+        if (!c->amg32.ready) throw Error(SEMO_ERR_STATE, "no hierarchy: run a forward solve first");
+        pcg<float>(c, c->amg32, st.cy32, st.outer, c->A_ptr, c->A_col, c->A_val, n, g, lam, true, info);
+        fill_info(c->amg32, c->nnz, info);
+    } else {
+        if (!c->amg64.ready) throw Error(SEMO_ERR_STATE, "no hierarchy: run a forward solve first");
+        pcg<double>(c, c->amg64, st.cy64, st.outer, c->A_ptr, c->A_col, c->A_val, n, g, lam, true, info);
+        fill_info(c->amg64, c->nnz, info);
+    }
+    SEMO_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
+    float t1 = 0;
+    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
+    info->setup_ms = 0.0;
+    info->solve_ms = t1;
+}
+
+}  // namespace semo

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -163,6 +164,7 @@ struct semo_ctx {
     semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
     semo::DBuf<float> kz32, kr32;
     double* hpin = nullptr;                       // pinned host scalars for convergence checks
+    std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -232,7 +234,14 @@ void assemble_pressure(semo_ctx* c);
 double pressure_update(semo_ctx* c);
 void assemble_face_values(semo_ctx* c);
 
-// solve.cu
+// amg_setup.cu: smoothed-aggregation hierarchy (value type float or double)
+template <class V>
+void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n,
+                     int64_t nnz);
+// exclusive scan of d[0..n) in place on the context's stream; returns the total
+int device_scan(cudaStream_t s, int* d, int n);
+
+// cycle.cu
 void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double* d_val, int n, int64_t nnz,
                   const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess);
 
