@@ -185,6 +185,24 @@ semo_status semo_stage_time(semo_ctx* ctx, const char* stage, double* total_ms, 
 semo_status semo_reset_stats(semo_ctx* ctx);
 /* Kernel launches made by this library in this process so far. */
 int64_t semo_kernel_launches(void);
+/* Allocation-free relative residual ||b - A x|| / ||b|| of a CSR system
+   already in device memory (ptr, col, val, x, b are device pointers).  No
+   reference counterpart: it is for callers that cannot call cudaMalloc --
+   code that runs inside a memory arena or pool it manages itself, under a
+   strict device-memory budget, or in a loop that must not synchronise the
+   device through allocation calls.  It allocates nothing: its only scratch
+   (one pair of partial sums per 32 rows) is a fixed 1 MiB array in the
+   library's static device memory, held by every GPU that loads the library
+   until the process exits.  Writes {||r||/||b||, ||r||, ||b||} to out3
+   (device, 3 doubles) asynchronously on `stream` (a cudaStream_t, NULL for
+   the default stream).  Rows above SEMO_STATIC_MAX_ROWS are rejected with
+   SEMO_ERR_ARGUMENT.  The first call on a device resolves the array's device
+   address; make it before any stream capture.  Every call shares the array:
+   calls that overlap on a GPU race. */
+#define SEMO_STATIC_MAX_ROWS 2097152
+semo_status semo_residual_norm_static(const int32_t* ptr, const int32_t* col, const double* val, int n,
+                                      const double* x, const double* b, double* out3, void* stream);
+
 /* Mesh counts: out[0..6) = cells, faces, internal faces, boundary faces,
    vertex-stencil entries, matrix nonzeros. */
 semo_status semo_mesh_info(semo_ctx* ctx, int64_t* out6);

@@ -25,6 +25,7 @@ UNITS = [
     ("assemble.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
+    ("noalloc.cu", []),
     ("capi.cpp", []),
     ("rcm.cpp", []),
 ]
