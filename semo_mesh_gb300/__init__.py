@@ -277,7 +277,8 @@ class Context:
 
     # ---- measurement hooks -------------------------------------------------
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
-              "gauss_green", "update", "vcycle")
+              "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
+              "setup_level", "setup_coarse")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

@@ -425,13 +425,36 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
         __syncwarp();
         int distinct = 0;
         bool full = false;
-        for (int ka = aptr[row]; ka < aptr[row + 1] && !full; ++ka) {
-            const int a = acol[ka];
-            const double av = (double)aval[ka];
-            const int bb = bptr[a], be = bptr[a + 1];
-            for (int q0 = bb; q0 < be; q0 += 32) {
-                const int q = q0 + lane;
-                const bool act = q < be;
+        // Products are taken in a fixed flattened order: up to 32 A entries at
+        // a time, their B rows laid end to end, 32 products per step.
+        const int ab = aptr[row], ae = aptr[row + 1];
+        for (int k0 = ab; k0 < ae && !full; k0 += 32) {
+            const int k = k0 + lane;
+            const bool ka = k < ae;
+            const int a = ka ? acol[k] : 0;
+            const double avk = ka ? (double)aval[k] : 0.0;
+            const int bb = ka ? bptr[a] : 0;
+            const int blen = ka ? bptr[a + 1] - bb : 0;
+            int incl = blen;   // inclusive scan of the B row lengths over the lanes
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - blen;
+            for (int t0 = 0; t0 < total; t0 += 32) {
+                const int t = t0 + lane;
+                const bool act = t < total;
+                // owner lane: the last lane whose B-row run starts at or before t
+                int j = 0;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int e = __shfl_sync(0xffffffffu, excl, j + step);
+                    if (e <= t) j += step;
+                }
+                const int q = __shfl_sync(0xffffffffu, bb, j) + (t - __shfl_sync(0xffffffffu, excl, j));
+                const double av = __shfl_sync(0xffffffffu, avk, j);
                 const int c = act ? bcol[q] : -1;
                 int slot = -1;
                 bool fresh = false;
@@ -446,9 +469,19 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 }
                 distinct += __popc(__ballot_sync(0xffffffffu, fresh));
                 const bool lost = __any_sync(0xffffffffu, act && slot < 0);
-                // the lanes of one chunk hold distinct columns of one B row, so
-                // no two lanes share a slot; chunks are applied in order
-                if (pass == 1 && !lost && act) vals[slot] += av * (double)bval[q];
+                if (pass == 1 && !lost) {
+                    // lanes that hit the same column are summed in lane order by the lowest one
+                    const double pv = act ? av * (double)bval[q] : 0.0;
+                    const unsigned grp = __match_any_sync(0xffffffffu, act ? slot : -1 - lane);
+                    double sum = 0.0;
+                    unsigned m = grp;
+                    while (m) {
+                        const int l = __ffs(m) - 1;
+                        sum += __shfl_sync(grp, pv, l);
+                        m &= m - 1;
+                    }
+                    if (act && lane == __ffs(grp) - 1) vals[slot] += sum;
+                }
                 __syncwarp();
                 if (lost || distinct > (ht * 3) / 4) { full = true; break; }
             }
@@ -686,7 +719,10 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     for (int l = 0;; ++l) {
         AmgLevel<V>& L = h.lev[l];
         DBuf<V> dia;
-        level_prepare(c, L, dia);
+        {
+            StageScope sc(c, ST_SETUP_LEVEL);
+            level_prepare(c, L, dia);
+        }
         h.total_nnz += L.A.nnz;
         const int nl = L.A.n;
         if (nl <= c->prm.coarse_enough || l == c->prm.max_levels - 1) break;
@@ -699,32 +735,43 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         m1.alloc(nl, s);
         const double eps2 = (double)(eps * eps);
         eps *= 0.5f;
-        k_strength<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, dia, eps2, strong, state);
-        SEMO_CHECK_LAUNCH();
-        for (int round = 0; round < 200; ++round) {
-            undec.zero();
-            k_mis_max1<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, m1);
+        int nagg = 0;
+        {
+            StageScope sc(c, ST_SETUP_AGG);
+            k_strength<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, dia, eps2, strong, state);
             SEMO_CHECK_LAUNCH();
-            k_mis_max2<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, undec);
+            // rounds are launched in pairs between checks: a round after the
+            // last undecided node is gone changes nothing
+            int hu = 1;
+            for (int round = 0; round < 200 && hu; round += 2) {
+                for (int k = 0; k < 2; ++k) {
+                    undec.zero();
+                    k_mis_max1<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, m1);
+                    SEMO_CHECK_LAUNCH();
+                    k_mis_max2<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, undec);
+                    SEMO_CHECK_LAUNCH();
+                }
+                SEMO_CUDA(cudaMemcpyAsync(&hu, undec.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+                SEMO_CUDA(cudaStreamSynchronize(s));
+            }
+            if (hu) throw Error(SEMO_ERR_CUDA, "MIS(2) aggregation did not terminate");
+            k_root_flags<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2);
             SEMO_CHECK_LAUNCH();
-            int u = 0;
-            SEMO_CUDA(cudaMemcpyAsync(&u, undec.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-            SEMO_CUDA(cudaStreamSynchronize(s));
-            if (u == 0) break;
-            if (round == 199) throw Error(SEMO_ERR_CUDA, "MIS(2) aggregation did not terminate");
+            nagg = scan_exclusive(s, agg2.p, nl);
+            if (nagg > 0 && nagg < nl) {
+                k_root_ids<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2, agg);
+                SEMO_CHECK_LAUNCH();
+                for (int pass = 0; pass < 2; ++pass) {
+                    k_agg_join<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, agg, agg2);
+                    SEMO_CHECK_LAUNCH();
+                    std::swap(agg.p, agg2.p);
+                }
+            }
         }
-        k_root_flags<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2);
-        SEMO_CHECK_LAUNCH();
-        const int nagg = scan_exclusive(s, agg2.p, nl);
         if (nagg == 0 || nagg >= nl) break;
-        k_root_ids<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2, agg);
-        SEMO_CHECK_LAUNCH();
-        for (int pass = 0; pass < 2; ++pass) {
-            k_agg_join<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, agg, agg2);
-            SEMO_CHECK_LAUNCH();
-            std::swap(agg.p, agg2.p);
-        }
         L.nagg = nagg;
+        {
+        StageScope sp(c, ST_SETUP_PROLONG);
         // smoothed prolongation
         L.P.n = nl; L.P.m = nagg;
         L.P.ptr.alloc(nl + 1, s);
@@ -738,14 +785,17 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
                                                           L.P.col, L.P.val);
         SEMO_CHECK_LAUNCH();
         transpose(s, L.P, L.R);
+        }
+        StageScope sg(c, ST_SETUP_GALERKIN);
         DCsr<V> AP;
         spgemm(s, c, L.A, L.P, AP);
-        h.lev.emplace_back();
+        h.lev.emplace_back();   // capacity reserved above: L stays valid
         AmgLevel<V>& Lc = h.lev.back();
         AmgLevel<V>& Lf = h.lev[h.lev.size() - 2];
         spgemm(s, c, Lf.R, AP, Lc.A);
         Lc.A.m = Lc.A.n;
     }
+    StageScope scs(c, ST_SETUP_COARSE);
     // coarsest level: explicit FP64 inverse (Gauss-Jordan, partial pivoting)
     AmgLevel<V>& Lc = h.lev.back();
     const int m = Lc.A.n;

@@ -37,9 +37,12 @@ extern long long g_kernel_launches;
 
 // Named stages timed with CUDA events on the context's stream when profiling is on.
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
-             ST_GG, ST_UPDATE, ST_VCYCLE, ST_COUNT };
+             ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
+             ST_SETUP_COARSE, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
-                                                  "amg_setup", "pcg", "gauss_green", "update", "vcycle"};
+                                                  "amg_setup", "pcg", "gauss_green", "update", "vcycle",
+                                                  "setup_aggregate", "setup_prolong", "setup_galerkin",
+                                                  "setup_level", "setup_coarse"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
