@@ -383,6 +383,78 @@ __global__ void k_max_int(int n, const int* __restrict__ a, int* __restrict__ ou
     }
 }
 
+// Thread-per-row SpGEMM for rows with few distinct columns (the finest
+// level's A*P: 7-entry rows times 2-7-entry rows).  The row's columns are
+// kept sorted in a small local array and products are consumed in row order,
+// so every sum has a fixed order.  Rows with more than kSmallCap distinct
+// columns are marked -1 and left to the warp kernel.
+// The row is held in registers (every index below is a compile-time constant
+// after unrolling): columns sorted ascending with INT_MAX padding, a new
+// column is bubbled into place by compare-and-swap.
+constexpr int kSmallCap = 16;
+constexpr int kSmallMaxProducts = 64;
+template <class V>
+__global__ void __launch_bounds__(128) k_spgemm_small(int n, const int* __restrict__ aptr,
+                                                      const int* __restrict__ acol, const V* __restrict__ aval,
+                                                      const int* __restrict__ bptr, const int* __restrict__ bcol,
+                                                      const V* __restrict__ bval, int pass, int* __restrict__ small,
+                                                      const int* __restrict__ cptr, int* __restrict__ ccol,
+                                                      V* __restrict__ cval) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    if (pass == 1 && small[row] < 0) return;
+    const int ab = aptr[row], ae = aptr[row + 1];
+    if (pass == 0) {
+        int prod = 0;
+        for (int ka = ab; ka < ae; ++ka) prod += bptr[acol[ka] + 1] - bptr[acol[ka]];
+        if (prod > kSmallMaxProducts) { small[row] = -1; return; }
+    }
+    int cols[kSmallCap];
+    V vals[kSmallCap];
+#pragma unroll
+    for (int t = 0; t < kSmallCap; ++t) { cols[t] = 0x7FFFFFFF; vals[t] = V(0); }
+    int d = 0;
+    bool over = false;
+    for (int ka = ab; ka < ae && !over; ++ka) {
+        const int a = acol[ka];
+        const V av = aval[ka];
+        for (int q = bptr[a]; q < bptr[a + 1]; ++q) {
+            const int cq = bcol[q];
+            const V pv = (pass == 1) ? av * bval[q] : V(0);
+            bool found = false;
+#pragma unroll
+            for (int t = 0; t < kSmallCap; ++t)
+                if (cols[t] == cq) { vals[t] += pv; found = true; }
+            if (found) continue;
+            if (d == kSmallCap) { over = true; break; }
+            int cn = cq;
+            V vn = pv;
+#pragma unroll
+            for (int t = 0; t < kSmallCap; ++t) {
+                if (cn < cols[t]) {
+                    const int tc = cols[t]; cols[t] = cn; cn = tc;
+                    const V tv = vals[t]; vals[t] = vn; vn = tv;
+                }
+            }
+            ++d;
+        }
+    }
+    if (pass == 0) {
+        small[row] = over ? -1 : d;
+    } else {
+        const int base = cptr[row];
+#pragma unroll
+        for (int t = 0; t < kSmallCap; ++t)
+            if (t < d) { ccol[base + t] = cols[t]; cval[base + t] = vals[t]; }
+    }
+}
+__global__ void k_count_negative(int n, const int* __restrict__ a, int* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool neg = i < n && a[i] < 0;
+    const unsigned b = __ballot_sync(0xffffffffu, neg);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, __popc(b));
+}
+
 // Row-wise SpGEMM C = A * B, one warp per row, open-addressing hash table in
 // shared memory.  Pass 0 counts distinct columns (flagging rows that fill
 // more than 3/4 of the table); pass 1 fills.  Products are consumed in a fixed
@@ -398,7 +470,8 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                                                             const V* __restrict__ bval, int pass,
                                                             int* __restrict__ cnt, const int* __restrict__ cptr,
                                                             int* __restrict__ ccol, V* __restrict__ cval,
-                                                            int* __restrict__ overflow) {
+                                                            int* __restrict__ overflow,
+                                                            const int* __restrict__ small) {
     extern __shared__ unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // per warp: keys[HT] int, ckeys[HT] int, vals[HT] double, cvals[HT] double
@@ -407,6 +480,10 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
     double* vals = reinterpret_cast<double*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
     double* cvals = vals + HT;
     for (int row = blockIdx.x * kGemmWarps + wid; row < n; row += gridDim.x * kGemmWarps) {
+        if (small && small[row] >= 0) {   // the row was done by the thread-per-row kernel
+            if (pass == 0 && lane == 0) cnt[row] = small[row];
+            continue;
+        }
         // table size for this row (power of two, 32..HT): from the product
         // count in the counting pass, from the known column count when filling
         int need;
@@ -582,7 +659,7 @@ int pick_vs(const DCsr<V>& A) {
 
 template <class V>
 void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C, int* cnt,
-                 int* overflow) {
+                 int* overflow, const int* small) {
     const int n = A.n;
     const size_t shm = (size_t)kGemmWarps * ht * 2 * (sizeof(int) + sizeof(double));
     const int grid = std::max(1, std::min(blocks(n, kGemmWarps), 152 * 32));
@@ -591,7 +668,7 @@ void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<
         if (shm > 48 * 1024)                                                                                     \
             SEMO_CUDA(cudaFuncSetAttribute(k_spgemm<V, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm)); \
         k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, pass, cnt,  \
-                                                           C.ptr, C.col.p, C.val.p, overflow);                   \
+                                                           C.ptr, C.col.p, C.val.p, overflow, small);            \
         break;
     switch (ht) {
         SEMO_GEMM_CASE(64)
@@ -612,19 +689,36 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     C.n = n;
     C.m = B.m;
     C.ptr.alloc(n + 1, s);
-    DBuf<int> flags;
+    DBuf<int> flags, small;
     flags.alloc(2, s);
-    // pass 0 with a growing table until no row overflows; counts land in C.ptr
+    small.alloc(std::max(n, 1), s);
+    // thread-per-row counting pass; rows it cannot hold are marked -1
+    flags.zero();
+    k_spgemm_small<V><<<blocks(n, 128), 128, 0, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, 0, small.p,
+                                                     nullptr, nullptr, nullptr);
+    SEMO_CHECK_LAUNCH();
+    k_count_negative<<<blocks(n, 256), 256, 0, s>>>(n, small.p, flags.p + 1);
+    SEMO_CHECK_LAUNCH();
+    int nbig = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&nbig, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    // warp counting pass for the marked rows, with a growing table until none
+    // overflows; all counts land in C.ptr
     int ht = 256, of = 0;
-    for (;;) {
-        flags.zero();
+    if (nbig == 0) {
+        SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, small.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
         SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
-        spgemm_pass(s, ht, 0, A, B, C, C.ptr.p, flags.p);
-        SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        if (!of) break;
-        if (ht >= 2048) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
-        ht <<= 1;
+    } else {
+        for (;;) {
+            flags.zero();
+            SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
+            spgemm_pass(s, ht, 0, A, B, C, C.ptr.p, flags.p, small.p);
+            SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SEMO_CUDA(cudaStreamSynchronize(s));
+            if (!of) break;
+            if (ht >= 2048) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
+            ht <<= 1;
+        }
     }
     // pass 1 with the smallest table that holds the densest row at <= 3/4 load
     DBuf<int> mx;
@@ -641,10 +735,15 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     C.col.alloc(std::max(nnz, 1), s);
     C.val.alloc(std::max(nnz, 1), s);
     flags.zero();
-    spgemm_pass(s, ht1, 1, A, B, C, nullptr, flags.p);
-    SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM numeric pass overflowed its table");
+    k_spgemm_small<V><<<blocks(n, 128), 128, 0, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, 1, small.p,
+                                                     C.ptr.p, C.col.p, C.val.p);
+    SEMO_CHECK_LAUNCH();
+    if (nbig > 0) {
+        spgemm_pass(s, ht1, 1, A, B, C, nullptr, flags.p, small.p);
+        SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM numeric pass overflowed its table");
+    }
     (void)c;
 }
 

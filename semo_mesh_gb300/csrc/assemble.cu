@@ -94,7 +94,7 @@ __global__ void k_grav_face(int nf, int ni, int nc, int nb, const int* __restric
                             const double* __restrict__ fn, const double* __restrict__ wc,
                             const double* __restrict__ pf, const double* __restrict__ nfv,
                             const double* __restrict__ U, const double* __restrict__ V,
-                            const double* __restrict__ W, const double* __restrict__ rho,
+                            const double* __restrict__ W, const double* __restrict__ irho,
                             const double* __restrict__ bf, double g0, double g1, double g2,
                             double* __restrict__ out) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,20 +102,20 @@ __global__ void k_grav_face(int nf, int ni, int nc, int nb, const int* __restric
     const int o = own[f];
     const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f];
     const double wL = wc[f], wR = 1.0 - wL;
-    double uL, vL, wwL, uR, vR, wwR, rL, rR;
+    double uL, vL, wwL, uR, vR, wwR, irL, irR;
     if (f < ni) {
         const int q = nei[f];
         uL = U[o]; vL = V[o]; wwL = W[o]; uR = U[q]; vR = V[q]; wwR = W[q];
-        rL = rho[o]; rR = rho[q];
+        irL = irho[o]; irR = irho[q];   // face densities equal the cells' (same EOS of the same VF)
     } else {
         const int b = f - ni;
         uL = uR = bf[nb + b]; vL = vR = bf[2 * nb + b]; wwL = wwR = bf[3 * nb + b];
-        rL = rR = bf[5 * nb + b];
+        irL = irR = 1.0 / bf[5 * nb + b];
     }
     const double UnL = uL * n0 + vL * n1 + wwL * n2;
     const double UnR = uR * n0 + vR * n1 + wwR * n2;
     const double UnF = wL * UnL + wR * UnR;
-    const double RhoF = 1.0 / (wL / rL + wR / rR);
+    const double RhoF = 1.0 / (wL * irL + wR * irR);
     double gL = 0.0, gR = 0.0;
     gL += g0 * pf[f]; gL += g1 * pf[nf + f]; gL += g2 * pf[2 * nf + f];
     gR += g0 * nfv[f]; gR += g1 * nfv[nf + f]; gR += g2 * nfv[2 * nf + f];
@@ -129,19 +129,20 @@ __global__ void k_grav_cell(int nc, int nf, const int* __restrict__ cfp, const i
                             const double* __restrict__ vol, const double* __restrict__ gf, double* __restrict__ sg) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
-    const double v = vol[i];
+    // one reciprocal per cell instead of four divisions per face (FP64 division
+    // is the bottleneck here on GB300); agrees with SEMO's x*n*A/V to rounding
+    const double iv = 1.0 / vol[i];
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
         const int e = cfi[k], f = e & kFaceMask;
         const double n0 = fn[f], n1 = fn[nf + f], n2 = fn[2 * nf + f], a = fa[f];
+        const double un = gf[2 * nf + f];
         if (e >> 30) {
-            const double t = gf[nf + f];
-            s0 -= ((t * n0) * a / v); s1 -= ((t * n1) * a / v); s2 -= ((t * n2) * a / v);
-            s3 -= ((t * gf[2 * nf + f]) * a / v);
+            const double w = gf[nf + f] * a * iv;
+            s0 -= w * n0; s1 -= w * n1; s2 -= w * n2; s3 -= w * un;
         } else {
-            const double t = gf[f];
-            s0 += ((t * n0) * a / v); s1 += ((t * n1) * a / v); s2 += ((t * n2) * a / v);
-            s3 += ((t * gf[2 * nf + f]) * a / v);
+            const double w = gf[f] * a * iv;
+            s0 += w * n0; s1 += w * n1; s2 += w * n2; s3 += w * un;
         }
     }
     sg[i] = s0; sg[nc + i] = s1; sg[2 * nc + i] = s2; sg[3 * nc + i] = s3;
@@ -357,12 +358,12 @@ __global__ void k_gg_cell(int nc, int nf, const int* __restrict__ cfp, const int
                           const double* __restrict__ vol, const double* __restrict__ vF, double* __restrict__ g) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
-    const double v = vol[i];
+    const double iv = 1.0 / vol[i];   // one reciprocal per cell, not three divisions per face
     double g0 = 0.0, g1 = 0.0, g2 = 0.0;
     for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
         const int e = cfi[k], f = e & kFaceMask;
-        const double t = vF[f], a = fa[f];
-        const double c0 = t * fn[f] * a / v, c1 = t * fn[nf + f] * a / v, c2 = t * fn[2 * nf + f] * a / v;
+        const double w = vF[f] * fa[f] * iv;
+        const double c0 = w * fn[f], c1 = w * fn[nf + f], c2 = w * fn[2 * nf + f];
         if (e >> 30) { g0 -= c0; g1 -= c1; g2 -= c2; }
         else { g0 += c0; g1 += c1; g2 += c2; }
     }
@@ -454,7 +455,7 @@ void assemble_pressure(semo_ctx* c) {
     if (c->phys.use_gravity) {
         StageScope sc(c, ST_GRAVITY);
         k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
-                                                 c->W, c->rho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
+                                                 c->W, c->irho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
                                                  c->phys.gravity[2], c->fscr);
         SEMO_CHECK_LAUNCH();
         k_grav_cell<<<blocks(nc, T), T, 0, s>>>(nc, nf, c->cf_ptr, c->cf_idx, c->fn, c->fa, c->vol, c->fscr, c->sg);

@@ -294,6 +294,36 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         std::vector<int> own_r(nf), nei_r(std::max(ni, 1));
         for (int f = 0; f < nf; ++f) own_r[f] = iperm[owner[f]];
         for (int f = 0; f < ni; ++f) nei_r[f] = iperm[neighbour[f]];
+        // Faces are stored in an order that follows the RCM cell order
+        // (internal faces by new owner then new neighbour, boundary faces by
+        // new owner inside their patch) so the cell gathers read per-face
+        // arrays coherently.  Cell->face lists keep SEMO's ascending original
+        // face order, so every accumulation order is unchanged.
+        std::vector<int>& fperm = c->fperm;     // fperm[stored] = caller's face index
+        std::vector<int>& fiperm = c->fiperm;
+        fperm.assign(nf, 0);
+        fiperm.assign(nf, 0);
+        {
+            std::vector<int> cnt(nc + 1, 0);
+            for (int f = 0; f < ni; ++f) cnt[own_r[f] + 1]++;
+            for (int i = 0; i < nc; ++i) cnt[i + 1] += cnt[i];
+            std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+            for (int f = 0; f < ni; ++f) fperm[pos[own_r[f]]++] = f;
+            for (int i = 0; i < nc; ++i)
+                std::sort(fperm.begin() + cnt[i], fperm.begin() + cnt[i + 1],
+                          [&](int a, int b) { return nei_r[a] < nei_r[b] || (nei_r[a] == nei_r[b] && a < b); });
+            for (int p = 0; p < n_patches; ++p) {
+                const int b0 = patch_start[p], b1 = b0 + patch_size[p];
+                for (int f = b0; f < b1; ++f) fperm[f] = f;
+                std::stable_sort(fperm.begin() + b0, fperm.begin() + b1,
+                                 [&](int a, int b) { return own_r[a] < own_r[b]; });
+            }
+            for (int k = 0; k < nf; ++k) fiperm[fperm[k]] = k;
+        }
+        std::vector<int> own_n(nf), nei_n(std::max(ni, 1));
+        for (int k = 0; k < nf; ++k) own_n[k] = own_r[fperm[k]];
+        for (int k = 0; k < ni; ++k) nei_n[k] = nei_r[fperm[k]];
+        for (auto& e : cfi) e = fiperm[e & 0x3FFFFFFF] | (e & (1 << 30));
         std::vector<int> rcfp(nc + 1, 0), rcfi(cfi.size()), rstp(nc + 1, 0), rsti(sti.size());
         for (int r = 0; r < nc; ++r) {
             int o = perm[r];
@@ -326,7 +356,7 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
                 int f = fe & 0x3FFFFFFF;
                 if (f >= ni) continue;
                 bool nb_side = (fe >> 30) & 1;
-                acol[d] = nb_side ? own_r[f] : nei_r[f];
+                acol[d] = nb_side ? own_n[f] : nei_n[f];
                 if (nb_side) arl[f] = d; else alr[f] = d;
                 ++d;
             }
@@ -338,8 +368,8 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
 
         // ---- upload ----
         cudaStream_t s = c->stream;
-        c->own.upload(own_r.data(), nf, s);
-        c->nei.upload(nei_r.data(), std::max(ni, 1), s);
+        c->own.upload(own_n.data(), nf, s);
+        c->nei.upload(nei_n.data(), std::max(ni, 1), s);
         c->cf_ptr.upload(rcfp.data(), nc + 1, s);
         c->cf_idx.upload(rcfi.data(), rcfi.size(), s);
         c->st_ptr.upload(rstp.data(), nc + 1, s);
@@ -357,9 +387,17 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         semo::DBuf<double> d_pts;
         semo::DBuf<int> d_fptr, d_fpts;
         d_pts.upload(points, 3 * (size_t)n_points, s);
-        d_fptr.upload(face_ptr, nf + 1, s);
-        d_fpts.upload(face_pts, face_ptr[nf], s);
-        semo::geometry_build(c, d_pts.p, d_fptr.p, d_fpts.p, own_r);
+        {
+            // face point loops in the stored face order
+            std::vector<int> pptr(nf + 1, 0), ppts(face_ptr[nf]);
+            for (int k = 0; k < nf; ++k) pptr[k + 1] = pptr[k] + (face_ptr[fperm[k] + 1] - face_ptr[fperm[k]]);
+            for (int k = 0; k < nf; ++k)
+                std::copy(face_pts + face_ptr[fperm[k]], face_pts + face_ptr[fperm[k] + 1], ppts.begin() + pptr[k]);
+            d_fptr.upload(pptr.data(), nf + 1, s);
+            d_fpts.upload(ppts.data(), ppts.size(), s);
+            SEMO_CUDA(cudaStreamSynchronize(s));   // the host vectors go out of scope
+        }
+        semo::geometry_build(c, d_pts.p, d_fptr.p, d_fpts.p, own_n);
         // field storage
         for (auto* b : {&c->P, &c->U, &c->V, &c->W, &c->VF, &c->rho, &c->irho, &c->x}) b->alloc(nc, s);
         c->grad.alloc(15 * (size_t)nc, s);
@@ -493,8 +531,8 @@ semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t c
             std::vector<double> tmp((size_t)len * planes);
             SEMO_CUDA(cudaMemcpyAsync(tmp.data(), d, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, c->stream));
             SEMO_CUDA(cudaStreamSynchronize(c->stream));
-            for (int64_t f = 0; f < len; ++f)
-                for (int q = 0; q < planes; ++q) out[f * planes + q] = tmp[(size_t)q * len + f];
+            for (int64_t f = 0; f < len; ++f)   // back to the caller's face order
+                for (int q = 0; q < planes; ++q) out[f * planes + q] = tmp[(size_t)q * len + c->fiperm[f]];
         };
         const char* grads[5] = {"grad_P", "grad_U", "grad_V", "grad_W", "grad_VF"};
         for (int g = 0; g < 5; ++g)

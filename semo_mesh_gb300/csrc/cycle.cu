@@ -74,7 +74,7 @@ struct CsrView {
 };
 
 // SELL-32: slice s holds rows 32s..32s+31; entry j of row 32s+l at
-// sptr[s] + 32j + l; padding entries point at the row itself with value 0.
+// sptr[s] + 32j + l; padding entries point at column 0 with value 0.
 template <class V>
 struct SellView {
     static constexpr int kVS = 1;
@@ -181,8 +181,8 @@ __global__ void __launch_bounds__(256) k_post1(M A, const V* __restrict__ dinv, 
 }
 // finest-level post-smoothing step 1 (SELL), also folding in the CG dots
 // z.r and z.q (q = A p of the previous iteration); grid-stride, fixed grid
-template <class V>
-__global__ void __launch_bounds__(kRedThreads) k_post1_dots(SellView<V> A, const V* __restrict__ dinv,
+template <class M, class V>
+__global__ void __launch_bounds__(kRedThreads) k_post1_dots(M A, const V* __restrict__ dinv,
                                                             const V* __restrict__ b, V c1, V c2,
                                                             const V* __restrict__ y, const V* __restrict__ d,
                                                             V* __restrict__ z, const double* __restrict__ r,
@@ -190,13 +190,16 @@ __global__ void __launch_bounds__(kRedThreads) k_post1_dots(SellView<V> A, const
                                                             double* __restrict__ part) {
     __shared__ double sh[32];
     double zr = 0.0, zq = 0.0;
-    const int stride = gridDim.x * blockDim.x;
-    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += stride) {
-        const V s = A.dot(row, 0, Vec<V, V>{y});
-        const V zi = y[row] + c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
-        z[row] = zi;
-        zr += (double)zi * r[row];
-        zq += (double)zi * q[row];
+    const int per_block = blockDim.x / M::kVS, lane = threadIdx.x % M::kVS;
+    for (int row0 = blockIdx.x * per_block; row0 < A.n; row0 += gridDim.x * per_block) {
+        const int row = row0 + threadIdx.x / M::kVS;   // every lane runs the dot's shuffles
+        const V s = A.dot(row, lane, Vec<V, V>{y});
+        if (row < A.n && lane == 0) {
+            const V zi = y[row] + c1 * d[row] + c2 * (dinv[row] * (b[row] - s));
+            z[row] = zi;
+            zr += (double)zi * r[row];
+            zq += (double)zi * q[row];
+        }
     }
     zr = block_sum(zr, sh);
     zq = block_sum(zq, sh);
@@ -366,11 +369,11 @@ __global__ void k_sell_fill(int n, const int* __restrict__ ptr, const int* __res
     const int sl = row >> 5, l = row & 31;
     const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
     const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
-    const int self = (row < n) ? row : 0;
     for (int j = 0; j < w; ++j) {
         const int k = b + 32 * j + l;
+        // padding reads column 0, which exists for every operator (P and R are not square)
         if (j < len) { scol[k] = col[rb + j]; sval[k] = (W)val[rb + j]; }
-        else { scol[k] = self; sval[k] = W(0); }
+        else { scol[k] = 0; sval[k] = W(0); }
     }
 }
 
@@ -433,11 +436,26 @@ ChebCoef cheb2(double lam) {
     return ChebCoef{1.0 / theta, rho1 * rho0, 2.0 * rho1 / delta};
 }
 
-// Everything the V-cycle needs beyond the hierarchy: the finest level in SELL.
+// Everything the V-cycle needs beyond the hierarchy: SELL copies of the
+// operators of every level big enough for them to pay (small coarse levels
+// are launch-latency bound and stay CSR).
+constexpr int kSellMinRows = 4096;
+template <class V>
+struct LevelMats {
+    Sell<V> A, P, R;
+    bool a = false, p = false, r = false;
+};
 template <class V>
 struct Cycle {
-    Sell<V> fine;
+    std::vector<LevelMats<V>> lev;
 };
+
+// run f on the SELL view of a level operator if it has one, else on CSR
+template <class V, class F>
+void with_op(const Sell<V>& S, bool use_sell, const DCsr<V>& M, F&& f) {
+    if (use_sell) f(S.view());
+    else with_csr(M, f);
+}
 
 template <class V>
 void chebyshev_generic(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_start) {
@@ -472,9 +490,9 @@ void chebyshev_generic(cudaStream_t s, AmgLevel<V>& L, int degree, bool zero_sta
     }
 }
 
-// V-cycle below the finest level (CSR levels), input L.b, output L.x
+// V-cycle from level l down, input L.b, output L.x
 template <class V>
-void vcycle_csr(semo_ctx* c, Amg<V>& h, int l) {
+void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     cudaStream_t s = c->stream;
     AmgLevel<V>& L = h.lev[l];
     if (l == (int)h.lev.size() - 1) {
@@ -482,33 +500,37 @@ void vcycle_csr(semo_ctx* c, Amg<V>& h, int l) {
         SEMO_CHECK_LAUNCH();
         return;
     }
+    const LevelMats<V>& M = cy.lev[l];
     const int degree = c->prm.cheb_degree;
     const ChebCoef cc = cheb2(L.lam_max);
     if (degree == 2) {
-        with_csr(L.A, [&](auto M) {
-            k_pre2<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
+        with_op(M.A, M.a, L.A, [&](auto A) {
+            k_pre2<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
         });
+        SEMO_CHECK_LAUNCH();
     } else {
         chebyshev_generic(s, L, degree, true);
     }
-    SEMO_CHECK_LAUNCH();
-    with_csr(L.A, [&](auto M) { k_res<<<grid_for(M), 256, 0, s>>>(M, L.x.p, L.b.p, L.r.p); });
+    with_op(M.A, M.a, L.A, [&](auto A) { k_res<<<grid_for(A), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p); });
     SEMO_CHECK_LAUNCH();
     AmgLevel<V>& C = h.lev[l + 1];
-    with_csr(L.R, [&](auto M) { k_mv<<<grid_for(M), 256, 0, s>>>(M, L.r.p, C.b.p); });
+    with_op(M.R, M.r, L.R, [&](auto R) { k_mv<<<grid_for(R), 256, 0, s>>>(R, L.r.p, C.b.p); });
     SEMO_CHECK_LAUNCH();
-    vcycle_csr(c, h, l + 1);
-    with_csr(L.P, [&](auto M) { k_prolong_add<<<grid_for(M), 256, 0, s>>>(M, C.x.p, L.x.p); });
+    vcycle_from(c, h, cy, l + 1);
+    with_op(M.P, M.p, L.P, [&](auto P) { k_prolong_add<<<grid_for(P), 256, 0, s>>>(P, C.x.p, L.x.p); });
     SEMO_CHECK_LAUNCH();
     if (degree == 2) {
-        with_csr(L.A, [&](auto M) {
-            k_post0<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
+        with_op(M.A, M.a, L.A, [&](auto A) {
+            k_post0<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
         });
         SEMO_CHECK_LAUNCH();
-        with_csr(L.A, [&](auto M) {
-            k_post1<<<grid_for(M), 256, 0, s>>>(M, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
-        });
-        SEMO_CHECK_LAUNCH();
+        if (l > 0) {
+            with_op(M.A, M.a, L.A, [&](auto A) {
+                k_post1<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
+            });
+            SEMO_CHECK_LAUNCH();
+        }
+        // on the finest level the last step is fused with the CG dot products (cg_iteration)
     } else {
         chebyshev_generic(s, L, degree, false);
     }
@@ -541,25 +563,15 @@ void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& oute
         SEMO_CHECK_LAUNCH();
     } else if (degree == 2) {
         const ChebCoef cc = cheb2(L.lam_max);
-        const SellView<V> A = cy.fine.view();
-        k_pre2<<<blocks(n, 256), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
-        SEMO_CHECK_LAUNCH();
-        k_res<<<blocks(n, 256), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p);
-        SEMO_CHECK_LAUNCH();
-        AmgLevel<V>& C = h.lev[1];
-        with_csr(L.R, [&](auto M) { k_mv<<<grid_for(M), 256, 0, s>>>(M, L.r.p, C.b.p); });
-        SEMO_CHECK_LAUNCH();
-        vcycle_csr(c, h, 1);
-        with_csr(L.P, [&](auto M) { k_prolong_add<<<grid_for(M), 256, 0, s>>>(M, C.x.p, L.x.p); });
-        SEMO_CHECK_LAUNCH();
-        k_post0<<<blocks(n, 256), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
-        SEMO_CHECK_LAUNCH();
+        vcycle_from(c, h, cy, 0);   // everything but the last smoothing step of the finest level
         // z lands in L.x; z.r and z.q folded in
-        k_post1_dots<V><<<kRedBlocks, kRedThreads, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p,
-                                                           L.x.p, r, q, R.part);
+        with_op(cy.lev[0].A, cy.lev[0].a, L.A, [&](auto A) {
+            k_post1_dots<<<kRedBlocks, kRedThreads, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p,
+                                                            L.x.p, r, q, R.part);
+        });
         SEMO_CHECK_LAUNCH();
     } else {
-        vcycle_csr(c, h, 0);
+        vcycle_from(c, h, cy, 0);
         k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L.x.p, r, q, R.part);
         SEMO_CHECK_LAUNCH();
     }
@@ -684,8 +696,19 @@ ApplyState& apply_state(semo_ctx* c) {
 
 template <class V>
 void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
-    AmgLevel<V>& L = h.lev[0];
-    build_sell<V, V>(c->stream, L.A.ptr, L.A.col, L.A.val, L.A.n, cy.fine);
+    cudaStream_t s = c->stream;
+    const int nl = (int)h.lev.size();
+    cy.lev.resize(std::max(nl - 1, 0));
+    for (int l = 0; l + 1 < nl; ++l) {
+        AmgLevel<V>& L = h.lev[l];
+        LevelMats<V>& M = cy.lev[l];
+        M.a = L.A.n >= kSellMinRows;
+        M.p = L.P.n >= kSellMinRows;
+        M.r = L.R.n >= kSellMinRows;
+        if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
+        if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
+        if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R);
+    }
 }
 
 }  // namespace

@@ -124,6 +124,7 @@ struct semo_ctx {
     int np = 0, nf = 0, ni = 0, nc = 0, nb = 0, npatch = 0;
     int64_t nnz = 0, st_nnz = 0, cf_nnz = 0;
     std::vector<int> perm, iperm;                 // RCM
+    std::vector<int> fperm, fiperm;               // stored face order: fperm[stored] = caller's face
     std::vector<int> patch_start, patch_size;
     std::vector<int> h_bc_type;                   // npatch*3
     std::vector<double> h_bc_value;               // npatch*5
