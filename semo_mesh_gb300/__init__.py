@@ -200,9 +200,14 @@ class Context:
         self.set_physics(case)
         self.set_fields(case.P, case.U, case.V, case.W, case.VF)
 
-    def fields(self) -> dict:
+    def fields(self, out: dict | None = None) -> dict:
+        """P, U, V, W in the caller's cell order (into `out`'s arrays if given, e.g. pinned buffers)."""
         n = self.n_cells
-        out = {k: np.empty(n) for k in ("P", "U", "V", "W")}
+        if out is None:
+            out = {k: np.empty(n) for k in ("P", "U", "V", "W")}
+        for k in ("P", "U", "V", "W"):
+            if out[k].dtype != np.float64 or not out[k].flags.c_contiguous or out[k].shape != (n,):
+                raise ValueError(f"output array {k} must be contiguous float64 of length {n}")
         ptrs = [out[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("P", "U", "V", "W")]
         self._check(self.L.semo_get_fields(self.h, *ptrs))
         return out

@@ -429,9 +429,66 @@ __global__ void k_finish2(const double* __restrict__ part, double* __restrict__ 
     if (threadIdx.x == 0) { out[0] = a; out[1] = b; }
 }
 
+// caller order <-> RCM order for up to 5 cell planes
+struct Planes5 {
+    double* p[5];
+};
+struct CPlanes5 {
+    const double* p[5];
+};
+__global__ void k_from_caller(int nc, int planes, const int* __restrict__ perm, const double* __restrict__ src,
+                              Planes5 dst, int* __restrict__ bad) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nc) return;
+    const int o = perm[r];
+    bool ok = true;
+    for (int q = 0; q < planes; ++q) {
+        const double v = src[(size_t)q * nc + o];
+        ok &= isfinite(v);
+        dst.p[q][r] = v;
+    }
+    if (!ok) atomicExch(bad, 1);
+}
+__global__ void k_to_caller(int nc, int planes, const int* __restrict__ perm, CPlanes5 src,
+                            double* __restrict__ dst) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nc) return;
+    const int o = perm[r];
+    for (int q = 0; q < planes; ++q) dst[(size_t)q * nc + o] = src.p[q][r];
+}
+__global__ void k_cell_product(int nc, const double* __restrict__ a, const double* __restrict__ b,
+                               double* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nc) out[r] = a[r] * b[r];
+}
+
 }  // namespace
 
 namespace semo {
+
+bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes) {
+    Planes5 d{};
+    for (int q = 0; q < planes; ++q) d.p[q] = dst[q];
+    SEMO_CUDA(cudaMemsetAsync(c->flag.p + 8, 0, sizeof(int), c->stream));
+    k_from_caller<<<blocks(c->nc, 256), 256, 0, c->stream>>>(c->nc, planes, c->dperm, src, d, c->flag.p + 8);
+    SEMO_CHECK_LAUNCH();
+    int bad = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&bad, c->flag.p + 8, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SEMO_CUDA(cudaStreamSynchronize(c->stream));
+    return bad == 0;
+}
+
+void cellwise_product(semo_ctx* c, const double* a, const double* b, double* out) {
+    k_cell_product<<<blocks(c->nc, 256), 256, 0, c->stream>>>(c->nc, a, b, out);
+    SEMO_CHECK_LAUNCH();
+}
+
+void fields_to_caller_order(semo_ctx* c, const double* const* src, double* dst, int planes) {
+    CPlanes5 s{};
+    for (int q = 0; q < planes; ++q) s.p[q] = src[q];
+    k_to_caller<<<blocks(c->nc, 256), 256, 0, c->stream>>>(c->nc, planes, c->dperm, s, dst);
+    SEMO_CHECK_LAUNCH();
+}
 
 void assemble_face_values(semo_ctx* c) {
     const int T = 256;

@@ -368,6 +368,7 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
 
         // ---- upload ----
         cudaStream_t s = c->stream;
+        c->dperm.upload(perm.data(), nc, s);
         c->own.upload(own_n.data(), nf, s);
         c->nei.upload(nei_n.data(), std::max(ni, 1), s);
         c->cf_ptr.upload(rcfp.data(), nc + 1, s);
@@ -445,14 +446,6 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
     });
 }
 
-static void upload_permuted(semo_ctx* c, const double* h, semo::DBuf<double>& d, std::vector<double>& tmp) {
-    const int n = c->nc;
-    tmp.resize(n);
-    for (int r = 0; r < n; ++r) tmp[r] = h[c->perm[r]];
-    SEMO_CUDA(cudaMemcpyAsync(d.p, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    SEMO_CUDA(cudaStreamSynchronize(c->stream));
-}
-
 static void download_permuted(semo_ctx* c, const double* d, double* h, int planes = 1, bool interleave = false) {
     const int n = c->nc;
     std::vector<double> tmp((size_t)n * planes);
@@ -465,19 +458,23 @@ static void download_permuted(semo_ctx* c, const double* d, double* h, int plane
         }
 }
 
+// Fields cross the boundary in the caller's cell order: the host arrays are
+// copied as they are (a DMA straight from pinned memory when the caller's
+// buffers are pinned) and reordered and checked on the GPU.
 semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const double* V, const double* W,
                             const double* VF) {
     return guarded(c, [&] {
         need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
         need(P && U && V && W && VF, SEMO_ERR_ARGUMENT, "null field");
-        for (const double* a : {P, U, V, W, VF})
-            for (int i = 0; i < c->nc; ++i) need(std::isfinite(a[i]), SEMO_ERR_NAN, "non-finite input field value");
-        std::vector<double> tmp;
-        upload_permuted(c, P, c->P, tmp);
-        upload_permuted(c, U, c->U, tmp);
-        upload_permuted(c, V, c->V, tmp);
-        upload_permuted(c, W, c->W, tmp);
-        upload_permuted(c, VF, c->VF, tmp);
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        const double* src[5] = {P, U, V, W, VF};
+        for (int q = 0; q < 5; ++q)
+            SEMO_CUDA(cudaMemcpyAsync(c->stage.p + q * n, src[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        double* dst[5] = {c->P.p, c->U.p, c->V.p, c->W.p, c->VF.p};
+        if (!semo::fields_from_caller_order(c, c->stage.p, dst, 5))
+            throw Error(SEMO_ERR_NAN, "non-finite input field value");
         c->fields_ready = true;
         c->assembled = false;
     });
@@ -486,10 +483,16 @@ semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const
 semo_status semo_get_fields(semo_ctx* c, double* P, double* U, double* V, double* W) {
     return guarded(c, [&] {
         need(c->fields_ready, SEMO_ERR_STATE, "no fields set");
-        if (P) download_permuted(c, c->P, P);
-        if (U) download_permuted(c, c->U, U);
-        if (V) download_permuted(c, c->V, V);
-        if (W) download_permuted(c, c->W, W);
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        const double* src[4] = {c->P.p, c->U.p, c->V.p, c->W.p};
+        semo::fields_to_caller_order(c, src, c->stage.p, 4);
+        double* dst[4] = {P, U, V, W};
+        for (int q = 0; q < 4; ++q)
+            if (dst[q])
+                SEMO_CUDA(cudaMemcpyAsync(dst[q], c->stage.p + q * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
     });
 }
 
@@ -568,7 +571,13 @@ semo_status semo_solve_pressure(semo_ctx* c, double* x, semo_solve_info* info) {
         semo_solve_info inf{};
         semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
         if (info) *info = inf;
-        if (x) download_permuted(c, c->x.p, x);
+        if (x) {
+            c->stage.alloc(5 * (size_t)c->nc, c->stream);
+            const double* src[1] = {c->x.p};
+            semo::fields_to_caller_order(c, src, c->stage.p, 1);
+            SEMO_CUDA(cudaMemcpyAsync(x, c->stage.p, sizeof(double) * c->nc, cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        }
         if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
     });
     if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
@@ -675,10 +684,16 @@ semo_status semo_set_source(semo_ctx* c, const double* src) {
     return guarded(c, [&] {
         need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
         if (!src) { c->has_src = false; c->assembled = false; return; }
-        for (int i = 0; i < c->nc; ++i) need(std::isfinite(src[i]), SEMO_ERR_NAN, "non-finite source");
-        c->src.alloc(c->nc, c->stream);
-        std::vector<double> tmp;
-        upload_permuted(c, src, c->src, tmp);
+        const size_t n = (size_t)c->nc;
+        c->src.alloc(n, c->stream);
+        c->stage.alloc(5 * n, c->stream);
+        SEMO_CUDA(cudaMemcpyAsync(c->stage.p, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        double* dst[1] = {c->src.p};
+        if (!semo::fields_from_caller_order(c, c->stage.p, dst, 1)) {
+            c->has_src = false;
+            c->assembled = false;
+            throw Error(SEMO_ERR_NAN, "non-finite source");
+        }
         c->has_src = true;
         c->assembled = false;
     });
@@ -690,22 +705,26 @@ semo_status semo_vjp_source(semo_ctx* c, const double* dJ_dx, double* lambda, do
         need(c->assembled, SEMO_ERR_STATE, "no assembled system: run a forward pass first");
         need(dJ_dx != nullptr, SEMO_ERR_ARGUMENT, "null dJ/dx");
         SEMO_CUDA(cudaSetDevice(c->device));
-        const int n = c->nc;
-        semo::DBuf<double> g, lam, out;
-        g.alloc(n, c->stream);
-        lam.alloc(n, c->stream);
-        std::vector<double> tmp;
-        upload_permuted(c, dJ_dx, g, tmp);
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        semo::DBuf<double> g, lam, djds;
+        g.alloc(n, s);
+        lam.alloc(n, s);
+        djds.alloc(n, s);
+        c->stage.alloc(5 * n, s);
+        SEMO_CUDA(cudaMemcpyAsync(c->stage.p, dJ_dx, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        double* gdst[1] = {g.p};
+        if (!semo::fields_from_caller_order(c, c->stage.p, gdst, 1)) throw Error(SEMO_ERR_NAN, "non-finite dJ/dx");
         semo_solve_info inf{};
         semo::solve_transpose_reuse(c, g.p, lam.p, &inf);
         if (info) *info = inf;
-        if (lambda) download_permuted(c, lam.p, lambda);
-        if (dJ_ds) {
-            std::vector<double> l(n), v(n);
-            download_permuted(c, lam.p, l.data());
-            download_permuted(c, c->vol.p, v.data());
-            for (int i = 0; i < n; ++i) dJ_ds[i] = l[i] * v[i];
-        }
+        // dJ/ds_i = V_i lambda_i (s enters the right-hand side as s_i V_i)
+        semo::cellwise_product(c, lam.p, c->vol.p, djds.p);
+        const double* src[2] = {lam.p, djds.p};
+        semo::fields_to_caller_order(c, src, c->stage.p, 2);
+        if (lambda) SEMO_CUDA(cudaMemcpyAsync(lambda, c->stage.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        if (dJ_ds) SEMO_CUDA(cudaMemcpyAsync(dJ_ds, c->stage.p + n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
         if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
     });
     if (st == SEMO_OK && conv != SEMO_OK) c->err = "adjoint solve did not reach the tolerance";

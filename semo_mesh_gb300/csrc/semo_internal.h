@@ -158,6 +158,8 @@ struct semo_ctx {
     semo::DBuf<double> unf;                       // UnF per face
     semo::DBuf<double> x, gx;                     // solution and its Gauss-Green gradient (3 planes)
     semo::DBuf<double> src;                       // optional per-cell source s (b_i += s_i V_i)
+    semo::DBuf<double> stage;                     // caller-order staging for field copies (5 planes)
+    semo::DBuf<int> dperm;                        // RCM permutation on the device: dperm[r] = caller's cell
     bool has_src = false;
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
@@ -237,6 +239,12 @@ void geometry_build(semo_ctx* c, const double* d_points, const int* d_fptr, cons
 void assemble_pressure(semo_ctx* c);
 double pressure_update(semo_ctx* c);
 void assemble_face_values(semo_ctx* c);
+// dst[q][r] = src[q*n + perm[r]] for q < planes; false if any value is not finite (syncs)
+bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes);
+// dst[q*n + perm[r]] = src[q][r] for q < planes (async)
+void fields_to_caller_order(semo_ctx* c, const double* const* src, double* dst, int planes);
+// out[i] = a[i] * b[i] over the cells (async)
+void cellwise_product(semo_ctx* c, const double* a, const double* b, double* out);
 
 // amg_setup.cu: smoothed-aggregation hierarchy (value type float or double)
 template <class V>
