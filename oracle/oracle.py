@@ -49,6 +49,11 @@ def lib():
         L.orc_solve.argtypes = [vp, C.c_int, C.c_double, C.c_int, vp]
         L.orc_update.restype = C.c_double
         L.orc_update.argtypes = [vp, vp]
+        L.orc_assemble_momentum.argtypes = [vp]
+        L.orc_solve_momentum.restype = C.c_int
+        L.orc_solve_momentum.argtypes = [vp, C.c_int, C.c_double, C.c_int, vp, vp]
+        L.orc_update_momentum.restype = C.c_double
+        L.orc_update_momentum.argtypes = [vp, vp, vp, vp]
         L.orc_num_threads.restype = C.c_int
     return _lib
 
@@ -104,9 +109,12 @@ class Oracle:
         prm[:12] = [case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
                     case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf, case.pre_u_urf,
                     1.0 if case.use_gravity else 0.0]
+        prm[12] = case.mom_u_urf
         lib().orc_set_case(self.h, _p(bt), _p(bv), _p(prm))
         for nm in ("P", "U", "V", "W", "VF"):
             self.set(nm, getattr(case, nm))
+        for nm, a in zip(("oldU", "oldV", "oldW", "old2U", "old2V", "old2W"), case.history()):
+            self.set(nm, a)
 
     def assemble(self) -> None:
         lib().orc_assemble_pressure(self.h)
@@ -127,6 +135,33 @@ class Oracle:
     def update(self, x: np.ndarray) -> float:
         xa = np.ascontiguousarray(x, dtype=np.float64)
         return float(lib().orc_update(self.h, _p(xa)))
+
+    def assemble_momentum(self) -> None:
+        """calcMomentumEqs assembly: COO (mom_A_*), CSR (mom_csr_*), RHS planes mom_B."""
+        lib().orc_assemble_momentum(self.h)
+
+    def solve_momentum(self, tol: float = 1e-9, maxiter: int = 1000) -> dict:
+        """Jacobi-BiCGStab on each of the three right-hand sides (x0 = 0)."""
+        n = self.mesh.n_cells
+        xs, its, res = [], [], []
+        for j in range(3):
+            x = np.empty(n)
+            rr = np.zeros(1)
+            its.append(int(lib().orc_solve_momentum(self.h, j, tol, maxiter, _p(x), _p(rr))))
+            xs.append(x)
+            res.append(float(rr[0]))
+        return {"x": xs, "iters": its, "rel_res": res}
+
+    def update_momentum(self, xs) -> float:
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in xs]
+        return float(lib().orc_update_momentum(self.h, _p(a[0]), _p(a[1]), _p(a[2])))
+
+    def momentum_pass(self, tol: float = 1e-9) -> dict:
+        """One calcMomentumEqs: assemble, solve the three components, update U, V, W."""
+        self.assemble_momentum()
+        sol = self.solve_momentum(tol)
+        sol["norm"] = self.update_momentum(sol["x"])
+        return sol
 
     def pressure_pass(self, case, tol: float = 1e-8) -> dict:
         """One full calcPressureEq: assemble, solve, Gauss-Green, update."""

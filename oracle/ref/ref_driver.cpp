@@ -7,9 +7,12 @@
 // SEMO's loader and initialiser do (src/load/loadOpenFoam.cpp:356-374,
 // src/solvers/build.cpp:5-41, src/controls/build.cpp:626+) and calls the
 // reference functions in the order of one pressure-correction pass of
-// src/solvers/pressureBased.cpp:17-31, :139-141, :211-212.
+// src/solvers/pressureBased.cpp:17-31, :139-141, :211-212.  With case flag 2
+// the pass is a whole outer iteration instead: cell transport, then the
+// momentum equation (:201-202) followed by the pressure correction (:211-212),
+// with old and second-old velocities read from the case.
 //
-// usage: semo_ref <case.bin> <out.bin> [flags]
+// usage: semo_ref <case.bin> <out.bin>
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -32,6 +35,13 @@ struct CapturedSystem {
     int calls = 0;
 };
 CapturedSystem g_captured;
+struct CapturedMomentum {
+    vector<int> rows, cols;
+    vector<double> vals, b[3], x[3];
+    double solve_seconds = 0.0;
+    int calls = 0;
+};
+CapturedMomentum g_momentum;
 
 // Called from ref_capture.cpp: forwards to the reference's real solver.
 void semo_ref_forward_solve(const string& eq, SEMO_Mesh_Builder& mesh, int B_n,
@@ -42,6 +52,16 @@ void semo_ref_forward_solve(const string& eq, SEMO_Mesh_Builder& mesh, int B_n,
     solver.solveAMGCL(eq, mesh, B_n, r, c, v, b, x);
     auto t1 = chrono::steady_clock::now();
     g_captured.solve_seconds += chrono::duration<double>(t1 - t0).count();
+}
+void semo_ref_forward_solve3(const string& eq, SEMO_Mesh_Builder& mesh, int B_n,
+                             vector<int>& r, vector<int>& c, vector<double>& v,
+                             vector<double>& b0, vector<double>& b1, vector<double>& b2,
+                             vector<double>& x0, vector<double>& x1, vector<double>& x2) {
+    SEMO_Solvers_Builder solver;
+    auto t0 = chrono::steady_clock::now();
+    solver.solveAMGCL(eq, mesh, B_n, r, c, v, b0, b1, b2, x0, x1, x2);
+    auto t1 = chrono::steady_clock::now();
+    g_momentum.solve_seconds += chrono::duration<double>(t1 - t0).count();
 }
 
 static FILE* g_out = nullptr;
@@ -78,6 +98,10 @@ int main(int argc, char** argv) {
     vector<double> P(nc), U(nc), V(nc), W(nc), VF(nc);
     rd(f, P.data(), nc); rd(f, U.data(), nc); rd(f, V.data(), nc); rd(f, W.data(), nc); rd(f, VF.data(), nc);
     double prm[16]; rd(f, prm, 16);
+    // flag 2: old (n-1) and second-old (n-2) velocities for the BDF2 term
+    vector<double> old[6];
+    if (flags & 2)
+        for (int k = 0; k < 6; ++k) { old[k].resize(nc); rd(f, old[k].data(), nc); }
     fclose(f);
 
     // ---- species (two incompressible phases; VF[0] is the first) -------
@@ -91,6 +115,10 @@ int main(int argc, char** argv) {
     controls.gravityAcceleration = {prm[6], prm[7], prm[8]};
     controls.prePreURF = prm[9];
     controls.preVelURF = prm[10];
+    controls.momVelURF = prm[12];
+    controls.turbType = "laminar";
+    controls.oldTimeStep = controls.timeStep;
+    controls.old2TimeStep = controls.timeStep;
     controls.minP = -1e300; controls.maxP = 1e300;
     controls.minU = -1e300; controls.maxU = 1e300;
     controls.minV = -1e300; controls.maxV = 1e300;
@@ -145,9 +173,14 @@ int main(int argc, char** argv) {
         auto& c = mesh.cells[i];
         c.var[controls.P] = P[i]; c.var[controls.U] = U[i]; c.var[controls.V] = V[i];
         c.var[controls.W] = W[i]; c.var[controls.VF[0]] = VF[i]; c.var[controls.kappa] = 0.0;
+        if (flags & 2) {
+            c.var[controls.oldU] = old[0][i]; c.var[controls.oldV] = old[1][i]; c.var[controls.oldW] = old[2][i];
+            c.var[controls.Qm[0]] = old[3][i]; c.var[controls.Qm[1]] = old[4][i]; c.var[controls.Qm[2]] = old[5][i];
+        }
     }
     auto t0 = chrono::steady_clock::now();
     solver.calcIncomCellEOSVF(mesh, controls, species);
+    if (flags & 2) solver.calcCellTransport(mesh, controls, species);
     solver.setIncomValuesLeftRightFace(mesh, controls, species);
     solver.setCellVarMinMax(mesh, controls.VF[0], controls.maximumVF[0], controls.minimumVF[0]);
     if (flags & 1) solver.calcSourceGravity(mesh, controls, species);
@@ -201,6 +234,39 @@ int main(int argc, char** argv) {
         put("CRS_dig", mesh.CRS_col_ptr_dig); put("CRS_LR", mesh.CRS_col_ptr_LR); put("CRS_RL", mesh.CRS_col_ptr_RL);
     }
 
+    // momentum equation (outer iteration only) ---------------------------
+    double tmom = 0.0;
+    if (flags & 2) {
+        vector<double> mu(nc);
+        for (int i = 0; i < nc; ++i) mu[i] = mesh.cells[i].var[controls.mu];
+        put("mu", mu);
+        auto m0 = chrono::steady_clock::now();
+        solver.setIncomValuesLeftRightFace(mesh, controls, species);
+        double mnorm = solver.calcMomentumEqs(mesh, controls, species);
+        auto m1 = chrono::steady_clock::now();
+        tmom = chrono::duration<double>(m1 - m0).count();
+        vector<double> g(3 * nc);
+        const int tgt[5] = {controls.P, controls.U, controls.V, controls.W, controls.VF[0]};
+        const char* gname[5] = {"mom_grad_P", "mom_grad_U", "mom_grad_V", "mom_grad_W", "mom_grad_VF"};
+        for (int t = 0; t < 5; ++t) {
+            for (int i = 0; i < nc; ++i) for (int k = 0; k < 3; ++k) g[3 * i + k] = mesh.cellsGradientVar[tgt[t]][i][k];
+            put(gname[t], g);
+        }
+        vector<double> mmp(2 * nc), un(nc), vn(nc), wn(nc);
+        for (int i = 0; i < nc; ++i) {
+            auto& c = mesh.cells[i];
+            mmp[2 * i] = c.var[controls.maximumP]; mmp[2 * i + 1] = c.var[controls.minimumP];
+            un[i] = c.var[controls.U]; vn[i] = c.var[controls.V]; wn[i] = c.var[controls.W];
+        }
+        put("mom_minmax_p", mmp);
+        put("mom_A_rows", g_momentum.rows); put("mom_A_cols", g_momentum.cols); put("mom_A_vals", g_momentum.vals);
+        put("mom_B0", g_momentum.b[0]); put("mom_B1", g_momentum.b[1]); put("mom_B2", g_momentum.b[2]);
+        put("mom_x0", g_momentum.x[0]); put("mom_x1", g_momentum.x[1]); put("mom_x2", g_momentum.x[2]);
+        put("mom_U_new", un); put("mom_V_new", vn); put("mom_W_new", wn);
+        put("mom_norm", &mnorm, 1);
+        solver.setIncomValuesLeftRightFace(mesh, controls, species);
+    }
+
     // pressure-correction equation ---------------------------------------
     auto t2 = chrono::steady_clock::now();
     double norm = solver.calcPressureEq(mesh, controls, species, 1);
@@ -243,6 +309,10 @@ int main(int argc, char** argv) {
             chrono::duration<double>(t5 - t4).count(),                       // RCM
             (double)g_captured.calls};
         put("timings", tm, 5);
+        if (flags & 2) {
+            double tmm[2] = {tmom - g_momentum.solve_seconds, g_momentum.solve_seconds};
+            put("mom_timings", tmm, 2);
+        }
     }
     fclose(g_out);
     return 0;

@@ -27,7 +27,7 @@
 #include <omp.h>
 #endif
 
-#define ORC_MAX_ARR 96
+#define ORC_MAX_ARR 192
 
 typedef struct {
     char name[32];
@@ -43,7 +43,7 @@ typedef struct {
     /* bc per patch: type p/u/vf and values p,u,v,w,vf */
     int* bct; double* bcv;
     /* parameters */
-    double dt, rho0, rho1, urf_p, urf_u, g[3];
+    double dt, rho0, rho1, mu0, mu1, urf_p, urf_u, urf_mom, g[3];
     int use_gravity;
     double minP, maxP, minU, maxU, minV, maxV, minW, maxW;
     /* registry of named arrays (owned) */
@@ -507,7 +507,8 @@ void orc_destroy(orc_ctx* c) {
 void orc_set_case(orc_ctx* c, const int* bct, const double* bcv, const double* prm) {
     memcpy(c->bct, bct, sizeof(int) * 3 * c->npatch);
     memcpy(c->bcv, bcv, sizeof(double) * 5 * c->npatch);
-    c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2];
+    c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2]; c->mu0 = prm[3]; c->mu1 = prm[4];
+    c->urf_mom = prm[12];
     c->g[0] = prm[6]; c->g[1] = prm[7]; c->g[2] = prm[8];
     c->urf_p = prm[9]; c->urf_u = prm[10]; c->use_gravity = prm[11] != 0.0;
 }
@@ -1221,4 +1222,301 @@ int orc_num_threads(void) {
 #else
     return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* momentum equation: src/solvers/transport.cpp:9-98 (calcCellTransport,      */
+/* laminar), src/solvers/reconIncom.cpp:501-545, :1015-1030 (face viscosity),  */
+/* src/solvers/eqMomentum.cpp:9-1122 (calcMomentumEqs, 3-argument overload):   */
+/* BDF2 diagonal and RHS :223-326, internal faces :331-787, boundary faces     */
+/* :795-1008, update + norm :1029-1119.  COO order: N diagonals, then per      */
+/* internal face (LR, RL), each left out when |a| < DBL_MIN (:699-711).        */
+/* Old (n-1) and second-old (n-2) velocities come from arrays oldU/V/W and     */
+/* old2U/V/W; absent, they default to the current velocity.                    */
+/* ------------------------------------------------------------------------ */
+static double* hist(orc_ctx* c, const char* name, const double* cur) {
+    double* p = dget(c, name);
+    return p ? p : (double*)cur;
+}
+
+void orc_assemble_momentum(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    face_values(c);
+    gravity_source(c);
+    double *P = dget(c, "P"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *VF = dget(c, "VF");
+    double *rho = dget(c, "rho"), *sg = dget(c, "src_grav"), *vol = dget(c, "cell_vol");
+    /* calcCellTransport: mu = VF mu0 + (1 - VF) mu1 on the clamped VF */
+    double* mu = dreg(c, "mu", nc);
+    for (int i = 0; i < nc; ++i) {
+        double t = 0.0; t += VF[i];
+        double v1 = 1.0 - t;
+        double m = 0.0; m += VF[i] * c->mu0; m += v1 * c->mu1;
+        m += 0.0;                                   /* muT, laminar */
+        mu[i] = m;
+    }
+    /* stencil min/max of P, U, V, W (eqMomentum.cpp:40-43) */
+    double* mmp = dreg(c, "mom_minmax_p", 2LL * nc);
+    double* mm = dreg(c, "mom_minmax_uvw", 6LL * nc);
+    double *t1 = (double*)malloc(sizeof(double) * nc), *t2 = (double*)malloc(sizeof(double) * nc);
+    minmax(c, P, t1, t2); for (int i = 0; i < nc; ++i) { mmp[2 * i] = t1[i]; mmp[2 * i + 1] = t2[i]; }
+    minmax(c, U, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i] = t1[i]; mm[6 * i + 1] = t2[i]; }
+    minmax(c, V, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 2] = t1[i]; mm[6 * i + 3] = t2[i]; }
+    minmax(c, W, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 4] = t1[i]; mm[6 * i + 5] = t2[i]; }
+    free(t1); free(t2);
+    /* gradients (eqMomentum.cpp:94-105) */
+    double *pr = dget(c, "face_pR"), *ur = dget(c, "face_uR"), *vr = dget(c, "face_vfR");
+    double* tmp = (double*)malloc(sizeof(double) * nf);
+    double* gP = dreg(c, "mom_grad_P", 3LL * nc); lsq_grad(c, P, pr, gP);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f];
+    double* gU = dreg(c, "mom_grad_U", 3LL * nc); lsq_grad(c, U, tmp, gU);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 1];
+    double* gV = dreg(c, "mom_grad_V", 3LL * nc); lsq_grad(c, V, tmp, gV);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 2];
+    double* gW = dreg(c, "mom_grad_W", 3LL * nc); lsq_grad(c, W, tmp, gW);
+    double* gVF = dreg(c, "mom_grad_VF", 3LL * nc); lsq_grad(c, VF, vr, gVF);
+    free(tmp);
+
+    double *oU = hist(c, "oldU", U), *oV = hist(c, "oldV", V), *oW = hist(c, "oldW", W);
+    double *o2U = hist(c, "old2U", U), *o2V = hist(c, "old2V", V), *o2W = hist(c, "old2W", W);
+    const double dt = c->dt;
+    int cap = nc + 2 * ni;
+    int* ar = ireg(c, "mom_A_rows", cap); int* acl = ireg(c, "mom_A_cols", cap);
+    double* av = dreg(c, "mom_A_vals", cap);
+    double* B = dreg(c, "mom_B", 3LL * nc);          /* 3 planes: B0 | B1 | B2 */
+    double *B0 = B, *B1 = B + nc, *B2 = B + 2 * (size_t)nc;
+    for (int i = 0; i < nc; ++i) {
+        double Rho = rho[i], volume = vol[i];
+        ar[i] = i; acl[i] = i;
+        av[i] = Rho * 1.5 * volume / dt;
+        B0[i] = -Rho * (1.5 * U[i] - 2.0 * oU[i] + 0.5 * o2U[i]) * volume / dt;
+        B1[i] = -Rho * (1.5 * V[i] - 2.0 * oV[i] + 0.5 * o2V[i]) * volume / dt;
+        B2[i] = -Rho * (1.5 * W[i] - 2.0 * oW[i] + 0.5 * o2W[i]) * volume / dt;
+        B0[i] += volume * sg[4 * i]; B1[i] += volume * sg[4 * i + 1]; B2[i] += volume * sg[4 * i + 2];
+        B0[i] += volume * 0.0; B1[i] += volume * 0.0; B2[i] += volume * 0.0;   /* surface tension, sigma = 0 */
+    }
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *mpn = dget(c, "face_magPN"), *al = dget(c, "face_alphaF"), *epn = dget(c, "face_ePN");
+    double *sk = dget(c, "face_skew"), *ul = dget(c, "face_uL"), *pl = dget(c, "face_pL"), *rl = dget(c, "face_rhoL");
+    double* unf = dreg(c, "mom_face_UnF", nf);
+    int nnz = nc;
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f; const double* s = sk + 3 * f;
+        double area = fa[f], wCL = wc[f], wCR = 1.0 - wCL;
+        double UL_HO = U[o], VL_HO = V[o], WL_HO = W[o], UR_HO = U[q], VR_HO = V[q], WR_HO = W[q];
+        double muF = 1.0 / (wCL / mu[o] + wCR / mu[q]);
+        double RhoL = rho[o], RhoR = rho[q], PL = P[o], PR = P[q];
+        double UL = U[o], VL = V[o], WL = W[o], UR = U[q], VR = V[q], WR = W[q];
+        double dPN = mpn[f], alpha = al[f];
+        double ULs = UL, VLs = VL, WLs = WL, URs = UR, VRs = VR, WRs = WR;
+        for (int k = 0; k < 3; ++k) {
+            ULs += gU[3 * o + k] * s[k]; URs += gU[3 * q + k] * s[k];
+            VLs += gV[3 * o + k] * s[k]; VRs += gV[3 * q + k] * s[k];
+            WLs += gW[3 * o + k] * s[k]; WRs += gW[3 * q + k] * s[k];
+        }
+        ULs = smax(mm[6 * o + 1], smin(mm[6 * o + 0], ULs)); URs = smax(mm[6 * q + 1], smin(mm[6 * q + 0], URs));
+        VLs = smax(mm[6 * o + 3], smin(mm[6 * o + 2], VLs)); VRs = smax(mm[6 * q + 3], smin(mm[6 * q + 2], VRs));
+        WLs = smax(mm[6 * o + 5], smin(mm[6 * o + 4], WLs)); WRs = smax(mm[6 * q + 5], smin(mm[6 * q + 4], WRs));
+        double UnL = ULs * n[0] + VLs * n[1] + WLs * n[2];
+        double UnR = URs * n[0] + VRs * n[1] + WRs * n[2];
+        double UnF = wCL * UnL + wCR * UnR;
+        /* surfaceNormalVelocity.cpp:125-155 (pressure) */
+        double rs = 1.0 / (wCL / RhoL + wCR / RhoR);
+        double tt = dt / rs;
+        UnF -= alpha * tt * (PR - PL) / dPN;
+        for (int k = 0; k < 3; ++k) {
+            UnF -= tt * rs * wCL / RhoL * gP[3 * o + k] * (n[k] - alpha * e[k]);
+            UnF -= tt * rs * wCR / RhoR * gP[3 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * gP[3 * o + k] * n[k];
+            UnF += tt * rs * wCR / RhoR * gP[3 * q + k] * n[k];
+        }
+        /* surfaceNormalVelocity.cpp:156-187 (gravity); surface tension vanishes with sigma = 0 */
+        for (int k = 0; k < 3; ++k) UnF += alpha * tt * rs * c->g[k] * alpha * e[k];
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * sg[4 * o + k] * (n[k] - alpha * e[k]);
+            UnF += tt * rs * wCR / RhoR * sg[4 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
+            UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
+        }
+        unf[f] = UnF;
+        double weightL = (UnF > 0.0) ? 1.0 : 0.0;
+        double weightR = 1.0 - weightL;
+        double PF = wCL * PL + wCR * PR;
+        double UF_HO = weightL * UL_HO + weightR * UR_HO;
+        double VF_HO = weightL * VL_HO + weightR * VR_HO;
+        double WF_HO = weightL * WL_HO + weightR * WR_HO;
+        PF = wCL * PL + wCR * PR;
+        for (int k = 0; k < 3; ++k) {
+            PF += wCL * gP[3 * o + k] * s[k];
+            PF += wCR * gP[3 * q + k] * s[k];
+        }
+        PF = smax(mmp[2 * o + 1], smin(mmp[2 * o], PF));
+        PF = smax(mmp[2 * q + 1], smin(mmp[2 * q], PF));
+        /* coefficients (eqMomentum.cpp:694-712) */
+        av[o] += (weightL * RhoL * UnF * area + alpha * muF / dPN * area);
+        {
+            double a = (weightR * RhoL * UnF * area - alpha * muF / dPN * area);
+            if (!(fabs(a) < 2.2250738585072014e-308)) { ar[nnz] = o; acl[nnz] = q; av[nnz] = a; ++nnz; }
+        }
+        av[q] -= (weightR * RhoR * UnF * area - alpha * muF / dPN * area);
+        {
+            double a = -(weightL * RhoR * UnF * area + alpha * muF / dPN * area);
+            if (!(fabs(a) < 2.2250738585072014e-308)) { ar[nnz] = q; acl[nnz] = o; av[nnz] = a; ++nnz; }
+        }
+        /* fluxes (eqMomentum.cpp:740-779) */
+        double cL[3], cR[3], d[3], dL[3], dR[3];
+        cL[0] = (RhoL * UF_HO * UnF + PF * n[0]) * area;
+        cL[1] = (RhoL * VF_HO * UnF + PF * n[1]) * area;
+        cL[2] = (RhoL * WF_HO * UnF + PF * n[2]) * area;
+        cR[0] = (RhoR * UF_HO * UnF + PF * n[0]) * area;
+        cR[1] = (RhoR * VF_HO * UnF + PF * n[1]) * area;
+        cR[2] = (RhoR * WF_HO * UnF + PF * n[2]) * area;
+        d[0] = alpha * muF * (UR - UL) / dPN * area;
+        d[1] = alpha * muF * (VR - VL) / dPN * area;
+        d[2] = alpha * muF * (WR - WL) / dPN * area;
+        for (int k = 0; k < 3; ++k) {
+            d[0] += (muF * (wCL * gU[3 * o + k] + wCR * gU[3 * q + k]) * (n[k] - alpha * e[k]) * area);
+            d[1] += (muF * (wCL * gV[3 * o + k] + wCR * gV[3 * q + k]) * (n[k] - alpha * e[k]) * area);
+            d[2] += (muF * (wCL * gW[3 * o + k] + wCR * gW[3 * q + k]) * (n[k] - alpha * e[k]) * area);
+        }
+        dL[0] = ((gU[3 * o] * n[0] + gU[3 * o + 1] * n[1] + gU[3 * o + 2] * n[2]) * muF * area);
+        dL[1] = ((gV[3 * o] * n[0] + gV[3 * o + 1] * n[1] + gV[3 * o + 2] * n[2]) * muF * area);
+        dL[2] = ((gW[3 * o] * n[0] + gW[3 * o + 1] * n[1] + gW[3 * o + 2] * n[2]) * muF * area);
+        dR[0] = ((gU[3 * q] * n[0] + gU[3 * q + 1] * n[1] + gU[3 * q + 2] * n[2]) * muF * area);
+        dR[1] = ((gV[3 * q] * n[0] + gV[3 * q + 1] * n[1] + gV[3 * q + 2] * n[2]) * muF * area);
+        dR[2] = ((gW[3 * q] * n[0] + gW[3 * q + 1] * n[1] + gW[3 * q + 2] * n[2]) * muF * area);
+        B0[o] -= (cL[0] - d[0] - dL[0]); B1[o] -= (cL[1] - d[1] - dL[1]); B2[o] -= (cL[2] - d[2] - dL[2]);
+        B0[q] += (cR[0] - d[0] - dR[0]); B1[q] += (cR[1] - d[1] - dR[1]); B2[q] += (cR[2] - d[2] - dR[2]);
+    }
+    /* boundary faces, patch by patch (eqMomentum.cpp:795-1008) */
+    for (int f = ni; f < nf; ++f) {
+        int p = patch_of(c, f), o = c->own[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f;
+        const double* uL = ul + 3 * f; const double* uR = ur + 3 * f;
+        double area = fa[f];
+        double UnL = uL[0] * n[0] + uL[1] * n[1] + uL[2] * n[2];
+        double UnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
+        double UnF = 0.5 * UnL + 0.5 * UnR;
+        double RhoL = rl[f];
+        double tmp1 = 1.0 / RhoL * dt;
+        double UF = 0.5 * uL[0] + 0.5 * uR[0], VF_ = 0.5 * uL[1] + 0.5 * uR[1], WF = 0.5 * uL[2] + 0.5 * uR[2];
+        double PF = 0.5 * pl[f] + 0.5 * pr[f];
+        int tu = c->bct[3 * p + 1];
+        double cU = 0.0, cUd = 0.0;
+        if (tu == 1) { cU = 0.0; cUd = 1.0; }        /* fixedValue */
+        else if (tu == 0) { cU = 1.0; cUd = 0.0; }   /* zeroGradient */
+        else if (tu == 3) { cU = 0.0; cUd = 0.0; }   /* slip */
+        else { cU = 0.0; cUd = 1.0; }                /* noSlip */
+        double muF = 0.5 * mu[o] + 0.5 * mu[o];
+        double orgUL = U[o], orgUR = uR[0], orgVL = V[o], orgVR = uR[1], orgWL = W[o], orgWR = uR[2];
+        double dPN = 0.5 * mpn[f], alpha = al[f];
+        if (c->bct[3 * p] == 1) {
+            double orgPL = P[o], orgPR = c->bcv[5 * p];
+            UnF -= alpha * tmp1 * (orgPR - orgPL) / dPN;
+            for (int k = 0; k < 3; ++k) UnF += alpha * tmp1 * gP[3 * o + k] * e[k];
+        }
+        unf[f] = UnF;
+        double dU = 0.0, dV = 0.0, dW = 0.0;
+        dU += alpha * (orgUR - orgUL) / dPN;
+        dV += alpha * (orgVR - orgVL) / dPN;
+        dW += alpha * (orgWR - orgWL) / dPN;
+        for (int k = 0; k < 3; ++k) {
+            double tv = n[k] - alpha * e[k];
+            dU += gU[3 * o + k] * tv; dV += gV[3 * o + k] * tv; dW += gW[3 * o + k] * tv;
+        }
+        for (int k = 0; k < 3; ++k) { dU += (gU[3 * o + k] * n[k]); dV += (gV[3 * o + k] * n[k]); dW += (gW[3 * o + k] * n[k]); }
+        av[o] += cU * (RhoL * UnF * area);
+        av[o] += cUd * (muF * alpha / dPN * area);
+        B0[o] -= (RhoL * UF * UnF * area + PF * n[0] * area - muF * dU * area);
+        B1[o] -= (RhoL * VF_ * UnF * area + PF * n[1] * area - muF * dV * area);
+        B2[o] -= (RhoL * WF * UnF * area + PF * n[2] * area - muF * dW * area);
+    }
+    /* trim the COO arrays to the entries kept */
+    orc_arr* a;
+    a = find(c, "mom_A_rows"); a->n = nnz;
+    a = find(c, "mom_A_cols"); a->n = nnz;
+    a = find(c, "mom_A_vals"); a->n = nnz;
+    /* COO -> CSR as solveAMGCL.cpp:1129-1172 (in-row order = COO order) */
+    int* ptr = ireg(c, "mom_csr_ptr", nc + 1); int* col = ireg(c, "mom_csr_col", nnz);
+    double* val = dreg(c, "mom_csr_val", nnz);
+    for (int k = 0; k < nnz; ++k) ptr[ar[k]]++;
+    for (int i = 0, s2 = 0; i < nc; ++i) { int t = ptr[i]; ptr[i] = s2; s2 += t; }
+    ptr[nc] = nnz;
+    for (int k = 0; k < nnz; ++k) { int d = ptr[ar[k]]++; col[d] = acl[k]; val[d] = av[k]; }
+    for (int i = 0, last = 0; i <= nc; ++i) { int t = ptr[i]; ptr[i] = last; last = t; }
+}
+
+/* BiCGStab with a Jacobi preconditioner on the momentum CSR, one right-hand
+   side (plane j of mom_B), x0 = 0.  Not AMGCL's FGMRES: the GPU solver's
+   algorithm, restated for the CPU baseline and the parity tests. */
+int orc_solve_momentum(orc_ctx* c, int j, double tol, int maxiter, double* out_x, double* out_relres) {
+    int n = c->nc;
+    int* ptr = iget(c, "mom_csr_ptr"); int* col = iget(c, "mom_csr_col"); double* val = dget(c, "mom_csr_val");
+    double* b = dget(c, "mom_B") + (size_t)j * n;
+    double* w = (double*)calloc(8 * (size_t)n, sizeof(double));
+    double *r = w, *rh = w + n, *p = w + 2 * (size_t)n, *v = w + 3 * (size_t)n, *s = w + 4 * (size_t)n;
+    double *t = w + 5 * (size_t)n, *ph = w + 6 * (size_t)n, *dinv = w + 7 * (size_t)n;
+    double* x = out_x;
+    for (int i = 0; i < n; ++i) {
+        x[i] = 0.0; r[i] = b[i]; rh[i] = b[i];
+        double d = 0.0;
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) if (col[k] == i) d += val[k];
+        dinv[i] = 1.0 / d;
+    }
+    double bn = sqrt(dot(b, b, n));
+    if (bn == 0.0) { free(w); if (out_relres) *out_relres = 0.0; return 0; }
+    double rho = 1.0, alpha = 1.0, omega = 1.0, rn = bn;
+    int it = 0;
+    while (it < maxiter && rn > tol * bn) {
+        double rho1 = dot(rh, r, n);
+        double beta = (rho1 / rho) * (alpha / omega);
+        rho = rho1;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) { p[i] = r[i] + beta * (p[i] - omega * v[i]); ph[i] = dinv[i] * p[i]; }
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) { double a = 0.0; for (int k = ptr[i]; k < ptr[i + 1]; ++k) a += val[k] * ph[col[k]]; v[i] = a; }
+        alpha = rho / dot(rh, v, n);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) s[i] = r[i] - alpha * v[i];
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) { double a = 0.0; for (int k = ptr[i]; k < ptr[i + 1]; ++k) a += val[k] * dinv[col[k]] * s[col[k]]; t[i] = a; }
+        double tt = dot(t, t, n);
+        omega = (tt > 0.0) ? dot(t, s, n) / tt : 0.0;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) { x[i] += alpha * ph[i] + omega * dinv[i] * s[i]; r[i] = s[i] - omega * t[i]; }
+        rn = sqrt(dot(r, r, n));
+        ++it;
+    }
+    /* true residual */
+    double tr = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double a = 0.0; for (int k = ptr[i]; k < ptr[i + 1]; ++k) a += val[k] * x[col[k]];
+        tr += (b[i] - a) * (b[i] - a);
+    }
+    if (out_relres) *out_relres = sqrt(tr) / bn;
+    free(w);
+    return it;
+}
+
+/* eqMomentum.cpp:1029-1119: U += urf x, clamp, norm = |x| / |U| */
+double orc_update_momentum(orc_ctx* c, const double* x0, const double* x1, const double* x2) {
+    int nc = c->nc;
+    double *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W");
+    double nd = 0.0, npn = 0.0;
+    for (int i = 0; i < nc; ++i) {
+        U[i] += c->urf_mom * x0[i]; V[i] += c->urf_mom * x1[i]; W[i] += c->urf_mom * x2[i];
+        if (U[i] <= c->minU) U[i] = c->minU;
+        if (U[i] >= c->maxU) U[i] = c->maxU;
+        if (V[i] <= c->minV) V[i] = c->minV;
+        if (V[i] >= c->maxV) V[i] = c->maxV;
+        if (W[i] <= c->minW) W[i] = c->minW;
+        if (W[i] >= c->maxW) W[i] = c->maxW;
+        nd += x0[i] * x0[i]; nd += x1[i] * x1[i]; nd += x2[i] * x2[i];
+        npn += U[i] * U[i]; npn += V[i] * V[i]; npn += W[i] * W[i];
+    }
+    return sqrt(nd) / sqrt(npn);
 }

@@ -50,7 +50,19 @@ class Case:
     use_gravity: bool = False
     pre_p_urf: float = 0.3
     pre_u_urf: float = 0.3
+    mom_u_urf: float = 0.3          # momentumEq U relaxation (fvSolution default)
+    # BDF2 history for the momentum equation: (U, V, W) at steps n-1 and n-2;
+    # None means "same as the current field" (the first step of a run)
+    old: tuple = None
+    old2: tuple = None
     extra: dict = field(default_factory=dict)
+
+    def history(self):
+        """(oldU, oldV, oldW, old2U, old2V, old2W), defaulting to the current velocity."""
+        cur = (self.U, self.V, self.W)
+        o = self.old if self.old is not None else cur
+        o2 = self.old2 if self.old2 is not None else cur
+        return tuple(np.ascontiguousarray(a, dtype=np.float64) for a in (*o, *o2))
 
 
 def approx_cell_centres(mesh: PolyMesh) -> np.ndarray:
@@ -104,6 +116,16 @@ def vof_case(n: int, jitter: float = 0.2, mesh_seed: int = 1234) -> Case:
     return Case(name=f"vof{n}", mesh=mesh, P=np.zeros(mesh.n_cells), U=U, V=V, W=W, VF=alpha,
                 bc_type=bt, bc_value=bv, dt=1e-4, rho=(1000.0, 1.2), mu=(1e-3, 1.8e-5),
                 gravity=(0.0, 0.0, -9.81), use_gravity=True)
+
+
+def with_history(case: Case, seed: int, scale: float = 0.1) -> Case:
+    """Seeded old / second-old velocities near the current one (exercises BDF2)."""
+    rng = np.random.default_rng(seed)
+    n = case.mesh.n_cells
+    cur = (case.U, case.V, case.W)
+    case.old = tuple(c + scale * rng.uniform(-1.0, 1.0, size=n) for c in cur)
+    case.old2 = tuple(c + scale * rng.uniform(-1.0, 1.0, size=n) for c in cur)
+    return case
 
 
 def with_fields(case: Case, seed: int, p_scale: float = 1.0) -> Case:

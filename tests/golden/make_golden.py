@@ -3,7 +3,9 @@
 Builds oracle/_ref/semo_ref from the reference sources (oracle/ref/Makefile),
 runs it on small seeded cases and stores inputs and every dumped intermediate
 as .npz.  The fixtures are committed so the parity tests need neither the
-reference tree nor its build.
+reference tree nor its build.  Fixtures named outer_* hold a whole outer
+iteration (momentum equation, then the pressure correction) with seeded old
+and second-old velocities for the BDF2 term.
 
     python tests/golden/make_golden.py [REF_DIR]
 """
@@ -19,7 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from semo_mesh_gb300.cases import box_case, vof_case, with_fields, BC_FIXED_VALUE  # noqa: E402
+from semo_mesh_gb300.cases import (box_case, vof_case, with_fields, with_history, BC_FIXED_VALUE,  # noqa: E402
+                                   BC_NO_SLIP, BC_SLIP)
 from oracle.refcase import run_reference  # noqa: E402
 
 
@@ -41,16 +44,38 @@ def golden_cases():
     return cs
 
 
-def save(name: str, case, ref: dict) -> None:
+def outer_cases():
+    cs = []
+    c = with_history(with_fields(vof_case(6), seed=11, p_scale=80.0), seed=12)
+    # walls of every supported velocity type exercise the momentum boundary loop
+    c.bc_type[c.mesh.patch_names.index("xmin"), 1] = BC_NO_SLIP
+    c.bc_type[c.mesh.patch_names.index("ymax"), 1] = BC_SLIP
+    c.bc_type[c.mesh.patch_names.index("ymin"), 1] = BC_FIXED_VALUE
+    c.bc_value[c.mesh.patch_names.index("ymin"), 1:4] = (0.5, -0.25, 0.125)
+    c.name = "outer_vof6"
+    cs.append(("outer_vof6", c))
+    c = with_history(box_case(7, jitter=0.3, mesh_seed=77), seed=13, scale=0.3)
+    c.dt = 0.01
+    c.P = np.random.default_rng(14).uniform(-1, 1, c.mesh.n_cells)
+    c.mom_u_urf = 0.7
+    c.name = "outer_box7j"
+    cs.append(("outer_box7j", c))
+    return cs
+
+
+def save(name: str, case, ref: dict, momentum: bool = False) -> None:
     m = case.mesh
     out = {f"ref_{k}": v for k, v in ref.items()}
+    if momentum:
+        out["history"] = np.stack(case.history())
     out.update(points=m.points, face_ptr=m.face_ptr, face_pts=m.face_pts, owner=m.owner,
                neighbour=m.neighbour, patch_start=m.patch_start, patch_size=m.patch_size,
                n_cells=np.int64(m.n_cells), P=case.P, U=case.U, V=case.V, W=case.W, VF=case.VF,
                bc_type=case.bc_type, bc_value=case.bc_value,
                params=np.array([case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
                                 case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf,
-                                case.pre_u_urf, 1.0 if case.use_gravity else 0.0]))
+                                case.pre_u_urf, 1.0 if case.use_gravity else 0.0, case.mom_u_urf,
+                                1.0 if momentum else 0.0]))
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
@@ -62,6 +87,10 @@ def main():
         ref = run_reference(case, threads=1)
         save(name, case, ref)
         print(name, case.mesh.n_cells, "cells")
+    for name, case in outer_cases():
+        ref = run_reference(case, threads=1, momentum=True)
+        save(name, case, ref, momentum=True)
+        print(name, case.mesh.n_cells, "cells (outer iteration)")
 
 
 if __name__ == "__main__":

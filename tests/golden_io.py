@@ -10,8 +10,18 @@ from semo_mesh_gb300.meshgen import PATCH_NAMES, PolyMesh
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names():
+def _all():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def names():
+    """Fixtures of one pressure-correction pass."""
+    return [n for n in _all() if not n.startswith("outer_")]
+
+
+def outer_names():
+    """Fixtures of a whole outer iteration: momentum equation, then pressure correction."""
+    return [n for n in _all() if n.startswith("outer_")]
 
 
 def load(name):
@@ -25,5 +35,11 @@ def load(name):
                 rho=(float(p[1]), float(p[2])), mu=(float(p[3]), float(p[4])), sigma=float(p[5]),
                 gravity=(float(p[6]), float(p[7]), float(p[8])), use_gravity=bool(p[11]),
                 pre_p_urf=float(p[9]), pre_u_urf=float(p[10]))
+    if p.size > 12:
+        case.mom_u_urf = float(p[12])
+    if "history" in z.files:
+        h = z["history"]
+        case.old = (h[0].copy(), h[1].copy(), h[2].copy())
+        case.old2 = (h[3].copy(), h[4].copy(), h[5].copy())
     ref = {k[4:]: z[k] for k in z.files if k.startswith("ref_")}
     return case, ref
