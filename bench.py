@@ -1,20 +1,28 @@
 #!/usr/bin/env python
-"""Benchmark: SEMO's per-outer-iteration pressure-correction pass on one GB300.
+"""Benchmark: SEMO's outer iteration (momentum + pressure correction) on one GB300.
 
 Workload: jittered hex box 128^3 (2,097,152 cells, 6,340,608 faces), two-phase
-VOF fields (water drop in air, gravity), seeded synthetic inputs.  One step is
-one full pass: EOS and face values, gravity source, stencil min/max, five LSQ
-gradients, face-loop assembly of the pressure-correction system, smoothed-
-aggregation AMG setup, CG to a 1e-8 FP64 relative residual, two Gauss-Green
-sweeps and the P/U/V/W update -- what calcPressureEq does per outer
-iteration.  Mesh data (several GB) is far larger than the 129 MB L2, so no
-flush is needed between steps.
+VOF fields (water drop in air, gravity) with seeded old and second-old
+velocities, seeded synthetic inputs.  One step is one outer iteration of the
+pressure-based solver with one pressure correction:
+  momentum  cell viscosity, face values, stencil min/max, five LSQ gradients,
+            BDF2 + convection + diffusion assembly (one matrix, three RHS), the
+            three solves (BiCGStab, Jacobi) to 1e-9, U/V/W update;
+  pressure  EOS and face values, gravity source, stencil pass, face-loop
+            assembly, smoothed-aggregation AMG setup, CG to a 1e-8 FP64
+            relative residual, two Gauss-Green sweeps, P/U/V/W update.
+Successive steps continue from the updated fields, as SEMO's outer loop does.
+Mesh data (several GB) is far larger than the 129 MB L2, so no flush is
+needed between steps.
 
-  value    Mcells/s per pass, inputs resident in HBM, FP32 AMG inside FP64 CG
-  e2e      the same through the public C-ABI with host buffers: fields copied in,
-           the pass, fields copied out, every step (wall clock)
-  fp64     the same pass with an all-FP64 hierarchy and V-cycle
-  adjoint  A^T lambda = dJ/dx on the forward hierarchy, time vs the forward solve
+  value          Mcells/s per outer iteration, inputs resident in HBM, FP32 AMG
+                 inside FP64 CG for the pressure
+  pressure_pass  the pressure-correction pass alone (calcPressureEq)
+  e2e            the outer iteration through the public C-ABI with host buffers:
+                 fields and old velocities copied in, the iteration, fields
+                 copied out, every step (wall clock)
+  fp64           the same with an all-FP64 hierarchy and V-cycle
+  adjoint        A^T lambda = dJ/dx on the forward hierarchy, time vs the forward solve
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 128]
 """
@@ -122,59 +130,90 @@ def pface_bytes(m: dict) -> float:
     return m["internal_faces"] * (8 + 72 + 8 + 32 + 8 + 16 + 24) + m["cells"] * 216
 
 
-KERNEL_OF_STAGE = {"stencil": ("k_stencil", stencil_bytes), "pface": ("k_pface", pface_bytes)}
+def mface_bytes(m: dict) -> float:
+    """Algorithmic bytes of one k_mface launch.
+
+    per internal face: as k_pface's face reads (136) plus 8 face terms (64)
+    and 2 off-diagonals (16) written; per cell, read once: 1/rho, rho, 1/mu,
+    P, U, V, W, 15 gradient components, 8 limits, 3 gravity sources (272).
+    """
+    return m["internal_faces"] * (8 + 72 + 8 + 32 + 8 + 64 + 16) + m["cells"] * 272
 
 
-def cpu_baseline(case, passes: int = 1) -> dict:
-    """The oracle (restated reference pass) timed on this host's cores."""
+# stage -> (kernel, algorithmic bytes per launch); each of these stages is one launch
+KERNEL_OF_STAGE = {"stencil": ("k_stencil", stencil_bytes), "pface": ("k_pface", pface_bytes),
+                   "mface": ("k_mface", mface_bytes)}
+
+
+def oracle_outer_iteration(o) -> dict:
+    """One outer iteration on the oracle: momentum pass, then pressure pass."""
+    m = o.momentum_pass(1e-9)
+    o.assemble()
+    s = o.solve(False, 1e-8)
+    o.update(s["x"])
+    return {"mom_iters": m["iters"], "iters": s["iters"]}
+
+
+def cpu_baseline(case, steps: int = 1) -> dict:
+    """The oracle (restated reference outer iteration) timed on this host's cores."""
     from oracle.oracle import Oracle, build
     build()
     o = Oracle(case.mesh)
+    o.set_case(case)
     t_total = 0.0
-    for _ in range(passes):
-        o.set_case(case)
+    for _ in range(steps):
         t0 = time.perf_counter()
-        o.assemble()
-        s = o.solve(False, 1e-8)
-        o.update(s["x"])
+        r = oracle_outer_iteration(o)
         t_total += time.perf_counter() - t0
     n = case.mesh.n_cells
-    return {"value": round(n * passes / t_total / 1e6, 4), "unit": UNIT, "cores": Oracle.threads(),
+    return {"value": round(n * steps / t_total / 1e6, 4), "unit": UNIT, "cores": Oracle.threads(),
             "kind": "port", "seconds": round(t_total, 2),
-            "sample": f"{passes} full pass(es) of the same {n}-cell workload: serial assembly as in SEMO, "
-                      f"OpenMP SA-AMG + CG solve ({s['iters']} iterations)"}
+            "sample": f"{steps} outer iteration(s) of the same {n}-cell workload: serial assembly as in SEMO, "
+                      f"OpenMP Jacobi-BiCGStab momentum solves ({r['mom_iters']} iterations) and SA-AMG + CG "
+                      f"pressure solve ({r['iters']} iterations)"}
+
+
+def bench_case(n: int):
+    from semo_mesh_gb300.cases import vof_case, with_history
+    return with_history(vof_case(n), seed=5, scale=0.05)
 
 
 def run_gpu_arm(args, rank, world, local) -> None:
     import torch
     import semo_mesh_gb300 as S
     from semo_mesh_gb300.build import build
-    from semo_mesh_gb300.cases import vof_case
 
     build()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
-    case = vof_case(args.n)
+    case = bench_case(args.n)
     mesh = case.mesh
     nc = mesh.n_cells
     inputs = tuple(a.copy() for a in (case.P, case.U, case.V, case.W, case.VF))
+    history = case.history()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    def passes(ctx, strm, k):
+    def timed(ctx, strm, k, fn):
         infos = []
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(strm)
         for _ in range(k):
-            infos.append(ctx.calc_pressure_eq()[1])
+            infos.append(fn(ctx)[1])
         e1.record(strm)
         e1.synchronize()
         return e0.elapsed_time(e1) / k, infos
+
+    def outer(ctx):
+        return ctx.outer_iteration()
+
+    def pressure(ctx):
+        return ctx.calc_pressure_eq()
 
     ctx = S.Context(precision="mixed", tol=1e-8, device=local)
     ctx.set_case(case)
@@ -183,14 +222,14 @@ def run_gpu_arm(args, rank, world, local) -> None:
 
     # ---- mixed precision, inputs resident in HBM (the headline value) ------
     for _ in range(args.warmup):
-        ctx.calc_pressure_eq()
+        ctx.outer_iteration()
     ctx.reset_stats()
     ctx.set_profiling(True)
     l0 = ctx.kernel_launches()
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        ms_mixed, infos = passes(ctx, strm, args.steps)
+        ms_mixed, infos = timed(ctx, strm, args.steps, outer)
     torch.cuda.synchronize()
     barrier()
     launches = ctx.kernel_launches() - l0
@@ -200,6 +239,12 @@ def run_gpu_arm(args, rank, world, local) -> None:
         t = torch.tensor([ms_mixed], device=f"cuda:{local}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_mixed = float(t.item())
+
+    # ---- the pressure-correction pass alone (calcPressureEq) ---------------
+    ctx.set_case(case)
+    for _ in range(args.warmup):
+        ctx.calc_pressure_eq()
+    ms_pres, infos_p = timed(ctx, strm, args.steps, pressure)
 
     # ---- end to end through the C-ABI, host buffers ------------------------
     # inputs and outputs live in pinned host memory, as a caller streaming
@@ -212,31 +257,35 @@ def run_gpu_arm(args, rank, world, local) -> None:
         return t, v
     pin_in = [pinned(a) for a in inputs]
     h_in = [v for _, v in pin_in]
+    pin_hist = [pinned(a) for a in history]
+    h_hist = [v for _, v in pin_hist]
     pin_out = {k: pinned() for k in ("P", "U", "V", "W")}
     out = {k: v for k, (_, v) in pin_out.items()}
-    for _ in range(2):
+
+    def e2e_step():
         ctx.set_fields(*h_in)
-        ctx.calc_pressure_eq()
+        ctx.set_old_velocity(h_hist[:3], h_hist[3:])
+        ctx.outer_iteration()
         ctx.fields(out)
+    for _ in range(2):
+        e2e_step()
     torch.cuda.synchronize()
     e2e_t0 = torch.cuda.Event(enable_timing=True)
     e2e_t1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     e2e_t0.record(strm)
     for _ in range(args.steps):
-        ctx.set_fields(*h_in)
-        ctx.calc_pressure_eq()
-        ctx.fields(out)
+        e2e_step()
     e2e_t1.record(strm)
     e2e_t1.synchronize()
     ms_e2e_wall = (time.perf_counter() - t0) * 1e3 / args.steps
     ms_e2e = max(ms_e2e_wall, e2e_t0.elapsed_time(e2e_t1) / args.steps)
     if not np.isfinite(out["P"]).all():
-        raise RuntimeError("non-finite pressure after the e2e passes")
+        raise RuntimeError("non-finite pressure after the e2e steps")
 
     # ---- adjoint: A^T lambda = dJ/dx, J = sum of p'^2 over the z=1 cells -----
     zc = mesh.patch_cells("zmax")
-    ctx.set_fields(*inputs)
+    ctx.set_case(case)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ctx.assemble()
@@ -259,8 +308,12 @@ def run_gpu_arm(args, rank, world, local) -> None:
     ctx64.set_case(case)
     strm64 = torch.cuda.ExternalStream(ctx64.stream, device=torch.device(f"cuda:{local}"))
     for _ in range(args.warmup):
+        ctx64.outer_iteration()
+    ms_fp64, infos64 = timed(ctx64, strm64, args.steps, outer)
+    ctx64.set_case(case)
+    for _ in range(args.warmup):
         ctx64.calc_pressure_eq()
-    ms_fp64, infos64 = passes(ctx64, strm64, args.steps)
+    ms_fp64_p, infos64_p = timed(ctx64, strm64, args.steps, pressure)
     ctx64.close()
 
     if rank != 0:
@@ -271,7 +324,7 @@ def run_gpu_arm(args, rank, world, local) -> None:
     # ---- roofline for the dominant single-kernel stage ----------------------
     peak, peak_src = hbm_peak()
     single = {k: v for k, v in stages.items() if k in KERNEL_OF_STAGE and v[1] > 0}
-    dom = max(single, key=lambda k: single[k][0])
+    dom = max(single, key=lambda k: single[k][0])   # largest total device time per step
     kname, fbytes = KERNEL_OF_STAGE[dom]
     per_launch_ms = single[dom][0] / single[dom][1]
     algo = fbytes(minfo)
@@ -289,33 +342,42 @@ def run_gpu_arm(args, rank, world, local) -> None:
     cells_all = nc * world
     value = cells_all / (ms_mixed * 1e-3) / 1e6
     clocks = clk.summary()
+    mc = lambda ms: round(cells_all / (ms * 1e-3) / 1e6, 3)   # noqa: E731
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_mixed, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 assembly + f32 AMG in f64 CG",
-        "data": "synthetic (seeded jittered hex mesh and VOF fields)",
-        "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF pressure-correction pass "
-                               f"(assembly + SA-AMG setup + CG to 1e-8 + update)",
+        "data": "synthetic (seeded jittered hex mesh, VOF fields, old velocities)",
+        "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF outer iteration: momentum (assembly + "
+                               f"3 BiCGStab solves to 1e-9 + update) then pressure correction (assembly + "
+                               f"SA-AMG setup + CG to 1e-8 + update)",
                    "cells": nc, "faces": minfo["faces"], "nnz": minfo["nnz"],
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (mesh + fields several GB), no flush"},
-        "iterations": [i["iterations"] for i in infos][:3], "rel_residual": max(i["rel_residual"] for i in infos),
-        "amg_levels": infos[-1]["levels"], "operator_complexity": round(infos[-1]["operator_complexity"], 3),
-        "fp64": {"value": round(cells_all / (ms_fp64 * 1e-3) / 1e6, 3), "ms_per_step": round(ms_fp64, 3),
-                 "iterations": infos64[-1]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3)},
+        "iterations": [i[3]["iterations"] for i in infos][:3],
+        "momentum_iterations": [i[0]["iterations"] for i in infos][:3],
+        "rel_residual": max(i[3]["rel_residual"] for i in infos),
+        "amg_levels": infos[-1][3]["levels"], "operator_complexity": round(infos[-1][3]["operator_complexity"], 3),
+        "pressure_pass": {"value": mc(ms_pres), "ms_per_step": round(ms_pres, 3),
+                          "iterations": [i["iterations"] for i in infos_p][:3]},
+        "fp64": {"value": mc(ms_fp64), "ms_per_step": round(ms_fp64, 3),
+                 "iterations": infos64[-1][3]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3),
+                 "pressure_pass_ms": round(ms_fp64_p, 3),
+                 "pressure_pass_mixed_speedup": round(ms_fp64_p / ms_pres, 3)},
         "adjoint": {"ms_adjoint_solve": round(ms_adj, 3), "ms_forward_solve": round(ms_fwd, 3),
                     "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
-                    "adj_over_fwd_pass": round(ms_adj / ms_mixed, 3), "iterations": ainfo["iterations"]},
+                    "adj_over_fwd_pass": round(ms_adj / ms_pres, 3), "iterations": ainfo["iterations"]},
         "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1] > 0},
-        "e2e": {"value": round(cells_all / (ms_e2e * 1e-3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms_e2e, 3),
-                "host_buffers": "pinned, caller cell order; semo_set_fields + semo_pressure_pass + semo_get_fields",
-                "h2d_bytes_per_step": 5 * 8 * nc, "d2h_bytes_per_step": 4 * 8 * nc},
+        "e2e": {"value": mc(ms_e2e), "unit": UNIT, "ms_per_step": round(ms_e2e, 3),
+                "host_buffers": "pinned, caller cell order; semo_set_fields + semo_set_old_velocity + "
+                                "semo_outer_iteration + semo_get_fields",
+                "h2d_bytes_per_step": 11 * 8 * nc, "d2h_bytes_per_step": 4 * 8 * nc},
         "gpu_launches": int(launches),
         "roofline": roofline,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(case, passes=1)
+        line["cpu_baseline"] = cpu_baseline(case, steps=1)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -325,34 +387,33 @@ def run_reference_arm(args, rank, world) -> None:
     """The reference's CPU implementation of the path (oracle port), same workload."""
     if rank != 0:
         return
-    from semo_mesh_gb300.cases import vof_case
     from oracle.oracle import Oracle, build
     build()
-    case = vof_case(args.n)
+    case = bench_case(args.n)
     o = Oracle(case.mesh)
+    o.set_case(case)
     times, iters = [], []
     for k in range(args.warmup + args.steps):
-        o.set_case(case)
         t0 = time.perf_counter()
-        o.assemble()
-        s = o.solve(False, 1e-8)
-        o.update(s["x"])
+        r = oracle_outer_iteration(o)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
-            iters.append(s["iters"])
+            iters.append(r["iters"])
     nc = case.mesh.n_cells
     ms = 1e3 * sum(times) / len(times)
     value = nc / (ms * 1e-3) / 1e6
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered hex mesh and VOF fields)",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded jittered hex mesh, VOF fields, old velocities)",
             "impl": "reference",
-            "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF pressure-correction pass "
-                                   f"(assembly + SA-AMG setup + CG to 1e-8 + update)", "cells": nc},
+            "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF outer iteration: momentum (assembly + "
+                                   f"3 BiCGStab solves to 1e-9 + update) then pressure correction (assembly + "
+                                   f"SA-AMG setup + CG to 1e-8 + update)", "cells": nc},
             "iterations": iters[:3],
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
-                             "sample": f"each step one full pass over all {nc} cells on the host cores"},
+                             "sample": f"each step one full outer iteration over all {nc} cells on the host cores"},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

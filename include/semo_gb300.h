@@ -1,11 +1,13 @@
 /*
  * semo_gb300.h -- C-ABI of the GB300 (sm_103a) pressure-correction hot path.
  *
- * Drop-in for SEMO's per-outer-iteration pressure path: owner/neighbour face
+ * Drop-in for SEMO's per-outer-iteration hot path: owner/neighbour face
  * lists go in (OpenFOAM polyMesh order, as SEMO loads them), the assembled
  * pressure-correction system comes out as an RCM-reordered CSR matrix plus
  * right-hand side, and the solution vector of the AMG-preconditioned Krylov
- * solve comes out in the caller's cell order.
+ * solve comes out in the caller's cell order.  The momentum equation that
+ * precedes it in each outer iteration (one matrix, three right-hand sides)
+ * is assembled and solved the same way.
  *
  * Conventions
  *  - plain pointers and sizes; no CUDA or torch types.  Host pointers unless a
@@ -63,9 +65,12 @@ typedef struct {
     int coarse_enough;           /* direct solve at or below this size; default 64 */
     int max_levels;              /* default 24 */
     int cheb_degree;             /* Chebyshev pre/post smoothing degree; default 2 */
+    /* momentum solve (BiCGStab, Jacobi preconditioner, per right-hand side) */
+    double mom_tol;              /* relative residual, default 1e-9 (SEMO's momentum tolerance) */
+    int mom_max_iter;            /* default 1000 */
 } semo_params;
 
-/* Physics of one pressure-correction pass (calcPressureEq inputs). */
+/* Physics of one outer iteration (calcMomentumEqs / calcPressureEq inputs). */
 typedef struct {
     double dt;                   /* controls.timeStep */
     double rho[2];               /* phase densities; phase 0 is the volume fraction VF */
@@ -74,6 +79,8 @@ typedef struct {
     double urf_p;                /* controls.prePreURF */
     double urf_u;                /* controls.preVelURF */
     double p_min, p_max, u_min, u_max, v_min, v_max, w_min, w_max;  /* controls.min/max clamps */
+    double mu[2];                /* phase viscosities (species[].mu), laminar */
+    double urf_mom;              /* controls.momVelURF */
 } semo_physics;
 
 typedef struct {
@@ -137,6 +144,50 @@ semo_status semo_get_fields(semo_ctx* ctx, double* P, double* U, double* V, doub
    (src/solvers/pressureBased.cpp:139-141, :211). */
 semo_status semo_pressure_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
 
+/* Old (n-1) and second-old (n-2) velocities for the BDF2 time term of the
+   momentum equation, caller's cell order (host pointers, n_cells each).  All
+   NULL clears them: the momentum pass then uses the current velocity for both,
+   as SEMO does on the first time step (src/solvers/pressureBased.cpp:33-52).
+   Replaces: cell.var[oldU/oldV/oldW] and cell.var[Qm[0..2]]. */
+semo_status semo_set_old_velocity(semo_ctx* ctx, const double* oldU, const double* oldV, const double* oldW,
+                                  const double* old2U, const double* old2V, const double* old2W);
+
+/* One momentum pass: cell viscosity, face values, stencil min/max of P, U, V,
+   W, five LSQ gradients, BDF2 + upwind convection + over-relaxed diffusion
+   assembly of one matrix with three right-hand sides (x, y, z), the three
+   solves, and U,V,W += urf_mom x with the clamps.  Returns SEMO's
+   ||dU||/||U|| in *norm; info points to 3 entries (x, y, z), or NULL.
+   Replaces: SEMO_Solvers_Builder::calcCellTransport (src/solvers/transport.cpp:
+   9-98) + calcMomentumEqs (src/solvers/build.h:135-139, src/solvers/
+   eqMomentum.cpp:9-1122) and its 3-RHS solveAMGCL call (src/solvers/build.h:
+   233-239, src/solvers/solveAMGCL.cpp:1116-1271), with Jacobi-preconditioned
+   BiCGStab instead of AMGCL's aggregation/ILU0 FGMRES. */
+semo_status semo_momentum_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
+
+/* Momentum assembly only. */
+semo_status semo_assemble_momentum(semo_ctx* ctx);
+
+/* The assembled momentum system in SEMO's own layout, as solveAMGCL's COO to
+   CSR conversion leaves it (src/solvers/solveAMGCL.cpp:1129-1172): caller's
+   cell numbering, each row's entries in COO order (diagonal first, then one
+   entry per internal face in face order), off-diagonals with |a| < DBL_MIN
+   left out as calcMomentumEqs leaves them out (eqMomentum.cpp:699-711).  ptr
+   is n_cells+1, col/val nnz, b 3*n_cells (x, y, z planes).  *nnz gets the
+   entry count; every output may be NULL (call with NULLs to size). */
+semo_status semo_get_momentum_system(semo_ctx* ctx, int32_t* ptr, int32_t* col, double* val, double* b,
+                                     int64_t* nnz);
+
+/* Solve the assembled momentum system; x is 3*n_cells (x, y, z planes) in
+   the caller's cell order; info points to 3 entries or NULL. */
+semo_status semo_solve_momentum(semo_ctx* ctx, double* x, semo_solve_info* info);
+
+/* One outer iteration of the pressure-based solver with one pressure
+   correction (src/solvers/pressureBased.cpp:200-213, iterPreMax = 1): the
+   momentum pass, then the pressure pass on the updated velocity.  norms[0]
+   momentum, norms[1] pressure; info points to 4 entries (momentum x, y, z,
+   pressure) or NULL. */
+semo_status semo_outer_iteration(semo_ctx* ctx, double* norms, semo_solve_info* info);
+
 /* Assembly only (steps up to the face loop of calcPressureEq).  After it, the
    system can be read out or solved. */
 semo_status semo_assemble_pressure(semo_ctx* ctx);
@@ -148,8 +199,9 @@ semo_status semo_get_system_rcm(semo_ctx* ctx, int32_t* ptr, int32_t* col, doubl
 
 /* Intermediates of the last assembly, in the caller's cell order, for
    checking: name is one of "grad_P","grad_U","grad_V","grad_W","grad_VF"
-   (3*n_cells, xyz interleaved), "minmax_uvw" (6*n_cells), "rho" (n_cells),
-   "src_grav" (4*n_cells), "face_UnF" (n_faces, face order), "geometry:<name>". */
+   (3*n_cells, xyz interleaved), "minmax_uvw" (6*n_cells), "minmax_vf",
+   "minmax_p" (2*n_cells), "rho", "mu" (n_cells), "src_grav" (4*n_cells),
+   "face_UnF" (n_faces, face order), "geometry:<name>". */
 semo_status semo_get_array(semo_ctx* ctx, const char* name, double* out, int64_t count);
 
 /* Solve the assembled pressure system; x in the caller's cell order. */

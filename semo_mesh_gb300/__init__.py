@@ -43,14 +43,15 @@ class SemoError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("eps_strong", C.c_double), ("coarse_enough", C.c_int), ("max_levels", C.c_int),
-                ("cheb_degree", C.c_int)]
+                ("cheb_degree", C.c_int), ("mom_tol", C.c_double), ("mom_max_iter", C.c_int)]
 
 
 class Physics(C.Structure):
     _fields_ = [("dt", C.c_double), ("rho", C.c_double * 2), ("gravity", C.c_double * 3),
                 ("use_gravity", C.c_int), ("urf_p", C.c_double), ("urf_u", C.c_double),
                 ("p_min", C.c_double), ("p_max", C.c_double), ("u_min", C.c_double), ("u_max", C.c_double),
-                ("v_min", C.c_double), ("v_max", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double)]
+                ("v_min", C.c_double), ("v_max", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double),
+                ("mu", C.c_double * 2), ("urf_mom", C.c_double)]
 
 
 class SolveInfo(C.Structure):
@@ -102,6 +103,12 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_reset_stats.argtypes = [vp]
     L.semo_kernel_launches.restype = C.c_int64
     L.semo_mesh_info.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.semo_set_old_velocity.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p]
+    L.semo_momentum_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_assemble_momentum.argtypes = [vp]
+    L.semo_get_momentum_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
+    L.semo_solve_momentum.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_outer_iteration.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     _lib = L
     return L
 
@@ -126,7 +133,8 @@ class Context:
     """One GPU context (semo_ctx) holding a mesh, its fields and the solver."""
 
     def __init__(self, precision: str = "mixed", tol: float = 1e-8, max_iter: int = 500, device: int = 0,
-                 eps_strong: float = 0.08, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24):
+                 eps_strong: float = 0.08, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24,
+                 mom_tol: float = 1e-9, mom_max_iter: int = 1000):
         self.L = load_library()
         p = Params()
         self.L.semo_params_default(C.byref(p))
@@ -138,6 +146,8 @@ class Context:
         p.coarse_enough = coarse_enough
         p.cheb_degree = cheb_degree
         p.max_levels = max_levels
+        p.mom_tol = mom_tol
+        p.mom_max_iter = mom_max_iter
         h = C.c_void_p()
         st = self.L.semo_ctx_create(C.byref(h), C.byref(p))
         if st != SEMO_OK:
@@ -186,6 +196,8 @@ class Context:
         ph.use_gravity = 1 if case.use_gravity else 0
         ph.urf_p = case.pre_p_urf
         ph.urf_u = case.pre_u_urf
+        ph.mu[0], ph.mu[1] = case.mu
+        ph.urf_mom = case.mom_u_urf
         bt, btp = _i32(case.bc_type.reshape(-1))
         bv, bvp = _f64(case.bc_value.reshape(-1))
         self._check(self.L.semo_set_physics(self.h, C.byref(ph), btp, bvp))
@@ -199,6 +211,19 @@ class Context:
             self.upload_mesh(case.mesh)
         self.set_physics(case)
         self.set_fields(case.P, case.U, case.V, case.W, case.VF)
+        if case.old is None and case.old2 is None:
+            self.set_old_velocity(None)
+        else:
+            h = case.history()
+            self.set_old_velocity(h[:3], h[3:])
+
+    def set_old_velocity(self, old, old2=None) -> None:
+        """BDF2 history: old = (U, V, W) at n-1, old2 at n-2; None clears both."""
+        if old is None:
+            self._check(self.L.semo_set_old_velocity(self.h, None, None, None, None, None, None))
+            return
+        arrs = [_f64(a) for a in (*old, *old2)]
+        self._check(self.L.semo_set_old_velocity(self.h, *[a[1] for a in arrs]))
 
     def fields(self, out: dict | None = None) -> dict:
         """P, U, V, W in the caller's cell order (into `out`'s arrays if given, e.g. pinned buffers)."""
@@ -226,6 +251,45 @@ class Context:
         info = SolveInfo()
         self._check(self.L.semo_pressure_pass(self.h, C.byref(norm), C.byref(info)))
         return norm.value, info.as_dict()
+
+    def calc_momentum_eqs(self) -> tuple:
+        """calcMomentumEqs: one momentum pass; returns (norm, [info x, y, z])."""
+        norm = C.c_double()
+        info = (SolveInfo * 3)()
+        self._check(self.L.semo_momentum_pass(self.h, C.byref(norm), info))
+        return norm.value, [i.as_dict() for i in info]
+
+    def outer_iteration(self) -> tuple:
+        """Momentum then pressure (one pressure correction): ((norm_mom, norm_p), [4 infos])."""
+        norms = (C.c_double * 2)()
+        info = (SolveInfo * 4)()
+        self._check(self.L.semo_outer_iteration(self.h, norms, info))
+        return (norms[0], norms[1]), [i.as_dict() for i in info]
+
+    def assemble_momentum(self) -> None:
+        self._check(self.L.semo_assemble_momentum(self.h))
+
+    def momentum_system(self) -> dict:
+        """The momentum system in SEMO's layout (caller numbering, COO-scatter rows)."""
+        n = self.n_cells
+        nnz = C.c_int64()
+        self._check(self.L.semo_get_momentum_system(self.h, None, None, None, None, C.byref(nnz)))
+        ptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz.value, dtype=np.int32)
+        val = np.empty(nnz.value)
+        b = np.empty(3 * n)
+        self._check(self.L.semo_get_momentum_system(self.h, ptr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                    col.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                    val.ctypes.data_as(C.POINTER(C.c_double)),
+                                                    b.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nnz)))
+        return {"ptr": ptr, "col": col, "val": val, "b": b.reshape(3, n)}
+
+    def solve_momentum(self) -> tuple:
+        """Solve the assembled momentum system: (x of shape (3, n), [3 infos])."""
+        x = np.empty(3 * self.n_cells)
+        info = (SolveInfo * 3)()
+        self._check(self.L.semo_solve_momentum(self.h, x.ctypes.data_as(C.POINTER(C.c_double)), info))
+        return x.reshape(3, self.n_cells), [i.as_dict() for i in info]
 
     def lib_rcm(self) -> tuple:
         """lib_RCM: (perm, iperm) = (cells[i].RCM, cells[i].invRCM)."""
@@ -283,7 +347,7 @@ class Context:
     # ---- measurement hooks -------------------------------------------------
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
-              "setup_level", "setup_coarse")
+              "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

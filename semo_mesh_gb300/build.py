@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("geometry.cu", ["--fmad=false"]),
     ("assemble.cu", []),
+    ("momentum.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
     ("noalloc.cu", []),
@@ -47,7 +48,7 @@ def _stale(out: str, deps: list[str]) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "semo_internal.h"),
+    headers = [os.path.join(CSRC, "semo_internal.h"), os.path.join(CSRC, "face_common.cuh"),
                os.path.join(os.path.dirname(HERE), "include", "semo_gb300.h")]
     procs = []
     objs = []

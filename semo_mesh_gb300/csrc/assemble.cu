@@ -22,29 +22,18 @@
 
 #include <cmath>
 
+#include "face_common.cuh"
 #include "semo_internal.h"
 
 namespace {
 
-constexpr int kFaceMask = 0x3FFFFFFF;
-inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+using namespace semo::face;
 
-// Order-preserving int64 image of a double (for min/max on the integer
-// pipes instead of the FP64 unit); the map is its own inverse.
-__device__ __forceinline__ long long okey(double x) {
-    long long b = __double_as_longlong(x);
-    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
-}
-__device__ __forceinline__ double ounkey(long long k) {
-    return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
-}
-// std::max(a,b) = (a<b)?b:a ; std::min(a,b) = (b<a)?b:a
-__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double clamp01(double x) { return smax(0.0, smin(1.0, x)); }
-
-__global__ void k_cell_eos(int nc, double r0, double r1, double* __restrict__ VF, double* __restrict__ rho,
-                           double* __restrict__ irho) {
+// EOS (eos.cpp:10-151) and, when mu is given, the laminar viscosity of
+// calcCellTransport (transport.cpp:9-98): mu = VF mu0 + (1 - VF) mu1 on the
+// clamped VF, with its reciprocal in a second plane.
+__global__ void k_cell_eos(int nc, double r0, double r1, double m0, double m1, double* __restrict__ VF,
+                           double* __restrict__ rho, double* __restrict__ irho, double* __restrict__ mu) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     const double mf = clamp01(VF[i]);
@@ -56,6 +45,11 @@ __global__ void k_cell_eos(int nc, double r0, double r1, double* __restrict__ VF
     rho[i] = r;
     irho[i] = 1.0 / r;
     VF[i] = v0;
+    if (mu) {
+        const double m = __dadd_rn(__dmul_rn(v0, m0), __dmul_rn(__dsub_rn(1.0, v0), m1));
+        mu[i] = m;
+        mu[nc + i] = 1.0 / m;
+    }
 }
 
 // boundary-face values (left == right for every supported condition);
@@ -149,7 +143,8 @@ __global__ void k_grav_cell(int nc, int nf, const int* __restrict__ cfp, const i
 }
 
 // One pass over each cell's vertex stencil: LSQ gradients of P,U,V,W,VF and
-// stencil min/max of U,V,W,VF.  Stencil weights w_k*d_k are precomputed.
+// stencil min/max of U,V,W,VF,P (mm planes maxU,minU,maxV,minV,maxW,minW,
+// maxVF,minVF,maxP,minP).  Stencil weights w_k*d_k are precomputed.
 __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb, const int* __restrict__ stp,
                                                  const int* __restrict__ sti, const double* __restrict__ stw,
                                                  int64_t stn, const int* __restrict__ cfp,
@@ -165,6 +160,7 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
     double g[5][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     long long kmaxu = okey(ui), kminu = kmaxu, kmaxv = okey(vi), kminv = kmaxv;
     long long kmaxw = okey(wi), kminw = kmaxw, kmaxf = okey(fi), kminf = kmaxf;
+    long long kmaxp = okey(pi), kminp = kmaxp;
     const int kb = stp[i], ke = stp[i + 1];
     for (int k = kb; k < ke; ++k) {
         const int j = __ldg(sti + k);
@@ -181,6 +177,7 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
         t = okey(vj); kmaxv = (kmaxv < t) ? t : kmaxv; kminv = (t < kminv) ? t : kminv;
         t = okey(wj); kmaxw = (kmaxw < t) ? t : kmaxw; kminw = (t < kminw) ? t : kminw;
         t = okey(fj); kmaxf = (kmaxf < t) ? t : kmaxf; kminf = (t < kminf) ? t : kminf;
+        t = okey(pj); kmaxp = (kmaxp < t) ? t : kmaxp; kminp = (t < kminp) ? t : kminp;
     }
     // boundary faces (face index >= ni) come last in the ascending list
     {
@@ -212,69 +209,20 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
     mm[2 * (size_t)nc + i] = ounkey(kmaxv); mm[3 * (size_t)nc + i] = ounkey(kminv);
     mm[4 * (size_t)nc + i] = ounkey(kmaxw); mm[5 * (size_t)nc + i] = ounkey(kminw);
     mm[6 * (size_t)nc + i] = ounkey(kmaxf); mm[7 * (size_t)nc + i] = ounkey(kminf);
+    mm[8 * (size_t)nc + i] = ounkey(kmaxp); mm[9 * (size_t)nc + i] = ounkey(kminp);
 }
 
-struct FaceArgs {
-    int ni, nf, nc;
-    const int *own, *nei, *lr, *rl;
-    const double *fn, *epn, *skew, *alf, *fk;
-    const double *P, *U, *V, *W, *irho, *grad, *mm, *sg;
-    double dt, g0, g1, g2;
-    int use_gravity;
-    double *val, *coef, *flux, *unf;
-};
-
-// Internal faces of calcPressureEq.  The Rhie-Chow terms are evaluated in
-// reduced form: (dt/rho*)*rho* = dt, and the (n - alpha e) and n pieces of
-// the non-orthogonal correction combine to alpha e; agreement with SEMO's
-// operation order is to rounding (a few ulp), not bit-for-bit.
+// Internal faces of calcPressureEq (UnF as face_unf).
 __global__ void __launch_bounds__(256) k_pface(FaceArgs a) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= a.ni) return;
-    const int nf = a.nf, nc = a.nc, ni = a.ni;
     const int o = a.own[f], q = a.nei[f];
-    const double n0 = a.fn[f], n1 = a.fn[nf + f], n2 = a.fn[2 * nf + f];
-    const double s0 = a.skew[f], s1 = a.skew[nf + f], s2 = a.skew[2 * nf + f];
-    const double alpha = a.alf[f];
-    const double ae0 = alpha * a.epn[f], ae1 = alpha * a.epn[nf + f], ae2 = alpha * a.epn[2 * nf + f];
-    const double kA = a.fk[f], kP = a.fk[ni + f], area = a.fk[2 * ni + f], wL = a.fk[3 * ni + f];
-    const double wR = 1.0 - wL;
+    const FaceGeo g = load_geo(a, f);
+    const double UnF = face_unf(a, g, o, q);
     const double iRL = __ldg(a.irho + o), iRR = __ldg(a.irho + q);
-    const double* G = a.grad;
-    const size_t N = nc;
-    // skew-corrected, stencil-limited velocities (eqPressure.cpp:416-451)
-    double ul = __ldg(a.U + o) + __ldg(G + 3 * N + o) * s0 + __ldg(G + 4 * N + o) * s1 + __ldg(G + 5 * N + o) * s2;
-    double vl = __ldg(a.V + o) + __ldg(G + 6 * N + o) * s0 + __ldg(G + 7 * N + o) * s1 + __ldg(G + 8 * N + o) * s2;
-    double wl = __ldg(a.W + o) + __ldg(G + 9 * N + o) * s0 + __ldg(G + 10 * N + o) * s1 + __ldg(G + 11 * N + o) * s2;
-    double ur = __ldg(a.U + q) + __ldg(G + 3 * N + q) * s0 + __ldg(G + 4 * N + q) * s1 + __ldg(G + 5 * N + q) * s2;
-    double vr = __ldg(a.V + q) + __ldg(G + 6 * N + q) * s0 + __ldg(G + 7 * N + q) * s1 + __ldg(G + 8 * N + q) * s2;
-    double wr = __ldg(a.W + q) + __ldg(G + 9 * N + q) * s0 + __ldg(G + 10 * N + q) * s1 + __ldg(G + 11 * N + q) * s2;
-    const double* M = a.mm;
-    ul = smax(__ldg(M + N + o), smin(__ldg(M + o), ul));
-    ur = smax(__ldg(M + N + q), smin(__ldg(M + q), ur));
-    vl = smax(__ldg(M + 3 * N + o), smin(__ldg(M + 2 * N + o), vl));
-    vr = smax(__ldg(M + 3 * N + q), smin(__ldg(M + 2 * N + q), vr));
-    wl = smax(__ldg(M + 5 * N + o), smin(__ldg(M + 4 * N + o), wl));
-    wr = smax(__ldg(M + 5 * N + q), smin(__ldg(M + 4 * N + q), wr));
-    const double UnL = ul * n0 + vl * n1 + wl * n2;
-    const double UnR = ur * n0 + vr * n1 + wr * n2;
-    double UnF = wL * UnL + wR * UnR;
-    // pressure Rhie-Chow (surfaceNormalVelocity.cpp:125-155)
-    const double tt = a.dt * (wL * iRL + wR * iRR);
-    UnF -= tt * kP * (__ldg(a.P + q) - __ldg(a.P + o));
-    const double aL = a.dt * wL * iRL, aR = a.dt * wR * iRR;
-    UnF += aL * (__ldg(G + o) * ae0 + __ldg(G + N + o) * ae1 + __ldg(G + 2 * N + o) * ae2);
-    UnF += aR * (__ldg(G + q) * ae0 + __ldg(G + N + q) * ae1 + __ldg(G + 2 * N + q) * ae2);
-    if (a.use_gravity) {
-        // gravity Rhie-Chow (surfaceNormalVelocity.cpp:156-187)
-        UnF += a.dt * alpha * (a.g0 * ae0 + a.g1 * ae1 + a.g2 * ae2);
-        const double t0 = n0 - ae0 - alpha * n0, t1 = n1 - ae1 - alpha * n1, t2 = n2 - ae2 - alpha * n2;
-        const double* S = a.sg;
-        UnF += aL * (__ldg(S + o) * t0 + __ldg(S + N + o) * t1 + __ldg(S + 2 * N + o) * t2);
-        UnF += aR * (__ldg(S + q) * t0 + __ldg(S + N + q) * t1 + __ldg(S + 2 * N + q) * t2);
-    }
+    const double area = g.area;
     // off-diagonal coefficient, with SEMO's rho* = 1/(wCR/rhoL + wCR/rhoR) (eqPressure.cpp:396)
-    const double coef = kA * (a.dt * (wR * iRL + wR * iRR));
+    const double coef = g.kA * (a.dt * (g.wR * iRL + g.wR * iRR));
     a.val[a.lr[f]] = -coef;
     a.val[a.rl[f]] = -coef;
     a.coef[f] = coef;
@@ -370,23 +318,6 @@ __global__ void k_gg_cell(int nc, int nf, const int* __restrict__ cfp, const int
     g[i] = g0; g[nc + i] = g1; g[2 * (size_t)nc + i] = g2;
 }
 
-constexpr int kRedBlocks = 608;   // 4 x 152 SMs; fixed so reductions are deterministic
-constexpr int kRedThreads = 256;
-
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    v = 0.0;
-    if (threadIdx.x < 32) {
-        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    }
-    __syncthreads();
-    return v;
-}
-
 __global__ void __launch_bounds__(kRedThreads) k_update(int nc, double urf_p, double urf_u, double dt,
                                                         const double* __restrict__ x,
                                                         const double* __restrict__ g,
@@ -418,15 +349,6 @@ __global__ void __launch_bounds__(kRedThreads) k_update(int nc, double urf_p, do
     nd = block_sum(nd, sh);
     np = block_sum(np, sh);
     if (threadIdx.x == 0) { part[blockIdx.x] = nd; part[kRedBlocks + blockIdx.x] = np; }
-}
-
-__global__ void k_finish2(const double* __restrict__ part, double* __restrict__ out) {
-    __shared__ double sh[32];
-    double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) { a += part[i]; b += part[kRedBlocks + i]; }
-    a = block_sum(a, sh);
-    b = block_sum(b, sh);
-    if (threadIdx.x == 0) { out[0] = a; out[1] = b; }
 }
 
 // caller order <-> RCM order for up to 5 cell planes
@@ -465,6 +387,16 @@ __global__ void k_cell_product(int nc, const double* __restrict__ a, const doubl
 }  // namespace
 
 namespace semo {
+namespace face {
+__global__ void k_finish2(const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) { a += part[i]; b += part[kRedBlocks + i]; }
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) { out[0] = a; out[1] = b; }
+}
+}  // namespace face
 
 bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes) {
     Planes5 d{};
@@ -490,11 +422,13 @@ void fields_to_caller_order(semo_ctx* c, const double* const* src, double* dst, 
     SEMO_CHECK_LAUNCH();
 }
 
-void assemble_face_values(semo_ctx* c) {
+void assemble_face_values(semo_ctx* c, bool with_mu) {
     const int T = 256;
     cudaStream_t s = c->stream;
     StageScope sc(c, ST_FACE_VALUES);
-    k_cell_eos<<<blocks(c->nc, T), T, 0, s>>>(c->nc, c->phys.rho[0], c->phys.rho[1], c->VF, c->rho, c->irho);
+    if (with_mu) c->mu.alloc(2 * (size_t)c->nc, s);
+    k_cell_eos<<<blocks(c->nc, T), T, 0, s>>>(c->nc, c->phys.rho[0], c->phys.rho[1], c->phys.mu[0], c->phys.mu[1],
+                                               c->VF, c->rho, c->irho, with_mu ? c->mu.p : nullptr);
     SEMO_CHECK_LAUNCH();
     if (c->nb > 0) {
         k_bface_values<<<blocks(c->nb, T), T, 0, s>>>(c->nb, c->ni, c->nf, c->own, c->bpatch, c->bc_type, c->bc_value,
@@ -504,11 +438,11 @@ void assemble_face_values(semo_ctx* c) {
     }
 }
 
-void assemble_pressure(semo_ctx* c) {
+// gravity source and the stencil pass, shared by the pressure and momentum assemblies
+void assemble_gravity_stencil(semo_ctx* c) {
     const int T = 256;
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
-    assemble_face_values(c);
     if (c->phys.use_gravity) {
         StageScope sc(c, ST_GRAVITY);
         k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
@@ -527,6 +461,14 @@ void assemble_pressure(semo_ctx* c) {
                                                c->grad, c->mm);
     SEMO_CHECK_LAUNCH();
     }
+}
+
+void assemble_pressure(semo_ctx* c) {
+    const int T = 256;
+    cudaStream_t s = c->stream;
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    assemble_face_values(c, false);
+    assemble_gravity_stencil(c);
     double* coef = c->fscr.p;
     double* flux = c->fscr.p + nf;
     if (ni > 0) {

@@ -58,6 +58,8 @@ void semo_params_default(semo_params* p) {
     p->coarse_enough = 64;
     p->max_levels = 24;
     p->cheb_degree = 2;
+    p->mom_tol = 1e-9;
+    p->mom_max_iter = 1000;
 }
 
 void semo_physics_default(semo_physics* p) {
@@ -69,6 +71,8 @@ void semo_physics_default(semo_physics* p) {
     p->urf_u = 0.3;
     p->p_min = p->u_min = p->v_min = p->w_min = -1e300;
     p->p_max = p->u_max = p->v_max = p->w_max = 1e300;
+    p->mu[0] = p->mu[1] = 1e-3;
+    p->urf_mom = 0.3;
 }
 
 semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
@@ -80,7 +84,8 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
     semo_physics_default(&c->phys);
     semo_status st = guarded(c, [&] {
         need(c->prm.tol > 0.0 && c->prm.max_iter > 0 && c->prm.coarse_enough > 0 && c->prm.max_levels > 0 &&
-                 c->prm.cheb_degree > 0 && c->prm.cheb_degree <= 16 &&
+                 c->prm.cheb_degree > 0 && c->prm.cheb_degree <= 16 && c->prm.mom_tol > 0.0 &&
+                 c->prm.mom_max_iter > 0 &&
                  (c->prm.precision == SEMO_PREC_FP64 || c->prm.precision == SEMO_PREC_MIXED),
              SEMO_ERR_ARGUMENT, "invalid semo_params");
         int ndev = 0;
@@ -402,7 +407,7 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         // field storage
         for (auto* b : {&c->P, &c->U, &c->V, &c->W, &c->VF, &c->rho, &c->irho, &c->x}) b->alloc(nc, s);
         c->grad.alloc(15 * (size_t)nc, s);
-        c->mm.alloc(8 * (size_t)nc, s);
+        c->mm.alloc(10 * (size_t)nc, s);
         c->sg.alloc(4 * (size_t)nc, s);
         c->gx.alloc(3 * (size_t)nc, s);
         c->bface.alloc(10 * (size_t)std::max(c->nb, 1), s);
@@ -428,6 +433,7 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         need(phys && (bc_type || c->npatch == 0) && (bc_value || c->npatch == 0), SEMO_ERR_ARGUMENT, "null argument");
         need(std::isfinite(phys->dt) && phys->dt > 0.0, SEMO_ERR_ARGUMENT, "dt must be positive");
         need(phys->rho[0] > 0.0 && phys->rho[1] > 0.0, SEMO_ERR_ARGUMENT, "densities must be positive");
+        need(phys->mu[0] >= 0.0 && phys->mu[1] >= 0.0, SEMO_ERR_ARGUMENT, "viscosities must be non-negative");
         for (int p = 0; p < c->npatch; ++p) {
             need(bc_type[3 * p] == SEMO_BC_ZERO_GRADIENT || bc_type[3 * p] == SEMO_BC_FIXED_VALUE, SEMO_ERR_ARGUMENT,
                  "pressure BC must be zeroGradient or fixedValue");
@@ -443,6 +449,7 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         SEMO_CUDA(cudaStreamSynchronize(c->stream));
         c->phys_ready = true;
         c->assembled = false;
+        c->mom_assembled = false;
     });
 }
 
@@ -477,6 +484,7 @@ semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const
             throw Error(SEMO_ERR_NAN, "non-finite input field value");
         c->fields_ready = true;
         c->assembled = false;
+        c->mom_assembled = false;
     });
 }
 
@@ -539,10 +547,16 @@ semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t c
         };
         const char* grads[5] = {"grad_P", "grad_U", "grad_V", "grad_W", "grad_VF"};
         for (int g = 0; g < 5; ++g)
-            if (nm == grads[g]) { need(c->assembled, SEMO_ERR_STATE, "not assembled"); cell_planes(c->grad.p + (size_t)3 * g * n, 3, true); return; }
+            if (nm == grads[g]) {
+                need(c->assembled || c->mom_assembled, SEMO_ERR_STATE, "not assembled");
+                cell_planes(c->grad.p + (size_t)3 * g * n, 3, true);
+                return;
+            }
         if (nm == "minmax_uvw") { cell_planes(c->mm.p, 6, true); return; }
         if (nm == "minmax_vf") { cell_planes(c->mm.p + (size_t)6 * n, 2, true); return; }
+        if (nm == "minmax_p") { cell_planes(c->mm.p + (size_t)8 * n, 2, true); return; }
         if (nm == "rho") { cell_planes(c->rho.p, 1, false); return; }
+        if (nm == "mu") { need(c->mu.n == 2 * (size_t)n, SEMO_ERR_STATE, "no momentum assembly"); cell_planes(c->mu.p, 1, false); return; }
         if (nm == "src_grav") { cell_planes(c->sg.p, 4, true); return; }
         if (nm == "grad_x") { cell_planes(c->gx.p, 3, true); return; }
         if (nm == "face_UnF") { face_planes(c->unf.p, 1, nf); return; }
@@ -584,23 +598,170 @@ semo_status semo_solve_pressure(semo_ctx* c, double* x, semo_solve_info* info) {
     return st != SEMO_OK ? st : conv;
 }
 
+namespace {
+
+// calcPressureEq: assemble, solve, update.  Returns the convergence status.
+semo_status pressure_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info) {
+    need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+         "mesh, physics and fields must be set before a pass");
+    SEMO_CUDA(cudaSetDevice(c->device));
+    semo::assemble_pressure(c);
+    c->assembled = true;
+    semo_solve_info inf{};
+    semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
+    double nrm = semo::pressure_update(c);
+    c->mom_assembled = false;
+    if (norm) *norm = nrm;
+    if (info) *info = inf;
+    if (!(inf.rel_residual <= c->prm.tol)) return std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    return SEMO_OK;
+}
+
+// calcMomentumEqs: assemble, three solves, update (skipped after a breakdown).
+semo_status momentum_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info) {
+    need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+         "mesh, physics and fields must be set before a pass");
+    SEMO_CUDA(cudaSetDevice(c->device));
+    semo::assemble_momentum(c);
+    c->mom_assembled = true;
+    semo_solve_info inf[3] = {};
+    semo_status conv = semo::solve_momentum(c, inf);
+    if (info) for (int j = 0; j < 3; ++j) info[j] = inf[j];
+    if (conv == SEMO_ERR_BREAKDOWN) return conv;
+    double nrm = semo::momentum_update(c);
+    c->assembled = false;
+    if (norm) *norm = nrm;
+    return conv;
+}
+
+semo_status finish(semo_ctx* c, semo_status st, semo_status conv, const char* what) {
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = what;
+    return st != SEMO_OK ? st : conv;
+}
+
+}  // namespace
+
 semo_status semo_pressure_pass(semo_ctx* c, double* norm, semo_solve_info* info) {
     semo_status conv = SEMO_OK;
-    semo_status st = guarded(c, [&] {
-        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
-             "mesh, physics and fields must be set before a pass");
+    semo_status st = guarded(c, [&] { conv = pressure_pass_impl(c, norm, info); });
+    return finish(c, st, conv, "Krylov solve did not reach the tolerance");
+}
+
+semo_status semo_set_old_velocity(semo_ctx* c, const double* oU, const double* oV, const double* oW,
+                                  const double* o2U, const double* o2V, const double* o2W) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        const double* src[6] = {oU, oV, oW, o2U, o2V, o2W};
+        int given = 0;
+        for (auto p : src) given += p != nullptr;
+        c->mom_assembled = false;
+        if (given == 0) { c->has_old = false; return; }
+        need(given == 6, SEMO_ERR_ARGUMENT, "give all six old velocity components or none");
         SEMO_CUDA(cudaSetDevice(c->device));
-        semo::assemble_pressure(c);
-        c->assembled = true;
-        semo_solve_info inf{};
-        semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
-        double nrm = semo::pressure_update(c);
-        if (norm) *norm = nrm;
-        if (info) *info = inf;
-        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        c->old.alloc(6 * n, s);
+        for (int half = 0; half < 2; ++half) {
+            for (int q = 0; q < 3; ++q)
+                SEMO_CUDA(cudaMemcpyAsync(c->stage.p + q * n, src[3 * half + q], sizeof(double) * n,
+                                          cudaMemcpyHostToDevice, s));
+            double* dst[3] = {c->old.p + (3 * half) * n, c->old.p + (3 * half + 1) * n, c->old.p + (3 * half + 2) * n};
+            if (!semo::fields_from_caller_order(c, c->stage.p, dst, 3)) {
+                c->has_old = false;
+                throw Error(SEMO_ERR_NAN, "non-finite old velocity");
+            }
+        }
+        c->has_old = true;
     });
-    if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
-    return st != SEMO_OK ? st : conv;
+}
+
+semo_status semo_assemble_momentum(semo_ctx* c) {
+    return guarded(c, [&] {
+        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+             "mesh, physics and fields must be set before assembly");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::assemble_momentum(c);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->mom_assembled = true;
+    });
+}
+
+semo_status semo_momentum_pass(semo_ctx* c, double* norm, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] { conv = momentum_pass_impl(c, norm, info); });
+    return finish(c, st, conv, "momentum solve did not reach the tolerance");
+}
+
+semo_status semo_solve_momentum(semo_ctx* c, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->mom_assembled, SEMO_ERR_STATE, "momentum system not assembled");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo_solve_info inf[3] = {};
+        conv = semo::solve_momentum(c, inf);
+        if (info) for (int j = 0; j < 3; ++j) info[j] = inf[j];
+        if (x) {
+            const size_t n = (size_t)c->nc;
+            c->stage.alloc(5 * n, c->stream);
+            const double* src[3] = {c->xm.p, c->xm.p + n, c->xm.p + 2 * n};
+            semo::fields_to_caller_order(c, src, c->stage.p, 3);
+            SEMO_CUDA(cudaMemcpyAsync(x, c->stage.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        }
+    });
+    return finish(c, st, conv, "momentum solve did not reach the tolerance");
+}
+
+semo_status semo_outer_iteration(semo_ctx* c, double* norms, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        semo_solve_info inf[4] = {};
+        double nm[2] = {0.0, 0.0};
+        semo_status cm = momentum_pass_impl(c, &nm[0], inf);
+        if (cm == SEMO_ERR_BREAKDOWN) { conv = cm; }
+        else {
+            semo_status cp = pressure_pass_impl(c, &nm[1], &inf[3]);
+            conv = (cp != SEMO_OK) ? cp : cm;
+        }
+        if (norms) { norms[0] = nm[0]; norms[1] = nm[1]; }
+        if (info) for (int j = 0; j < 4; ++j) info[j] = inf[j];
+    });
+    return finish(c, st, conv, "a solve of the outer iteration did not reach its tolerance");
+}
+
+semo_status semo_get_momentum_system(semo_ctx* c, int32_t* ptr, int32_t* col, double* val, double* b,
+                                     int64_t* nnz_out) {
+    return guarded(c, [&] {
+        need(c->mom_assembled, SEMO_ERR_STATE, "momentum system not assembled");
+        cudaStream_t s = c->stream;
+        const int n = c->nc;
+        std::vector<int> hp(n + 1), hc(c->nnz);
+        std::vector<double> hv(c->nnz), hb(3 * (size_t)n);
+        SEMO_CUDA(cudaMemcpyAsync(hp.data(), c->A_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaMemcpyAsync(hc.data(), c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaMemcpyAsync(hv.data(), c->Am_val.p, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaMemcpyAsync(hb.data(), c->bm.p, sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        // rows back in the caller's numbering; each row keeps SEMO's in-row order,
+        // its diagonal first, and drops the off-diagonals calcMomentumEqs leaves out
+        int64_t k_out = 0;
+        if (ptr) ptr[0] = 0;
+        for (int i = 0; i < n; ++i) {
+            const int r = c->iperm[i];
+            for (int k = hp[r]; k < hp[r + 1]; ++k) {
+                if (k != hp[r] && hv[k] == 0.0) continue;
+                if (col) col[k_out] = c->perm[hc[k]];
+                if (val) val[k_out] = hv[k];
+                ++k_out;
+            }
+            if (ptr) ptr[i + 1] = (int32_t)k_out;
+        }
+        if (b)
+            for (int j = 0; j < 3; ++j)
+                for (int r = 0; r < n; ++r) b[(size_t)j * n + c->perm[r]] = hb[(size_t)j * n + r];
+        if (nnz_out) *nnz_out = k_out;
+    });
 }
 
 semo_status semo_solve_coo(semo_ctx* c, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,

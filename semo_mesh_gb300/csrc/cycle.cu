@@ -437,9 +437,20 @@ ChebCoef cheb2(double lam) {
 }
 
 // Everything the V-cycle needs beyond the hierarchy: SELL copies of the
-// operators of every level big enough for them to pay (small coarse levels
-// are launch-latency bound and stay CSR).
+// operators it pays for.  SELL runs one thread per row, so it needs enough
+// rows to fill the GPU (65536 rows = 2048 warps, ~13 per SM) unless rows are
+// short; a few thousand long rows (a coarse level, ~60 entries each) would
+// leave ~2 warps per SM walking 60 dependent loads, and run faster as CSR
+// with 32 lanes a row.  Small operators are launch-latency bound either way
+// and stay CSR.
 constexpr int kSellMinRows = 4096;
+constexpr int kSellFullRows = 65536;
+constexpr double kSellMaxAvgRow = 12.0;
+template <class V>
+bool sell_pays(const DCsr<V>& M) {
+    if (M.n < kSellMinRows) return false;
+    return M.n >= kSellFullRows || (double)M.nnz <= kSellMaxAvgRow * (double)M.n;
+}
 template <class V>
 struct LevelMats {
     Sell<V> A, P, R;
@@ -702,13 +713,250 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
     for (int l = 0; l + 1 < nl; ++l) {
         AmgLevel<V>& L = h.lev[l];
         LevelMats<V>& M = cy.lev[l];
-        M.a = L.A.n >= kSellMinRows;
-        M.p = L.P.n >= kSellMinRows;
-        M.r = L.R.n >= kSellMinRows;
+        M.a = sell_pays(L.A);
+        M.p = sell_pays(L.P);
+        M.r = sell_pays(L.R);
         if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
         if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
         if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R);
     }
+}
+
+// ------------------------------------------------ momentum: batched BiCGStab
+// Three right-hand sides (x, y, z velocity) share one matrix: every kernel
+// walks the rows once and serves all three, so the operator is read once per
+// product for the three systems.  Right preconditioning by D^-1 (the momentum
+// matrix is dominated by its BDF2 diagonal at the time steps of interest).
+// Per system j the scalars live at scal[16 j + k]:
+//   0 rho, 1 alpha, 2 omega, 3 beta, 4 (rh,v), 5 (t,s), 6 (t,t), 7 (r,r),
+//   8 (b,b), 9 active, 10 breakdown
+constexpr int kMomScal = 16;
+__device__ __forceinline__ bool mom_active(const double* scal, int j) { return scal[kMomScal * j + 9] != 0.0; }
+
+__device__ __forceinline__ void sell_mv3(const SellView<double>& A, int row, const double* __restrict__ x, size_t N,
+                                         double& s0, double& s1, double& s2) {
+    s0 = s1 = s2 = 0.0;
+    const int sl = row >> 5, l = row & 31;
+    const int b = A.sptr[sl], w = (A.sptr[sl + 1] - b) >> 5;
+    for (int j = 0, k = b + l; j < w; ++j, k += 32) {
+        const int c = A.col[k];
+        const double v = A.val[k];
+        s0 += v * __ldg(x + c);
+        s1 += v * __ldg(x + N + c);
+        s2 += v * __ldg(x + 2 * N + c);
+    }
+}
+
+// x = 0, r = rh = b, p = v = 0;  part = (b,b) per system
+__global__ void __launch_bounds__(kRedThreads) k_bi_init(int n, const double* __restrict__ b, double* __restrict__ x,
+                                                         double* __restrict__ r, double* __restrict__ rh,
+                                                         double* __restrict__ p, double* __restrict__ v,
+                                                         double* __restrict__ part) {
+    __shared__ double sh[32];
+    double bb[3] = {0.0, 0.0, 0.0};
+    const size_t N = n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int j = 0; j < 3; ++j) {
+            const double bi = b[j * N + i];
+            x[j * N + i] = 0.0; r[j * N + i] = bi; rh[j * N + i] = bi; p[j * N + i] = 0.0; v[j * N + i] = 0.0;
+            bb[j] += bi * bi;
+        }
+    for (int j = 0; j < 3; ++j) {
+        const double t = block_sum(bb[j], sh);
+        if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
+    }
+}
+__global__ void k_bi_fin0(const double* __restrict__ part, double* __restrict__ scal, double tol2) {
+    __shared__ double sh[32];
+    for (int j = 0; j < 3; ++j) {
+        const double bb = sum_parts(part + j * kRedBlocks, sh);
+        if (threadIdx.x == 0) {
+            double* S = scal + kMomScal * j;
+            for (int k = 0; k < kMomScal; ++k) S[k] = 0.0;
+            S[0] = bb; S[1] = 1.0; S[2] = 1.0; S[3] = 0.0; S[7] = bb; S[8] = bb;
+            S[9] = (bb > 0.0 && !(bb <= tol2 * bb)) ? 1.0 : 0.0;
+        }
+    }
+}
+// p = r + beta (p - omega v);  ph = D^-1 p
+__global__ void k_bi_p(int n, const double* __restrict__ dinv, const double* __restrict__ r, double* __restrict__ p,
+                       const double* __restrict__ v, double* __restrict__ ph, const double* __restrict__ scal) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = n;
+    const double di = dinv[i];
+    for (int j = 0; j < 3; ++j) {
+        if (!mom_active(scal, j)) continue;
+        const double beta = scal[kMomScal * j + 3], omega = scal[kMomScal * j + 2];
+        const double pi = r[j * N + i] + beta * (p[j * N + i] - omega * v[j * N + i]);
+        p[j * N + i] = pi;
+        ph[j * N + i] = di * pi;
+    }
+}
+// y = A x for the three systems;  part = (rh, y) per system
+__global__ void __launch_bounds__(kRedThreads) k_bi_mv1(SellView<double> A, const double* __restrict__ x,
+                                                        double* __restrict__ y, const double* __restrict__ rh,
+                                                        const double* __restrict__ scal, double* __restrict__ part) {
+    __shared__ double sh[32];
+    const size_t N = A.n;
+    double d[3] = {0.0, 0.0, 0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+        double s[3];
+        sell_mv3(A, row, x, N, s[0], s[1], s[2]);
+        for (int j = 0; j < 3; ++j) {
+            if (!mom_active(scal, j)) continue;
+            y[j * N + row] = s[j];
+            d[j] += rh[j * N + row] * s[j];
+        }
+    }
+    for (int j = 0; j < 3; ++j) {
+        const double t = block_sum(d[j], sh);
+        if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
+    }
+}
+__global__ void k_bi_fin1(const double* __restrict__ part, double* __restrict__ scal) {
+    __shared__ double sh[32];
+    for (int j = 0; j < 3; ++j) {
+        const double rv = sum_parts(part + j * kRedBlocks, sh);
+        if (threadIdx.x == 0) {
+            double* S = scal + kMomScal * j;
+            if (S[9] != 0.0) {
+                S[4] = rv;
+                if (rv == 0.0 || !isfinite(rv)) { S[10] = 1.0; S[9] = 0.0; }
+                else S[1] = S[0] / rv;
+            }
+        }
+    }
+}
+// s = r - alpha v (in place in r);  sh = D^-1 s
+__global__ void k_bi_s(int n, const double* __restrict__ dinv, double* __restrict__ r, const double* __restrict__ v,
+                       double* __restrict__ shv, const double* __restrict__ scal) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = n;
+    const double di = dinv[i];
+    for (int j = 0; j < 3; ++j) {
+        if (!mom_active(scal, j)) continue;
+        const double si = r[j * N + i] - scal[kMomScal * j + 1] * v[j * N + i];
+        r[j * N + i] = si;
+        shv[j * N + i] = di * si;
+    }
+}
+// t = A sh;  part = (t,s), (t,t) per system
+__global__ void __launch_bounds__(kRedThreads) k_bi_mv2(SellView<double> A, const double* __restrict__ x,
+                                                        double* __restrict__ t, const double* __restrict__ s,
+                                                        const double* __restrict__ scal, double* __restrict__ part) {
+    __shared__ double sh[32];
+    const size_t N = A.n;
+    double ts[3] = {0.0, 0.0, 0.0}, tt[3] = {0.0, 0.0, 0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+        double y[3];
+        sell_mv3(A, row, x, N, y[0], y[1], y[2]);
+        for (int j = 0; j < 3; ++j) {
+            if (!mom_active(scal, j)) continue;
+            t[j * N + row] = y[j];
+            ts[j] += y[j] * s[j * N + row];
+            tt[j] += y[j] * y[j];
+        }
+    }
+    for (int j = 0; j < 3; ++j) {
+        const double a = block_sum(ts[j], sh);
+        const double b = block_sum(tt[j], sh);
+        if (threadIdx.x == 0) { part[(2 * j) * kRedBlocks + blockIdx.x] = a; part[(2 * j + 1) * kRedBlocks + blockIdx.x] = b; }
+    }
+}
+__global__ void k_bi_fin2(const double* __restrict__ part, double* __restrict__ scal) {
+    __shared__ double sh[32];
+    for (int j = 0; j < 3; ++j) {
+        const double ts = sum_parts(part + (2 * j) * kRedBlocks, sh);
+        const double tt = sum_parts(part + (2 * j + 1) * kRedBlocks, sh);
+        if (threadIdx.x == 0) {
+            double* S = scal + kMomScal * j;
+            if (S[9] != 0.0) { S[5] = ts; S[6] = tt; S[2] = (tt > 0.0) ? ts / tt : 0.0; }
+        }
+    }
+}
+// x += alpha ph + omega sh;  r = s - omega t;  part = (rh,r), (r,r)
+__global__ void __launch_bounds__(kRedThreads) k_bi_xr(int n, double* __restrict__ x, const double* __restrict__ ph,
+                                                       const double* __restrict__ shv, double* __restrict__ r,
+                                                       const double* __restrict__ t, const double* __restrict__ rh,
+                                                       const double* __restrict__ scal, double* __restrict__ part) {
+    __shared__ double sh[32];
+    const size_t N = n;
+    double a[3] = {0.0, 0.0, 0.0}, b[3] = {0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int j = 0; j < 3; ++j) {
+            if (!mom_active(scal, j)) continue;
+            const double alpha = scal[kMomScal * j + 1], omega = scal[kMomScal * j + 2];
+            x[j * N + i] += alpha * ph[j * N + i] + omega * shv[j * N + i];
+            const double ri = r[j * N + i] - omega * t[j * N + i];
+            r[j * N + i] = ri;
+            a[j] += rh[j * N + i] * ri;
+            b[j] += ri * ri;
+        }
+    for (int j = 0; j < 3; ++j) {
+        const double u = block_sum(a[j], sh);
+        const double w = block_sum(b[j], sh);
+        if (threadIdx.x == 0) { part[(2 * j) * kRedBlocks + blockIdx.x] = u; part[(2 * j + 1) * kRedBlocks + blockIdx.x] = w; }
+    }
+}
+__global__ void k_bi_fin3(const double* __restrict__ part, double* __restrict__ scal, double tol2) {
+    __shared__ double sh[32];
+    for (int j = 0; j < 3; ++j) {
+        const double rho1 = sum_parts(part + (2 * j) * kRedBlocks, sh);
+        const double rr = sum_parts(part + (2 * j + 1) * kRedBlocks, sh);
+        if (threadIdx.x == 0) {
+            double* S = scal + kMomScal * j;
+            if (S[9] != 0.0) {
+                S[7] = rr;
+                if (rr <= tol2 * S[8]) {
+                    S[9] = 0.0;                                     // converged
+                } else if (rho1 == 0.0 || S[2] == 0.0 || !isfinite(rr)) {
+                    S[10] = 1.0; S[9] = 0.0;                        // breakdown
+                } else {
+                    S[3] = (rho1 / S[0]) * (S[1] / S[2]);
+                    S[0] = rho1;
+                }
+            }
+        }
+    }
+}
+// r = b - A x;  part = (r,r) per system
+__global__ void __launch_bounds__(kRedThreads) k_bi_res(SellView<double> A, const double* __restrict__ x,
+                                                        const double* __restrict__ b, double* __restrict__ part) {
+    __shared__ double sh[32];
+    const size_t N = A.n;
+    double d[3] = {0.0, 0.0, 0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+        double y[3];
+        sell_mv3(A, row, x, N, y[0], y[1], y[2]);
+        for (int j = 0; j < 3; ++j) { const double ri = b[j * N + row] - y[j]; d[j] += ri * ri; }
+    }
+    for (int j = 0; j < 3; ++j) {
+        const double t = block_sum(d[j], sh);
+        if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
+    }
+}
+__global__ void k_bi_fin_res(const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sh[32];
+    for (int j = 0; j < 3; ++j) {
+        const double rr = sum_parts(part + j * kRedBlocks, sh);
+        if (threadIdx.x == 0) out[j] = rr;
+    }
+}
+__global__ void k_dinv_dig(int n, const int* __restrict__ dig, const double* __restrict__ val,
+                           double* __restrict__ dinv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dinv[i] = 1.0 / val[dig[i]];
+}
+
+struct MomState {
+    Sell<double> A;
+    DBuf<double> dinv, vec, part, scal;
+};
+MomState& mom_state(semo_ctx* c) {
+    if (!c->mom_apply) c->mom_apply = std::shared_ptr<void>(new MomState(), [](void* p) { delete (MomState*)p; });
+    return *(MomState*)c->mom_apply.get();
 }
 
 }  // namespace
@@ -750,6 +998,102 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
     SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
     info->setup_ms = t0;
     info->solve_ms = t1;
+}
+
+semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
+    StageScope stage(c, ST_MSOLVE);
+    cudaStream_t s = c->stream;
+    const int n = c->nc;
+    const size_t N = n;
+    MomState& st = mom_state(c);
+    c->xm.alloc(3 * N, s);
+    st.dinv.alloc(N, s);
+    st.vec.alloc(7 * 3 * N, s);       // r, rh, p, v, ph, sh, t
+    st.part.alloc(6 * kRedBlocks, s);
+    st.scal.alloc(3 * kMomScal, s);
+    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
+    double* r = st.vec.p;
+    double* rh = r + 3 * N;
+    double* p = rh + 3 * N;
+    double* v = p + 3 * N;
+    double* ph = v + 3 * N;
+    double* shv = ph + 3 * N;
+    double* t = shv + 3 * N;
+    // the recurrence residual is driven to half the tolerance so that the true
+    // residual, checked at the end, lands under it
+    const double tol2 = 0.25 * c->prm.mom_tol * c->prm.mom_tol;
+    SEMO_CUDA(cudaEventRecord(c->ev[0], s));
+    build_sell<double, double>(s, c->A_ptr, c->A_col, c->Am_val, n, st.A);
+    k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, c->A_dig, c->Am_val, st.dinv);
+    SEMO_CHECK_LAUNCH();
+    SEMO_CUDA(cudaEventRecord(c->ev[1], s));
+    const SellView<double> A = st.A.view();
+    k_bi_init<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->bm, c->xm, r, rh, p, v, st.part);
+    SEMO_CHECK_LAUNCH();
+    k_bi_fin0<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
+    SEMO_CHECK_LAUNCH();
+    double hs[3 * kMomScal];
+    SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    int iters[3] = {0, 0, 0};
+    for (int j = 0; j < 3; ++j)
+        if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite momentum right-hand side");
+    auto any_active = [&] { return hs[9] != 0.0 || hs[kMomScal + 9] != 0.0 || hs[2 * kMomScal + 9] != 0.0; };
+    int it = 0;
+    while (any_active() && it < c->prm.mom_max_iter) {
+        for (int j = 0; j < 3; ++j) if (hs[kMomScal * j + 9] != 0.0) ++iters[j];
+        k_bi_p<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, p, v, ph, st.scal);
+        SEMO_CHECK_LAUNCH();
+        k_bi_mv1<<<kRedBlocks, kRedThreads, 0, s>>>(A, ph, v, rh, st.scal, st.part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_fin1<<<1, 256, 0, s>>>(st.part, st.scal);
+        SEMO_CHECK_LAUNCH();
+        k_bi_s<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, v, shv, st.scal);
+        SEMO_CHECK_LAUNCH();
+        k_bi_mv2<<<kRedBlocks, kRedThreads, 0, s>>>(A, shv, t, r, st.scal, st.part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_fin2<<<1, 256, 0, s>>>(st.part, st.scal);
+        SEMO_CHECK_LAUNCH();
+        k_bi_xr<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->xm, ph, shv, r, t, rh, st.scal, st.part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_fin3<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
+        SEMO_CHECK_LAUNCH();
+        SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        ++it;
+        for (int j = 0; j < 3; ++j)
+            if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the momentum residual");
+    }
+    // true FP64 residuals of the returned solutions
+    k_bi_res<<<kRedBlocks, kRedThreads, 0, s>>>(A, c->xm, c->bm, st.part);
+    SEMO_CHECK_LAUNCH();
+    k_bi_fin_res<<<1, 256, 0, s>>>(st.part, st.scal.p + 3 * kMomScal - 3);
+    SEMO_CHECK_LAUNCH();
+    double tr[3];
+    SEMO_CUDA(cudaMemcpyAsync(tr, st.scal.p + 3 * kMomScal - 3, sizeof(tr), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaEventRecord(c->ev[2], s));
+    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
+    float t0 = 0, t1 = 0;
+    SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
+    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
+    semo_status worst = SEMO_OK;
+    for (int j = 0; j < 3; ++j) {
+        const double bb = hs[kMomScal * j + 8];
+        const double rel = (bb > 0.0) ? std::sqrt(tr[j] / bb) : 0.0;
+        if (info) {
+            info[j] = semo_solve_info{};
+            info[j].iterations = iters[j];
+            info[j].rel_residual = rel;
+            info[j].levels = 1;
+            info[j].coarse_size = n;
+            info[j].operator_complexity = 1.0;
+            info[j].setup_ms = t0;
+            info[j].solve_ms = t1;
+        }
+        if (hs[kMomScal * j + 10] != 0.0 && !(rel <= c->prm.mom_tol)) worst = SEMO_ERR_BREAKDOWN;
+        else if (!(rel <= c->prm.mom_tol) && worst == SEMO_OK) worst = SEMO_ERR_NOT_CONVERGED;
+    }
+    return worst;
 }
 
 // Adjoint solve on the hierarchy of the last forward solve (the pressure

@@ -38,11 +38,12 @@ extern long long g_kernel_launches;
 // Named stages timed with CUDA events on the context's stream when profiling is on.
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
-             ST_SETUP_COARSE, ST_COUNT };
+             ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
-                                                  "setup_level", "setup_coarse"};
+                                                  "setup_level", "setup_coarse", "mface", "mcell", "msolve",
+                                                  "mupdate"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -151,7 +152,7 @@ struct semo_ctx {
     // ---- fields (RCM order) ----
     semo::DBuf<double> P, U, V, W, VF, rho, irho;
     semo::DBuf<double> grad;                      // 15 planes: P,U,V,W,VF x (x,y,z)
-    semo::DBuf<double> mm;                        // 8 planes: maxU,minU,maxV,minV,maxW,minW,maxVF,minVF
+    semo::DBuf<double> mm;                        // 10 planes: maxU,minU,maxV,minV,maxW,minW,maxVF,minVF,maxP,minP
     semo::DBuf<double> sg;                        // 4 planes gravity source
     semo::DBuf<double> bface;                     // boundary face values: 10 planes of nb
     semo::DBuf<double> fscr;                      // face scratch: 3 planes of nf
@@ -161,6 +162,16 @@ struct semo_ctx {
     semo::DBuf<double> stage;                     // caller-order staging for field copies (5 planes)
     semo::DBuf<int> dperm;                        // RCM permutation on the device: dperm[r] = caller's cell
     bool has_src = false;
+
+    // ---- momentum equation (RCM order; matrix on the A_ptr/A_col pattern) ----
+    semo::DBuf<double> mu;                        // 2 planes: cell viscosity, its reciprocal
+    semo::DBuf<double> old;                       // 6 planes: oldU, oldV, oldW, old2U, old2V, old2W
+    bool has_old = false;
+    semo::DBuf<double> Am_val;                    // values; dropped off-diagonals hold 0
+    semo::DBuf<double> bm, xm;                    // 3 planes each (x, y, z)
+    semo::DBuf<double> msc;                       // face scratch: 8 planes of nf
+    bool mom_assembled = false;
+    std::shared_ptr<void> mom_apply;              // momentum Krylov state (cycle.cu)
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
 
@@ -238,7 +249,10 @@ void geometry_build(semo_ctx* c, const double* d_points, const int* d_fptr, cons
 // assemble.cu
 void assemble_pressure(semo_ctx* c);
 double pressure_update(semo_ctx* c);
-void assemble_face_values(semo_ctx* c);
+// EOS + boundary face values (+ cell viscosity when with_mu)
+void assemble_face_values(semo_ctx* c, bool with_mu);
+// gravity source + one stencil pass (gradients of P,U,V,W,VF; min/max of U,V,W,VF,P)
+void assemble_gravity_stencil(semo_ctx* c);
 // dst[q][r] = src[q*n + perm[r]] for q < planes; false if any value is not finite (syncs)
 bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes);
 // dst[q*n + perm[r]] = src[q][r] for q < planes (async)
@@ -258,6 +272,13 @@ void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double*
                   const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess);
 
 void solve_transpose_reuse(semo_ctx* c, const double* d_g, double* d_lam, semo_solve_info* info);
+// three right-hand sides of the momentum system (c->Am_val, c->bm) -> c->xm; info[3]; returns the
+// worst status (SEMO_OK, SEMO_ERR_NOT_CONVERGED or SEMO_ERR_BREAKDOWN)
+semo_status solve_momentum(semo_ctx* c, semo_solve_info* info);
+
+// momentum.cu
+void assemble_momentum(semo_ctx* c);
+double momentum_update(semo_ctx* c);
 
 int sm_count(int device);
 
