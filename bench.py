@@ -215,7 +215,8 @@ def run_gpu_arm(args, rank, world, local) -> None:
     def pressure(ctx):
         return ctx.calc_pressure_eq()
 
-    ctx = S.Context(precision="mixed", tol=1e-8, device=local)
+    # every step rebuilds the AMG hierarchy, as SEMO's solveAMGCL does per call
+    ctx = S.Context(precision="mixed", tol=1e-8, device=local, reuse_hierarchy=False)
     ctx.set_case(case)
     minfo = ctx.mesh_info()
     strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
@@ -303,8 +304,17 @@ def run_gpu_arm(args, rank, world, local) -> None:
     ms_adj = e0.elapsed_time(e1)
     ctx.close()
 
+    # ---- hierarchy kept across outer iterations (bit-identical pressure matrix) --
+    ctxr = S.Context(precision="mixed", tol=1e-8, device=local, reuse_hierarchy=True)
+    ctxr.set_case(case)
+    strmr = torch.cuda.ExternalStream(ctxr.stream, device=torch.device(f"cuda:{local}"))
+    for _ in range(args.warmup):
+        ctxr.outer_iteration()
+    ms_reuse, infos_r = timed(ctxr, strmr, args.steps, outer)
+    ctxr.close()
+
     # ---- all-FP64 hierarchy and V-cycle ------------------------------------
-    ctx64 = S.Context(precision="fp64", tol=1e-8, device=local)
+    ctx64 = S.Context(precision="fp64", tol=1e-8, device=local, reuse_hierarchy=False)
     ctx64.set_case(case)
     strm64 = torch.cuda.ExternalStream(ctx64.stream, device=torch.device(f"cuda:{local}"))
     for _ in range(args.warmup):
@@ -364,6 +374,11 @@ def run_gpu_arm(args, rank, world, local) -> None:
                  "iterations": infos64[-1][3]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3),
                  "pressure_pass_ms": round(ms_fp64_p, 3),
                  "pressure_pass_mixed_speedup": round(ms_fp64_p / ms_pres, 3)},
+        "hierarchy_reuse": {"value": mc(ms_reuse), "ms_per_step": round(ms_reuse, 3),
+                            "iterations": infos_r[-1][3]["iterations"],
+                            "setup_ms_last_step": round(infos_r[-1][3]["setup_ms"], 3),
+                            "note": "pressure AMG hierarchy kept while the assembled matrix stays bit-identical "
+                                    "(outer iterations within a time step); the headline rebuilds it every step"},
         "adjoint": {"ms_adjoint_solve": round(ms_adj, 3), "ms_forward_solve": round(ms_fwd, 3),
                     "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
                     "adj_over_fwd_pass": round(ms_adj / ms_pres, 3), "iterations": ainfo["iterations"]},

@@ -65,6 +65,8 @@ typedef struct {
     int coarse_enough;           /* direct solve at or below this size; default 64 */
     int max_levels;              /* default 24 */
     int cheb_degree;             /* Chebyshev pre/post smoothing degree; default 2 */
+    int reuse_hierarchy;         /* keep the pressure AMG hierarchy when the assembled matrix is bit-identical
+                                    to the one it was built from (same hierarchy, same result); default 1 */
     /* momentum solve (BiCGStab, Jacobi preconditioner, per right-hand side) */
     double mom_tol;              /* relative residual, default 1e-9 (SEMO's momentum tolerance) */
     int mom_max_iter;            /* default 1000 */

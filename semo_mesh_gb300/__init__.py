@@ -43,7 +43,8 @@ class SemoError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("eps_strong", C.c_double), ("coarse_enough", C.c_int), ("max_levels", C.c_int),
-                ("cheb_degree", C.c_int), ("mom_tol", C.c_double), ("mom_max_iter", C.c_int)]
+                ("cheb_degree", C.c_int), ("reuse_hierarchy", C.c_int), ("mom_tol", C.c_double),
+                ("mom_max_iter", C.c_int)]
 
 
 class Physics(C.Structure):
@@ -134,7 +135,7 @@ class Context:
 
     def __init__(self, precision: str = "mixed", tol: float = 1e-8, max_iter: int = 500, device: int = 0,
                  eps_strong: float = 0.08, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24,
-                 mom_tol: float = 1e-9, mom_max_iter: int = 1000):
+                 mom_tol: float = 1e-9, mom_max_iter: int = 1000, reuse_hierarchy: bool = True):
         self.L = load_library()
         p = Params()
         self.L.semo_params_default(C.byref(p))
@@ -146,6 +147,7 @@ class Context:
         p.coarse_enough = coarse_enough
         p.cheb_degree = cheb_degree
         p.max_levels = max_levels
+        p.reuse_hierarchy = 1 if reuse_hierarchy else 0
         p.mom_tol = mom_tol
         p.mom_max_iter = mom_max_iter
         h = C.c_void_p()

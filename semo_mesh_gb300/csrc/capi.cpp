@@ -58,6 +58,7 @@ void semo_params_default(semo_params* p) {
     p->coarse_enough = 64;
     p->max_levels = 24;
     p->cheb_degree = 2;
+    p->reuse_hierarchy = 1;
     p->mom_tol = 1e-9;
     p->mom_max_iter = 1000;
 }
@@ -175,7 +176,10 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         c->np = n_points; c->nf = nf; c->ni = ni; c->nc = nc; c->nb = nf - ni; c->npatch = n_patches;
         c->patch_start.assign(patch_start, patch_start + n_patches);
         c->patch_size.assign(patch_size, patch_size + n_patches);
-        c->mesh_ready = c->phys_ready = c->fields_ready = c->assembled = false;
+        c->mesh_ready = c->phys_ready = c->fields_ready = c->assembled = c->mom_assembled = false;
+        c->amg32.clear();
+        c->amg64.clear();
+        c->has_old = c->has_src = false;
 
         // ---- cell -> faces, ascending face index (connectCelltoFaces, build.cpp:587-608) ----
         std::vector<int> cfp(nc + 1, 0), cfi;
@@ -583,7 +587,7 @@ semo_status semo_solve_pressure(semo_ctx* c, double* x, semo_solve_info* info) {
         need(c->assembled, SEMO_ERR_STATE, "system not assembled");
         SEMO_CUDA(cudaSetDevice(c->device));
         semo_solve_info inf{};
-        semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
+        semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true, true);
         if (info) *info = inf;
         if (x) {
             c->stage.alloc(5 * (size_t)c->nc, c->stream);
@@ -608,7 +612,7 @@ semo_status pressure_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info)
     semo::assemble_pressure(c);
     c->assembled = true;
     semo_solve_info inf{};
-    semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true);
+    semo::solve_system(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, c->b.p, c->x.p, &inf, true, true);
     double nrm = semo::pressure_update(c);
     c->mom_assembled = false;
     if (norm) *norm = nrm;

@@ -699,7 +699,21 @@ struct ApplyState {
     Cycle<float> cy32;
     Cycle<double> cy64;
     Sell<double> outer;
+    // the matrix values the current hierarchy was built from (pressure path only)
+    DBuf<double> src_val;
+    int src_n = 0;
+    int64_t src_nnz = 0;
+    int src_prec = -1;
 };
+
+// flag[0] = 1 if a and b differ anywhere (bit patterns)
+__global__ void k_differs(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                          int* __restrict__ flag) {
+    bool d = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d |= __double_as_longlong(a[i]) != __double_as_longlong(b[i]);
+    if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) flag[0] = 1;
+}
 ApplyState& apply_state(semo_ctx* c) {
     if (!c->apply) c->apply = std::shared_ptr<void>(new ApplyState(), [](void* p) { delete (ApplyState*)p; });
     return *(ApplyState*)c->apply.get();
@@ -962,23 +976,51 @@ MomState& mom_state(semo_ctx* c) {
 }  // namespace
 
 void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
-                  const double* b, double* x, semo_solve_info* info, bool zero_guess) {
+                  const double* b, double* x, semo_solve_info* info, bool zero_guess, bool may_reuse) {
     cudaStream_t s = c->stream;
     ApplyState& st = apply_state(c);
     c->flag.zero();
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
     {
         StageScope sc(c, ST_AMG_SETUP);
-        if (c->prm.precision == SEMO_PREC_MIXED) {
-            c->amg64.clear();
-            build_hierarchy<float>(c, c->amg32, ptr, col, val, n, nnz);
-            prepare_cycle(c, c->amg32, st.cy32);
-        } else {
-            c->amg32.clear();
-            build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
-            prepare_cycle(c, c->amg64, st.cy64);
+        // The hierarchy is a deterministic function of the matrix: when the
+        // values are bit-identical to the ones it was built from (the pressure
+        // matrix depends only on geometry, dt and the densities, so it repeats
+        // across the outer iterations of a time step), rebuilding would give
+        // the same hierarchy bit for bit, and it is kept instead.
+        bool reuse = false;
+        const Amg<float>& h32 = c->amg32;
+        const Amg<double>& h64 = c->amg64;
+        const bool have = (c->prm.precision == SEMO_PREC_MIXED) ? h32.ready : h64.ready;
+        if (may_reuse && c->prm.reuse_hierarchy && have && st.src_prec == c->prm.precision && st.src_n == n &&
+            st.src_nnz == nnz) {
+            k_differs<<<kRedBlocks, kRedThreads, 0, s>>>(nnz, val, st.src_val, c->flag.p + 10);
+            SEMO_CHECK_LAUNCH();
+            int differs = 1;
+            SEMO_CUDA(cudaMemcpyAsync(&differs, c->flag.p + 10, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SEMO_CUDA(cudaStreamSynchronize(s));
+            reuse = differs == 0;
         }
-        build_sell<double, double>(s, ptr, col, val, n, st.outer);
+        if (!reuse) {
+            if (c->prm.precision == SEMO_PREC_MIXED) {
+                c->amg64.clear();
+                build_hierarchy<float>(c, c->amg32, ptr, col, val, n, nnz);
+                prepare_cycle(c, c->amg32, st.cy32);
+            } else {
+                c->amg32.clear();
+                build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
+                prepare_cycle(c, c->amg64, st.cy64);
+            }
+            build_sell<double, double>(s, ptr, col, val, n, st.outer);
+            st.src_prec = -1;
+            if (may_reuse && c->prm.reuse_hierarchy) {
+                st.src_val.alloc(nnz, s);
+                SEMO_CUDA(cudaMemcpyAsync(st.src_val.p, val, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, s));
+                st.src_n = n;
+                st.src_nnz = nnz;
+                st.src_prec = c->prm.precision;
+            }
+        }
     }
     SEMO_CUDA(cudaEventRecord(c->ev[1], s));
     {

@@ -268,8 +268,10 @@ void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, con
 int device_scan(cudaStream_t s, int* d, int n);
 
 // cycle.cu
+// may_reuse: the matrix is the context's own pressure system, so a hierarchy
+// built from bit-identical values may be kept (semo_params.reuse_hierarchy)
 void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double* d_val, int n, int64_t nnz,
-                  const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess);
+                  const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess, bool may_reuse = false);
 
 void solve_transpose_reuse(semo_ctx* c, const double* d_g, double* d_lam, semo_solve_info* info);
 // three right-hand sides of the momentum system (c->Am_val, c->bm) -> c->xm; info[3]; returns the
