@@ -21,6 +21,8 @@
 // deterministic run to run.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -38,64 +40,6 @@ __device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
     // integer avalanche mixer (public-domain "lowbias32" constants)
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
     return x;
-}
-
-// ------------------------------------------------------------------ reductions
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    v = 0.0;
-    if (threadIdx.x < 32) {
-        v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-        v = warp_sum(v);
-    }
-    __syncthreads();
-    return v;
-}
-
-// part[blockIdx] = sum a_i b_i over a grid-stride slice
-template <class A, class B>
-__global__ void __launch_bounds__(kRedThreads) k_dot(int n, const A* __restrict__ a, const B* __restrict__ b,
-                                                     double* __restrict__ part) {
-    __shared__ double sh[32];
-    double s = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        s += (double)a[i] * (double)b[i];
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-// two dots at once: part[blk] = a.b, part[kRedBlocks+blk] = a.c
-template <class A>
-__global__ void __launch_bounds__(kRedThreads) k_dot2(int n, const A* __restrict__ a, const double* __restrict__ b,
-                                                      const double* __restrict__ c, double* __restrict__ part) {
-    __shared__ double sh[32];
-    double s = 0.0, t = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double ai = (double)a[i];
-        s += ai * b[i];
-        t += ai * c[i];
-    }
-    s = block_sum(s, sh);
-    t = block_sum(t, sh);
-    if (threadIdx.x == 0) { part[blockIdx.x] = s; part[kRedBlocks + blockIdx.x] = t; }
-}
-
-// sum `count` partial arrays (each kRedBlocks long) in fixed order -> out[0..count)
-__global__ void k_finish(const double* __restrict__ part, int count, double* __restrict__ out) {
-    __shared__ double sh[32];
-    for (int c = 0; c < count; ++c) {
-        double s = 0.0;
-        for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) s += part[c * kRedBlocks + i];
-        s = block_sum(s, sh);
-        if (threadIdx.x == 0) out[c] = s;
-    }
 }
 
 // --------------------------------------------------------------------- scans
@@ -195,22 +139,53 @@ __global__ void __launch_bounds__(kRedThreads) k_max(int n, const double* __rest
     }
 }
 
-template <class V>
+// The per-row setup kernels below run VS lanes per row (VS = 1: a thread per
+// row).  Fine levels have ~7 entries a row and use one thread; coarse levels
+// (tens to hundreds of entries a row, few rows) use 8 or 32 lanes so that a
+// row is not one thread walking hundreds of dependent loads.  Lanes of a row
+// are consecutive within a warp; every lane reaches the group shuffles.
+constexpr unsigned kFull = 0xffffffffu;
+template <int VS>
+__device__ __forceinline__ void row_lane(int& i, int& lane) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    i = g / VS;
+    lane = g % VS;
+}
+template <int VS>
+__device__ __forceinline__ unsigned long long grp_max(unsigned long long v) {
+#pragma unroll
+    for (int o = VS / 2; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(kFull, v, o, VS);
+        v = (t > v) ? t : v;
+    }
+    return v;
+}
+template <int VS>
+__device__ __forceinline__ int grp_sum(int v) {
+#pragma unroll
+    for (int o = VS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o, VS);
+    return v;
+}
+
+template <class V, int VS>
 __global__ void k_strength(int n, const int* __restrict__ ptr, const int* __restrict__ col, const V* __restrict__ val,
                            const V* __restrict__ dia, double eps2, unsigned char* __restrict__ strong,
                            int* __restrict__ state) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const V ed = (V)(eps2 * (double)dia[i]);
+    int i, lane;
+    row_lane<VS>(i, lane);
     int has = 0;
-    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
-        const int j = col[k];
-        const V v = val[k];
-        const unsigned char s = (j != i) && (ed * dia[j] < v * v);
-        strong[k] = s;
-        has |= s;
+    if (i < n) {
+        const V ed = (V)(eps2 * (double)dia[i]);
+        for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS) {
+            const int j = col[k];
+            const V v = val[k];
+            const unsigned char s = (j != i) && (ed * dia[j] < v * v);
+            strong[k] = s;
+            has |= s;
+        }
     }
-    state[i] = has ? 1 : -1;   // -1: no strong connection, never aggregated
+    has = grp_sum<VS>(has);
+    if (i < n && lane == 0) state[i] = has ? 1 : -1;   // -1: no strong connection, never aggregated
 }
 
 __device__ __forceinline__ unsigned long long mis_key(int st, int i) {
@@ -218,28 +193,39 @@ __device__ __forceinline__ unsigned long long mis_key(int st, int i) {
     return (s << 62) | ((unsigned long long)hash_u32((uint32_t)i) << 30) | (unsigned long long)i;
 }
 
+template <int VS>
 __global__ void k_mis_max1(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                            const unsigned char* __restrict__ strong, const int* __restrict__ state,
                            unsigned long long* __restrict__ m1) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned long long m = mis_key(state[i], i);
-    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
-        if (strong[k]) {
-            const int j = col[k];
-            const unsigned long long t = mis_key(state[j], j);
-            m = (t > m) ? t : m;
-        }
-    m1[i] = m;
+    int i, lane;
+    row_lane<VS>(i, lane);
+    unsigned long long m = 0;
+    if (i < n) {
+        if (lane == 0) m = mis_key(state[i], i);
+        for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS)
+            if (strong[k]) {
+                const int j = col[k];
+                const unsigned long long t = mis_key(state[j], j);
+                m = (t > m) ? t : m;
+            }
+    }
+    m = grp_max<VS>(m);
+    if (i < n && lane == 0) m1[i] = m;
 }
+template <int VS>
 __global__ void k_mis_max2(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                            const unsigned char* __restrict__ strong, const unsigned long long* __restrict__ m1,
                            int* __restrict__ state, int* __restrict__ undecided) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned long long m = m1[i];
-    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
-        if (strong[k]) { const unsigned long long t = m1[col[k]]; m = (t > m) ? t : m; }
+    int i, lane;
+    row_lane<VS>(i, lane);
+    unsigned long long m = 0;
+    if (i < n) {
+        if (lane == 0) m = m1[i];
+        for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS)
+            if (strong[k]) { const unsigned long long t = m1[col[k]]; m = (t > m) ? t : m; }
+    }
+    m = grp_max<VS>(m);
+    if (i >= n || lane != 0) return;
     const int st = state[i];
     if (st != 1) return;
     // decided from the round's snapshot (m1 was computed before any update)
@@ -258,27 +244,34 @@ __global__ void k_root_ids(int n, const int* __restrict__ state, const int* __re
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) agg[i] = (state[i] == 2) ? scanned[i] : -1;
 }
+// an undecided node joins the aggregate of its strong neighbour with the
+// largest (hash, index) key; keys are unique, so the choice is order-free
+template <int VS>
 __global__ void k_agg_join(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                            const unsigned char* __restrict__ strong, const int* __restrict__ state,
                            const int* __restrict__ agg_in, int* __restrict__ agg_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int a = agg_in[i];
-    if (a < 0 && state[i] >= 0) {
-        unsigned long long best = 0;
-        int ba = -1;
-        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+    int i, lane;
+    row_lane<VS>(i, lane);
+    const bool look = i < n && agg_in[i] < 0 && state[i] >= 0;
+    unsigned long long best = 0;   // key + 1; 0 = none
+    if (look)
+        for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS) {
             const int j = col[k];
             if (!strong[k] || agg_in[j] < 0) continue;
-            const unsigned long long kj = ((unsigned long long)hash_u32((uint32_t)j) << 32) | (unsigned long long)j;
-            if (ba < 0 || kj > best) { best = kj; ba = agg_in[j]; }
+            const unsigned long long kj = (((unsigned long long)hash_u32((uint32_t)j) << 32) | (unsigned long long)j) + 1;
+            best = (kj > best) ? kj : best;
         }
-        a = ba;
-    }
-    agg_out[i] = a;
+    best = grp_max<VS>(best);
+    if (i >= n || lane != 0) return;
+    agg_out[i] = look ? (best ? agg_in[(int)((best - 1) & 0xffffffffull)] : -1) : agg_in[i];
 }
 
 // prolongation row i: (1-w) e_agg(i) + sum over strong j of (-w/df_i) a_ij e_agg(j), merged, sorted
+__device__ __forceinline__ bool p_eligible(int i, int k, const int* col, const unsigned char* strong,
+                                           const int* agg) {
+    const int j = col[k];
+    return (j == i || strong[k]) && agg[j] >= 0;
+}
 template <class V>
 __global__ void k_prolong_count(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                 const unsigned char* __restrict__ strong, const int* __restrict__ agg,
@@ -334,6 +327,62 @@ __global__ void k_prolong_fill(int n, const int* __restrict__ ptr, const int* __
         pval[t + 1] = vv;
     }
 }
+// the same rows with VS lanes: first[k] marks an entry whose aggregate has not
+// appeared earlier in its row; a row's output is its first entries ranked by
+// aggregate, each summing its aggregate's contributions in entry order -- the
+// same values and order as the one-thread kernels above.
+template <int VS>
+__global__ void k_prolong_count_vs(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                   const unsigned char* __restrict__ strong, const int* __restrict__ agg,
+                                   unsigned char* __restrict__ first, int* __restrict__ cnt) {
+    int i, lane;
+    row_lane<VS>(i, lane);
+    int c = 0;
+    if (i < n)
+        for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS) {
+            bool f = p_eligible(i, k, col, strong, agg);
+            if (f) {
+                const int g = agg[col[k]];
+                for (int t = ptr[i]; t < k; ++t)
+                    if (p_eligible(i, t, col, strong, agg) && agg[col[t]] == g) { f = false; break; }
+            }
+            first[k] = f;
+            c += f;
+        }
+    c = grp_sum<VS>(c);
+    if (i < n && lane == 0) cnt[i] = c;
+}
+template <class V, int VS>
+__global__ void k_prolong_fill_vs(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                  const V* __restrict__ val, const unsigned char* __restrict__ strong,
+                                  const int* __restrict__ agg, const unsigned char* __restrict__ first, double omega,
+                                  const int* __restrict__ pptr, int* __restrict__ pcol, V* __restrict__ pval) {
+    int i, lane;
+    row_lane<VS>(i, lane);
+    if (i >= n) return;   // no group collectives below
+    const int kb = ptr[i], ke = ptr[i + 1];
+    double df = 0.0;
+    for (int k = kb; k < ke; ++k)
+        if (col[k] == i || !strong[k]) df += (double)val[k];
+    df = -omega * (1.0 / df);
+    for (int k = kb + lane; k < ke; k += VS) {
+        if (!first[k]) continue;
+        const int g = agg[col[k]];
+        int rank = 0;
+        double sum = 0.0;
+        bool started = false;
+        for (int t = kb; t < ke; ++t) {
+            if (first[t] && agg[col[t]] < g) ++rank;
+            if (t >= k && p_eligible(i, t, col, strong, agg) && agg[col[t]] == g) {
+                const double v = (col[t] == i) ? (1.0 - omega) : df * (double)val[t];
+                sum = started ? (double)(V)(sum + v) : (double)(V)v;
+                started = true;
+            }
+        }
+        pcol[pptr[i] + rank] = g;
+        pval[pptr[i] + rank] = (V)sum;
+    }
+}
 
 // transpose: count per column, then place, then sort each row by column
 __global__ void k_col_count(int64_t nnz, const int* __restrict__ col, int* __restrict__ cnt) {
@@ -369,18 +418,28 @@ __global__ void k_sort_rows(int n, const int* __restrict__ ptr, const int* __res
     }
 }
 
-__global__ void k_max_int(int n, const int* __restrict__ a, int* __restrict__ out) {
-    __shared__ int sh[32];
-    int m = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, a[i]);
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int r = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = max(r, sh[w]);
-        atomicMax(out, r);
-    }
+
+// products of row i of A*B (sum of the B-row lengths it touches); out[n] stays 0
+__global__ void k_row_products(int n, const int* __restrict__ aptr, const int* __restrict__ acol,
+                               const int* __restrict__ bptr, int* __restrict__ prod, int* __restrict__ maxprod) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int p = 0;
+    if (i < n)
+        for (int k = aptr[i]; k < aptr[i + 1]; ++k) p += bptr[acol[k] + 1] - bptr[acol[k]];
+    if (i < n) prod[i] = p;
+    int m = p;
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxprod, m);
+}
+// copy row i from its upper-bound slot (uptr) to its exact place (cptr), one warp a row
+template <class V>
+__global__ void k_compact_rows(int n, const int* __restrict__ uptr, const int* __restrict__ cptr,
+                               const int* __restrict__ tcol, const V* __restrict__ tval, int* __restrict__ ccol,
+                               V* __restrict__ cval) {
+    const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const int src = uptr[row], dst = cptr[row], len = cptr[row + 1] - dst;
+    for (int e = lane; e < len; e += 32) { ccol[dst + e] = tcol[src + e]; cval[dst + e] = tval[src + e]; }
 }
 
 // Thread-per-row SpGEMM for rows with few distinct columns (the finest
@@ -404,7 +463,7 @@ __global__ void __launch_bounds__(128) k_spgemm_small(int n, const int* __restri
     if (row >= n) return;
     if (pass == 1 && small[row] < 0) return;
     const int ab = aptr[row], ae = aptr[row + 1];
-    if (pass == 0) {
+    if (pass != 1) {
         int prod = 0;
         for (int ka = ab; ka < ae; ++ka) prod += bptr[acol[ka] + 1] - bptr[acol[ka]];
         if (prod > kSmallMaxProducts) { small[row] = -1; return; }
@@ -420,7 +479,7 @@ __global__ void __launch_bounds__(128) k_spgemm_small(int n, const int* __restri
         const V av = aval[ka];
         for (int q = bptr[a]; q < bptr[a + 1]; ++q) {
             const int cq = bcol[q];
-            const V pv = (pass == 1) ? av * bval[q] : V(0);
+            const V pv = (pass != 0) ? av * bval[q] : V(0);
             bool found = false;
 #pragma unroll
             for (int t = 0; t < kSmallCap; ++t)
@@ -442,17 +501,15 @@ __global__ void __launch_bounds__(128) k_spgemm_small(int n, const int* __restri
     if (pass == 0) {
         small[row] = over ? -1 : d;
     } else {
+        if (pass == 2) {
+            small[row] = over ? -1 : d;
+            if (over) return;
+        }
         const int base = cptr[row];
 #pragma unroll
         for (int t = 0; t < kSmallCap; ++t)
             if (t < d) { ccol[base + t] = cols[t]; cval[base + t] = vals[t]; }
     }
-}
-__global__ void k_count_negative(int n, const int* __restrict__ a, int* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool neg = i < n && a[i] < 0;
-    const unsigned b = __ballot_sync(0xffffffffu, neg);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, __popc(b));
 }
 
 // Row-wise SpGEMM C = A * B, one warp per row, open-addressing hash table in
@@ -471,7 +528,8 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                                                             int* __restrict__ cnt, const int* __restrict__ cptr,
                                                             int* __restrict__ ccol, V* __restrict__ cval,
                                                             int* __restrict__ overflow,
-                                                            const int* __restrict__ small) {
+                                                            const int* __restrict__ small, int defer,
+                                                            int* __restrict__ list, int* __restrict__ nlist) {
     extern __shared__ unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // per warp: keys[HT] int, ckeys[HT] int, vals[HT] double, cvals[HT] double
@@ -479,11 +537,15 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
     int* ckeys = keys + HT;
     double* vals = reinterpret_cast<double*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
     double* cvals = vals + HT;
-    for (int row = blockIdx.x * kGemmWarps + wid; row < n; row += gridDim.x * kGemmWarps) {
+    // rows: all of them, or (list given, defer 0) the ones a previous launch deferred
+    const int nrows = (list && !defer) ? *nlist : n;
+    for (int idx = blockIdx.x * kGemmWarps + wid; idx < nrows; idx += gridDim.x * kGemmWarps) {
+        const int row = (list && !defer) ? list[idx] : idx;
         if (small && small[row] >= 0) {   // the row was done by the thread-per-row kernel
             if (pass == 0 && lane == 0) cnt[row] = small[row];
             continue;
         }
+        __syncwarp();
         // table size for this row (power of two, 32..HT): from the product
         // count in the counting pass, from the known column count when filling
         int need;
@@ -546,7 +608,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 }
                 distinct += __popc(__ballot_sync(0xffffffffu, fresh));
                 const bool lost = __any_sync(0xffffffffu, act && slot < 0);
-                if (pass == 1 && !lost) {
+                if (pass != 0 && !lost) {
                     // lanes that hit the same column are summed in lane order by the lowest one
                     const double pv = act ? av * (double)bval[q] : 0.0;
                     const unsigned grp = __match_any_sync(0xffffffffu, act ? slot : -1 - lane);
@@ -563,9 +625,16 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 if (lost || distinct > (ht * 3) / 4) { full = true; break; }
             }
         }
+        if (full && pass == 2 && defer) {
+            // single pass: a row that fills this launch's table is left for
+            // the next launch, made with a larger one (it has written nothing)
+            if (lane == 0) list[atomicAdd(nlist, 1)] = row;   // list order does not affect any result
+            __syncwarp();
+            continue;
+        }
         if (full) {
             if (lane == 0) atomicExch(overflow, 1);
-            if (pass == 0 && lane == 0) cnt[row] = 0;
+            if (pass != 1 && lane == 0) cnt[row] = 0;
             __syncwarp();
             continue;
         }
@@ -585,6 +654,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 }
                 base_c += __popc(bal);
             }
+            if (pass == 2 && lane == 0) cnt[row] = base_c;
             __syncwarp();
             const int out = cptr[row];
             for (int e = lane; e < base_c; e += 32) {
@@ -651,6 +721,15 @@ __global__ void k_gauss_jordan(int n, double* __restrict__ a, double* __restrict
 }
 
 // ------------------------------------------------------------- host helpers
+// lanes per row for the per-row setup kernels, from the average row length
+template <class F>
+void with_row_lanes(int64_t nnz, int n, F&& f) {
+    const double avg = n ? (double)nnz / n : 1.0;
+    if (avg <= 12.0) f(std::integral_constant<int, 1>{});
+    else if (avg <= 48.0) f(std::integral_constant<int, 8>{});
+    else f(std::integral_constant<int, 32>{});
+}
+
 template <class V>
 int pick_vs(const DCsr<V>& A) {
     const double avg = A.n ? (double)A.nnz / A.n : 1.0;
@@ -659,7 +738,8 @@ int pick_vs(const DCsr<V>& A) {
 
 template <class V>
 void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C, int* cnt,
-                 int* overflow, const int* small) {
+                 int* overflow, const int* small, const int* cptr, int* ccol, V* cval, int defer, int* list,
+                 int* nlist) {
     const int n = A.n;
     const size_t shm = (size_t)kGemmWarps * ht * 2 * (sizeof(int) + sizeof(double));
     const int grid = std::max(1, std::min(blocks(n, kGemmWarps), 152 * 32));
@@ -668,7 +748,7 @@ void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<
         if (shm > 48 * 1024)                                                                                     \
             SEMO_CUDA(cudaFuncSetAttribute(k_spgemm<V, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm)); \
         k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, pass, cnt,  \
-                                                           C.ptr, C.col.p, C.val.p, overflow, small);            \
+                                                           cptr, ccol, cval, overflow, small, defer, list, nlist); \
         break;
     switch (ht) {
         SEMO_GEMM_CASE(64)
@@ -683,67 +763,66 @@ void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<
     SEMO_CHECK_LAUNCH();
 }
 
+// C = A * B in one numeric pass: every row is computed into a slot sized by
+// its product count (an upper bound on its distinct columns), then the rows
+// are compacted to their exact lengths.  Rows with few products go to the
+// thread-per-row kernel, the rest to the warp hash kernel.
 template <class V>
 void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C) {
     const int n = A.n;
     C.n = n;
     C.m = B.m;
     C.ptr.alloc(n + 1, s);
-    DBuf<int> flags, small;
+    DBuf<int> up, cnt, flags;
+    up.alloc(n + 1, s);
+    cnt.alloc(std::max(n, 1), s);
     flags.alloc(2, s);
-    small.alloc(std::max(n, 1), s);
-    // thread-per-row counting pass; rows it cannot hold are marked -1
     flags.zero();
-    k_spgemm_small<V><<<blocks(n, 128), 128, 0, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, 0, small.p,
-                                                     nullptr, nullptr, nullptr);
+    SEMO_CUDA(cudaMemsetAsync(up.p + n, 0, sizeof(int), s));
+    k_row_products<<<blocks(n, 256), 256, 0, s>>>(n, A.ptr, A.col, B.ptr, up.p, flags.p + 1);
     SEMO_CHECK_LAUNCH();
-    k_count_negative<<<blocks(n, 256), 256, 0, s>>>(n, small.p, flags.p + 1);
-    SEMO_CHECK_LAUNCH();
-    int nbig = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&nbig, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    const int64_t total = scan_exclusive(s, up.p, n + 1);   // syncs
+    int maxprod = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&maxprod, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
-    // warp counting pass for the marked rows, with a growing table until none
-    // overflows; all counts land in C.ptr
-    int ht = 256, of = 0;
-    if (nbig == 0) {
-        SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, small.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
-        SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
-    } else {
-        for (;;) {
-            flags.zero();
-            SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
-            spgemm_pass(s, ht, 0, A, B, C, C.ptr.p, flags.p, small.p);
-            SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-            SEMO_CUDA(cudaStreamSynchronize(s));
-            if (!of) break;
-            if (ht >= 2048) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
-            ht <<= 1;
-        }
-    }
-    // pass 1 with the smallest table that holds the densest row at <= 3/4 load
-    DBuf<int> mx;
-    mx.alloc(1, s);
-    mx.zero();
-    k_max_int<<<std::min(blocks(n, 256), 1024), 256, 0, s>>>(n, C.ptr, mx);
+    DBuf<int> tcol;
+    DBuf<V> tval;
+    tcol.alloc(std::max<int64_t>(total, 1), s);
+    tval.alloc(std::max<int64_t>(total, 1), s);
+    k_spgemm_small<V><<<blocks(n, 128), 128, 0, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, 2, cnt.p, up.p,
+                                                     tcol.p, tval.p);
     SEMO_CHECK_LAUNCH();
-    int maxd = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&maxd, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (maxprod > kSmallMaxProducts) {
+        // tables sized per row from its products (<= 3/4 load); most rows fit
+        // a 256-slot table, which keeps shared memory per block small; the
+        // rest go to one more launch sized for the densest row
+        int ht = 64;
+        while (ht < 2048 && ht * 3 / 4 < maxprod + 2) ht <<= 1;
+        const int first = std::min(ht, 256);
+        DBuf<int> list, nlist;
+        if (ht > first) {
+            list.alloc(std::max(n, 1), s);
+            nlist.alloc(1, s);
+            nlist.zero();
+        }
+        spgemm_pass(s, first, 2, A, B, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, ht > first ? 1 : 0, list.p,
+                    nlist.p);
+        if (ht > first)
+            spgemm_pass(s, ht, 2, A, B, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, 0, list.p, nlist.p);
+    }
+    SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, cnt.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+    SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
     const int nnz = scan_exclusive(s, C.ptr.p, n + 1);   // syncs
-    int ht1 = 64;
-    while (ht1 * 3 / 4 < maxd + 32 && ht1 < ht) ht1 <<= 1;
+    int of = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
     C.nnz = nnz;
     C.col.alloc(std::max(nnz, 1), s);
     C.val.alloc(std::max(nnz, 1), s);
-    flags.zero();
-    k_spgemm_small<V><<<blocks(n, 128), 128, 0, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, 1, small.p,
-                                                     C.ptr.p, C.col.p, C.val.p);
+    k_compact_rows<V><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, up.p, C.ptr.p, tcol.p, tval.p, C.col.p,
+                                                                   C.val.p);
     SEMO_CHECK_LAUNCH();
-    if (nbig > 0) {
-        spgemm_pass(s, ht1, 1, A, B, C, nullptr, flags.p, small.p);
-        SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM numeric pass overflowed its table");
-    }
     (void)c;
 }
 
@@ -837,7 +916,11 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         int nagg = 0;
         {
             StageScope sc(c, ST_SETUP_AGG);
-            k_strength<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, dia, eps2, strong, state);
+            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                constexpr int VS = decltype(vs)::value;
+                k_strength<V, VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, dia,
+                                                                                eps2, strong, state);
+            });
             SEMO_CHECK_LAUNCH();
             // rounds are launched in pairs between checks: a round after the
             // last undecided node is gone changes nothing
@@ -845,10 +928,14 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
             for (int round = 0; round < 200 && hu; round += 2) {
                 for (int k = 0; k < 2; ++k) {
                     undec.zero();
-                    k_mis_max1<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, m1);
-                    SEMO_CHECK_LAUNCH();
-                    k_mis_max2<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, undec);
-                    SEMO_CHECK_LAUNCH();
+                    with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                        constexpr int VS = decltype(vs)::value;
+                        const int g = blocks((int64_t)nl * VS, 256);
+                        k_mis_max1<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, m1);
+                        SEMO_CHECK_LAUNCH();
+                        k_mis_max2<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, undec);
+                        SEMO_CHECK_LAUNCH();
+                    });
                 }
                 SEMO_CUDA(cudaMemcpyAsync(&hu, undec.p, sizeof(int), cudaMemcpyDeviceToHost, s));
                 SEMO_CUDA(cudaStreamSynchronize(s));
@@ -861,7 +948,11 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
                 k_root_ids<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2, agg);
                 SEMO_CHECK_LAUNCH();
                 for (int pass = 0; pass < 2; ++pass) {
-                    k_agg_join<<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, agg, agg2);
+                    with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                        constexpr int VS = decltype(vs)::value;
+                        k_agg_join<VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong,
+                                                                                     state, agg, agg2);
+                    });
                     SEMO_CHECK_LAUNCH();
                     std::swap(agg.p, agg2.p);
                 }
@@ -875,13 +966,35 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         L.P.n = nl; L.P.m = nagg;
         L.P.ptr.alloc(nl + 1, s);
         SEMO_CUDA(cudaMemsetAsync(L.P.ptr.p + nl, 0, sizeof(int), s));
-        k_prolong_count<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg, L.P.ptr);
+        DBuf<unsigned char> first;
+        int lanes = 1;
+        with_row_lanes(L.A.nnz, nl, [&](auto vs) { lanes = decltype(vs)::value; });
+        if (lanes == 1) {
+            k_prolong_count<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg, L.P.ptr);
+        } else {
+            first.alloc(std::max<int64_t>(L.A.nnz, 1), s);
+            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                constexpr int VS = decltype(vs)::value;
+                if constexpr (VS > 1)
+                    k_prolong_count_vs<VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong,
+                                                                                         agg, first, L.P.ptr);
+            });
+        }
         SEMO_CHECK_LAUNCH();
         L.P.nnz = scan_exclusive(s, L.P.ptr.p, nl + 1);
         L.P.col.alloc(std::max<int64_t>(L.P.nnz, 1), s);
         L.P.val.alloc(std::max<int64_t>(L.P.nnz, 1), s);
-        k_prolong_fill<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, strong, agg, omega, L.P.ptr,
-                                                          L.P.col, L.P.val);
+        if (lanes == 1) {
+            k_prolong_fill<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, strong, agg, omega,
+                                                              L.P.ptr, L.P.col, L.P.val);
+        } else {
+            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                constexpr int VS = decltype(vs)::value;
+                if constexpr (VS > 1)
+                    k_prolong_fill_vs<V, VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(
+                        nl, L.A.ptr, L.A.col, L.A.val, strong, agg, first, omega, L.P.ptr, L.P.col, L.P.val);
+            });
+        }
         SEMO_CHECK_LAUNCH();
         transpose(s, L.P, L.R);
         }

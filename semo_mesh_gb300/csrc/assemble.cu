@@ -144,7 +144,10 @@ __global__ void k_grav_cell(int nc, int nf, const int* __restrict__ cfp, const i
 
 // One pass over each cell's vertex stencil: LSQ gradients of P,U,V,W,VF and
 // stencil min/max of U,V,W,VF,P (mm planes maxU,minU,maxV,minV,maxW,minW,
-// maxVF,minVF,maxP,minP).  Stencil weights w_k*d_k are precomputed.
+// maxVF,minVF,maxP,minP).  Stencil weights w_k*d_k are precomputed.  With
+// kPVF false only the U,V,W parts are computed and the P and VF planes are
+// left as they are (they are still current: see assemble_gravity_stencil).
+template <bool kPVF>
 __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb, const int* __restrict__ stp,
                                                  const int* __restrict__ sti, const double* __restrict__ stw,
                                                  int64_t stn, const int* __restrict__ cfp,
@@ -165,19 +168,22 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
     for (int k = kb; k < ke; ++k) {
         const int j = __ldg(sti + k);
         const double wx = __ldg(stw + k), wy = __ldg(stw + stn + k), wz = __ldg(stw + 2 * stn + k);
-        const double pj = __ldg(P + j), uj = __ldg(U + j), vj = __ldg(V + j), wj = __ldg(W + j), fj = __ldg(VF + j);
+        const double uj = __ldg(U + j), vj = __ldg(V + j), wj = __ldg(W + j);
         double d;
-        d = pj - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
+        long long t;
+        if constexpr (kPVF) {
+            const double pj = __ldg(P + j), fj = __ldg(VF + j);
+            d = pj - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
+            d = fj - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
+            t = okey(fj); kmaxf = (kmaxf < t) ? t : kmaxf; kminf = (t < kminf) ? t : kminf;
+            t = okey(pj); kmaxp = (kmaxp < t) ? t : kmaxp; kminp = (t < kminp) ? t : kminp;
+        }
         d = uj - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
         d = vj - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
         d = wj - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
-        d = fj - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
-        long long t;
         t = okey(uj); kmaxu = (kmaxu < t) ? t : kmaxu; kminu = (t < kminu) ? t : kminu;
         t = okey(vj); kmaxv = (kmaxv < t) ? t : kmaxv; kminv = (t < kminv) ? t : kminv;
         t = okey(wj); kmaxw = (kmaxw < t) ? t : kmaxw; kminw = (t < kminw) ? t : kminw;
-        t = okey(fj); kmaxf = (kmaxf < t) ? t : kmaxf; kminf = (t < kminf) ? t : kminf;
-        t = okey(pj); kmaxp = (kmaxp < t) ? t : kmaxp; kminp = (t < kminp) ? t : kminp;
     }
     // boundary faces (face index >= ni) come last in the ascending list
     {
@@ -187,17 +193,17 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
             const int b = (cfi[k] & kFaceMask) - ni;
             const double wx = bfw[b], wy = bfw[nb + b], wz = bfw[2 * nb + b];
             double d;
-            d = bf[b] - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
+            if constexpr (kPVF) { d = bf[b] - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d; }
             d = bf[nb + b] - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
             d = bf[2 * nb + b] - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
             d = bf[3 * nb + b] - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
-            d = bf[4 * nb + b] - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
+            if constexpr (kPVF) { d = bf[4 * nb + b] - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d; }
         }
     }
     const double m0 = minv[i], m1 = minv[nc + i], m2 = minv[2 * nc + i];
     const double m3 = minv[3 * nc + i], m4 = minv[4 * nc + i], m5 = minv[5 * nc + i];
 #pragma unroll
-    for (int q = 0; q < 5; ++q) {
+    for (int q = kPVF ? 0 : 1; q < (kPVF ? 5 : 4); ++q) {
         double t0 = 0.0; t0 += m0 * g[q][0]; t0 += m1 * g[q][1]; t0 += m2 * g[q][2];
         double t1 = 0.0; t1 += m1 * g[q][0]; t1 += m3 * g[q][1]; t1 += m4 * g[q][2];
         double t2 = 0.0; t2 += m2 * g[q][0]; t2 += m4 * g[q][1]; t2 += m5 * g[q][2];
@@ -208,8 +214,10 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
     mm[i] = ounkey(kmaxu); mm[nc + i] = ounkey(kminu);
     mm[2 * (size_t)nc + i] = ounkey(kmaxv); mm[3 * (size_t)nc + i] = ounkey(kminv);
     mm[4 * (size_t)nc + i] = ounkey(kmaxw); mm[5 * (size_t)nc + i] = ounkey(kminw);
-    mm[6 * (size_t)nc + i] = ounkey(kmaxf); mm[7 * (size_t)nc + i] = ounkey(kminf);
-    mm[8 * (size_t)nc + i] = ounkey(kmaxp); mm[9 * (size_t)nc + i] = ounkey(kminp);
+    if constexpr (kPVF) {
+        mm[6 * (size_t)nc + i] = ounkey(kmaxf); mm[7 * (size_t)nc + i] = ounkey(kminf);
+        mm[8 * (size_t)nc + i] = ounkey(kmaxp); mm[9 * (size_t)nc + i] = ounkey(kminp);
+    }
 }
 
 // Internal faces of calcPressureEq (UnF as face_unf).
@@ -438,12 +446,20 @@ void assemble_face_values(semo_ctx* c, bool with_mu) {
     }
 }
 
-// gravity source and the stencil pass, shared by the pressure and momentum assemblies
+// Gravity source and the stencil pass, shared by the pressure and momentum
+// assemblies.  The momentum pass leaves P and VF unchanged, so after it
+// (c->pvf_current) the pressure pass keeps the P and VF gradients and limits
+// and the gravity source -- SEMO too computes that source once per time step,
+// before its outer loop (src/solvers/pressureBased.cpp:141) -- and recomputes
+// only what depends on U, V, W.
 void assemble_gravity_stencil(semo_ctx* c) {
     const int T = 256;
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
-    if (c->phys.use_gravity) {
+    const bool keep = c->pvf_current;
+    if (keep) {
+        // gravity source kept
+    } else if (c->phys.use_gravity) {
         StageScope sc(c, ST_GRAVITY);
         k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
                                                  c->W, c->irho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
@@ -456,9 +472,13 @@ void assemble_gravity_stencil(semo_ctx* c) {
     }
     {
     StageScope sc(c, ST_STENCIL);
-    k_stencil<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
-                                               c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
-                                               c->grad, c->mm);
+    auto launch = [&](auto kern) {
+        kern<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
+                                             c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
+                                             c->grad, c->mm);
+    };
+    if (keep) launch(k_stencil<false>);
+    else launch(k_stencil<true>);
     SEMO_CHECK_LAUNCH();
     }
 }
@@ -497,6 +517,7 @@ void assemble_pressure(semo_ctx* c) {
 }
 
 double pressure_update(semo_ctx* c) {
+    c->pvf_current = false;   // P changes below
     const int T = 256;
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;

@@ -180,6 +180,8 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         c->amg32.clear();
         c->amg64.clear();
         c->has_old = c->has_src = false;
+        c->pvf_current = false;
+        ++c->mesh_gen;
 
         // ---- cell -> faces, ascending face index (connectCelltoFaces, build.cpp:587-608) ----
         std::vector<int> cfp(nc + 1, 0), cfi;
@@ -454,6 +456,7 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         c->phys_ready = true;
         c->assembled = false;
         c->mom_assembled = false;
+        c->pvf_current = false;
     });
 }
 
@@ -489,6 +492,7 @@ semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const
         c->fields_ready = true;
         c->assembled = false;
         c->mom_assembled = false;
+        c->pvf_current = false;
     });
 }
 

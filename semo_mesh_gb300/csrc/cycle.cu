@@ -607,6 +607,21 @@ struct GraphGuard {
     }
 };
 
+// End of one CG iteration on the device: count it and decide whether the
+// loop goes on (scal[13] iterations, scal[14] status: 1 NaN/Inf, 2 p.q <= 0).
+// The loop is a conditional WHILE node, so no iteration waits for the host;
+// max_iter bounds it.
+__global__ void k_cg_check(cudaGraphConditionalHandle h, double* __restrict__ scal, double stop_rr, int max_iter) {
+    const double it = scal[13] + 1.0;
+    scal[13] = it;
+    const double pq = scal[2], rr = scal[3];
+    unsigned go = 1;
+    if (!isfinite(rr) || !isfinite(pq)) { scal[14] = 1.0; go = 0; }
+    else if (!(pq > 0.0)) { scal[14] = 2.0; go = 0; }
+    else if (!(rr > stop_rr) || it >= (double)max_iter) go = 0;
+    cudaGraphSetConditional(h, go);
+}
+
 template <class V>
 void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, const int* ptr, const int* col,
          const double* val, int n, const double* b, double* x, bool zero_guess, semo_solve_info* info) {
@@ -644,34 +659,47 @@ void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, const 
     if (!std::isfinite(bn) || !std::isfinite(rn)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
     const double bnorm = (bn > 0.0) ? bn : 1.0;
     int it = 0;
-    // One iteration is captured once per hierarchy and replayed; the
-    // residual norm is read back after every iteration.
-    GraphGuard gg;
-    size_t graph_nodes = 0;
+    // The whole iteration loop is one graph: a conditional WHILE node whose
+    // body is one CG iteration (~30 kernels) plus k_cg_check, which decides
+    // on the device whether to go on.  The host waits once, at the end.
     if (rn > c->prm.tol * bnorm && c->prm.max_iter > 0) {
+        GraphGuard gg;
+        SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
+        cudaGraphConditionalHandle handle;
+        SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, gg.g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop;
+        SEMO_CUDA(cudaGraphAddNode(&loop, gg.g, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        const double stop_rr = (c->prm.tol * bnorm) * (c->prm.tol * bnorm);
         const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
             cg_iteration(c, h, cy, outer, x, R);
+            k_cg_check<<<1, 1, 0, s>>>(handle, R.scal, stop_rr, c->prm.max_iter);
+            SEMO_CHECK_LAUNCH();
         } catch (...) {
             cudaGraph_t junk = nullptr;
             cudaStreamEndCapture(s, &junk);
-            if (junk) cudaGraphDestroy(junk);
             throw;
         }
-        SEMO_CUDA(cudaStreamEndCapture(s, &gg.g));
-        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
-        SEMO_CUDA(cudaGraphGetNodes(gg.g, nullptr, &graph_nodes));
+        cudaGraph_t captured = nullptr;
+        SEMO_CUDA(cudaStreamEndCapture(s, &captured));
+        size_t body_nodes = 0;
+        SEMO_CUDA(cudaGraphGetNodes(body, nullptr, &body_nodes));
         __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
-    }
-    while (it < c->prm.max_iter && rn > c->prm.tol * bnorm) {
+        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
         SEMO_CUDA(cudaGraphLaunch(gg.e, s));
-        __atomic_add_fetch(&g_kernel_launches, (long long)graph_nodes, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
-        ++it;
-        if (!std::isfinite(h2[3]) || !std::isfinite(h2[2])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
-        if (!(h2[2] > 0.0)) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
+        it = (int)h2[13];
+        __atomic_add_fetch(&g_kernel_launches, (long long)body_nodes * it, __ATOMIC_RELAXED);
+        if (h2[14] == 1.0) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
+        if (h2[14] == 2.0) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
         rn = std::sqrt(h2[3]);
     }
     // true FP64 residual of the returned solution
@@ -743,7 +771,7 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
 // matrix is dominated by its BDF2 diagonal at the time steps of interest).
 // Per system j the scalars live at scal[16 j + k]:
 //   0 rho, 1 alpha, 2 omega, 3 beta, 4 (rh,v), 5 (t,s), 6 (t,t), 7 (r,r),
-//   8 (b,b), 9 active, 10 breakdown
+//   8 (b,b), 9 active, 10 breakdown, 11 iterations
 constexpr int kMomScal = 16;
 __device__ __forceinline__ bool mom_active(const double* scal, int j) { return scal[kMomScal * j + 9] != 0.0; }
 
@@ -922,6 +950,7 @@ __global__ void k_bi_fin3(const double* __restrict__ part, double* __restrict__ 
         if (threadIdx.x == 0) {
             double* S = scal + kMomScal * j;
             if (S[9] != 0.0) {
+                S[11] += 1.0;                                        // iterations of this system
                 S[7] = rr;
                 if (rr <= tol2 * S[8]) {
                     S[9] = 0.0;                                     // converged
@@ -966,8 +995,19 @@ __global__ void k_dinv_dig(int n, const int* __restrict__ dig, const double* __r
 
 struct MomState {
     Sell<double> A;
+    int gen = -1;                 // mesh generation the SELL layout was built for
     DBuf<double> dinv, vec, part, scal;
 };
+
+// end of one batched BiCGStab iteration on the device: go on while a system
+// is active and the cap is not reached (scal[3*16+0] counts iterations)
+__global__ void k_bi_check(cudaGraphConditionalHandle h, double* __restrict__ scal, int max_iter) {
+    double* it = scal + 3 * kMomScal;
+    it[0] += 1.0;
+    bool any = false;
+    for (int j = 0; j < 3; ++j) any |= scal[kMomScal * j + 9] != 0.0;
+    cudaGraphSetConditional(h, (any && it[0] < (double)max_iter) ? 1u : 0u);
+}
 MomState& mom_state(semo_ctx* c) {
     if (!c->mom_apply) c->mom_apply = std::shared_ptr<void>(new MomState(), [](void* p) { delete (MomState*)p; });
     return *(MomState*)c->mom_apply.get();
@@ -1052,7 +1092,7 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
     st.dinv.alloc(N, s);
     st.vec.alloc(7 * 3 * N, s);       // r, rh, p, v, ph, sh, t
     st.part.alloc(6 * kRedBlocks, s);
-    st.scal.alloc(3 * kMomScal, s);
+    st.scal.alloc(4 * kMomScal, s);
     if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* r = st.vec.p;
     double* rh = r + 3 * N;
@@ -1065,7 +1105,14 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
     // residual, checked at the end, lands under it
     const double tol2 = 0.25 * c->prm.mom_tol * c->prm.mom_tol;
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
-    build_sell<double, double>(s, c->A_ptr, c->A_col, c->Am_val, n, st.A);
+    if (st.gen != c->mesh_gen) {
+        build_sell<double, double>(s, c->A_ptr, c->A_col, c->Am_val, n, st.A);
+        st.gen = c->mesh_gen;
+    } else {   // same pattern (the mesh's): refill the values into the kept layout
+        k_sell_fill<double, double><<<blocks((int64_t)st.A.nslices * 32, 256), 256, 0, s>>>(
+            n, c->A_ptr, c->A_col, c->Am_val, st.A.sptr, st.A.col, st.A.val);
+        SEMO_CHECK_LAUNCH();
+    }
     k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, c->A_dig, c->Am_val, st.dinv);
     SEMO_CHECK_LAUNCH();
     SEMO_CUDA(cudaEventRecord(c->ev[1], s));
@@ -1081,30 +1128,64 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
     for (int j = 0; j < 3; ++j)
         if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite momentum right-hand side");
     auto any_active = [&] { return hs[9] != 0.0 || hs[kMomScal + 9] != 0.0 || hs[2 * kMomScal + 9] != 0.0; };
-    int it = 0;
-    while (any_active() && it < c->prm.mom_max_iter) {
-        for (int j = 0; j < 3; ++j) if (hs[kMomScal * j + 9] != 0.0) ++iters[j];
-        k_bi_p<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, p, v, ph, st.scal);
-        SEMO_CHECK_LAUNCH();
-        k_bi_mv1<<<kRedBlocks, kRedThreads, 0, s>>>(A, ph, v, rh, st.scal, st.part);
-        SEMO_CHECK_LAUNCH();
-        k_bi_fin1<<<1, 256, 0, s>>>(st.part, st.scal);
-        SEMO_CHECK_LAUNCH();
-        k_bi_s<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, v, shv, st.scal);
-        SEMO_CHECK_LAUNCH();
-        k_bi_mv2<<<kRedBlocks, kRedThreads, 0, s>>>(A, shv, t, r, st.scal, st.part);
-        SEMO_CHECK_LAUNCH();
-        k_bi_fin2<<<1, 256, 0, s>>>(st.part, st.scal);
-        SEMO_CHECK_LAUNCH();
-        k_bi_xr<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->xm, ph, shv, r, t, rh, st.scal, st.part);
-        SEMO_CHECK_LAUNCH();
-        k_bi_fin3<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
-        SEMO_CHECK_LAUNCH();
-        SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    // the iterations run as one graph: a conditional WHILE node around one
+    // iteration (8 kernels + k_bi_check); the host waits once
+    if (any_active() && c->prm.mom_max_iter > 0) {
+        GraphGuard gg;
+        SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
+        cudaGraphConditionalHandle handle;
+        SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, gg.g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop;
+        SEMO_CUDA(cudaGraphAddNode(&loop, gg.g, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        SEMO_CUDA(cudaMemsetAsync(st.scal.p + 3 * kMomScal, 0, sizeof(double) * kMomScal, s));
+        const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+        SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+            k_bi_p<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, p, v, ph, st.scal);
+            SEMO_CHECK_LAUNCH();
+            k_bi_mv1<<<kRedBlocks, kRedThreads, 0, s>>>(A, ph, v, rh, st.scal, st.part);
+            SEMO_CHECK_LAUNCH();
+            k_bi_fin1<<<1, 256, 0, s>>>(st.part, st.scal);
+            SEMO_CHECK_LAUNCH();
+            k_bi_s<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, v, shv, st.scal);
+            SEMO_CHECK_LAUNCH();
+            k_bi_mv2<<<kRedBlocks, kRedThreads, 0, s>>>(A, shv, t, r, st.scal, st.part);
+            SEMO_CHECK_LAUNCH();
+            k_bi_fin2<<<1, 256, 0, s>>>(st.part, st.scal);
+            SEMO_CHECK_LAUNCH();
+            k_bi_xr<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->xm, ph, shv, r, t, rh, st.scal, st.part);
+            SEMO_CHECK_LAUNCH();
+            k_bi_fin3<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
+            SEMO_CHECK_LAUNCH();
+            k_bi_check<<<1, 1, 0, s>>>(handle, st.scal, c->prm.mom_max_iter);
+            SEMO_CHECK_LAUNCH();
+        } catch (...) {
+            cudaGraph_t junk = nullptr;
+            cudaStreamEndCapture(s, &junk);
+            throw;
+        }
+        cudaGraph_t captured = nullptr;
+        SEMO_CUDA(cudaStreamEndCapture(s, &captured));
+        __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
+        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
+        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
+        double hit[4 * kMomScal];
+        SEMO_CUDA(cudaMemcpyAsync(hit, st.scal.p, sizeof(hit), cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
-        ++it;
-        for (int j = 0; j < 3; ++j)
+        const int it = (int)hit[3 * kMomScal];
+        __atomic_add_fetch(&g_kernel_launches, 9LL * it, __ATOMIC_RELAXED);
+        std::copy(hit, hit + 3 * kMomScal, hs);
+        for (int j = 0; j < 3; ++j) {
             if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the momentum residual");
+            // systems converge one after another; each counts the iterations it was active
+            iters[j] = (int)hs[kMomScal * j + 11];
+        }
     }
     // true FP64 residuals of the returned solutions
     k_bi_res<<<kRedBlocks, kRedThreads, 0, s>>>(A, c->xm, c->bm, st.part);

@@ -221,7 +221,9 @@ void assemble_momentum(semo_ctx* c) {
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
     assemble_face_values(c, true);
+    c->pvf_current = false;
     assemble_gravity_stencil(c);
+    c->pvf_current = true;
     c->Am_val.alloc(c->nnz, s);
     c->bm.alloc(3 * (size_t)nc, s);
     c->msc.alloc(8 * (size_t)nf, s);

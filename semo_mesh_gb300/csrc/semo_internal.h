@@ -171,6 +171,10 @@ struct semo_ctx {
     semo::DBuf<double> bm, xm;                    // 3 planes each (x, y, z)
     semo::DBuf<double> msc;                       // face scratch: 8 planes of nf
     bool mom_assembled = false;
+    // grad P, grad VF, their stencil limits and the gravity source match the
+    // current P and VF (set by the momentum assembly, cleared when P, VF or the
+    // physics change); the pressure assembly then recomputes only the U,V,W parts
+    bool pvf_current = false;
     std::shared_ptr<void> mom_apply;              // momentum Krylov state (cycle.cu)
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
@@ -184,6 +188,7 @@ struct semo_ctx {
     std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
+    int mesh_gen = 0;                             // bumped by every mesh upload (cached layouts check it)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // profiling: per-stage device time from event pairs, resolved after each call
