@@ -236,6 +236,8 @@ def run_gpu_arm(args, rank, world, local) -> None:
     launches = ctx.kernel_launches() - l0
     stages = ctx.stage_times()
     ctx.set_profiling(False)
+    free_b, total_b = torch.cuda.mem_get_info(local)
+    used_gb = (total_b - free_b) / 1e9   # the context's mesh, fields, hierarchy and pools, plus torch's own
     if world > 1:
         t = torch.tensor([ms_mixed], device=f"cuda:{local}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -388,6 +390,7 @@ def run_gpu_arm(args, rank, world, local) -> None:
                                 "semo_outer_iteration + semo_get_fields",
                 "h2d_bytes_per_step": 11 * 8 * nc, "d2h_bytes_per_step": 4 * 8 * nc},
         "gpu_launches": int(launches),
+        "memory": {"device_used_gb": round(used_gb, 2), "device_total_gb": round(total_b / 1e9, 1)},
         "roofline": roofline,
         "clocks": clocks,
     }

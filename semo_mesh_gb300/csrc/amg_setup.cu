@@ -431,15 +431,36 @@ __global__ void k_row_products(int n, const int* __restrict__ aptr, const int* _
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(maxprod, m);
 }
-// copy row i from its upper-bound slot (uptr) to its exact place (cptr), one warp a row
+// copy rows from their upper-bound slots (uptr) to their exact places (cptr).
+// A warp takes 32 consecutive rows; their outputs are contiguous, so the
+// lanes stride over the concatenated output entries (coalesced stores) and
+// find each entry's row by a search over the 32 row starts.
 template <class V>
 __global__ void k_compact_rows(int n, const int* __restrict__ uptr, const int* __restrict__ cptr,
                                const int* __restrict__ tcol, const V* __restrict__ tval, int* __restrict__ ccol,
                                V* __restrict__ cval) {
-    const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (row >= n) return;
-    const int src = uptr[row], dst = cptr[row], len = cptr[row + 1] - dst;
-    for (int e = lane; e < len; e += 32) { ccol[dst + e] = tcol[src + e]; cval[dst + e] = tval[src + e]; }
+    const int warp = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int r0 = warp * 32;
+    if (r0 >= n) return;
+    const int row = min(r0 + lane, n);
+    const int start = cptr[row];                      // lane's row start (n: the end)
+    const int src = (r0 + lane < n) ? uptr[r0 + lane] : 0;
+    const int base = __shfl_sync(0xffffffffu, start, 0);
+    const int end = cptr[min(r0 + 32, n)];
+    for (int e0 = base; e0 < end; e0 += 32) {        // uniform trip count: shuffles below are warp-wide
+        const int e = e0 + lane;
+        int j = 0;                                    // last lane whose row starts at or before e
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int sj = __shfl_sync(0xffffffffu, start, j + step);
+            if (sj <= e) j += step;
+        }
+        const int sr = __shfl_sync(0xffffffffu, src, j) + (e - __shfl_sync(0xffffffffu, start, j));
+        if (e < end) {
+            ccol[e] = tcol[sr];
+            cval[e] = tval[sr];
+        }
+    }
 }
 
 // Thread-per-row SpGEMM for rows with few distinct columns (the finest
@@ -820,7 +841,7 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     C.nnz = nnz;
     C.col.alloc(std::max(nnz, 1), s);
     C.val.alloc(std::max(nnz, 1), s);
-    k_compact_rows<V><<<blocks((int64_t)n * 32, 256), 256, 0, s>>>(n, up.p, C.ptr.p, tcol.p, tval.p, C.col.p,
+    k_compact_rows<V><<<blocks(n, 256), 256, 0, s>>>(n, up.p, C.ptr.p, tcol.p, tval.p, C.col.p,
                                                                    C.val.p);
     SEMO_CHECK_LAUNCH();
     (void)c;
@@ -967,18 +988,15 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         L.P.ptr.alloc(nl + 1, s);
         SEMO_CUDA(cudaMemsetAsync(L.P.ptr.p + nl, 0, sizeof(int), s));
         DBuf<unsigned char> first;
-        int lanes = 1;
-        with_row_lanes(L.A.nnz, nl, [&](auto vs) { lanes = decltype(vs)::value; });
+        // one thread a row costs O(row length x aggregates in the row), the
+        // lane version O(row length^2 / lanes): lanes only for the longest rows
+        const int lanes = ((double)L.A.nnz > 48.0 * (double)nl) ? 32 : 1;
         if (lanes == 1) {
             k_prolong_count<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg, L.P.ptr);
         } else {
             first.alloc(std::max<int64_t>(L.A.nnz, 1), s);
-            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
-                constexpr int VS = decltype(vs)::value;
-                if constexpr (VS > 1)
-                    k_prolong_count_vs<VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong,
-                                                                                         agg, first, L.P.ptr);
-            });
+            k_prolong_count_vs<32><<<blocks((int64_t)nl * 32, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg,
+                                                                                 first, L.P.ptr);
         }
         SEMO_CHECK_LAUNCH();
         L.P.nnz = scan_exclusive(s, L.P.ptr.p, nl + 1);
@@ -988,12 +1006,8 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
             k_prolong_fill<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, strong, agg, omega,
                                                               L.P.ptr, L.P.col, L.P.val);
         } else {
-            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
-                constexpr int VS = decltype(vs)::value;
-                if constexpr (VS > 1)
-                    k_prolong_fill_vs<V, VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(
-                        nl, L.A.ptr, L.A.col, L.A.val, strong, agg, first, omega, L.P.ptr, L.P.col, L.P.val);
-            });
+            k_prolong_fill_vs<V, 32><<<blocks((int64_t)nl * 32, 256), 256, 0, s>>>(
+                nl, L.A.ptr, L.A.col, L.A.val, strong, agg, first, omega, L.P.ptr, L.P.col, L.P.val);
         }
         SEMO_CHECK_LAUNCH();
         transpose(s, L.P, L.R);
