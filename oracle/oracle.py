@@ -54,6 +54,11 @@ def lib():
         L.orc_solve_momentum.argtypes = [vp, C.c_int, C.c_double, C.c_int, vp, vp]
         L.orc_update_momentum.restype = C.c_double
         L.orc_update_momentum.argtypes = [vp, vp, vp, vp]
+        L.orc_assemble_vof.argtypes = [vp]
+        L.orc_solve_vof.restype = C.c_int
+        L.orc_solve_vof.argtypes = [vp, C.c_double, C.c_int, vp, vp]
+        L.orc_update_vof.restype = C.c_double
+        L.orc_update_vof.argtypes = [vp, vp]
         L.orc_num_threads.restype = C.c_int
     return _lib
 
@@ -110,10 +115,13 @@ class Oracle:
                     case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf, case.pre_u_urf,
                     1.0 if case.use_gravity else 0.0]
         prm[12] = case.mom_u_urf
+        prm[13] = case.vof_urf
         lib().orc_set_case(self.h, _p(bt), _p(bv), _p(prm))
         for nm in ("P", "U", "V", "W", "VF"):
             self.set(nm, getattr(case, nm))
         for nm, a in zip(("oldU", "oldV", "oldW", "old2U", "old2V", "old2W"), case.history()):
+            self.set(nm, a)
+        for nm, a in zip(("oldVF", "old2VF"), case.vf_history()):
             self.set(nm, a)
 
     def assemble(self) -> None:
@@ -161,6 +169,27 @@ class Oracle:
         self.assemble_momentum()
         sol = self.solve_momentum(tol)
         sol["norm"] = self.update_momentum(sol["x"])
+        return sol
+
+    def assemble_vof(self) -> None:
+        """MSTACS face values + calcVolfracEq assembly: vof_A_*, vof_csr_*, vof_B, vof_face_vf{L,R}."""
+        lib().orc_assemble_vof(self.h)
+
+    def solve_vof(self, tol: float = 1e-9, maxiter: int = 1000) -> dict:
+        x = np.empty(self.mesh.n_cells)
+        rr = np.zeros(1)
+        it = int(lib().orc_solve_vof(self.h, tol, maxiter, _p(x), _p(rr)))
+        return {"x": x, "iters": it, "rel_res": float(rr[0])}
+
+    def update_vof(self, x) -> float:
+        xa = np.ascontiguousarray(x, dtype=np.float64)
+        return float(lib().orc_update_vof(self.h, _p(xa)))
+
+    def vof_pass(self, tol: float = 1e-9) -> dict:
+        """One volume-fraction sub-iteration: reconstruct, assemble, solve, update VF."""
+        self.assemble_vof()
+        sol = self.solve_vof(tol)
+        sol["norm"] = self.update_vof(sol["x"])
         return sol
 
     def pressure_pass(self, case, tol: float = 1e-8) -> dict:

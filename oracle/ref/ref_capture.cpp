@@ -2,8 +2,8 @@
 //
 // The Makefile compiles the reference's equation translation units (and this
 // file) with -DsolveAMGCL=semo_ref_capture_solveAMGCL, so the calls at
-// src/solvers/eqPressure.cpp:677 (scalar) and src/solvers/eqMomentum.cpp:1017
-// (three right-hand sides) land here.  The assembled COO system is copied out
+// src/solvers/eqPressure.cpp:677 and src/solvers/eqVolfrac.cpp:766 (scalar)
+// and src/solvers/eqMomentum.cpp:1017 (three right-hand sides) land here.  The assembled COO system is copied out
 // for the checker and then handed to the real solver, so the reference's pass
 // continues exactly as it would.
 #include <string>
@@ -27,6 +27,7 @@ struct CapturedMomentum {
     int calls = 0;
 };
 extern CapturedMomentum g_momentum;
+extern CapturedSystem g_vof;
 void semo_ref_forward_solve(const string& eq, SEMO_Mesh_Builder& mesh, int B_n,
                             vector<int>& r, vector<int>& c, vector<double>& v,
                             vector<double>& b, vector<double>& x);
@@ -39,13 +40,16 @@ void SEMO_Solvers_Builder::semo_ref_capture_solveAMGCL(
     string equation, SEMO_Mesh_Builder& mesh, int B_n,
     vector<int>& A_rows, vector<int>& A_cols, vector<double>& A_vals,
     vector<double>& B_vals, vector<double>& resiVar) {
-    if (equation == "pressure" && g_captured.calls == 0) {
-        g_captured.rows = A_rows; g_captured.cols = A_cols; g_captured.vals = A_vals;
-        g_captured.b = B_vals;
+    CapturedSystem* cap = (equation == "pressure") ? &g_captured
+                        : (equation == "volume_fraction") ? &g_vof : nullptr;
+    const bool first = cap && cap->calls == 0;
+    if (first) {
+        cap->rows = A_rows; cap->cols = A_cols; cap->vals = A_vals;
+        cap->b = B_vals;
     }
     semo_ref_forward_solve(equation, mesh, B_n, A_rows, A_cols, A_vals, B_vals, resiVar);
-    if (equation == "pressure" && g_captured.calls == 0) g_captured.x = resiVar;
-    ++g_captured.calls;
+    if (first) cap->x = resiVar;
+    if (cap) ++cap->calls;
 }
 
 void SEMO_Solvers_Builder::semo_ref_capture_solveAMGCL(

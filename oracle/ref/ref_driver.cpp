@@ -10,7 +10,9 @@
 // src/solvers/pressureBased.cpp:17-31, :139-141, :211-212.  With case flag 2
 // the pass is a whole outer iteration instead: cell transport, then the
 // momentum equation (:201-202) followed by the pressure correction (:211-212),
-// with old and second-old velocities read from the case.
+// with old and second-old velocities read from the case.  With case flag 4 the
+// pass is one volume-fraction sub-iteration instead (:104-112): MSTACS face
+// reconstruction and calcVolfracEq, with old and second-old VF from the case.
 //
 // usage: semo_ref <case.bin> <out.bin>
 #include <chrono>
@@ -42,6 +44,7 @@ struct CapturedMomentum {
     int calls = 0;
 };
 CapturedMomentum g_momentum;
+CapturedSystem g_vof;
 
 // Called from ref_capture.cpp: forwards to the reference's real solver.
 void semo_ref_forward_solve(const string& eq, SEMO_Mesh_Builder& mesh, int B_n,
@@ -102,6 +105,10 @@ int main(int argc, char** argv) {
     vector<double> old[6];
     if (flags & 2)
         for (int k = 0; k < 6; ++k) { old[k].resize(nc); rd(f, old[k].data(), nc); }
+    // flag 4: old and second-old volume fraction
+    vector<double> oldvf[2];
+    if (flags & 4)
+        for (int k = 0; k < 2; ++k) { oldvf[k].resize(nc); rd(f, oldvf[k].data(), nc); }
     fclose(f);
 
     // ---- species (two incompressible phases; VF[0] is the first) -------
@@ -116,6 +123,7 @@ int main(int argc, char** argv) {
     controls.prePreURF = prm[9];
     controls.preVelURF = prm[10];
     controls.momVelURF = prm[12];
+    controls.vofVofURF = prm[13];
     controls.turbType = "laminar";
     controls.oldTimeStep = controls.timeStep;
     controls.old2TimeStep = controls.timeStep;
@@ -177,6 +185,7 @@ int main(int argc, char** argv) {
             c.var[controls.oldU] = old[0][i]; c.var[controls.oldV] = old[1][i]; c.var[controls.oldW] = old[2][i];
             c.var[controls.Qm[0]] = old[3][i]; c.var[controls.Qm[1]] = old[4][i]; c.var[controls.Qm[2]] = old[5][i];
         }
+        if (flags & 4) { c.var[controls.oldVF[0]] = oldvf[0][i]; c.var[controls.Qm[3]] = oldvf[1][i]; }
     }
     auto t0 = chrono::steady_clock::now();
     solver.calcIncomCellEOSVF(mesh, controls, species);
@@ -232,6 +241,32 @@ int main(int argc, char** argv) {
         put("face_uL", ful); put("face_uR", fur);
         put("CRS_ptr", mesh.CRS_ptr); put("CRS_col", mesh.CRS_col);
         put("CRS_dig", mesh.CRS_col_ptr_dig); put("CRS_LR", mesh.CRS_col_ptr_LR); put("CRS_RL", mesh.CRS_col_ptr_RL);
+    }
+
+    // volume-fraction sub-iteration (flag 4): dump and stop --------------
+    if (flags & 4) {
+        solver.setIncomValuesLeftRightFaceWithVfMSTACS(mesh, controls, species);
+        vector<double> vl(nf), vr(nf);
+        for (int i = 0; i < nf; ++i) { vl[i] = mesh.faces[i].varL[controls.fVF[0]]; vr[i] = mesh.faces[i].varR[controls.fVF[0]]; }
+        put("vof_face_vfL", vl); put("vof_face_vfR", vr);
+        auto v0 = chrono::steady_clock::now();
+        double vnorm = solver.calcVolfracEq(mesh, controls, species);
+        auto v1 = chrono::steady_clock::now();
+        vector<double> g(3 * nc), vfn(nc);
+        const int tgt[5] = {controls.P, controls.U, controls.V, controls.W, controls.VF[0]};
+        const char* gname[5] = {"vof_grad_P", "vof_grad_U", "vof_grad_V", "vof_grad_W", "vof_grad_VF"};
+        for (int t = 0; t < 5; ++t) {
+            for (int i = 0; i < nc; ++i) for (int k = 0; k < 3; ++k) g[3 * i + k] = mesh.cellsGradientVar[tgt[t]][i][k];
+            put(gname[t], g);
+        }
+        for (int i = 0; i < nc; ++i) vfn[i] = mesh.cells[i].var[controls.VF[0]];
+        put("vof_A_rows", g_vof.rows); put("vof_A_cols", g_vof.cols); put("vof_A_vals", g_vof.vals);
+        put("vof_B", g_vof.b); put("vof_x", g_vof.x); put("vof_VF_new", vfn);
+        put("vof_norm", &vnorm, 1);
+        double tv[2] = {chrono::duration<double>(v1 - v0).count(), 0.0};
+        put("vof_timings", tv, 2);
+        fclose(g_out);
+        return 0;
     }
 
     // momentum equation (outer iteration only) ---------------------------

@@ -18,11 +18,12 @@ REF_BIN = os.path.join(HERE, "_ref", "semo_ref")
 MAGIC = 0x53454D4F
 
 
-def write_case(case, path: str, flags: int | None = None, momentum: bool = False) -> None:
-    """flags bit 0: gravity source; bit 1: whole outer iteration (momentum, then pressure)."""
+def write_case(case, path: str, flags: int | None = None, momentum: bool = False, vof: bool = False) -> None:
+    """flags bit 0: gravity source; bit 1: whole outer iteration (momentum, then
+    pressure); bit 2: one volume-fraction sub-iteration instead."""
     m = case.mesh
     if flags is None:
-        flags = (1 if case.use_gravity else 0) | (2 if momentum else 0)
+        flags = (1 if case.use_gravity else 0) | (2 if momentum else 0) | (4 if vof else 0)
     with open(path, "wb") as f:
         f.write(struct.pack("<8i", MAGIC, m.n_points, m.n_faces, m.n_internal, m.n_cells,
                             len(m.patch_names), int(m.face_pts.shape[0]), flags))
@@ -40,9 +41,13 @@ def write_case(case, path: str, flags: int | None = None, momentum: bool = False
         prm[:11] = [case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
                     case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf, case.pre_u_urf]
         prm[12] = case.mom_u_urf
+        prm[13] = case.vof_urf
         f.write(prm.astype("<f8").tobytes())
         if flags & 2:
             for a in case.history():
+                f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+        if flags & 4:
+            for a in case.vf_history():
                 f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
 
 
@@ -67,15 +72,17 @@ def have_reference_binary() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def run_reference(case, threads: int = 1, timeout: float = 3600.0, momentum: bool = False) -> dict:
-    """Run the reference's own code on `case` and return its dumped arrays
-    (one pressure pass, or with `momentum` a momentum + pressure outer iteration)."""
+def run_reference(case, threads: int = 1, timeout: float = 3600.0, momentum: bool = False,
+                  vof: bool = False) -> dict:
+    """Run the reference's own code on `case` and return its dumped arrays (one
+    pressure pass; with `momentum` a momentum + pressure outer iteration; with
+    `vof` one volume-fraction sub-iteration)."""
     if not have_reference_binary():
         raise FileNotFoundError(REF_BIN)
     with tempfile.TemporaryDirectory() as td:
         cp = os.path.join(td, "case.bin")
         op = os.path.join(td, "out.bin")
-        write_case(case, cp, momentum=momentum)
+        write_case(case, cp, momentum=momentum, vof=vof)
         env = dict(os.environ, OMP_NUM_THREADS=str(threads))
         subprocess.run([REF_BIN, cp, op], check=True, env=env, timeout=timeout,
                        stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)

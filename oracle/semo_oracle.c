@@ -43,7 +43,7 @@ typedef struct {
     /* bc per patch: type p/u/vf and values p,u,v,w,vf */
     int* bct; double* bcv;
     /* parameters */
-    double dt, rho0, rho1, mu0, mu1, urf_p, urf_u, urf_mom, g[3];
+    double dt, rho0, rho1, mu0, mu1, urf_p, urf_u, urf_mom, urf_vof, g[3];
     int use_gravity;
     double minP, maxP, minU, maxU, minV, maxV, minW, maxW;
     /* registry of named arrays (owned) */
@@ -508,7 +508,7 @@ void orc_set_case(orc_ctx* c, const int* bct, const double* bcv, const double* p
     memcpy(c->bct, bct, sizeof(int) * 3 * c->npatch);
     memcpy(c->bcv, bcv, sizeof(double) * 5 * c->npatch);
     c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2]; c->mu0 = prm[3]; c->mu1 = prm[4];
-    c->urf_mom = prm[12];
+    c->urf_mom = prm[12]; c->urf_vof = prm[13];
     c->g[0] = prm[6]; c->g[1] = prm[7]; c->g[2] = prm[8];
     c->urf_p = prm[9]; c->urf_u = prm[10]; c->use_gravity = prm[11] != 0.0;
 }
@@ -1453,10 +1453,16 @@ void orc_assemble_momentum(orc_ctx* c) {
 /* BiCGStab with a Jacobi preconditioner on the momentum CSR, one right-hand
    side (plane j of mom_B), x0 = 0.  Not AMGCL's FGMRES: the GPU solver's
    algorithm, restated for the CPU baseline and the parity tests. */
+static int bicgstab_jacobi(int n, const int* ptr, const int* col, const double* val, const double* b, double tol,
+                           int maxiter, double* out_x, double* out_relres);
 int orc_solve_momentum(orc_ctx* c, int j, double tol, int maxiter, double* out_x, double* out_relres) {
     int n = c->nc;
     int* ptr = iget(c, "mom_csr_ptr"); int* col = iget(c, "mom_csr_col"); double* val = dget(c, "mom_csr_val");
     double* b = dget(c, "mom_B") + (size_t)j * n;
+    return bicgstab_jacobi(n, ptr, col, val, b, tol, maxiter, out_x, out_relres);
+}
+static int bicgstab_jacobi(int n, const int* ptr, const int* col, const double* val, const double* b, double tol,
+                           int maxiter, double* out_x, double* out_relres) {
     double* w = (double*)calloc(8 * (size_t)n, sizeof(double));
     double *r = w, *rh = w + n, *p = w + 2 * (size_t)n, *v = w + 3 * (size_t)n, *s = w + 4 * (size_t)n;
     double *t = w + 5 * (size_t)n, *ph = w + 6 * (size_t)n, *dinv = w + 7 * (size_t)n;
@@ -1519,4 +1525,257 @@ double orc_update_momentum(orc_ctx* c, const double* x0, const double* x1, const
         npn += U[i] * U[i]; npn += V[i] * V[i]; npn += W[i] * W[i];
     }
     return sqrt(nd) / sqrt(npn);
+}
+
+/* ------------------------------------------------------------------------ */
+/* volume fraction: src/solvers/reconIncom.cpp:345-429                        */
+/* (setIncomValuesLeftRightFaceWithVfMSTACS: zero-order values, LSQ grad VF,  */
+/* MSTACS), src/solvers/NVD.cpp:1098-1790 (calcMSTACS),                        */
+/* src/solvers/eqVolfrac.cpp:9-795 (calcVolfracEq, 3-argument overload):      */
+/* BDF2 diagonal/RHS :222-260, internal faces :262-606, boundary :611-755,    */
+/* update + norm :770-793.  COO order as for the momentum equation (drops of  */
+/* |a| < DBL_MIN).  Old (n-1) and second-old VF come from arrays oldVF and    */
+/* old2VF (default: the current VF).                                          */
+/* ------------------------------------------------------------------------ */
+static void mstacs(orc_ctx* c, const double* gVF, double* fl, double* fr) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    double *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *VF = dget(c, "VF");
+    double *fa = dget(c, "face_area"), *vol = dget(c, "cell_vol"), *cc = dget(c, "cell_c");
+    double *fn = dget(c, "face_n"), *wc = dget(c, "face_wC"), *sk = dget(c, "face_skew");
+    int *cfp = iget(c, "cf_ptr"), *cfi = iget(c, "cf_idx");
+    const double eps = 1.e-12;
+    double* co = (double*)malloc(sizeof(double) * nc);
+    for (int i = 0; i < nc; ++i) {
+        double magVel = sqrt(U[i] * U[i] + V[i] * V[i] + W[i] * W[i]);
+        double maxA = 0.0;
+        for (int k = cfp[i]; k < cfp[i + 1]; ++k) maxA = smax(maxA, fa[cfi[k]]);
+        co[i] = 1.0 / 1.0 * magVel * c->dt * maxA / vol[i];
+    }
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        double wCL = wc[f], wCR = 1.0 - wCL;
+        double L1 = VF[o], R1 = VF[q];
+        const double* dL = gVF + 3 * o; const double* dR = gVF + 3 * q;
+        double coDDL = co[o], coDDR = co[q];
+        double pn[3] = {cc[3 * q] - cc[3 * o], cc[3 * q + 1] - cc[3 * o + 1], cc[3 * q + 2] - cc[3 * o + 2]};
+        double L2 = 0.0; for (int k = 0; k < 3; ++k) L2 += dL[k] * pn[k];
+        L2 = R1 - 2.0 * L2;
+        double R2 = 0.0; for (int k = 0; k < 3; ++k) R2 += dR[k] * pn[k];
+        R2 = L1 + 2.0 * R2;
+        L2 = smax(0.0, smin(1.0, L2));
+        R2 = smax(0.0, smin(1.0, R2));
+        double vfL = L1, vfR = R1;
+        const double* n = fn + 3 * f; const double* s = sk + 3 * f;
+        for (int LR = 0; LR < 2; ++LR) {
+            if (LR == 0 && (vfL > 1.0 - eps || vfL < eps)) continue;
+            if (LR == 1 && (vfR > 1.0 - eps || vfR < eps)) continue;
+            double alpU, alpD, alpA, coDD;
+            if (LR == 0) { alpU = L2; alpD = L1; alpA = R1; }
+            else { alpU = R2; alpD = R1; alpA = L1; }
+            coDD = smax(coDDL, coDDR);
+            double m[3] = {wCL * dL[0] + wCR * dR[0], wCL * dL[1] + wCR * dR[1], wCL * dL[2] + wCR * dR[2]};
+            double mag = m[0] * m[0]; mag += m[1] * m[1]; mag += m[2] * m[2];
+            mag = sqrt(mag);
+            for (int k = 0; k < 3; ++k) m[k] = m[k] / (mag + 1.e-200);
+            double cosTheta = m[0] * n[0]; cosTheta += m[1] * n[1]; cosTheta += m[2] * n[2];
+            cosTheta = fabs(cosTheta);
+            double gamF = smin(pow(cosTheta, 4.0), 1.0);
+            double tildeCd = (alpD - alpU) / (fabs(alpA - alpU) + 1.e-200) * (alpA > alpU ? 1.0 : -1.0);
+            double gamma_f;
+            if (tildeCd >= 0.0 && tildeCd < 1.0) {
+                if (coDD > 0.0 && coDD <= 0.33) {
+                    double tildeCf = smin(1.0, tildeCd / coDD);
+                    gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+                } else if (coDD > 0.33 && coDD <= 1.0) {
+                    double tildeCf = smin(1.0, 3.0 * tildeCd);
+                    gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+                } else gamma_f = 0.0;
+            } else gamma_f = 0.0;
+            if (LR == 0) gamma_f *= 2.0 * wCR;
+            if (LR == 1) gamma_f *= 2.0 * wCL;
+            gamma_f = smax(0.0, smin(1.0, gamma_f));
+            double vfC = alpD + gamma_f * (alpA - alpD);
+            for (int k = 0; k < 3; ++k) vfC += wCL * dL[k] * s[k];
+            for (int k = 0; k < 3; ++k) vfC += wCR * dR[k] * s[k];
+            vfC = smax(0.0, smin(1.0, vfC));
+            if (tildeCd >= 0.0 && tildeCd < 0.2) {
+                double tildeCf = smin(1.0, 3.0 * tildeCd);
+                gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+            } else if (tildeCd >= 0.2 && tildeCd < 0.5) {
+                double tildeCf = 0.5 + 0.5 * tildeCd;
+                gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+            } else if (tildeCd >= 0.5 && tildeCd < 0.8333) {
+                double tildeCf = 0.375 + 0.75 * tildeCd;
+                gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+            } else if (tildeCd >= 0.8333 && tildeCd < 1.0) {
+                double tildeCf = 1.0;
+                gamma_f = (tildeCf - tildeCd) / (1.0 - tildeCd);
+            } else gamma_f = 0.0;
+            if (LR == 0) gamma_f *= 2.0 * wCR;
+            if (LR == 1) gamma_f *= 2.0 * wCL;
+            gamma_f = smax(0.0, smin(1.0, gamma_f));
+            double vfD = alpD + gamma_f * (alpA - alpD);
+            for (int k = 0; k < 3; ++k) vfD += wCL * dL[k] * s[k];
+            for (int k = 0; k < 3; ++k) vfD += wCR * dR[k] * s[k];
+            vfD = smax(0.0, smin(1.0, vfD));
+            double vf = gamF * vfC + (1.0 - gamF) * vfD;
+            if (LR == 0) vfL = vf;
+            if (LR == 1) vfR = vf;
+        }
+        fl[f] = vfL; fr[f] = vfR;
+    }
+    free(co);
+}
+
+void orc_assemble_vof(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    face_values(c);
+    gravity_source(c);
+    double *P = dget(c, "P"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W"), *VF = dget(c, "VF");
+    double *rho = dget(c, "rho"), *sg = dget(c, "src_grav"), *vol = dget(c, "cell_vol");
+    double* mm = dreg(c, "vof_minmax_uvw", 6LL * nc);
+    double *t1 = (double*)malloc(sizeof(double) * nc), *t2 = (double*)malloc(sizeof(double) * nc);
+    minmax(c, U, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i] = t1[i]; mm[6 * i + 1] = t2[i]; }
+    minmax(c, V, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 2] = t1[i]; mm[6 * i + 3] = t2[i]; }
+    minmax(c, W, t1, t2); for (int i = 0; i < nc; ++i) { mm[6 * i + 4] = t1[i]; mm[6 * i + 5] = t2[i]; }
+    free(t1); free(t2);
+    double *pr = dget(c, "face_pR"), *ur = dget(c, "face_uR"), *vr = dget(c, "face_vfR");
+    double* tmp = (double*)malloc(sizeof(double) * nf);
+    double* gP = dreg(c, "vof_grad_P", 3LL * nc); lsq_grad(c, P, pr, gP);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f];
+    double* gU = dreg(c, "vof_grad_U", 3LL * nc); lsq_grad(c, U, tmp, gU);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 1];
+    double* gV = dreg(c, "vof_grad_V", 3LL * nc); lsq_grad(c, V, tmp, gV);
+    for (int f = 0; f < nf; ++f) tmp[f] = ur[3 * f + 2];
+    double* gW = dreg(c, "vof_grad_W", 3LL * nc); lsq_grad(c, W, tmp, gW);
+    double* gVF = dreg(c, "vof_grad_VF", 3LL * nc); lsq_grad(c, VF, vr, gVF);
+    free(tmp);
+    /* MSTACS face values; boundary faces keep the zero-order ones */
+    double *fl = dreg(c, "vof_face_vfL", nf), *fr = dreg(c, "vof_face_vfR", nf);
+    double* vl0 = dget(c, "face_vfL");
+    for (int f = ni; f < nf; ++f) { fl[f] = vl0[f]; fr[f] = vr[f]; }
+    mstacs(c, gVF, fl, fr);
+
+    double* oVF = hist(c, "oldVF", VF); double* o2VF = hist(c, "old2VF", VF);
+    const double dt = c->dt;
+    int cap = nc + 2 * ni;
+    int* ar = ireg(c, "vof_A_rows", cap); int* acl = ireg(c, "vof_A_cols", cap);
+    double* av = dreg(c, "vof_A_vals", cap);
+    double* B = dreg(c, "vof_B", nc);
+    for (int i = 0; i < nc; ++i) {
+        double volume = vol[i];
+        ar[i] = i; acl[i] = i;
+        av[i] = 1.5 * volume / dt;
+        B[i] = -(1.5 * VF[i] - 2.0 * oVF[i] + 0.5 * o2VF[i]) * volume / dt;
+    }
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *mpn = dget(c, "face_magPN"), *al = dget(c, "face_alphaF"), *epn = dget(c, "face_ePN");
+    double *sk = dget(c, "face_skew"), *ul = dget(c, "face_uL"), *rl = dget(c, "face_rhoL");
+    double* unf = dreg(c, "vof_face_UnF", nf);
+    int nnz = nc;
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f; const double* s = sk + 3 * f;
+        double area = fa[f], wCL = wc[f], wCR = 1.0 - wCL;
+        double RhoL = rho[o], RhoR = rho[q], PL = P[o], PR = P[q];
+        double dPN = mpn[f], alpha = al[f];
+        double ULs = U[o], VLs = V[o], WLs = W[o], URs = U[q], VRs = V[q], WRs = W[q];
+        for (int k = 0; k < 3; ++k) {
+            ULs += gU[3 * o + k] * s[k]; URs += gU[3 * q + k] * s[k];
+            VLs += gV[3 * o + k] * s[k]; VRs += gV[3 * q + k] * s[k];
+            WLs += gW[3 * o + k] * s[k]; WRs += gW[3 * q + k] * s[k];
+        }
+        ULs = smax(mm[6 * o + 1], smin(mm[6 * o + 0], ULs)); URs = smax(mm[6 * q + 1], smin(mm[6 * q + 0], URs));
+        VLs = smax(mm[6 * o + 3], smin(mm[6 * o + 2], VLs)); VRs = smax(mm[6 * q + 3], smin(mm[6 * q + 2], VRs));
+        WLs = smax(mm[6 * o + 5], smin(mm[6 * o + 4], WLs)); WRs = smax(mm[6 * q + 5], smin(mm[6 * q + 4], WRs));
+        double UnL = ULs * n[0] + VLs * n[1] + WLs * n[2];
+        double UnR = URs * n[0] + VRs * n[1] + WRs * n[2];
+        double UnF = wCL * UnL + wCR * UnR;
+        double rs = 1.0 / (wCL / RhoL + wCR / RhoR);
+        double tt = dt / rs;
+        UnF -= alpha * tt * (PR - PL) / dPN;
+        for (int k = 0; k < 3; ++k) {
+            UnF -= tt * rs * wCL / RhoL * gP[3 * o + k] * (n[k] - alpha * e[k]);
+            UnF -= tt * rs * wCR / RhoR * gP[3 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * gP[3 * o + k] * n[k];
+            UnF += tt * rs * wCR / RhoR * gP[3 * q + k] * n[k];
+        }
+        for (int k = 0; k < 3; ++k) UnF += alpha * tt * rs * c->g[k] * alpha * e[k];
+        for (int k = 0; k < 3; ++k) {
+            UnF += tt * rs * wCL / RhoL * sg[4 * o + k] * (n[k] - alpha * e[k]);
+            UnF += tt * rs * wCR / RhoR * sg[4 * q + k] * (n[k] - alpha * e[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
+            UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
+        }
+        unf[f] = UnF;
+        double weightL = (UnF > 0.0) ? 1.0 : 0.0;
+        double weightR = 1.0 - weightL;
+        double VFF_HO = weightL * fl[f] + weightR * fr[f];
+        av[o] += (weightL * UnF * area);
+        {
+            double a = (weightR * UnF * area);
+            if (!(fabs(a) < 2.2250738585072014e-308)) { ar[nnz] = o; acl[nnz] = q; av[nnz] = a; ++nnz; }
+        }
+        av[q] -= (weightR * UnF * area);
+        {
+            double a = -(weightL * UnF * area);
+            if (!(fabs(a) < 2.2250738585072014e-308)) { ar[nnz] = q; acl[nnz] = o; av[nnz] = a; ++nnz; }
+        }
+        B[o] -= (VFF_HO * UnF * area);
+        B[q] += (VFF_HO * UnF * area);
+    }
+    double* pRf = dget(c, "face_pR");
+    for (int f = ni; f < nf; ++f) {
+        int p = patch_of(c, f), o = c->own[f];
+        const double* n = fn + 3 * f; const double* e = epn + 3 * f;
+        double area = fa[f];
+        double UnL = ul[3 * f] * n[0] + ul[3 * f + 1] * n[1] + ul[3 * f + 2] * n[2];
+        double UnR = ur[3 * f] * n[0] + ur[3 * f + 1] * n[1] + ur[3 * f + 2] * n[2];
+        double UnF = 0.5 * UnL + 0.5 * UnR;
+        double RhoL = rl[f];
+        double tmp1 = 1.0 / RhoL * dt;
+        double VFF = 0.5 * fl[f] + 0.5 * fr[f];
+        double coeffVF = (c->bct[3 * p + 2] == 1) ? 0.0 : 1.0;   /* fixedValue 0, zeroGradient 1 */
+        double dPN = 0.5 * mpn[f], alpha = al[f];
+        if (c->bct[3 * p] == 1) {
+            double orgPL = P[o], orgPR = pRf[f];
+            UnF -= alpha * tmp1 * (orgPR - orgPL) / dPN;
+            for (int k = 0; k < 3; ++k) UnF += alpha * tmp1 * gP[3 * o + k] * e[k];
+        }
+        unf[f] = UnF;
+        av[o] += coeffVF * (UnF * area);
+        B[o] -= (VFF * UnF * area);
+    }
+    orc_arr* a;
+    a = find(c, "vof_A_rows"); a->n = nnz;
+    a = find(c, "vof_A_cols"); a->n = nnz;
+    a = find(c, "vof_A_vals"); a->n = nnz;
+    int* ptr = ireg(c, "vof_csr_ptr", nc + 1); int* col = ireg(c, "vof_csr_col", nnz);
+    double* val = dreg(c, "vof_csr_val", nnz);
+    for (int k = 0; k < nnz; ++k) ptr[ar[k]]++;
+    for (int i = 0, s2 = 0; i < nc; ++i) { int t = ptr[i]; ptr[i] = s2; s2 += t; }
+    ptr[nc] = nnz;
+    for (int k = 0; k < nnz; ++k) { int d = ptr[ar[k]]++; col[d] = acl[k]; val[d] = av[k]; }
+    for (int i = 0, last = 0; i <= nc; ++i) { int t = ptr[i]; ptr[i] = last; last = t; }
+}
+
+int orc_solve_vof(orc_ctx* c, double tol, int maxiter, double* out_x, double* out_relres) {
+    return bicgstab_jacobi(c->nc, iget(c, "vof_csr_ptr"), iget(c, "vof_csr_col"), dget(c, "vof_csr_val"),
+                           dget(c, "vof_B"), tol, maxiter, out_x, out_relres);
+}
+
+/* eqVolfrac.cpp:770-793: VF += urf x, clamp to [0, 1]; returns sqrt(sum x^2) */
+double orc_update_vof(orc_ctx* c, const double* x) {
+    double* VF = dget(c, "VF");
+    double nd = 0.0;
+    for (int i = 0; i < c->nc; ++i) {
+        VF[i] += c->urf_vof * x[i];
+        VF[i] = smax(0.0, smin(1.0, VF[i]));
+        nd += x[i] * x[i];
+    }
+    return sqrt(nd);
 }

@@ -51,11 +51,20 @@ class Case:
     pre_p_urf: float = 0.3
     pre_u_urf: float = 0.3
     mom_u_urf: float = 0.3          # momentumEq U relaxation (fvSolution default)
+    vof_urf: float = 0.3            # speciesEq VF relaxation (fvSolution default)
     # BDF2 history for the momentum equation: (U, V, W) at steps n-1 and n-2;
     # None means "same as the current field" (the first step of a run)
     old: tuple = None
     old2: tuple = None
+    old_vf: np.ndarray = None       # VF at steps n-1 and n-2 (None: the current VF)
+    old2_vf: np.ndarray = None
     extra: dict = field(default_factory=dict)
+
+    def vf_history(self):
+        """(oldVF, old2VF), defaulting to the current VF."""
+        o = self.old_vf if self.old_vf is not None else self.VF
+        o2 = self.old2_vf if self.old2_vf is not None else self.VF
+        return tuple(np.ascontiguousarray(a, dtype=np.float64) for a in (o, o2))
 
     def history(self):
         """(oldU, oldV, oldW, old2U, old2V, old2W), defaulting to the current velocity."""
@@ -125,6 +134,15 @@ def with_history(case: Case, seed: int, scale: float = 0.1) -> Case:
     cur = (case.U, case.V, case.W)
     case.old = tuple(c + scale * rng.uniform(-1.0, 1.0, size=n) for c in cur)
     case.old2 = tuple(c + scale * rng.uniform(-1.0, 1.0, size=n) for c in cur)
+    return case
+
+
+def with_vf_history(case: Case, seed: int, scale: float = 0.05) -> Case:
+    """Seeded old / second-old volume fractions near the current one, in [0, 1]."""
+    rng = np.random.default_rng(seed)
+    n = case.mesh.n_cells
+    case.old_vf = np.clip(case.VF + scale * rng.uniform(-1.0, 1.0, size=n), 0.0, 1.0)
+    case.old2_vf = np.clip(case.VF + scale * rng.uniform(-1.0, 1.0, size=n), 0.0, 1.0)
     return case
 
 

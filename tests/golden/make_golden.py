@@ -5,7 +5,9 @@ runs it on small seeded cases and stores inputs and every dumped intermediate
 as .npz.  The fixtures are committed so the parity tests need neither the
 reference tree nor its build.  Fixtures named outer_* hold a whole outer
 iteration (momentum equation, then the pressure correction) with seeded old
-and second-old velocities for the BDF2 term.
+and second-old velocities for the BDF2 term; fixtures named vofeq_* hold one
+volume-fraction sub-iteration (MSTACS reconstruction + calcVolfracEq) with
+seeded old and second-old volume fractions.
 
     python tests/golden/make_golden.py [REF_DIR]
 """
@@ -21,8 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from semo_mesh_gb300.cases import (box_case, vof_case, with_fields, with_history, BC_FIXED_VALUE,  # noqa: E402
-                                   BC_NO_SLIP, BC_SLIP)
+from semo_mesh_gb300.cases import (box_case, vof_case, with_fields, with_history, with_vf_history,  # noqa: E402
+                                   BC_FIXED_VALUE, BC_NO_SLIP, BC_SLIP)
 from oracle.refcase import run_reference  # noqa: E402
 
 
@@ -63,11 +65,28 @@ def outer_cases():
     return cs
 
 
-def save(name: str, case, ref: dict, momentum: bool = False) -> None:
+def vofeq_cases():
+    cs = []
+    c = with_vf_history(with_fields(vof_case(8, jitter=0.25), seed=5, p_scale=100.0), seed=9)
+    c.name = "vofeq_vof8"
+    cs.append(("vofeq_vof8", c))
+    c = with_vf_history(vof_case(7, jitter=0.2), seed=4)
+    # an inflow patch with a fixed volume fraction exercises the boundary coefficient
+    c.bc_type[c.mesh.patch_names.index("xmin"), 2] = BC_FIXED_VALUE
+    c.bc_value[c.mesh.patch_names.index("xmin"), 4] = 0.7
+    c.vof_urf = 0.5
+    c.name = "vofeq_vof7"
+    cs.append(("vofeq_vof7", c))
+    return cs
+
+
+def save(name: str, case, ref: dict, momentum: bool = False, vof: bool = False) -> None:
     m = case.mesh
     out = {f"ref_{k}": v for k, v in ref.items()}
     if momentum:
         out["history"] = np.stack(case.history())
+    if vof:
+        out["vf_history"] = np.stack(case.vf_history())
     out.update(points=m.points, face_ptr=m.face_ptr, face_pts=m.face_pts, owner=m.owner,
                neighbour=m.neighbour, patch_start=m.patch_start, patch_size=m.patch_size,
                n_cells=np.int64(m.n_cells), P=case.P, U=case.U, V=case.V, W=case.W, VF=case.VF,
@@ -75,7 +94,7 @@ def save(name: str, case, ref: dict, momentum: bool = False) -> None:
                params=np.array([case.dt, case.rho[0], case.rho[1], case.mu[0], case.mu[1], case.sigma,
                                 case.gravity[0], case.gravity[1], case.gravity[2], case.pre_p_urf,
                                 case.pre_u_urf, 1.0 if case.use_gravity else 0.0, case.mom_u_urf,
-                                1.0 if momentum else 0.0]))
+                                1.0 if momentum else 0.0, case.vof_urf]))
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
@@ -91,6 +110,10 @@ def main():
         ref = run_reference(case, threads=1, momentum=True)
         save(name, case, ref, momentum=True)
         print(name, case.mesh.n_cells, "cells (outer iteration)")
+    for name, case in vofeq_cases():
+        ref = run_reference(case, threads=1, vof=True)
+        save(name, case, ref, vof=True)
+        print(name, case.mesh.n_cells, "cells (volume-fraction sub-iteration)")
 
 
 if __name__ == "__main__":

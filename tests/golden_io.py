@@ -16,12 +16,17 @@ def _all():
 
 def names():
     """Fixtures of one pressure-correction pass."""
-    return [n for n in _all() if not n.startswith("outer_")]
+    return [n for n in _all() if not n.startswith(("outer_", "vofeq_"))]
 
 
 def outer_names():
     """Fixtures of a whole outer iteration: momentum equation, then pressure correction."""
     return [n for n in _all() if n.startswith("outer_")]
+
+
+def vofeq_names():
+    """Fixtures of one volume-fraction sub-iteration (MSTACS + calcVolfracEq)."""
+    return [n for n in _all() if n.startswith("vofeq_")]
 
 
 def load(name):
@@ -37,6 +42,11 @@ def load(name):
                 pre_p_urf=float(p[9]), pre_u_urf=float(p[10]))
     if p.size > 12:
         case.mom_u_urf = float(p[12])
+    if p.size > 14:
+        case.vof_urf = float(p[14])
+    if "vf_history" in z.files:
+        h = z["vf_history"]
+        case.old_vf, case.old2_vf = h[0].copy(), h[1].copy()
     if "history" in z.files:
         h = z["history"]
         case.old = (h[0].copy(), h[1].copy(), h[2].copy())
