@@ -83,6 +83,7 @@ typedef struct {
     double p_min, p_max, u_min, u_max, v_min, v_max, w_min, w_max;  /* controls.min/max clamps */
     double mu[2];                /* phase viscosities (species[].mu), laminar */
     double urf_mom;              /* controls.momVelURF */
+    double urf_vof;              /* controls.vofVofURF */
 } semo_physics;
 
 typedef struct {
@@ -190,6 +191,34 @@ semo_status semo_solve_momentum(semo_ctx* ctx, double* x, semo_solve_info* info)
    pressure) or NULL. */
 semo_status semo_outer_iteration(semo_ctx* ctx, double* norms, semo_solve_info* info);
 
+/* Old (n-1) and second-old (n-2) volume fraction for the BDF2 term of the
+   volume-fraction equation, caller's cell order; both NULL clears them (the
+   current VF is used for both).  Replaces: cell.var[oldVF[0]] and
+   cell.var[Qm[3]] (src/solvers/pressureBased.cpp:33-67). */
+semo_status semo_set_old_vf(semo_ctx* ctx, const double* oldVF, const double* old2VF);
+
+/* One volume-fraction sub-iteration: zero-order face values, LSQ gradients,
+   MSTACS face reconstruction of VF, BDF2 + upwind convection assembly with
+   the Rhie-Chow face velocity, the solve, VF += urf_vof x clamped to [0, 1].
+   Returns SEMO's sqrt(sum x^2) in *norm.  The gravity source is the one of
+   the time step: computed once after fields or physics are set, as SEMO
+   computes it once per time step.  Replaces:
+   setIncomValuesLeftRightFaceWithVfMSTACS (src/solvers/reconIncom.cpp:345-429,
+   src/solvers/NVD.cpp:1098-1790) + calcVolfracEq (src/solvers/build.h,
+   src/solvers/eqVolfrac.cpp:9-795) with its solveAMGCL("volume_fraction")
+   (src/solvers/solveAMGCL.cpp:862-884), with Jacobi-preconditioned BiCGStab. */
+semo_status semo_vof_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
+
+/* Volume-fraction assembly only. */
+semo_status semo_assemble_vof(semo_ctx* ctx);
+
+/* The assembled volume-fraction system in SEMO's layout (as
+   semo_get_momentum_system; b is n_cells). */
+semo_status semo_get_vof_system(semo_ctx* ctx, int32_t* ptr, int32_t* col, double* val, double* b, int64_t* nnz);
+
+/* Solve the assembled volume-fraction system; x in the caller's cell order. */
+semo_status semo_solve_vof(semo_ctx* ctx, double* x, semo_solve_info* info);
+
 /* Assembly only (steps up to the face loop of calcPressureEq).  After it, the
    system can be read out or solved. */
 semo_status semo_assemble_pressure(semo_ctx* ctx);
@@ -202,8 +231,10 @@ semo_status semo_get_system_rcm(semo_ctx* ctx, int32_t* ptr, int32_t* col, doubl
 /* Intermediates of the last assembly, in the caller's cell order, for
    checking: name is one of "grad_P","grad_U","grad_V","grad_W","grad_VF"
    (3*n_cells, xyz interleaved), "minmax_uvw" (6*n_cells), "minmax_vf",
-   "minmax_p" (2*n_cells), "rho", "mu" (n_cells), "src_grav" (4*n_cells),
-   "face_UnF" (n_faces, face order), "geometry:<name>". */
+   "minmax_p" (2*n_cells), "rho", "mu", "VF" (n_cells), "src_grav" (4*n_cells),
+   "face_UnF" (n_faces, face order), "face_VF_LR" (2*n_faces: the
+   reconstructed left/right face VF of the last VOF assembly, interleaved),
+   "geometry:<name>". */
 semo_status semo_get_array(semo_ctx* ctx, const char* name, double* out, int64_t count);
 
 /* Solve the assembled pressure system; x in the caller's cell order. */

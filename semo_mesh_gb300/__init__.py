@@ -52,7 +52,7 @@ class Physics(C.Structure):
                 ("use_gravity", C.c_int), ("urf_p", C.c_double), ("urf_u", C.c_double),
                 ("p_min", C.c_double), ("p_max", C.c_double), ("u_min", C.c_double), ("u_max", C.c_double),
                 ("v_min", C.c_double), ("v_max", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double),
-                ("mu", C.c_double * 2), ("urf_mom", C.c_double)]
+                ("mu", C.c_double * 2), ("urf_mom", C.c_double), ("urf_vof", C.c_double)]
 
 
 class SolveInfo(C.Structure):
@@ -110,6 +110,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_get_momentum_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
     L.semo_solve_momentum.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_outer_iteration.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_set_old_vf.argtypes = [vp, f64p, f64p]
+    L.semo_vof_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_assemble_vof.argtypes = [vp]
+    L.semo_get_vof_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
+    L.semo_solve_vof.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     _lib = L
     return L
 
@@ -200,6 +205,7 @@ class Context:
         ph.urf_u = case.pre_u_urf
         ph.mu[0], ph.mu[1] = case.mu
         ph.urf_mom = case.mom_u_urf
+        ph.urf_vof = case.vof_urf
         bt, btp = _i32(case.bc_type.reshape(-1))
         bv, bvp = _f64(case.bc_value.reshape(-1))
         self._check(self.L.semo_set_physics(self.h, C.byref(ph), btp, bvp))
@@ -218,6 +224,19 @@ class Context:
         else:
             h = case.history()
             self.set_old_velocity(h[:3], h[3:])
+        if case.old_vf is None and case.old2_vf is None:
+            self.set_old_vf(None)
+        else:
+            self.set_old_vf(*case.vf_history())
+
+    def set_old_vf(self, old_vf, old2_vf=None) -> None:
+        """BDF2 history of the volume fraction (n-1, n-2); None clears it."""
+        if old_vf is None:
+            self._check(self.L.semo_set_old_vf(self.h, None, None))
+            return
+        a, ap = _f64(old_vf)
+        b, bp = _f64(old2_vf)
+        self._check(self.L.semo_set_old_vf(self.h, ap, bp))
 
     def set_old_velocity(self, old, old2=None) -> None:
         """BDF2 history: old = (U, V, W) at n-1, old2 at n-2; None clears both."""
@@ -267,6 +286,37 @@ class Context:
         info = (SolveInfo * 4)()
         self._check(self.L.semo_outer_iteration(self.h, norms, info))
         return (norms[0], norms[1]), [i.as_dict() for i in info]
+
+    def calc_volfrac_eq(self) -> tuple:
+        """One volume-fraction sub-iteration (MSTACS + calcVolfracEq): (norm, info)."""
+        norm = C.c_double()
+        info = SolveInfo()
+        self._check(self.L.semo_vof_pass(self.h, C.byref(norm), C.byref(info)))
+        return norm.value, info.as_dict()
+
+    def assemble_vof(self) -> None:
+        self._check(self.L.semo_assemble_vof(self.h))
+
+    def vof_system(self) -> dict:
+        """The volume-fraction system in SEMO's layout (caller numbering, COO-scatter rows)."""
+        n = self.n_cells
+        nnz = C.c_int64()
+        self._check(self.L.semo_get_vof_system(self.h, None, None, None, None, C.byref(nnz)))
+        ptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz.value, dtype=np.int32)
+        val = np.empty(nnz.value)
+        b = np.empty(n)
+        self._check(self.L.semo_get_vof_system(self.h, ptr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               col.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               val.ctypes.data_as(C.POINTER(C.c_double)),
+                                               b.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nnz)))
+        return {"ptr": ptr, "col": col, "val": val, "b": b}
+
+    def solve_vof(self) -> SolveResult:
+        x = np.empty(self.n_cells)
+        info = SolveInfo()
+        self._check(self.L.semo_solve_vof(self.h, x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+        return SolveResult(x=x, info=info.as_dict())
 
     def assemble_momentum(self) -> None:
         self._check(self.L.semo_assemble_momentum(self.h))
@@ -349,7 +399,8 @@ class Context:
     # ---- measurement hooks -------------------------------------------------
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
-              "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate")
+              "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate", "mstacs", "vface",
+              "vsolve", "vupdate", "stencil_uvw")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

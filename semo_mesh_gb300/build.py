@@ -24,6 +24,7 @@ UNITS = [
     ("geometry.cu", ["--fmad=false"]),
     ("assemble.cu", []),
     ("momentum.cu", []),
+    ("vof.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
     ("noalloc.cu", []),

@@ -452,14 +452,11 @@ void assemble_face_values(semo_ctx* c, bool with_mu) {
 // and the gravity source -- SEMO too computes that source once per time step,
 // before its outer loop (src/solvers/pressureBased.cpp:141) -- and recomputes
 // only what depends on U, V, W.
-void assemble_gravity_stencil(semo_ctx* c) {
+void assemble_gravity(semo_ctx* c) {
     const int T = 256;
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
-    const bool keep = c->pvf_current;
-    if (keep) {
-        // gravity source kept
-    } else if (c->phys.use_gravity) {
+    if (c->phys.use_gravity) {
         StageScope sc(c, ST_GRAVITY);
         k_grav_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nc, nb, c->own, c->nei, c->fn, c->wc, c->pf, c->nfv, c->U, c->V,
                                                  c->W, c->irho, c->bface, c->phys.gravity[0], c->phys.gravity[1],
@@ -470,17 +467,27 @@ void assemble_gravity_stencil(semo_ctx* c) {
     } else {
         c->sg.zero();
     }
-    {
-    StageScope sc(c, ST_STENCIL);
+    c->sg_current = true;
+}
+
+void stencil_pass(semo_ctx* c, bool full) {
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    cudaStream_t s = c->stream;
+    StageScope sc(c, full ? ST_STENCIL : ST_STENCIL_UVW);
     auto launch = [&](auto kern) {
         kern<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
                                              c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
                                              c->grad, c->mm);
     };
-    if (keep) launch(k_stencil<false>);
-    else launch(k_stencil<true>);
+    if (full) launch(k_stencil<true>);
+    else launch(k_stencil<false>);
     SEMO_CHECK_LAUNCH();
-    }
+}
+
+void assemble_gravity_stencil(semo_ctx* c) {
+    const bool keep = c->pvf_current;
+    if (!keep) assemble_gravity(c);   // else the gravity source is kept
+    stencil_pass(c, !keep);
 }
 
 void assemble_pressure(semo_ctx* c) {

@@ -74,6 +74,7 @@ void semo_physics_default(semo_physics* p) {
     p->p_max = p->u_max = p->v_max = p->w_max = 1e300;
     p->mu[0] = p->mu[1] = 1e-3;
     p->urf_mom = 0.3;
+    p->urf_vof = 0.3;
 }
 
 semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
@@ -179,8 +180,8 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         c->mesh_ready = c->phys_ready = c->fields_ready = c->assembled = c->mom_assembled = false;
         c->amg32.clear();
         c->amg64.clear();
-        c->has_old = c->has_src = false;
-        c->pvf_current = false;
+        c->has_old = c->has_src = c->has_oldvf = false;
+        c->pvf_current = c->sg_current = c->vof_assembled = false;
         ++c->mesh_gen;
 
         // ---- cell -> faces, ascending face index (connectCelltoFaces, build.cpp:587-608) ----
@@ -456,7 +457,9 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         c->phys_ready = true;
         c->assembled = false;
         c->mom_assembled = false;
+        c->vof_assembled = false;
         c->pvf_current = false;
+        c->sg_current = false;
     });
 }
 
@@ -492,7 +495,9 @@ semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const
         c->fields_ready = true;
         c->assembled = false;
         c->mom_assembled = false;
+        c->vof_assembled = false;
         c->pvf_current = false;
+        c->sg_current = false;
     });
 }
 
@@ -556,7 +561,7 @@ semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t c
         const char* grads[5] = {"grad_P", "grad_U", "grad_V", "grad_W", "grad_VF"};
         for (int g = 0; g < 5; ++g)
             if (nm == grads[g]) {
-                need(c->assembled || c->mom_assembled, SEMO_ERR_STATE, "not assembled");
+                need(c->assembled || c->mom_assembled || c->vof_assembled, SEMO_ERR_STATE, "not assembled");
                 cell_planes(c->grad.p + (size_t)3 * g * n, 3, true);
                 return;
             }
@@ -564,10 +569,27 @@ semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t c
         if (nm == "minmax_vf") { cell_planes(c->mm.p + (size_t)6 * n, 2, true); return; }
         if (nm == "minmax_p") { cell_planes(c->mm.p + (size_t)8 * n, 2, true); return; }
         if (nm == "rho") { cell_planes(c->rho.p, 1, false); return; }
+        if (nm == "VF") { need(c->fields_ready, SEMO_ERR_STATE, "no fields set"); cell_planes(c->VF.p, 1, false); return; }
         if (nm == "mu") { need(c->mu.n == 2 * (size_t)n, SEMO_ERR_STATE, "no momentum assembly"); cell_planes(c->mu.p, 1, false); return; }
         if (nm == "src_grav") { cell_planes(c->sg.p, 4, true); return; }
         if (nm == "grad_x") { cell_planes(c->gx.p, 3, true); return; }
         if (nm == "face_UnF") { face_planes(c->unf.p, 1, nf); return; }
+        if (nm == "face_VF_LR") {
+            need(c->vof_assembled, SEMO_ERR_STATE, "no volume-fraction assembly");
+            need(count == 2 * (int64_t)nf, SEMO_ERR_ARGUMENT, "count mismatch for " + nm);
+            const int ni = c->ni, nb = c->nb;
+            std::vector<double> fl((size_t)2 * std::max(ni, 1)), bf((size_t)6 * std::max(nb, 1));
+            SEMO_CUDA(cudaMemcpyAsync(fl.data(), c->fvf.p, sizeof(double) * 2 * ni, cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaMemcpyAsync(bf.data(), c->bface.p, sizeof(double) * 6 * nb, cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaStreamSynchronize(c->stream));
+            for (int f = 0; f < nf; ++f) {   // the caller's face f is stored at fiperm[f]
+                const int sf = c->fiperm[f];
+                if (sf < ni) { out[2 * f] = fl[sf]; out[2 * f + 1] = fl[ni + sf]; }
+                else { out[2 * f] = out[2 * f + 1] = bf[4 * (size_t)nb + (sf - ni)]; }
+            }
+            return;
+        }
+
         if (nm == "geometry:cell_vol") { cell_planes(c->vol.p, 1, false); return; }
         if (nm == "geometry:cell_c") { cell_planes(c->cc.p, 3, true); return; }
         if (nm == "geometry:lsq_minv") { cell_planes(c->minv.p, 6, true); return; }
@@ -738,38 +760,129 @@ semo_status semo_outer_iteration(semo_ctx* c, double* norms, semo_solve_info* in
     return finish(c, st, conv, "a solve of the outer iteration did not reach its tolerance");
 }
 
+namespace {
+// A system held on the context's CSR pattern (RCM rows), written out in SEMO's
+// layout: rows back in the caller's numbering, each row in SEMO's in-row order
+// with its diagonal first, off-diagonals SEMO leaves out (stored as 0) dropped.
+void export_semo_layout(semo_ctx* c, const double* dval, const double* db, int planes, int32_t* ptr, int32_t* col,
+                        double* val, double* b, int64_t* nnz_out) {
+    cudaStream_t s = c->stream;
+    const int n = c->nc;
+    std::vector<int> hp(n + 1), hc(c->nnz);
+    std::vector<double> hv(c->nnz), hb((size_t)planes * n);
+    SEMO_CUDA(cudaMemcpyAsync(hp.data(), c->A_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hc.data(), c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hv.data(), dval, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hb.data(), db, sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    int64_t k_out = 0;
+    if (ptr) ptr[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        const int r = c->iperm[i];
+        for (int k = hp[r]; k < hp[r + 1]; ++k) {
+            if (k != hp[r] && hv[k] == 0.0) continue;
+            if (col) col[k_out] = c->perm[hc[k]];
+            if (val) val[k_out] = hv[k];
+            ++k_out;
+        }
+        if (ptr) ptr[i + 1] = (int32_t)k_out;
+    }
+    if (b)
+        for (int j = 0; j < planes; ++j)
+            for (int r = 0; r < n; ++r) b[(size_t)j * n + c->perm[r]] = hb[(size_t)j * n + r];
+    if (nnz_out) *nnz_out = k_out;
+}
+
+// calcVolfracEq: reconstruct, assemble, solve, update (skipped after a breakdown).
+semo_status vof_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info) {
+    need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+         "mesh, physics and fields must be set before a pass");
+    SEMO_CUDA(cudaSetDevice(c->device));
+    semo::assemble_vof(c);
+    c->vof_assembled = true;
+    semo_solve_info inf{};
+    semo_status conv = semo::solve_vof(c, &inf);
+    if (info) *info = inf;
+    if (conv == SEMO_ERR_BREAKDOWN) return conv;
+    const double nrm = semo::vof_update(c);
+    if (norm) *norm = nrm;
+    return conv;
+}
+}  // namespace
+
 semo_status semo_get_momentum_system(semo_ctx* c, int32_t* ptr, int32_t* col, double* val, double* b,
                                      int64_t* nnz_out) {
     return guarded(c, [&] {
         need(c->mom_assembled, SEMO_ERR_STATE, "momentum system not assembled");
-        cudaStream_t s = c->stream;
-        const int n = c->nc;
-        std::vector<int> hp(n + 1), hc(c->nnz);
-        std::vector<double> hv(c->nnz), hb(3 * (size_t)n);
-        SEMO_CUDA(cudaMemcpyAsync(hp.data(), c->A_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaMemcpyAsync(hc.data(), c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaMemcpyAsync(hv.data(), c->Am_val.p, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaMemcpyAsync(hb.data(), c->bm.p, sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        // rows back in the caller's numbering; each row keeps SEMO's in-row order,
-        // its diagonal first, and drops the off-diagonals calcMomentumEqs leaves out
-        int64_t k_out = 0;
-        if (ptr) ptr[0] = 0;
-        for (int i = 0; i < n; ++i) {
-            const int r = c->iperm[i];
-            for (int k = hp[r]; k < hp[r + 1]; ++k) {
-                if (k != hp[r] && hv[k] == 0.0) continue;
-                if (col) col[k_out] = c->perm[hc[k]];
-                if (val) val[k_out] = hv[k];
-                ++k_out;
-            }
-            if (ptr) ptr[i + 1] = (int32_t)k_out;
-        }
-        if (b)
-            for (int j = 0; j < 3; ++j)
-                for (int r = 0; r < n; ++r) b[(size_t)j * n + c->perm[r]] = hb[(size_t)j * n + r];
-        if (nnz_out) *nnz_out = k_out;
+        export_semo_layout(c, c->Am_val.p, c->bm.p, 3, ptr, col, val, b, nnz_out);
     });
+}
+
+semo_status semo_get_vof_system(semo_ctx* c, int32_t* ptr, int32_t* col, double* val, double* b,
+                                int64_t* nnz_out) {
+    return guarded(c, [&] {
+        need(c->vof_assembled, SEMO_ERR_STATE, "volume-fraction system not assembled");
+        export_semo_layout(c, c->Av_val.p, c->bvf.p, 1, ptr, col, val, b, nnz_out);
+    });
+}
+
+semo_status semo_set_old_vf(semo_ctx* c, const double* oldVF, const double* old2VF) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        c->vof_assembled = false;
+        if (!oldVF && !old2VF) { c->has_oldvf = false; return; }
+        need(oldVF && old2VF, SEMO_ERR_ARGUMENT, "give both old volume fractions or none");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        c->oldvf.alloc(2 * n, s);
+        SEMO_CUDA(cudaMemcpyAsync(c->stage.p, oldVF, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        SEMO_CUDA(cudaMemcpyAsync(c->stage.p + n, old2VF, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        double* dst[2] = {c->oldvf.p, c->oldvf.p + n};
+        if (!semo::fields_from_caller_order(c, c->stage.p, dst, 2)) {
+            c->has_oldvf = false;
+            throw Error(SEMO_ERR_NAN, "non-finite old volume fraction");
+        }
+        c->has_oldvf = true;
+    });
+}
+
+semo_status semo_vof_pass(semo_ctx* c, double* norm, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] { conv = vof_pass_impl(c, norm, info); });
+    return finish(c, st, conv, "volume-fraction solve did not reach the tolerance");
+}
+
+semo_status semo_assemble_vof(semo_ctx* c) {
+    return guarded(c, [&] {
+        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+             "mesh, physics and fields must be set before assembly");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::assemble_vof(c);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->vof_assembled = true;
+    });
+}
+
+semo_status semo_solve_vof(semo_ctx* c, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->vof_assembled, SEMO_ERR_STATE, "volume-fraction system not assembled");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo_solve_info inf{};
+        conv = semo::solve_vof(c, &inf);
+        if (info) *info = inf;
+        if (x) {
+            const size_t n = (size_t)c->nc;
+            c->stage.alloc(5 * n, c->stream);
+            const double* src[1] = {c->xvf.p};
+            semo::fields_to_caller_order(c, src, c->stage.p, 1);
+            SEMO_CUDA(cudaMemcpyAsync(x, c->stage.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+            SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        }
+    });
+    return finish(c, st, conv, "volume-fraction solve did not reach the tolerance");
 }
 
 semo_status semo_solve_coo(semo_ctx* c, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,

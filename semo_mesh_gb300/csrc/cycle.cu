@@ -29,7 +29,11 @@
 namespace semo {
 namespace {
 
-constexpr int kRedBlocks = 608;   // 4 x 152 SMs; fixed so every sum has a fixed order
+// Grid of the kernels that end in a reduction (dot products fused into the
+// SpMVs and vector updates): 16 blocks of 256 per SM on 152 SMs, enough
+// threads for the gathers to hide their latency; fixed, so every sum has a
+// fixed order.
+constexpr int kRedBlocks = 2432;
 constexpr int kRedThreads = 256;
 inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
@@ -764,10 +768,10 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
     }
 }
 
-// ------------------------------------------------ momentum: batched BiCGStab
-// Three right-hand sides (x, y, z velocity) share one matrix: every kernel
-// walks the rows once and serves all three, so the operator is read once per
-// product for the three systems.  Right preconditioning by D^-1 (the momentum
+// ---------------------------------- momentum and VOF: batched BiCGStab
+// NR right-hand sides (3 for the velocity components, 1 for the volume
+// fraction) share one matrix: every kernel walks the rows once and serves all
+// of them, so the operator is read once per product for the NR systems.  Right preconditioning by D^-1 (the momentum
 // matrix is dominated by its BDF2 diagonal at the time steps of interest).
 // Per system j the scalars live at scal[16 j + k]:
 //   0 rho, 1 alpha, 2 omega, 3 beta, 4 (rh,v), 5 (t,s), 6 (t,t), 7 (r,r),
@@ -775,42 +779,45 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
 constexpr int kMomScal = 16;
 __device__ __forceinline__ bool mom_active(const double* scal, int j) { return scal[kMomScal * j + 9] != 0.0; }
 
-__device__ __forceinline__ void sell_mv3(const SellView<double>& A, int row, const double* __restrict__ x, size_t N,
-                                         double& s0, double& s1, double& s2) {
-    s0 = s1 = s2 = 0.0;
+template <int NR>
+__device__ __forceinline__ void sell_mv(const SellView<double>& A, int row, const double* __restrict__ x, size_t N,
+                                       double* y) {
+#pragma unroll
+    for (int j = 0; j < NR; ++j) y[j] = 0.0;
     const int sl = row >> 5, l = row & 31;
     const int b = A.sptr[sl], w = (A.sptr[sl + 1] - b) >> 5;
-    for (int j = 0, k = b + l; j < w; ++j, k += 32) {
+    for (int e = 0, k = b + l; e < w; ++e, k += 32) {
         const int c = A.col[k];
         const double v = A.val[k];
-        s0 += v * __ldg(x + c);
-        s1 += v * __ldg(x + N + c);
-        s2 += v * __ldg(x + 2 * N + c);
+#pragma unroll
+        for (int j = 0; j < NR; ++j) y[j] += v * __ldg(x + j * N + c);
     }
 }
 
 // x = 0, r = rh = b, p = v = 0;  part = (b,b) per system
+template <int NR>
 __global__ void __launch_bounds__(kRedThreads) k_bi_init(int n, const double* __restrict__ b, double* __restrict__ x,
                                                          double* __restrict__ r, double* __restrict__ rh,
                                                          double* __restrict__ p, double* __restrict__ v,
                                                          double* __restrict__ part) {
     __shared__ double sh[32];
-    double bb[3] = {0.0, 0.0, 0.0};
+    double bb[NR] = {};
     const size_t N = n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < NR; ++j) {
             const double bi = b[j * N + i];
             x[j * N + i] = 0.0; r[j * N + i] = bi; rh[j * N + i] = bi; p[j * N + i] = 0.0; v[j * N + i] = 0.0;
             bb[j] += bi * bi;
         }
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double t = block_sum(bb[j], sh);
         if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
     }
 }
+template <int NR>
 __global__ void k_bi_fin0(const double* __restrict__ part, double* __restrict__ scal, double tol2) {
     __shared__ double sh[32];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double bb = sum_parts(part + j * kRedBlocks, sh);
         if (threadIdx.x == 0) {
             double* S = scal + kMomScal * j;
@@ -821,13 +828,14 @@ __global__ void k_bi_fin0(const double* __restrict__ part, double* __restrict__ 
     }
 }
 // p = r + beta (p - omega v);  ph = D^-1 p
+template <int NR>
 __global__ void k_bi_p(int n, const double* __restrict__ dinv, const double* __restrict__ r, double* __restrict__ p,
                        const double* __restrict__ v, double* __restrict__ ph, const double* __restrict__ scal) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = n;
     const double di = dinv[i];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         if (!mom_active(scal, j)) continue;
         const double beta = scal[kMomScal * j + 3], omega = scal[kMomScal * j + 2];
         const double pi = r[j * N + i] + beta * (p[j * N + i] - omega * v[j * N + i]);
@@ -836,29 +844,31 @@ __global__ void k_bi_p(int n, const double* __restrict__ dinv, const double* __r
     }
 }
 // y = A x for the three systems;  part = (rh, y) per system
+template <int NR>
 __global__ void __launch_bounds__(kRedThreads) k_bi_mv1(SellView<double> A, const double* __restrict__ x,
                                                         double* __restrict__ y, const double* __restrict__ rh,
                                                         const double* __restrict__ scal, double* __restrict__ part) {
     __shared__ double sh[32];
     const size_t N = A.n;
-    double d[3] = {0.0, 0.0, 0.0};
+    double d[NR] = {};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
-        double s[3];
-        sell_mv3(A, row, x, N, s[0], s[1], s[2]);
-        for (int j = 0; j < 3; ++j) {
+        double s[NR];
+        sell_mv<NR>(A, row, x, N, s);
+        for (int j = 0; j < NR; ++j) {
             if (!mom_active(scal, j)) continue;
             y[j * N + row] = s[j];
             d[j] += rh[j * N + row] * s[j];
         }
     }
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double t = block_sum(d[j], sh);
         if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
     }
 }
+template <int NR>
 __global__ void k_bi_fin1(const double* __restrict__ part, double* __restrict__ scal) {
     __shared__ double sh[32];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double rv = sum_parts(part + j * kRedBlocks, sh);
         if (threadIdx.x == 0) {
             double* S = scal + kMomScal * j;
@@ -871,13 +881,14 @@ __global__ void k_bi_fin1(const double* __restrict__ part, double* __restrict__ 
     }
 }
 // s = r - alpha v (in place in r);  sh = D^-1 s
+template <int NR>
 __global__ void k_bi_s(int n, const double* __restrict__ dinv, double* __restrict__ r, const double* __restrict__ v,
                        double* __restrict__ shv, const double* __restrict__ scal) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const size_t N = n;
     const double di = dinv[i];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         if (!mom_active(scal, j)) continue;
         const double si = r[j * N + i] - scal[kMomScal * j + 1] * v[j * N + i];
         r[j * N + i] = si;
@@ -885,31 +896,33 @@ __global__ void k_bi_s(int n, const double* __restrict__ dinv, double* __restric
     }
 }
 // t = A sh;  part = (t,s), (t,t) per system
+template <int NR>
 __global__ void __launch_bounds__(kRedThreads) k_bi_mv2(SellView<double> A, const double* __restrict__ x,
                                                         double* __restrict__ t, const double* __restrict__ s,
                                                         const double* __restrict__ scal, double* __restrict__ part) {
     __shared__ double sh[32];
     const size_t N = A.n;
-    double ts[3] = {0.0, 0.0, 0.0}, tt[3] = {0.0, 0.0, 0.0};
+    double ts[NR] = {}, tt[NR] = {};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
-        double y[3];
-        sell_mv3(A, row, x, N, y[0], y[1], y[2]);
-        for (int j = 0; j < 3; ++j) {
+        double y[NR];
+        sell_mv<NR>(A, row, x, N, y);
+        for (int j = 0; j < NR; ++j) {
             if (!mom_active(scal, j)) continue;
             t[j * N + row] = y[j];
             ts[j] += y[j] * s[j * N + row];
             tt[j] += y[j] * y[j];
         }
     }
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double a = block_sum(ts[j], sh);
         const double b = block_sum(tt[j], sh);
         if (threadIdx.x == 0) { part[(2 * j) * kRedBlocks + blockIdx.x] = a; part[(2 * j + 1) * kRedBlocks + blockIdx.x] = b; }
     }
 }
+template <int NR>
 __global__ void k_bi_fin2(const double* __restrict__ part, double* __restrict__ scal) {
     __shared__ double sh[32];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double ts = sum_parts(part + (2 * j) * kRedBlocks, sh);
         const double tt = sum_parts(part + (2 * j + 1) * kRedBlocks, sh);
         if (threadIdx.x == 0) {
@@ -919,15 +932,16 @@ __global__ void k_bi_fin2(const double* __restrict__ part, double* __restrict__ 
     }
 }
 // x += alpha ph + omega sh;  r = s - omega t;  part = (rh,r), (r,r)
+template <int NR>
 __global__ void __launch_bounds__(kRedThreads) k_bi_xr(int n, double* __restrict__ x, const double* __restrict__ ph,
                                                        const double* __restrict__ shv, double* __restrict__ r,
                                                        const double* __restrict__ t, const double* __restrict__ rh,
                                                        const double* __restrict__ scal, double* __restrict__ part) {
     __shared__ double sh[32];
     const size_t N = n;
-    double a[3] = {0.0, 0.0, 0.0}, b[3] = {0.0, 0.0, 0.0};
+    double a[NR] = {}, b[NR] = {};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < NR; ++j) {
             if (!mom_active(scal, j)) continue;
             const double alpha = scal[kMomScal * j + 1], omega = scal[kMomScal * j + 2];
             x[j * N + i] += alpha * ph[j * N + i] + omega * shv[j * N + i];
@@ -936,15 +950,16 @@ __global__ void __launch_bounds__(kRedThreads) k_bi_xr(int n, double* __restrict
             a[j] += rh[j * N + i] * ri;
             b[j] += ri * ri;
         }
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double u = block_sum(a[j], sh);
         const double w = block_sum(b[j], sh);
         if (threadIdx.x == 0) { part[(2 * j) * kRedBlocks + blockIdx.x] = u; part[(2 * j + 1) * kRedBlocks + blockIdx.x] = w; }
     }
 }
+template <int NR>
 __global__ void k_bi_fin3(const double* __restrict__ part, double* __restrict__ scal, double tol2) {
     __shared__ double sh[32];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double rho1 = sum_parts(part + (2 * j) * kRedBlocks, sh);
         const double rr = sum_parts(part + (2 * j + 1) * kRedBlocks, sh);
         if (threadIdx.x == 0) {
@@ -965,24 +980,26 @@ __global__ void k_bi_fin3(const double* __restrict__ part, double* __restrict__ 
     }
 }
 // r = b - A x;  part = (r,r) per system
+template <int NR>
 __global__ void __launch_bounds__(kRedThreads) k_bi_res(SellView<double> A, const double* __restrict__ x,
                                                         const double* __restrict__ b, double* __restrict__ part) {
     __shared__ double sh[32];
     const size_t N = A.n;
-    double d[3] = {0.0, 0.0, 0.0};
+    double d[NR] = {};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
-        double y[3];
-        sell_mv3(A, row, x, N, y[0], y[1], y[2]);
-        for (int j = 0; j < 3; ++j) { const double ri = b[j * N + row] - y[j]; d[j] += ri * ri; }
+        double y[NR];
+        sell_mv<NR>(A, row, x, N, y);
+        for (int j = 0; j < NR; ++j) { const double ri = b[j * N + row] - y[j]; d[j] += ri * ri; }
     }
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double t = block_sum(d[j], sh);
         if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
     }
 }
+template <int NR>
 __global__ void k_bi_fin_res(const double* __restrict__ part, double* __restrict__ out) {
     __shared__ double sh[32];
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double rr = sum_parts(part + j * kRedBlocks, sh);
         if (threadIdx.x == 0) out[j] = rr;
     }
@@ -1001,11 +1018,12 @@ struct MomState {
 
 // end of one batched BiCGStab iteration on the device: go on while a system
 // is active and the cap is not reached (scal[3*16+0] counts iterations)
+template <int NR>
 __global__ void k_bi_check(cudaGraphConditionalHandle h, double* __restrict__ scal, int max_iter) {
     double* it = scal + 3 * kMomScal;
     it[0] += 1.0;
     bool any = false;
-    for (int j = 0; j < 3; ++j) any |= scal[kMomScal * j + 9] != 0.0;
+    for (int j = 0; j < NR; ++j) any |= scal[kMomScal * j + 9] != 0.0;
     cudaGraphSetConditional(h, (any && it[0] < (double)max_iter) ? 1u : 0u);
 }
 MomState& mom_state(semo_ctx* c) {
@@ -1082,55 +1100,61 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
     info->solve_ms = t1;
 }
 
-semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
-    StageScope stage(c, ST_MSOLVE);
+namespace {
+
+// Jacobi-preconditioned BiCGStab on NR right-hand sides (planes of b, x) of
+// the matrix with values val on the context's CSR pattern.
+template <int NR>
+semo_status bicgstab_jacobi(semo_ctx* c, int stage, const double* val, const double* b, double* x,
+                            semo_solve_info* info) {
+    StageScope scope(c, stage);
     cudaStream_t s = c->stream;
     const int n = c->nc;
     const size_t N = n;
     MomState& st = mom_state(c);
-    c->xm.alloc(3 * N, s);
     st.dinv.alloc(N, s);
-    st.vec.alloc(7 * 3 * N, s);       // r, rh, p, v, ph, sh, t
+    st.vec.alloc(7 * 3 * N, s);       // r, rh, p, v, ph, sh, t (room for 3 systems)
     st.part.alloc(6 * kRedBlocks, s);
     st.scal.alloc(4 * kMomScal, s);
-    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* r = st.vec.p;
-    double* rh = r + 3 * N;
-    double* p = rh + 3 * N;
-    double* v = p + 3 * N;
-    double* ph = v + 3 * N;
-    double* shv = ph + 3 * N;
-    double* t = shv + 3 * N;
+    double* rh = r + NR * N;
+    double* p = rh + NR * N;
+    double* v = p + NR * N;
+    double* ph = v + NR * N;
+    double* shv = ph + NR * N;
+    double* t = shv + NR * N;
     // the recurrence residual is driven to half the tolerance so that the true
     // residual, checked at the end, lands under it
     const double tol2 = 0.25 * c->prm.mom_tol * c->prm.mom_tol;
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
     if (st.gen != c->mesh_gen) {
-        build_sell<double, double>(s, c->A_ptr, c->A_col, c->Am_val, n, st.A);
+        build_sell<double, double>(s, c->A_ptr, c->A_col, val, n, st.A);
         st.gen = c->mesh_gen;
     } else {   // same pattern (the mesh's): refill the values into the kept layout
         k_sell_fill<double, double><<<blocks((int64_t)st.A.nslices * 32, 256), 256, 0, s>>>(
-            n, c->A_ptr, c->A_col, c->Am_val, st.A.sptr, st.A.col, st.A.val);
+            n, c->A_ptr, c->A_col, val, st.A.sptr, st.A.col, st.A.val);
         SEMO_CHECK_LAUNCH();
     }
-    k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, c->A_dig, c->Am_val, st.dinv);
+    k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, c->A_dig, val, st.dinv);
     SEMO_CHECK_LAUNCH();
     SEMO_CUDA(cudaEventRecord(c->ev[1], s));
     const SellView<double> A = st.A.view();
-    k_bi_init<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->bm, c->xm, r, rh, p, v, st.part);
+    k_bi_init<NR><<<kRedBlocks, kRedThreads, 0, s>>>(n, b, x, r, rh, p, v, st.part);
     SEMO_CHECK_LAUNCH();
-    k_bi_fin0<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
+    k_bi_fin0<NR><<<1, 256, 0, s>>>(st.part, st.scal, tol2);
     SEMO_CHECK_LAUNCH();
     double hs[3 * kMomScal];
-    SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(double) * NR * kMomScal, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
-    int iters[3] = {0, 0, 0};
-    for (int j = 0; j < 3; ++j)
-        if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite momentum right-hand side");
-    auto any_active = [&] { return hs[9] != 0.0 || hs[kMomScal + 9] != 0.0 || hs[2 * kMomScal + 9] != 0.0; };
+    int iters[NR] = {};
+    bool any = false;
+    for (int j = 0; j < NR; ++j) {
+        if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
+        any |= hs[kMomScal * j + 9] != 0.0;
+    }
     // the iterations run as one graph: a conditional WHILE node around one
     // iteration (8 kernels + k_bi_check); the host waits once
-    if (any_active() && c->prm.mom_max_iter > 0) {
+    if (any && c->prm.mom_max_iter > 0) {
         GraphGuard gg;
         SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
         cudaGraphConditionalHandle handle;
@@ -1147,23 +1171,23 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
         const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
         SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
-            k_bi_p<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, p, v, ph, st.scal);
+            k_bi_p<NR><<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, p, v, ph, st.scal);
             SEMO_CHECK_LAUNCH();
-            k_bi_mv1<<<kRedBlocks, kRedThreads, 0, s>>>(A, ph, v, rh, st.scal, st.part);
+            k_bi_mv1<NR><<<kRedBlocks, kRedThreads, 0, s>>>(A, ph, v, rh, st.scal, st.part);
             SEMO_CHECK_LAUNCH();
-            k_bi_fin1<<<1, 256, 0, s>>>(st.part, st.scal);
+            k_bi_fin1<NR><<<1, 256, 0, s>>>(st.part, st.scal);
             SEMO_CHECK_LAUNCH();
-            k_bi_s<<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, v, shv, st.scal);
+            k_bi_s<NR><<<blocks(n, 256), 256, 0, s>>>(n, st.dinv, r, v, shv, st.scal);
             SEMO_CHECK_LAUNCH();
-            k_bi_mv2<<<kRedBlocks, kRedThreads, 0, s>>>(A, shv, t, r, st.scal, st.part);
+            k_bi_mv2<NR><<<kRedBlocks, kRedThreads, 0, s>>>(A, shv, t, r, st.scal, st.part);
             SEMO_CHECK_LAUNCH();
-            k_bi_fin2<<<1, 256, 0, s>>>(st.part, st.scal);
+            k_bi_fin2<NR><<<1, 256, 0, s>>>(st.part, st.scal);
             SEMO_CHECK_LAUNCH();
-            k_bi_xr<<<kRedBlocks, kRedThreads, 0, s>>>(n, c->xm, ph, shv, r, t, rh, st.scal, st.part);
+            k_bi_xr<NR><<<kRedBlocks, kRedThreads, 0, s>>>(n, x, ph, shv, r, t, rh, st.scal, st.part);
             SEMO_CHECK_LAUNCH();
-            k_bi_fin3<<<1, 256, 0, s>>>(st.part, st.scal, tol2);
+            k_bi_fin3<NR><<<1, 256, 0, s>>>(st.part, st.scal, tol2);
             SEMO_CHECK_LAUNCH();
-            k_bi_check<<<1, 1, 0, s>>>(handle, st.scal, c->prm.mom_max_iter);
+            k_bi_check<NR><<<1, 1, 0, s>>>(handle, st.scal, c->prm.mom_max_iter);
             SEMO_CHECK_LAUNCH();
         } catch (...) {
             cudaGraph_t junk = nullptr;
@@ -1181,26 +1205,26 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
         const int it = (int)hit[3 * kMomScal];
         __atomic_add_fetch(&g_kernel_launches, 9LL * it, __ATOMIC_RELAXED);
         std::copy(hit, hit + 3 * kMomScal, hs);
-        for (int j = 0; j < 3; ++j) {
-            if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the momentum residual");
+        for (int j = 0; j < NR; ++j) {
+            if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the BiCGStab residual");
             // systems converge one after another; each counts the iterations it was active
             iters[j] = (int)hs[kMomScal * j + 11];
         }
     }
     // true FP64 residuals of the returned solutions
-    k_bi_res<<<kRedBlocks, kRedThreads, 0, s>>>(A, c->xm, c->bm, st.part);
+    k_bi_res<NR><<<kRedBlocks, kRedThreads, 0, s>>>(A, x, b, st.part);
     SEMO_CHECK_LAUNCH();
-    k_bi_fin_res<<<1, 256, 0, s>>>(st.part, st.scal.p + 3 * kMomScal - 3);
+    k_bi_fin_res<NR><<<1, 256, 0, s>>>(st.part, st.scal.p + 3 * kMomScal - 3);
     SEMO_CHECK_LAUNCH();
     double tr[3];
-    SEMO_CUDA(cudaMemcpyAsync(tr, st.scal.p + 3 * kMomScal - 3, sizeof(tr), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(tr, st.scal.p + 3 * kMomScal - 3, sizeof(double) * NR, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaEventRecord(c->ev[2], s));
     SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
     float t0 = 0, t1 = 0;
     SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
     SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
     semo_status worst = SEMO_OK;
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < NR; ++j) {
         const double bb = hs[kMomScal * j + 8];
         const double rel = (bb > 0.0) ? std::sqrt(tr[j] / bb) : 0.0;
         if (info) {
@@ -1217,6 +1241,18 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
         else if (!(rel <= c->prm.mom_tol) && worst == SEMO_OK) worst = SEMO_ERR_NOT_CONVERGED;
     }
     return worst;
+}
+
+}  // namespace
+
+semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
+    c->xm.alloc(3 * (size_t)c->nc, c->stream);
+    return bicgstab_jacobi<3>(c, ST_MSOLVE, c->Am_val, c->bm, c->xm, info);
+}
+
+semo_status solve_vof(semo_ctx* c, semo_solve_info* info) {
+    c->xvf.alloc((size_t)c->nc, c->stream);
+    return bicgstab_jacobi<1>(c, ST_VSOLVE, c->Av_val, c->bvf, c->xvf, info);
 }
 
 // Adjoint solve on the hierarchy of the last forward solve (the pressure

@@ -38,12 +38,13 @@ extern long long g_kernel_launches;
 // Named stages timed with CUDA events on the context's stream when profiling is on.
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
-             ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_COUNT };
+             ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_MSTACS, ST_VFACE, ST_VSOLVE, ST_VUPDATE,
+             ST_STENCIL_UVW, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
                                                   "setup_level", "setup_coarse", "mface", "mcell", "msolve",
-                                                  "mupdate"};
+                                                  "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -175,6 +176,18 @@ struct semo_ctx {
     // current P and VF (set by the momentum assembly, cleared when P, VF or the
     // physics change); the pressure assembly then recomputes only the U,V,W parts
     bool pvf_current = false;
+    // the gravity source was computed since the last change of fields or physics
+    // (the VOF sub-iterations keep it, as SEMO keeps its per-time-step source)
+    bool sg_current = false;
+
+    // ---- volume fraction (RCM order; matrix on the A_ptr/A_col pattern) ----
+    semo::DBuf<double> oldvf;                     // 2 planes: oldVF, old2VF
+    bool has_oldvf = false;
+    semo::DBuf<double> Av_val, bvf, xvf;          // VOF matrix values, RHS, solution
+    semo::DBuf<double> vsc;                       // face scratch: 3 planes of nf
+    semo::DBuf<double> fvf;                       // MSTACS face values: 2 planes of nf (left, right)
+    semo::DBuf<double> co;                        // cell Courant number
+    bool vof_assembled = false;
     std::shared_ptr<void> mom_apply;              // momentum Krylov state (cycle.cu)
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
@@ -258,6 +271,9 @@ double pressure_update(semo_ctx* c);
 void assemble_face_values(semo_ctx* c, bool with_mu);
 // gravity source + one stencil pass (gradients of P,U,V,W,VF; min/max of U,V,W,VF,P)
 void assemble_gravity_stencil(semo_ctx* c);
+void assemble_gravity(semo_ctx* c);
+// full: all five fields; else U, V, W only (P and VF planes left as they are)
+void stencil_pass(semo_ctx* c, bool full);
 // dst[q][r] = src[q*n + perm[r]] for q < planes; false if any value is not finite (syncs)
 bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes);
 // dst[q*n + perm[r]] = src[q][r] for q < planes (async)
@@ -282,10 +298,16 @@ void solve_transpose_reuse(semo_ctx* c, const double* d_g, double* d_lam, semo_s
 // three right-hand sides of the momentum system (c->Am_val, c->bm) -> c->xm; info[3]; returns the
 // worst status (SEMO_OK, SEMO_ERR_NOT_CONVERGED or SEMO_ERR_BREAKDOWN)
 semo_status solve_momentum(semo_ctx* c, semo_solve_info* info);
+// the volume-fraction system (c->Av_val, c->bvf) -> c->xvf; info[1]
+semo_status solve_vof(semo_ctx* c, semo_solve_info* info);
 
 // momentum.cu
 void assemble_momentum(semo_ctx* c);
 double momentum_update(semo_ctx* c);
+
+// vof.cu
+void assemble_vof(semo_ctx* c);
+double vof_update(semo_ctx* c);
 
 int sm_count(int device);
 
