@@ -400,7 +400,7 @@ class Context:
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
               "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate", "mstacs", "vface",
-              "vsolve", "vupdate", "stencil_uvw")
+              "vsolve", "vupdate", "stencil_uvw", "mbface")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

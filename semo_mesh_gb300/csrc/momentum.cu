@@ -243,7 +243,7 @@ void assemble_momentum(semo_ctx* c) {
         SEMO_CHECK_LAUNCH();
     }
     if (nb > 0) {
-        StageScope sc(c, ST_MFACE);
+        StageScope sc(c, ST_MBFACE);
         k_mbface<<<blocks(nb, T), T, 0, s>>>(nb, ni, nf, nc, c->own, c->bpatch, c->bc_type, c->fn, c->fa, c->mpn,
                                               c->alf, c->epn, c->P, c->U, c->V, c->W, c->mu, c->grad, c->bface,
                                               c->phys.dt, c->msc);

@@ -39,12 +39,12 @@ extern long long g_kernel_launches;
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
              ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_MSTACS, ST_VFACE, ST_VSOLVE, ST_VUPDATE,
-             ST_STENCIL_UVW, ST_COUNT };
+             ST_STENCIL_UVW, ST_MBFACE, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
                                                   "setup_level", "setup_coarse", "mface", "mcell", "msolve",
-                                                  "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw"};
+                                                  "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw", "mbface"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
