@@ -350,14 +350,22 @@ def run_gpu_arm(args, rank, world, local) -> None:
     algo = fbytes(minfo)
     achieved = algo / (per_launch_ms * 1e-3) / 1e9
     traffic = None
+    fp64_pipe = None
     if os.path.exists(TRAFFIC):
         with open(TRAFFIC) as f:
             tr = json.load(f)
-        if kname in tr:
-            traffic = tr[kname]["dram_bytes_per_cell"] * nc
+        t = tr.get(kname)
+        if t and "dram_bytes_per_cell" in t:
+            traffic = t["dram_bytes_per_cell"] * nc
+        elif t and "dram_bytes_per_launch" in t:
+            # hex meshes keep faces/cells fixed, so traffic scales with the faces processed
+            traffic = round(t["dram_bytes_per_launch"] * minfo["faces"] / t["faces"])
+        if t and "fp64_pipe_pct" in t:
+            fp64_pipe = t["fp64_pipe_pct"] / 100.0
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "algorithmic_bytes": algo,
-                "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src}
+                "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src,
+                "fp64_pipe_frac_ncu": fp64_pipe}
 
     cells_all = nc * world
     value = cells_all / (ms_mixed * 1e-3) / 1e6

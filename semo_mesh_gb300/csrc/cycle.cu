@@ -105,6 +105,37 @@ struct SellView {
     }
 };
 
+// SELL-32 with the column stored as a 16-bit offset from the row: an
+// RCM-ordered mesh matrix has a small bandwidth (|col - row| ~ 12k at 2.1M
+// cells), so 6 bytes an FP32 entry move instead of 8.  Padding entries point
+// at the row itself with value 0.
+template <class V>
+struct Sell16View {
+    static constexpr int kVS = 1;
+    const int* __restrict__ sptr;
+    const short* __restrict__ dcol;
+    const V* __restrict__ val;
+    int n;
+    template <class F>
+    __device__ __forceinline__ V dot(int row, int, const F& x) const {
+        V s = V(0);
+        if (row < n) {
+            const int sl = row >> 5, l = row & 31;
+            const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+            int k = b + l;
+            int j = 0;
+            for (; j + 1 < w; j += 2, k += 64) {
+                const int c0 = row + dcol[k], c1 = row + dcol[k + 32];
+                const V v0 = val[k], v1 = val[k + 32];
+                s += v0 * x(c0);
+                s += v1 * x(c1);
+            }
+            if (j < w) s += val[k] * x(row + dcol[k]);
+        }
+        return s;
+    }
+};
+
 template <class V, class X>
 struct Vec {
     const X* __restrict__ p;
@@ -266,8 +297,8 @@ __global__ void k_fin_beta(const double* __restrict__ part, double* __restrict__
     }
 }
 // w = A z;  q = w + beta q;  p = z + beta p;  part = p.q   (FP64 SELL operator)
-template <class Z>
-__global__ void __launch_bounds__(kRedThreads) k_outer_mv(SellView<double> A, const Z* __restrict__ z,
+template <class M, class Z>
+__global__ void __launch_bounds__(kRedThreads) k_outer_mv(M A, const Z* __restrict__ z,
                                                           double* __restrict__ p, double* __restrict__ q,
                                                           const double* __restrict__ scal,
                                                           double* __restrict__ part) {
@@ -428,6 +459,76 @@ void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, in
     SEMO_CHECK_LAUNCH();
 }
 
+template <class V, class W>
+__global__ void k_sell16_fill(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                              const V* __restrict__ val, const int* __restrict__ sptr, short* __restrict__ dcol,
+                              W* __restrict__ sval, int* __restrict__ too_far) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= ((n + 31) & ~31)) return;
+    const int sl = row >> 5, l = row & 31;
+    const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+    const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
+    bool far = false;
+    for (int j = 0; j < w; ++j) {
+        const int k = b + 32 * j + l;
+        if (j < len) {
+            const int d = col[rb + j] - row;
+            far |= (d < -32768 || d > 32767);
+            dcol[k] = (short)d;
+            sval[k] = (W)val[rb + j];
+        } else {
+            dcol[k] = 0;   // the row itself (exists for rows < n; rows past n are never read)
+            sval[k] = W(0);
+        }
+    }
+    if (far) atomicExch(too_far, 1);
+}
+
+template <class V>
+struct Sell16 {
+    int n = 0, nslices = 0;
+    DBuf<int> sptr;
+    DBuf<short> dcol;
+    DBuf<V> val;
+    Sell16View<V> view() const { return Sell16View<V>{sptr.p, dcol.p, val.p, n}; }
+};
+
+// SELL-32 with 16-bit column offsets of a square CSR operator; false (and
+// nothing kept) if some column is 32768 or more away from its row
+template <class V, class W>
+bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int* flag) {
+    S.n = n;
+    S.nslices = (n + 31) / 32;
+    S.sptr.alloc(S.nslices + 1, s);
+    SEMO_CUDA(cudaMemsetAsync(S.sptr.p + S.nslices, 0, sizeof(int), s));
+    const int rows_pad = S.nslices * 32;
+    k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
+    SEMO_CHECK_LAUNCH();
+    const int total = device_scan(s, S.sptr.p, S.nslices + 1);
+    S.dcol.alloc(std::max(total, 1), s);
+    S.val.alloc(std::max(total, 1), s);
+    SEMO_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    k_sell16_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.dcol.p, S.val.p, flag);
+    SEMO_CHECK_LAUNCH();
+    int far = 1;
+    SEMO_CUDA(cudaMemcpyAsync(&far, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    if (far) { S.sptr.release(); S.dcol.release(); S.val.release(); S.n = 0; }
+    return !far;
+}
+
+// The FP64 outer operator: 16-bit column offsets when they fit, else SELL-32
+struct OuterOp {
+    Sell<double> s32;
+    Sell16<double> s16;
+    bool use16 = false;
+    template <class F>
+    void with(F&& f) const {
+        if (use16) f(s16.view());
+        else f(s32.view());
+    }
+};
+
 struct ChebCoef {
     double inv_theta, c1, c2;
 };
@@ -457,7 +558,8 @@ bool sell_pays(const DCsr<V>& M) {
 template <class V>
 struct LevelMats {
     Sell<V> A, P, R;
-    bool a = false, p = false, r = false;
+    Sell16<V> A16;
+    bool a = false, p = false, r = false, a16 = false;
 };
 template <class V>
 struct Cycle {
@@ -469,6 +571,12 @@ template <class V, class F>
 void with_op(const Sell<V>& S, bool use_sell, const DCsr<V>& M, F&& f) {
     if (use_sell) f(S.view());
     else with_csr(M, f);
+}
+// the level's A: 16-bit-offset SELL, SELL, or CSR
+template <class V, class F>
+void with_A(const LevelMats<V>& M, const DCsr<V>& A, F&& f) {
+    if (M.a16) f(M.A16.view());
+    else with_op(M.A, M.a, A, f);
 }
 
 template <class V>
@@ -518,14 +626,14 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     const int degree = c->prm.cheb_degree;
     const ChebCoef cc = cheb2(L.lam_max);
     if (degree == 2) {
-        with_op(M.A, M.a, L.A, [&](auto A) {
+        with_A(M, L.A, [&](auto A) {
             k_pre2<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
         });
         SEMO_CHECK_LAUNCH();
     } else {
         chebyshev_generic(s, L, degree, true);
     }
-    with_op(M.A, M.a, L.A, [&](auto A) { k_res<<<grid_for(A), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p); });
+    with_A(M, L.A, [&](auto A) { k_res<<<grid_for(A), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p); });
     SEMO_CHECK_LAUNCH();
     AmgLevel<V>& C = h.lev[l + 1];
     with_op(M.R, M.r, L.R, [&](auto R) { k_mv<<<grid_for(R), 256, 0, s>>>(R, L.r.p, C.b.p); });
@@ -534,12 +642,12 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     with_op(M.P, M.p, L.P, [&](auto P) { k_prolong_add<<<grid_for(P), 256, 0, s>>>(P, C.x.p, L.x.p); });
     SEMO_CHECK_LAUNCH();
     if (degree == 2) {
-        with_op(M.A, M.a, L.A, [&](auto A) {
+        with_A(M, L.A, [&](auto A) {
             k_post0<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
         });
         SEMO_CHECK_LAUNCH();
         if (l > 0) {
-            with_op(M.A, M.a, L.A, [&](auto A) {
+            with_A(M, L.A, [&](auto A) {
                 k_post1<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
             });
             SEMO_CHECK_LAUNCH();
@@ -561,7 +669,7 @@ Red red_area(semo_ctx* c) {
 
 // One preconditioned CG iteration.  In: r (FP64) and its copy L0.b in V; out: x, r, L0.b updated.
 template <class V>
-void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, double* x, const Red& R) {
+void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, double* x, const Red& R) {
     cudaStream_t s = c->stream;
     AmgLevel<V>& L = h.lev[0];
     const int n = L.A.n;
@@ -579,7 +687,7 @@ void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& oute
         const ChebCoef cc = cheb2(L.lam_max);
         vcycle_from(c, h, cy, 0);   // everything but the last smoothing step of the finest level
         // z lands in L.x; z.r and z.q folded in
-        with_op(cy.lev[0].A, cy.lev[0].a, L.A, [&](auto A) {
+        with_A(cy.lev[0], L.A, [&](auto A) {
             k_post1_dots<<<kRedBlocks, kRedThreads, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p,
                                                             L.x.p, r, q, R.part);
         });
@@ -591,7 +699,9 @@ void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& oute
     }
     k_fin_beta<<<1, 256, 0, s>>>(R.part, R.scal);
     SEMO_CHECK_LAUNCH();
-    k_outer_mv<V><<<kRedBlocks, kRedThreads, 0, s>>>(outer.view(), L.x.p, p, q, R.scal, R.part);
+    outer.with([&](auto A) {
+        k_outer_mv<<<kRedBlocks, kRedThreads, 0, s>>>(A, L.x.p, p, q, R.scal, R.part);
+    });
     SEMO_CHECK_LAUNCH();
     k_fin_alpha<<<1, 256, 0, s>>>(R.part, R.scal);
     SEMO_CHECK_LAUNCH();
@@ -626,7 +736,7 @@ __global__ void k_cg_check(cudaGraphConditionalHandle h, double* __restrict__ sc
 }
 
 template <class V>
-void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const Sell<double>& outer, const int* ptr, const int* col,
+void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, const int* ptr, const int* col,
          const double* val, int n, const double* b, double* x, bool zero_guess, semo_solve_info* info) {
     cudaStream_t s = c->stream;
     Red R = red_area(c);
@@ -729,7 +839,7 @@ void fill_info(const Amg<V>& h, int64_t nnz, semo_solve_info* info) {
 struct ApplyState {
     Cycle<float> cy32;
     Cycle<double> cy64;
-    Sell<double> outer;
+    OuterOp outer;
     // the matrix values the current hierarchy was built from (pressure path only)
     DBuf<double> src_val;
     int src_n = 0;
@@ -761,6 +871,8 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
         M.a = sell_pays(L.A);
         M.p = sell_pays(L.P);
         M.r = sell_pays(L.R);
+        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, c->flag.p + 11);
+        if (M.a16) M.a = false;
         if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
         if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
         if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R);
@@ -1068,7 +1180,8 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
                 build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
                 prepare_cycle(c, c->amg64, st.cy64);
             }
-            build_sell<double, double>(s, ptr, col, val, n, st.outer);
+            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->flag.p + 11);
+            if (!st.outer.use16) build_sell<double, double>(s, ptr, col, val, n, st.outer.s32);
             st.src_prec = -1;
             if (may_reuse && c->prm.reuse_hierarchy) {
                 st.src_val.alloc(nnz, s);

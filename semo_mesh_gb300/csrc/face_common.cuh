@@ -28,6 +28,16 @@ __device__ __forceinline__ double ounkey(long long k) {
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double clamp01(double x) { return smax(0.0, smin(1.0, x)); }
+// std::max(lo, std::min(hi, x)) with the comparisons on the integer pipes
+// (order-preserving keys); the FP64 pipe is the bottleneck of the face kernels.
+// Differs from the double compares only in the sign of a zero result.
+__device__ __forceinline__ double clamp_k(double x, double lo, double hi) {
+    long long k = okey(x);
+    const long long kh = okey(hi), kl = okey(lo);
+    k = (k < kh) ? k : kh;
+    k = (kl < k) ? k : kl;
+    return ounkey(k);
+}
 
 // Fixed-grid reductions: kRedBlocks partial sums summed by one block, so
 // every sum has the same order run to run.
@@ -100,12 +110,12 @@ __device__ __forceinline__ double face_unf(const FaceArgs& a, const FaceGeo& g, 
     double vr = __ldg(a.V + q) + __ldg(G + 6 * N + q) * g.s0 + __ldg(G + 7 * N + q) * g.s1 + __ldg(G + 8 * N + q) * g.s2;
     double wr = __ldg(a.W + q) + __ldg(G + 9 * N + q) * g.s0 + __ldg(G + 10 * N + q) * g.s1 + __ldg(G + 11 * N + q) * g.s2;
     const double* M = a.mm;
-    ul = smax(__ldg(M + N + o), smin(__ldg(M + o), ul));
-    ur = smax(__ldg(M + N + q), smin(__ldg(M + q), ur));
-    vl = smax(__ldg(M + 3 * N + o), smin(__ldg(M + 2 * N + o), vl));
-    vr = smax(__ldg(M + 3 * N + q), smin(__ldg(M + 2 * N + q), vr));
-    wl = smax(__ldg(M + 5 * N + o), smin(__ldg(M + 4 * N + o), wl));
-    wr = smax(__ldg(M + 5 * N + q), smin(__ldg(M + 4 * N + q), wr));
+    ul = clamp_k(ul, __ldg(M + N + o), __ldg(M + o));
+    ur = clamp_k(ur, __ldg(M + N + q), __ldg(M + q));
+    vl = clamp_k(vl, __ldg(M + 3 * N + o), __ldg(M + 2 * N + o));
+    vr = clamp_k(vr, __ldg(M + 3 * N + q), __ldg(M + 2 * N + q));
+    wl = clamp_k(wl, __ldg(M + 5 * N + o), __ldg(M + 4 * N + o));
+    wr = clamp_k(wr, __ldg(M + 5 * N + q), __ldg(M + 4 * N + q));
     const double UnL = ul * g.n0 + vl * g.n1 + wl * g.n2;
     const double UnR = ur * g.n0 + vr * g.n1 + wr * g.n2;
     double UnF = g.wL * UnL + g.wR * UnR;

@@ -55,7 +55,6 @@ __global__ void __launch_bounds__(256) k_mface(MomArgs m) {
     // harmonic viscosity (eqMomentum.cpp:373) from the cells' reciprocals (plane 1 of mu)
     const double muF = 1.0 / (g.wL * __ldg(m.mu + N + o) + g.wR * __ldg(m.mu + N + q));
     // first-order upwind on UnF (eqMomentum.cpp:613-620)
-    const double wLu = (UnF > 0.0) ? 1.0 : 0.0, wRu = 1.0 - wLu;
     // face pressure, skew-corrected and limited by both cells (eqMomentum.cpp:617-659)
     double PF = g.wL * __ldg(a.P + o) + g.wR * __ldg(a.P + q);
     PF += g.wL * __ldg(G + o) * g.s0;
@@ -64,22 +63,25 @@ __global__ void __launch_bounds__(256) k_mface(MomArgs m) {
     PF += g.wR * __ldg(G + N + q) * g.s1;
     PF += g.wL * __ldg(G + 2 * N + o) * g.s2;
     PF += g.wR * __ldg(G + 2 * N + q) * g.s2;
-    PF = smax(__ldg(M + 9 * N + o), smin(__ldg(M + 8 * N + o), PF));
-    PF = smax(__ldg(M + 9 * N + q), smin(__ldg(M + 8 * N + q), PF));
+    PF = clamp_k(PF, __ldg(M + 9 * N + o), __ldg(M + 8 * N + o));
+    PF = clamp_k(PF, __ldg(M + 9 * N + q), __ldg(M + 8 * N + q));
     const double UL = __ldg(a.U + o), VL = __ldg(a.V + o), WL = __ldg(a.W + o);
     const double UR = __ldg(a.U + q), VR = __ldg(a.V + q), WR = __ldg(a.W + q);
-    const double UF = wLu * UL + wRu * UR, VFh = wLu * VL + wRu * VR, WFh = wLu * WL + wRu * WR;
+    // the upwind weights are 0 or 1: selections, not FP64 arithmetic
+    const bool up = UnF > 0.0;
+    const double UF = up ? UL : UR, VFh = up ? VL : VR, WFh = up ? WL : WR;
     const double area = g.area, mf = UnF * area;
     const double ad = muF * g.kA;   // alpha muF / |PN| * area
+    const double rlm = RhoL * mf, rrm = RhoR * mf;
     // coefficients (eqMomentum.cpp:694-712)
-    const double dO = wLu * RhoL * mf + ad;
-    const double dN = wRu * RhoR * mf - ad;
-    a.val[a.lr[f]] = kept(wRu * RhoL * mf - ad);
-    a.val[a.rl[f]] = kept(-(wLu * RhoR * mf + ad));
+    const double dO = up ? rlm + ad : ad;
+    const double dN = up ? -ad : rrm - ad;
+    a.val[a.lr[f]] = kept(up ? -ad : rlm - ad);
+    a.val[a.rl[f]] = kept(up ? -(rrm + ad) : -ad);
     // convection + pressure, over-relaxed diffusion with its non-orthogonal
     // part on (n - alpha e), and SEMO's extra grad.n term (eqMomentum.cpp:739-779)
     const double t0 = g.n0 - g.ae0, t1 = g.n1 - g.ae1, t2 = g.n2 - g.ae2;
-    const double ma = muF * area;
+    const double ma = muF * area, pa = PF * area;
     double* sc = m.sc;
     sc[f] = dO;
     sc[NF + f] = dN;
@@ -91,14 +93,14 @@ __global__ void __launch_bounds__(256) k_mface(MomArgs m) {
         const double uf = (c == 0) ? UF : (c == 1 ? VFh : WFh);
         const double dl = (c == 0) ? UR - UL : (c == 1 ? VR - VL : WR - WL);
         const double nc = (c == 0) ? g.n0 : (c == 1 ? g.n1 : g.n2);
-        const double pn = PF * nc * area;
+        const double pn = pa * nc;
         // (wL gL + wR gR).t = wL (gL.t) + wR (gR.t): the projections serve both terms
         const double glt = gl0 * t0 + gl1 * t1 + gl2 * t2, grt = gr0 * t0 + gr1 * t1 + gr2 * t2;
         const double diff = ad * dl + ma * (g.wL * glt + g.wR * grt);
         const double dLn = ma * (gl0 * g.n0 + gl1 * g.n1 + gl2 * g.n2);
         const double dRn = ma * (gr0 * g.n0 + gr1 * g.n1 + gr2 * g.n2);
-        sc[(2 + c) * NF + f] = (RhoL * uf * mf + pn) - diff - dLn;
-        sc[(5 + c) * NF + f] = (RhoR * uf * mf + pn) - diff - dRn;
+        sc[(2 + c) * NF + f] = (rlm * uf + pn) - diff - dLn;
+        sc[(5 + c) * NF + f] = (rrm * uf + pn) - diff - dRn;
     }
 }
 
