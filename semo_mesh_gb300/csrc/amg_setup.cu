@@ -193,14 +193,19 @@ __device__ __forceinline__ unsigned long long mis_key(int st, int i) {
     return (s << 62) | ((unsigned long long)hash_u32((uint32_t)i) << 30) | (unsigned long long)i;
 }
 
+// need[i] marks the rows whose m1 an undecided row reads in the next round
+// (the undecided rows and their strong neighbours); every other m1 is left as
+// it is, so late rounds, with few undecided rows, touch little of the graph.
+// The keys read are the same as with a full recomputation.
 template <int VS>
 __global__ void k_mis_max1(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                            const unsigned char* __restrict__ strong, const int* __restrict__ state,
-                           unsigned long long* __restrict__ m1) {
+                           unsigned char* __restrict__ need, unsigned long long* __restrict__ m1) {
     int i, lane;
     row_lane<VS>(i, lane);
+    const bool go = i < n && need[i];
     unsigned long long m = 0;
-    if (i < n) {
+    if (go) {
         if (lane == 0) m = mis_key(state[i], i);
         for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS)
             if (strong[k]) {
@@ -210,31 +215,39 @@ __global__ void k_mis_max1(int n, const int* __restrict__ ptr, const int* __rest
             }
     }
     m = grp_max<VS>(m);
-    if (i < n && lane == 0) m1[i] = m;
+    if (go && lane == 0) { m1[i] = m; need[i] = 0; }
 }
 template <int VS>
 __global__ void k_mis_max2(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                            const unsigned char* __restrict__ strong, const unsigned long long* __restrict__ m1,
-                           int* __restrict__ state, int* __restrict__ undecided) {
+                           int* __restrict__ state, unsigned char* __restrict__ need, int* __restrict__ undecided) {
     int i, lane;
     row_lane<VS>(i, lane);
+    const bool active = i < n && state[i] == 1;
     unsigned long long m = 0;
-    if (i < n) {
+    if (active) {
         if (lane == 0) m = m1[i];
         for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS)
             if (strong[k]) { const unsigned long long t = m1[col[k]]; m = (t > m) ? t : m; }
     }
     m = grp_max<VS>(m);
-    if (i >= n || lane != 0) return;
-    const int st = state[i];
-    if (st != 1) return;
+    if (!active) return;
     // decided from the round's snapshot (m1 was computed before any update)
-    if (m == mis_key(1, i)) state[i] = 2;
-    else if ((m >> 62) == 2ull) state[i] = 0;
-    else atomicAdd(undecided, 1);
+    const bool root = m == mis_key(1, i);
+    const bool covered = !root && (m >> 62) == 2ull;
+    if (lane == 0) {
+        if (root) state[i] = 2;
+        else if (covered) state[i] = 0;
+        else atomicAdd(undecided, 1);
+    }
+    if (root || covered) return;
+    if (lane == 0) need[i] = 1;
+    for (int k = ptr[i] + lane; k < ptr[i + 1]; k += VS)
+        if (strong[k]) need[col[k]] = 1;
 }
 // state update must not be seen by other threads of the same round: k_mis_max2
-// reads only m1 (fixed for the round) and writes only its own state.
+// reads only m1 (fixed for the round) and writes only its own state; the need
+// flags it sets are read by the next round's k_mis_max1.
 
 __global__ void k_root_flags(int n, const int* __restrict__ state, int* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -930,7 +943,7 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         DBuf<int> state, agg, agg2, undec;
         DBuf<unsigned long long> m1;
         strong.alloc(std::max<int64_t>(L.A.nnz, 1), s);
-        state.alloc(nl, s); agg.alloc(nl + 1, s); agg2.alloc(nl, s); undec.alloc(1, s);
+        state.alloc(nl, s); agg.alloc(nl + 1, s); agg2.alloc(nl, s);
         m1.alloc(nl, s);
         const double eps2 = (double)(eps * eps);
         eps *= 0.5f;
@@ -943,23 +956,42 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
                                                                                 eps2, strong, state);
             });
             SEMO_CHECK_LAUNCH();
-            // rounds are launched in pairs between checks: a round after the
-            // last undecided node is gone changes nothing
-            int hu = 1;
-            for (int round = 0; round < 200 && hu; round += 2) {
-                for (int k = 0; k < 2; ++k) {
-                    undec.zero();
+            // Rounds go out in chunks; the undecided count after each chunk is
+            // copied to pinned memory and read by the host while the next chunk
+            // runs.  Rounds after the last undecided row is gone change nothing.
+            constexpr int kChunk = 4, kMaxRounds = 200;
+            DBuf<unsigned char> need;
+            need.alloc(nl, s);
+            SEMO_CUDA(cudaMemsetAsync(need.p, 1, nl, s));
+            undec.alloc(2, s);
+            if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
+            for (auto& e : c->sync_ev)
+                if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            int* const hcnt = c->hpin_int;
+            int hu = 1, ch = 0;
+            for (; ch * kChunk < kMaxRounds && hu; ++ch) {
+                int* const u = undec.p + (ch & 1);
+                for (int k = 0; k < kChunk; ++k) {
+                    SEMO_CUDA(cudaMemsetAsync(u, 0, sizeof(int), s));
                     with_row_lanes(L.A.nnz, nl, [&](auto vs) {
                         constexpr int VS = decltype(vs)::value;
                         const int g = blocks((int64_t)nl * VS, 256);
-                        k_mis_max1<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, m1);
+                        k_mis_max1<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, state, need, m1);
                         SEMO_CHECK_LAUNCH();
-                        k_mis_max2<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, undec);
+                        k_mis_max2<VS><<<g, 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, m1, state, need, u);
                         SEMO_CHECK_LAUNCH();
                     });
                 }
-                SEMO_CUDA(cudaMemcpyAsync(&hu, undec.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-                SEMO_CUDA(cudaStreamSynchronize(s));
+                SEMO_CUDA(cudaMemcpyAsync(hcnt + (ch & 1), u, sizeof(int), cudaMemcpyDeviceToHost, s));
+                SEMO_CUDA(cudaEventRecord(c->sync_ev[ch & 1], s));
+                if (ch > 0) {
+                    SEMO_CUDA(cudaEventSynchronize(c->sync_ev[(ch - 1) & 1]));
+                    hu = hcnt[(ch - 1) & 1];
+                }
+            }
+            if (hu) {   // the last chunk was launched but not yet read
+                SEMO_CUDA(cudaEventSynchronize(c->sync_ev[(ch - 1) & 1]));
+                hu = hcnt[(ch - 1) & 1];
             }
             if (hu) throw Error(SEMO_ERR_CUDA, "MIS(2) aggregation did not terminate");
             k_root_flags<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2);

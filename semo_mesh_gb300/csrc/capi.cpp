@@ -129,7 +129,9 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     semo::resolve_stage_timers(c);
     for (auto e : c->ev_pool) cudaEventDestroy(e);
+    for (auto& e : c->sync_ev) if (e) cudaEventDestroy(e);
     if (c->hpin) cudaFreeHost(c->hpin);
+    if (c->hpin_int) cudaFreeHost(c->hpin_int);
     cudaStream_t s = c->stream;
     delete c;  // DBuf destructors enqueue frees on the (still valid) stream
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }

@@ -198,6 +198,8 @@ struct semo_ctx {
     semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
     semo::DBuf<float> kz32, kr32;
     double* hpin = nullptr;                       // pinned host scalars for convergence checks
+    int* hpin_int = nullptr;                      // pinned host counters read while setup kernels run
+    cudaEvent_t sync_ev[2] = {nullptr, nullptr};  // completion of those counter copies
     std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
