@@ -60,6 +60,14 @@ def lib():
         L.orc_update_vof.restype = C.c_double
         L.orc_update_vof.argtypes = [vp, vp]
         L.orc_num_threads.restype = C.c_int
+        L.orc_set_coupled.argtypes = [vp, vp, vp, vp]
+        L.orc_coupled_terms.argtypes = [C.c_int]
+        L.orc_assemble_coupled.argtypes = [vp]
+        L.orc_coupled_bsr.argtypes = [vp, vp]
+        L.orc_solve_coupled.restype = C.c_int
+        L.orc_solve_coupled.argtypes = [vp, C.c_double, C.c_int, vp, vp]
+        L.orc_update_coupled.restype = C.c_double
+        L.orc_update_coupled.argtypes = [vp, vp, vp]
     return _lib
 
 
@@ -200,6 +208,49 @@ class Oracle:
         norm = self.update(sol["x"])
         sol["norm"] = norm
         return sol
+
+    # ---- compressible coupled 5x5 block system --------------------------------
+    def set_coupled(self, case) -> None:
+        """Fields, history, physics and boundary conditions of a CoupledCase."""
+        prm = np.array([case.cv, case.gamma, case.mu, case.dt, case.dt_old, case.dt_old2,
+                        case.gravity[0], case.gravity[1], case.gravity[2], case.urf], dtype=np.float64)
+        bt = np.ascontiguousarray(case.bc_type, dtype=np.int32)
+        bv = np.ascontiguousarray(case.bc_value, dtype=np.float64)
+        lib().orc_set_coupled(self.h, _p(prm), _p(bt), _p(bv))
+        for nm in ("P", "U", "V", "W", "T"):
+            self.set("cpl_" + nm, getattr(case, nm))
+        o, o2 = case.history()
+        self.set("cpl_old", o)
+        self.set("cpl_old2", o2)
+
+    def assemble_coupled(self, terms: int = 7) -> None:
+        """cpl_diag (25 per cell), cpl_LR / cpl_RL (25 per internal face), cpl_B (field-split).
+
+        ``terms`` picks the parts added: 1 cell terms, 2 internal faces, 4
+        boundary faces (tests take the system apart with it)."""
+        lib().orc_coupled_terms(int(terms))
+        try:
+            lib().orc_assemble_coupled(self.h)
+        finally:
+            lib().orc_coupled_terms(7)
+
+    def coupled_bsr(self):
+        """(ptr, col, val[nnz, 5, 5]) on the scalar pattern, caller cell order."""
+        ptr = self.get("CRS_ptr"); col = self.get("CRS_col")
+        val = np.empty(25 * int(ptr[-1]))
+        lib().orc_coupled_bsr(self.h, _p(val))
+        return ptr, col, val.reshape(-1, 5, 5)
+
+    def solve_coupled(self, tol: float = 1e-12, maxiter: int = 5000) -> dict:
+        x = np.empty(5 * self.mesh.n_cells)
+        rr = np.zeros(1)
+        it = int(lib().orc_solve_coupled(self.h, tol, maxiter, _p(x), _p(rr)))
+        return {"x": x, "iters": it, "rel_res": float(rr[0])}
+
+    def update_coupled(self, x, limits) -> float:
+        xa = np.ascontiguousarray(x, dtype=np.float64)
+        la = np.ascontiguousarray(limits, dtype=np.float64)
+        return float(lib().orc_update_coupled(self.h, _p(xa), _p(la)))
 
     @staticmethod
     def threads() -> int:

@@ -1779,3 +1779,496 @@ double orc_update_vof(orc_ctx* c, const double* x) {
     }
     return sqrt(nd);
 }
+
+/* ======================================================================== */
+/* Compressible coupled 5x5 block system.                                    */
+/*                                                                           */
+/* The reference's calcCompCoupledEq (src/solvers/compressible/coupled.cpp:  */
+/* 8-2711) has its whole body commented out; called by CompCoupled           */
+/* (src/solvers/compCoupled.cpp:188) it assembles and solves nothing.  This  */
+/* restates the state the body was in when it was last live -- the lines    */
+/* under exactly one comment level -- for one species (B_n = 5 unknowns per  */
+/* cell: p, u, v, w, T; the mass-fraction row and column of the 6x6 form are */
+/* dropped):                                                                 */
+/*   cell EOS        eos.cpp:310-437 (calcCellEOSMF, nSp = 1) over           */
+/*                   eos.cpp:805-844 (eosIdeal)                              */
+/*   face values     zero-order: L = owner, R = neighbour or the boundary    */
+/*                   value (reconComp.cpp:1087-1131), face EOS from them     */
+/*   gradients       LSQ cellVertex of P, U, V, W (the live calcLeastSquare; */
+/*                   the dead body calls the retired calcLeastSquare2nd)     */
+/*   cell terms      coupled.cpp:318-625 (diagonal time block, bounded BDF2  */
+/*                   right-hand side, gravity)                               */
+/*   internal faces  coupled.cpp:631-1936 (AUSM-type face velocity with     */
+/*                   Rhie-Chow, upwinded transport, Jacobian blocks, viscous */
+/*                   fluxes); the high-order face values equal the zero-     */
+/*                   order ones                                              */
+/*   boundary faces  coupled.cpp:1945-2368                                   */
+/*   update, norm    coupled.cpp:2494-2708                                   */
+/* Unpinned: there is no live reference to compare with.  The diagonal time */
+/* block is the exact derivative of the first-order part of the right-hand   */
+/* side, which the tests check by finite differences; the face blocks are    */
+/* the reference's approximate (frozen-coefficient) Jacobian.                */
+/*                                                                           */
+/* Storage: diagonal blocks cpl_diag[25 i + 5 a + b] (row equation a, column */
+/* variable b), off-diagonal blocks per internal face cpl_LR (owner row,     */
+/* neighbour column) and cpl_RL (neighbour row, owner column), right-hand    */
+/* side field-split cpl_B[a nc + i] as the reference orders it.              */
+/* ======================================================================== */
+typedef struct { double cv, gam, mu, dt, dto, dto2, g[3], urf; int terms; } cpl_prm_t;
+static cpl_prm_t g_cpl = {0, 0, 0, 0, 0, 0, {0, 0, 0}, 0, 7};
+
+/* which parts orc_assemble_coupled adds (tests take them apart):
+   1 = cell terms, 2 = internal faces, 4 = boundary faces */
+void orc_coupled_terms(int mask) { g_cpl.terms = mask; }
+
+void orc_set_coupled(orc_ctx* c, const double* prm, const int* bct, const double* bcv) {
+    g_cpl.cv = prm[0]; g_cpl.gam = prm[1]; g_cpl.mu = prm[2];
+    g_cpl.dt = prm[3]; g_cpl.dto = prm[4]; g_cpl.dto2 = prm[5];
+    g_cpl.g[0] = prm[6]; g_cpl.g[1] = prm[7]; g_cpl.g[2] = prm[8]; g_cpl.urf = prm[9];
+    int* t = ireg(c, "cpl_bct", 3LL * c->npatch); memcpy(t, bct, sizeof(int) * 3 * c->npatch);
+    double* v = dreg(c, "cpl_bcv", 5LL * c->npatch); memcpy(v, bcv, sizeof(double) * 5 * c->npatch);
+}
+
+/* AUSM split Mach number and pressure polynomials: src/solvers/flux.cpp:924-949 */
+static double m_func(double M, double op, double alp) {
+    if (fabs(M) > 1.0) return 0.5 * (M + op * fabs(M));
+    return op * 0.25 * ((M + op) * (M + op)) + op * alp * ((M * M - 1.0) * (M * M - 1.0));
+}
+static double pre_func(double M, double op, double alp) {
+    if (fabs(M) > 1.0) return 0.5 * (1.0 + op * (M > 0.0 ? 1.0 : -1.0));
+    return 0.25 * ((M + op) * (M + op)) * (2.0 - op * M) + op * alp * M * ((M * M - 1.0) * (M * M - 1.0));
+}
+
+/* eosIdeal (eos.cpp:805-844) folded through calcCellEOSMF with one species
+   (eos.cpp:310-437): out = rho, C, Ht, drho/dp, drho/dT, dHt/dp, dHt/dT */
+static void eos_ideal1(double cv, double gam, double P, double U, double V, double W, double T, double* o) {
+    double usqrt = U * U + V * V + W * W;
+    double ri = 1.0 / ((gam - 1.0) * cv * T / (P));
+    double dri_p = ri * ri * (1.0 / ri) / (P);
+    double dri_t = -ri * ri * (1.0 / ri) / T;
+    double dhi_p = 0.0, dhi_t = gam * cv;
+    double hti = gam * cv * T + 0.5 * usqrt;
+    double mf = smax(0.0, smin(1.0, 1.0 - 0.0));
+    double rho = 0.0; rho += mf / ri; rho = 1.0 / rho;
+    double ht = 0.0, drdp = 0.0, drdt = 0.0, dhdp = 0.0, dhdt = 0.0;
+    ht += mf * hti;
+    drdp += rho * rho * (mf / ri / ri * dri_p);
+    drdt += rho * rho * (mf / ri / ri * dri_t);
+    dhdp += mf * dhi_p;
+    dhdt += mf * dhi_t;
+    double cc = drdp + 1.0 / rho * drdt / dhdt * (1.0 - rho * dhdp);
+    o[0] = rho; o[1] = sqrt(1.0 / cc); o[2] = ht; o[3] = drdp; o[4] = drdt; o[5] = dhdp; o[6] = dhdt;
+}
+
+/* boundary right-state primitives (P, U, V, W, T) of boundary face f */
+static void cpl_bvalue(orc_ctx* c, int f, const double* cellv, double* r) {
+    int p = patch_of(c, f);
+    const int* t = iget(c, "cpl_bct") + 3 * p; const double* bv = dget(c, "cpl_bcv") + 5 * p;
+    const double* n = dget(c, "face_n") + 3 * f;
+    r[0] = (t[0] == 1) ? bv[0] : cellv[0];
+    if (t[1] == 1) { r[1] = bv[1]; r[2] = bv[2]; r[3] = bv[3]; }
+    else if (t[1] == 2) { r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; }
+    else if (t[1] == 3) {
+        double un = cellv[1] * n[0] + cellv[2] * n[1] + cellv[3] * n[2];
+        r[1] = cellv[1] - un * n[0]; r[2] = cellv[2] - un * n[1]; r[3] = cellv[3] - un * n[2];
+    } else { r[1] = cellv[1]; r[2] = cellv[2]; r[3] = cellv[3]; }
+    r[4] = (t[2] == 1) ? bv[4] : cellv[4];
+}
+
+void orc_assemble_coupled(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    const cpl_prm_t* q = &g_cpl;
+    double *P = dget(c, "cpl_P"), *U = dget(c, "cpl_U"), *V = dget(c, "cpl_V"), *W = dget(c, "cpl_W"), *T = dget(c, "cpl_T");
+    double *old = dget(c, "cpl_old"), *old2 = dget(c, "cpl_old2");   /* 5 nc each: P, U, V, W, T planes */
+    double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
+    double *mpn = dget(c, "face_magPN"), *alf = dget(c, "face_alphaF"), *epn = dget(c, "face_ePN");
+    double *skw = dget(c, "face_skew"), *vol = dget(c, "cell_vol");
+    /* cell EOS */
+    double* eos = dreg(c, "cpl_eos", 7LL * nc);
+    for (int i = 0; i < nc; ++i) eos_ideal1(q->cv, q->gam, P[i], U[i], V[i], W[i], T[i], eos + 7 * i);
+    /* boundary right states + their EOS */
+    int nb = nf - ni;
+    double* bR = dreg(c, "cpl_bR", 5LL * (nb > 0 ? nb : 1));
+    double* bE = dreg(c, "cpl_bE", 7LL * (nb > 0 ? nb : 1));
+    for (int f = ni; f < nf; ++f) {
+        int o = c->own[f];
+        double cv5[5] = {P[o], U[o], V[o], W[o], T[o]};
+        double* r = bR + 5 * (f - ni);
+        cpl_bvalue(c, f, cv5, r);
+        eos_ideal1(q->cv, q->gam, r[0], r[1], r[2], r[3], r[4], bE + 7 * (f - ni));
+    }
+    /* gradients of P, U, V, W (boundary phi_f = right state) */
+    double* phR = (double*)calloc((size_t)nf, sizeof(double));
+    double* gr[4]; const char* gn[4] = {"cpl_grad_P", "cpl_grad_U", "cpl_grad_V", "cpl_grad_W"};
+    double* fld[4] = {P, U, V, W};
+    for (int k = 0; k < 4; ++k) {
+        for (int f = ni; f < nf; ++f) phR[f] = bR[5 * (f - ni) + k];
+        gr[k] = dreg(c, gn[k], 3LL * nc);
+        lsq_grad(c, fld[k], phR, gr[k]);
+    }
+    free(phR);
+    double* D = dreg(c, "cpl_diag", 25LL * nc);
+    double* LR = dreg(c, "cpl_LR", 25LL * (ni > 0 ? ni : 1));
+    double* RL = dreg(c, "cpl_RL", 25LL * (ni > 0 ? ni : 1));
+    double* B = dreg(c, "cpl_B", 5LL * nc);
+    const double dt = q->dt; const double* g = q->g;
+    /* ---- cell terms: coupled.cpp:318-625 ---- */
+    for (int i = 0; i < nc && (g_cpl.terms & 1); ++i) {
+        const double* e = eos + 7 * i;
+        double Rho = e[0], Ht = e[2], dRhoDP = e[3], dRhoDT = e[4], dHtDP = e[5], dHtDT = e[6];
+        double eo[7], eo2[7];
+        eos_ideal1(q->cv, q->gam, old[i], old[nc + i], old[2 * nc + i], old[3 * nc + i], old[4 * nc + i], eo);
+        eos_ideal1(q->cv, q->gam, old2[i], old2[nc + i], old2[2 * nc + i], old2[3 * nc + i], old2[4 * nc + i], eo2);
+        double volume = vol[i], cTime = 1.0;
+        double u = U[i], v = V[i], w = W[i];
+        double* d = D + 25 * i;
+        d[0 * 5 + 0] = cTime * (dRhoDP) * volume / dt;
+        d[0 * 5 + 4] = cTime * (dRhoDT) * volume / dt;
+        double vel[3] = {u, v, w};
+        for (int m = 1; m <= 3; ++m) {
+            d[m * 5 + 0] = cTime * (dRhoDP * vel[m - 1]) * volume / dt;
+            d[m * 5 + 0] -= dRhoDP * g[m - 1] * volume;
+            d[m * 5 + m] = cTime * (Rho) * volume / dt;
+            d[m * 5 + 4] = cTime * (dRhoDT * vel[m - 1]) * volume / dt;
+            d[m * 5 + 4] -= dRhoDT * g[m - 1] * volume;
+        }
+        d[4 * 5 + 0] = cTime * (dRhoDP * Ht + dHtDP * Rho - 1.0) * volume / dt;
+        d[4 * 5 + 0] -= dRhoDP * (g[0] * u + g[1] * v + g[2] * w) * volume;
+        for (int k = 0; k < 3; ++k) {
+            d[4 * 5 + 1 + k] = cTime * (Rho * vel[k]) * volume / dt;
+            d[4 * 5 + 1 + k] -= Rho * (g[k]) * volume;
+        }
+        d[4 * 5 + 4] = cTime * (dRhoDT * Ht + dHtDT * Rho) * volume / dt;
+        d[4 * 5 + 4] -= dRhoDT * (g[0] * u + g[1] * v + g[2] * w) * volume;
+        double cn[5], c1[5], c2[5];
+        cn[0] = Rho; c1[0] = eo[0]; c2[0] = eo2[0];
+        cn[1] = Rho * u; c1[1] = eo[0] * old[nc + i]; c2[1] = eo2[0] * old2[nc + i];
+        cn[2] = Rho * v; c1[2] = eo[0] * old[2 * nc + i]; c2[2] = eo2[0] * old2[2 * nc + i];
+        cn[3] = Rho * w; c1[3] = eo[0] * old[3 * nc + i]; c2[3] = eo2[0] * old2[3 * nc + i];
+        cn[4] = Rho * Ht - P[i]; c1[4] = eo[0] * eo[2] - old[i]; c2[4] = eo2[0] * eo2[2] - old2[i];
+        double beta = 1.0;
+        for (int a = 0; a < 5; ++a) {
+            double sou = (c1[a] - c2[a]) / (cn[a] - c2[a] + 1.e-200);
+            if (0.0 < sou && sou < 1.0) beta = smin(beta, 0.0); else beta = smin(beta, 1.0);
+        }
+        for (int a = 0; a < 5; ++a) {
+            double co1 = q->dto / (dt + q->dto);
+            double co2 = q->dto2 / (q->dto + q->dto2);
+            double np12 = cn[a] + beta * co1 * (cn[a] - c1[a]);
+            double nm12 = c1[a] + beta * co2 * (c1[a] - c2[a]);
+            B[(size_t)a * nc + i] = -(np12 - nm12) * volume / dt;
+        }
+        B[(size_t)1 * nc + i] += Rho * g[0] * volume;
+        B[(size_t)2 * nc + i] += Rho * g[1] * volume;
+        B[(size_t)3 * nc + i] += Rho * g[2] * volume;
+        B[(size_t)4 * nc + i] += Rho * (g[0] * u + g[1] * v + g[2] * w) * volume;
+    }
+    /* ---- internal faces: coupled.cpp:631-1936 ---- */
+    for (int f = 0; f < ni && (g_cpl.terms & 2); ++f) {
+        int o = c->own[f], r = c->nei[f];
+        const double* n = fn + 3 * f;
+        double area = fa[f], wCL = wc[f], wCR = 1.0 - wCL;
+        const double *eL = eos + 7 * o, *eR = eos + 7 * r;
+        double UL = U[o], VL = V[o], WL = W[o], PL = P[o], RhoL = eL[0], CL = eL[1], HtL = eL[2];
+        double dRhoDPL = eL[3], dRhoDTL = eL[4], dHtDPL = eL[5], dHtDTL = eL[6], muL = q->mu;
+        double UR = U[r], VR = V[r], WR = W[r], PR = P[r], RhoR = eR[0], CR = eR[1], HtR = eR[2];
+        double dRhoDPR = eR[3], dRhoDTR = eR[4], dHtDPR = eR[5], dHtDTR = eR[6], muR = q->mu;
+        double UnL = UL * n[0] + VL * n[1] + WL * n[2];
+        double UnR = UR * n[0] + VR * n[1] + WR * n[2];
+        double UnF = wCL * UnL + wCR * UnR;
+        double muF = wCL * muL + wCR * muR;
+        double Rho_star = 1.0 / (wCL / RhoL + wCR / RhoR);
+        double tmp1 = dt / Rho_star;
+        double dPN = mpn[f], alpha = alf[f];
+        const double *ep = epn + 3 * f, *sk = skw + 3 * f;
+        const double *gPL = gr[0] + 3 * o, *gPR = gr[0] + 3 * r;
+        const double *gUL = gr[1] + 3 * o, *gUR = gr[1] + 3 * r;
+        const double *gVL = gr[2] + 3 * o, *gVR = gr[2] + 3 * r;
+        const double *gWL = gr[3] + 3 * o, *gWR = gr[3] + 3 * r;
+        double UnF_RC = 0.0;
+        UnF_RC -= alpha * tmp1 * (PR - PL) / dPN;
+        for (int ii = 0; ii < 3; ++ii) {
+            UnF_RC += alpha * tmp1 * Rho_star * wCL / RhoL * gPL[ii] * ep[ii];
+            UnF_RC += alpha * tmp1 * Rho_star * wCR / RhoR * gPR[ii] * ep[ii];
+        }
+        for (int ii = 0; ii < 3; ++ii) UnF_RC -= alpha * tmp1 * (gPR[ii] - gPL[ii]) * sk[ii] / dPN;
+        double Cbar = 0.5 * (CL + CR);
+        double ML = UnL / Cbar, MR = UnR / Cbar;
+        double MLP = m_func(ML, 1.0, 0.125), MRM = m_func(MR, -1.0, 0.125);
+        double PLP = pre_func(ML, 1.0, 0.1875), PRM = pre_func(MR, -1.0, 0.1875);
+        double KLR = sqrt(0.5 * (UL * UL + VL * VL + WL * WL + UR * UR + VR * VR + WR * WR));
+        double Mdash = smin(1.0, KLR / Cbar);
+        double chi = (1.0 - Mdash) * (1.0 - Mdash);
+        double rhohat = 0.5 * (RhoL + RhoR);
+        UnF = (MLP + MRM) * Cbar + UnF_RC - 0.5 * chi / rhohat / Cbar * (PR - PL);
+        double weightL = (UnF > 0.0) ? 1.0 : 0.0, weightR = 1.0 - weightL;
+        double WUL, WUR;
+        if (fabs(ML) > 1.0) WUL = 0.5 * (1.0 + ((ML > 0.0) ? 1.0 : -1.0));
+        else WUL = 0.5 * (ML + 1.0) + 0.125 * 2.0 * 2.0 * (ML * ML - 1.0);
+        if (fabs(MR) > 1.0) WUR = 0.5 * (1.0 - ((MR > 0.0) ? 1.0 : -1.0));
+        else WUR = -0.5 * (MR - 1.0) - 0.125 * 2.0 * 2.0 * (MR * MR - 1.0);
+        double WPL = 0.5 - 0.5 * Mdash * PLP * PRM * 0.5 / Cbar * (UnR - UnL) + 0.5 * Mdash * (PLP + PRM - 1.0) + 0.5 * (PLP - PRM);
+        double WPR = 0.5 - 0.5 * Mdash * PLP * PRM * 0.5 / Cbar * (UnR - UnL) + 0.5 * Mdash * (PLP + PRM - 1.0) - 0.5 * (PLP - PRM);
+        double diffPDU = 0.0;
+        double diffDP = alpha * tmp1 / dPN + 0.5 * chi / rhohat / Cbar;
+        double UF = weightL * UL + weightR * UR, VF = weightL * VL + weightR * VR, WF = weightL * WL + weightR * WR;
+        double RhoF = weightL * RhoL + weightR * RhoR, HtF = weightL * HtL + weightR * HtR;
+        double PF = WPL * PL + WPR * PR;
+        double dU[3] = {0, 0, 0}, dV[3] = {0, 0, 0}, dW[3] = {0, 0, 0};
+        double dUdn = 0.0, dVdn = 0.0, dWdn = 0.0;
+        for (int ii = 0; ii < 3; ++ii) {
+            dU[ii] += wCL * gUL[ii]; dU[ii] += wCR * gUR[ii];
+            dV[ii] += wCL * gVL[ii]; dV[ii] += wCR * gVR[ii];
+            dW[ii] += wCL * gWL[ii]; dW[ii] += wCR * gWR[ii];
+            double tvec = n[ii] - alpha * ep[ii];
+            dUdn += wCL * gUL[ii] * tvec; dUdn += wCR * gUR[ii] * tvec;
+            dVdn += wCL * gVL[ii] * tvec; dVdn += wCR * gVR[ii] * tvec;
+            dWdn += wCL * gWL[ii] * tvec; dWdn += wCR * gWR[ii] * tvec;
+            dUdn += alpha * (gUR[ii] - gUL[ii]) * sk[ii] / dPN;
+            dVdn += alpha * (gVR[ii] - gVL[ii]) * sk[ii] / dPN;
+            dWdn += alpha * (gWR[ii] - gWL[ii]) * sk[ii] / dPN;
+        }
+        dUdn += alpha * (UR - UL) / dPN; dVdn += alpha * (VR - VL) / dPN; dWdn += alpha * (WR - WL) / dPN;
+        double dv3 = dU[0] + dV[1] + dW[2];
+        double txx = dU[0] - 2.0 / 3.0 * dv3, txy = dV[0], txz = dW[0];
+        double tyx = dU[1], tyy = dV[1] - 2.0 / 3.0 * dv3, tyz = dW[1];
+        double tzx = dU[2], tzy = dV[2], tzz = dW[2] - 2.0 / 3.0 * dv3;
+        double diff_viscous = muF * alpha / dPN;
+        double visc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        visc[1] = muF * (txx * n[0] + txy * n[1] + txz * n[2] + dUdn) * area;
+        visc[2] = muF * (tyx * n[0] + tyy * n[1] + tyz * n[2] + dVdn) * area;
+        visc[3] = muF * (tzx * n[0] + tzy * n[1] + tzz * n[2] + dWdn) * area;
+        visc[4] = muF * (txx * UF + txy * VF + txz * WF + dU[0] * UF + dU[1] * VF + dU[2] * WF) * n[0] * area +
+                  muF * (tyx * UF + tyy * VF + tyz * WF + dV[0] * UF + dV[1] * VF + dV[2] * WF) * n[1] * area +
+                  muF * (tzx * UF + tzy * VF + tzz * WF + dW[0] * UF + dW[1] * VF + dW[2] * WF) * n[2] * area;
+        /* high-order values equal the zero-order ones */
+        double RhoF_HO = weightL * RhoL + weightR * RhoR, HtF_HO = weightL * HtL + weightR * HtR;
+        RhoF = RhoF_HO; HtF = HtF_HO;
+        double cL[25], cR[25];
+        memset(cL, 0, sizeof cL); memset(cR, 0, sizeof cR);
+        cL[0] = (weightL * dRhoDPL * UnF * area + RhoF * diffDP * area);
+        cR[0] = (weightR * dRhoDPR * UnF * area - RhoF * diffDP * area);
+        for (int k = 0; k < 3; ++k) { cL[1 + k] = (RhoF * WUL * n[k] * area); cR[1 + k] = (RhoF * WUR * n[k] * area); }
+        cL[4] = (weightL * dRhoDTL * UnF * area);
+        cR[4] = (weightR * dRhoDTR * UnF * area);
+        double phF[3] = {UF, VF, WF};
+        for (int m = 1; m <= 3; ++m) {
+            int k = m - 1; double ph = phF[k];
+            cL[5 * m + 0] = (weightL * dRhoDPL * UnF * ph * area + WPL * n[k] * area + RhoF * diffDP * ph * area);
+            cR[5 * m + 0] = (weightR * dRhoDPR * UnF * ph * area + WPR * n[k] * area - RhoF * diffDP * ph * area);
+            cL[5 * m + m] = (RhoF * WUL * n[k] * ph * area + RhoF * UnF * weightL * area + diff_viscous * area +
+                             diffPDU * n[k] * n[k] * area);
+            cR[5 * m + m] = (RhoF * WUR * n[k] * ph * area + RhoF * UnF * weightR * area - diff_viscous * area -
+                             diffPDU * n[k] * n[k] * area);
+            cL[5 * m + 4] = (weightL * dRhoDTL * UnF * ph * area);
+            cR[5 * m + 4] = (weightR * dRhoDTR * UnF * ph * area);
+        }
+        double velL[3] = {UL, VL, WL}, velR[3] = {UR, VR, WR};
+        cL[20] = (weightL * dRhoDPL * HtF * UnF * area + RhoF * weightL * dHtDPL * UnF * area + RhoF * diffDP * HtF * area);
+        cR[20] = (weightR * dRhoDPR * HtF * UnF * area + RhoF * weightR * dHtDPR * UnF * area - RhoF * diffDP * HtF * area);
+        for (int k = 0; k < 3; ++k) {
+            cL[21 + k] = (RhoF * WUL * n[k] * HtF * area + RhoF * UnF * weightL * velL[k] * area);
+            cR[21 + k] = (RhoF * WUR * n[k] * HtF * area + RhoF * UnF * weightR * velR[k] * area);
+        }
+        cL[24] = (weightL * dRhoDTL * UnF * HtF * area + RhoF * weightL * dHtDTL * UnF * area);
+        cR[24] = (weightR * dRhoDTR * UnF * HtF * area + RhoF * weightR * dHtDTR * UnF * area);
+        /* the six cross-momentum entries are absent from the reference's last
+           live state: they stay zero and are not accumulated */
+        double* dO = D + 25 * o; double* dN = D + 25 * r;
+        for (int e = 0; e < 25; ++e) {
+            LR[25 * (size_t)f + e] = cR[e]; RL[25 * (size_t)f + e] = -cL[e];
+            if (e == 7 || e == 8 || e == 11 || e == 13 || e == 16 || e == 17) continue;
+            dO[e] += cL[e]; dN[e] -= cR[e];
+        }
+        double conv[5];
+        conv[0] = RhoF_HO * UnF * area;
+        conv[1] = RhoF_HO * UnF * UF * area + PF * n[0] * area;
+        conv[2] = RhoF_HO * UnF * VF * area + PF * n[1] * area;
+        conv[3] = RhoF_HO * UnF * WF * area + PF * n[2] * area;
+        conv[4] = RhoF_HO * UnF * HtF_HO * area;
+        for (int a = 0; a < 5; ++a) B[(size_t)a * nc + o] -= (conv[a] - visc[a]);
+        for (int a = 0; a < 5; ++a) B[(size_t)a * nc + r] += (conv[a] - visc[a]);
+    }
+    /* ---- boundary faces: coupled.cpp:1945-2368 ---- */
+    int* bct = iget(c, "cpl_bct");
+    for (int p = 0; p < c->npatch && (g_cpl.terms & 4); ++p) {
+        const int* t = bct + 3 * p;
+        double cP = (t[0] == 1) ? 0.0 : 1.0, cPd = (t[0] == 1) ? 1.0 : 0.0;
+        double cUVW = (t[1] == 0) ? 1.0 : 0.0, cUVWd = (t[1] == 0) ? 0.0 : 1.0;
+        double cT = (t[2] == 1) ? 0.0 : 1.0;
+        for (int f = c->pstart[p]; f < c->pstart[p] + c->psize[p]; ++f) {
+            int o = c->own[f];
+            const double* n = fn + 3 * f;
+            const double* eL = eos + 7 * o;
+            const double* rv = bR + 5 * (f - ni); const double* eR = bE + 7 * (f - ni);
+            double area = fa[f];
+            double UnL = U[o] * n[0] + V[o] * n[1] + W[o] * n[2];
+            double UnR = rv[1] * n[0] + rv[2] * n[1] + rv[3] * n[2];
+            double UnF = 0.5 * UnL + 0.5 * UnR;
+            double RhoF = 0.5 * eL[0] + 0.5 * eR[0];
+            double UF = 0.5 * U[o] + 0.5 * rv[1], VF = 0.5 * V[o] + 0.5 * rv[2], WF = 0.5 * W[o] + 0.5 * rv[3];
+            double PF = 0.5 * P[o] + 0.5 * rv[0];
+            double dRhoDPF = 0.5 * eL[3] + 0.5 * eR[3], dRhoDTF = 0.5 * eL[4] + 0.5 * eR[4];
+            double dHtDPF = 0.5 * eL[5] + 0.5 * eR[5], dHtDTF = 0.5 * eL[6] + 0.5 * eR[6];
+            double HtF = 0.5 * eL[2] + 0.5 * eR[2];
+            double dPN = 0.5 * mpn[f], alpha = alf[f];
+            double RhoL = eL[0];
+            double tmp1 = 1.0 / RhoL * dt;
+            const double* ep = epn + 3 * f;
+            const double *gP = gr[0] + 3 * o, *gU = gr[1] + 3 * o, *gV = gr[2] + 3 * o, *gW = gr[3] + 3 * o;
+            UnF -= cPd * alpha * tmp1 * (rv[0] - P[o]) / dPN;
+            for (int ii = 0; ii < 3; ++ii) UnF += cPd * alpha * tmp1 * gP[ii] * ep[ii];
+            double muF = 0.5 * q->mu + 0.5 * q->mu;
+            double dU[3] = {0, 0, 0}, dV[3] = {0, 0, 0}, dW[3] = {0, 0, 0};
+            double dUdn = 0.0, dVdn = 0.0, dWdn = 0.0;
+            for (int ii = 0; ii < 3; ++ii) {
+                dU[ii] += gU[ii]; dV[ii] += gV[ii]; dW[ii] += gW[ii];
+                double tvec = n[ii] - alpha * ep[ii];
+                dUdn += gU[ii] * tvec; dVdn += gV[ii] * tvec; dWdn += gW[ii] * tvec;
+            }
+            dUdn += alpha * (rv[1] - U[o]) / dPN; dVdn += alpha * (rv[2] - V[o]) / dPN; dWdn += alpha * (rv[3] - W[o]) / dPN;
+            double dv3 = dU[0] + dV[1] + dW[2];
+            double txx = dU[0] - 2.0 / 3.0 * dv3, txy = dV[0], txz = dW[0];
+            double tyx = dU[1], tyy = dV[1] - 2.0 / 3.0 * dv3, tyz = dW[1];
+            double tzx = dU[2], tzy = dV[2], tzz = dW[2] - 2.0 / 3.0 * dv3;
+            double visc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            visc[1] = muF * (txx * n[0] + txy * n[1] + txz * n[2] + dUdn) * area;
+            visc[2] = muF * (tyx * n[0] + tyy * n[1] + tyz * n[2] + dVdn) * area;
+            visc[3] = muF * (tzx * n[0] + tzy * n[1] + tzz * n[2] + dWdn) * area;
+            visc[4] = muF * (txx * UF + txy * VF + txz * WF + dU[0] * UF + dU[1] * VF + dU[2] * WF) * n[0] * area +
+                      muF * (tyx * UF + tyy * VF + tyz * WF + dV[0] * UF + dV[1] * VF + dV[2] * WF) * n[1] * area +
+                      muF * (tzx * UF + tzy * VF + tzz * WF + dW[0] * UF + dW[1] * VF + dW[2] * WF) * n[2] * area;
+            double* d = D + 25 * o;
+            double phF[3] = {UF, VF, WF};
+            d[0] += cP * (dRhoDPF * UnF * area);
+            d[0] += cPd * (RhoF * tmp1 / dPN * area);
+            for (int k = 0; k < 3; ++k) d[1 + k] += cUVW * (RhoF * n[k] * area);
+            d[4] += cT * (dRhoDTF * UnF * area);
+            for (int m = 1; m <= 3; ++m) {
+                int k = m - 1; double ph = phF[k];
+                d[5 * m + 0] += cP * (dRhoDPF * UnF * ph * area);
+                d[5 * m + 0] += cPd * (RhoF * alpha * tmp1 / dPN * ph * area);
+                d[5 * m + m] += cUVW * (RhoF * n[k] * ph * area + RhoF * UnF * area);
+                d[5 * m + m] += cUVWd * (alpha * muF / dPN * area);
+                d[5 * m + 4] += cT * (dRhoDTF * UnF * ph * area);
+            }
+            d[20] += cP * (dRhoDPF * UnF * HtF * area + RhoF * UnF * dHtDPF * area);
+            d[20] += cPd * (RhoF * alpha * tmp1 / dPN * dHtDPF * area);
+            for (int k = 0; k < 3; ++k) d[21 + k] += cUVW * (RhoF * n[k] * HtF * area + RhoF * UnF * phF[k] * area);
+            d[24] += cT * (dRhoDTF * UnF * HtF * area + RhoF * UnF * dHtDTF * area);
+            double conv[5];
+            conv[0] = RhoF * UnF * area;
+            conv[1] = RhoF * UnF * UF * area + PF * n[0] * area;
+            conv[2] = RhoF * UnF * VF * area + PF * n[1] * area;
+            conv[3] = RhoF * UnF * WF * area + PF * n[2] * area;
+            conv[4] = RhoF * UnF * HtF * area;
+            for (int a = 0; a < 5; ++a) B[(size_t)a * nc + o] -= (conv[a] - visc[a]);
+        }
+    }
+}
+
+/* block CSR on the scalar pattern (row i: diagonal, then the internal faces
+   of i in face order), 25 values per slot, row-major (equation, variable) */
+static void cpl_bsr(orc_ctx* c, double* val) {
+    int* dig = iget(c, "CRS_dig"); int* lr = iget(c, "CRS_LR"); int* rl = iget(c, "CRS_RL");
+    double *D = dget(c, "cpl_diag"), *LR = dget(c, "cpl_LR"), *RL = dget(c, "cpl_RL");
+    for (int i = 0; i < c->nc; ++i) memcpy(val + 25 * (size_t)dig[i], D + 25 * (size_t)i, 25 * sizeof(double));
+    for (int f = 0; f < c->ni; ++f) {
+        memcpy(val + 25 * (size_t)lr[f], LR + 25 * (size_t)f, 25 * sizeof(double));
+        memcpy(val + 25 * (size_t)rl[f], RL + 25 * (size_t)f, 25 * sizeof(double));
+    }
+}
+void orc_coupled_bsr(orc_ctx* c, double* out_val) { cpl_bsr(c, out_val); }
+
+static void inv5(const double* a, double* x) {
+    double m[5][10];
+    for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) { m[i][j] = a[5 * i + j]; m[i][5 + j] = (i == j) ? 1.0 : 0.0; }
+    for (int k = 0; k < 5; ++k) {
+        int p = k; for (int i = k + 1; i < 5; ++i) if (fabs(m[i][k]) > fabs(m[p][k])) p = i;
+        if (p != k) for (int j = 0; j < 10; ++j) { double t = m[k][j]; m[k][j] = m[p][j]; m[p][j] = t; }
+        double piv = 1.0 / m[k][k];
+        for (int j = 0; j < 10; ++j) m[k][j] *= piv;
+        for (int i = 0; i < 5; ++i) if (i != k) { double f = m[i][k]; if (f != 0.0) for (int j = 0; j < 10; ++j) m[i][j] -= f * m[k][j]; }
+    }
+    for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) x[5 * i + j] = m[i][5 + j];
+}
+/* y = A x, x and y field-split (x[b nc + j]) */
+static void bsr_mv(int nc, const int* ptr, const int* col, const double* val, const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nc; ++i) {
+        double s[5] = {0, 0, 0, 0, 0};
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+            int j = col[k]; const double* blk = val + 25 * (size_t)k;
+            for (int a = 0; a < 5; ++a)
+                for (int b = 0; b < 5; ++b) s[a] += blk[5 * a + b] * x[(size_t)b * nc + j];
+        }
+        for (int a = 0; a < 5; ++a) y[(size_t)a * nc + i] = s[a];
+    }
+}
+static void bjac(int nc, const double* dinv, const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nc; ++i) {
+        const double* m = dinv + 25 * (size_t)i;
+        double v[5]; for (int b = 0; b < 5; ++b) v[b] = x[(size_t)b * nc + i];
+        for (int a = 0; a < 5; ++a) { double s = 0.0; for (int b = 0; b < 5; ++b) s += m[5 * a + b] * v[b]; y[(size_t)a * nc + i] = s; }
+    }
+}
+/* right-preconditioned BiCGStab with block-Jacobi (5x5 inverses) in FP64 */
+int orc_solve_coupled(orc_ctx* c, double tol, int maxiter, double* out_x, double* out_relres) {
+    int nc = c->nc; size_t n = 5 * (size_t)nc;
+    int* ptr = iget(c, "CRS_ptr"); int* col = iget(c, "CRS_col"); int* dig = iget(c, "CRS_dig");
+    double* val = (double*)malloc(sizeof(double) * 25 * (size_t)ptr[nc]);
+    cpl_bsr(c, val);
+    double* b = dget(c, "cpl_B");
+    double* dinv = (double*)malloc(sizeof(double) * 25 * (size_t)nc);
+    for (int i = 0; i < nc; ++i) inv5(val + 25 * (size_t)dig[i], dinv + 25 * (size_t)i);
+    double* w = (double*)calloc(7 * n, sizeof(double));
+    double *r = w, *rh = w + n, *p = w + 2 * n, *v = w + 3 * n, *s = w + 4 * n, *t = w + 5 * n, *z = w + 6 * n;
+    double* x = out_x;
+    for (size_t i = 0; i < n; ++i) { x[i] = 0.0; r[i] = b[i]; rh[i] = b[i]; }
+    double bn = sqrt(dot(b, b, (int)n));
+    if (bn == 0.0) { free(w); free(val); free(dinv); if (out_relres) *out_relres = 0.0; return 0; }
+    double rho = 1.0, alpha = 1.0, omega = 1.0, rn = bn;
+    int it = 0;
+    while (it < maxiter && rn > tol * bn) {
+        double rho1 = dot(rh, r, (int)n);
+        double beta = (rho1 / rho) * (alpha / omega);
+        rho = rho1;
+        for (size_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+        bjac(nc, dinv, p, z);
+        bsr_mv(nc, ptr, col, val, z, v);
+        alpha = rho / dot(rh, v, (int)n);
+        for (size_t i = 0; i < n; ++i) { x[i] += alpha * z[i]; s[i] = r[i] - alpha * v[i]; }
+        bjac(nc, dinv, s, z);
+        bsr_mv(nc, ptr, col, val, z, t);
+        double tt = dot(t, t, (int)n);
+        omega = (tt > 0.0) ? dot(t, s, (int)n) / tt : 0.0;
+        for (size_t i = 0; i < n; ++i) { x[i] += omega * z[i]; r[i] = s[i] - omega * t[i]; }
+        rn = sqrt(dot(r, r, (int)n));
+        ++it;
+    }
+    bsr_mv(nc, ptr, col, val, x, t);
+    double tr = 0.0;
+    for (size_t i = 0; i < n; ++i) tr += (b[i] - t[i]) * (b[i] - t[i]);
+    if (out_relres) *out_relres = sqrt(tr) / bn;
+    free(w); free(val); free(dinv);
+    return it;
+}
+
+/* coupled.cpp:2494-2708: primitives += urf x (urf = momVelURF for all five),
+   clamps, norm = sqrt(sum x^2) / sqrt(sum prim^2) / B_n */
+double orc_update_coupled(orc_ctx* c, const double* x, const double* lim) {
+    int nc = c->nc;
+    double* f[5] = {dget(c, "cpl_P"), dget(c, "cpl_U"), dget(c, "cpl_V"), dget(c, "cpl_W"), dget(c, "cpl_T")};
+    double nd = 0.0, np_ = 0.0, urf = g_cpl.urf;
+    for (int i = 0; i < nc; ++i) {
+        for (int a = 0; a < 5; ++a) f[a][i] += urf * x[(size_t)a * nc + i];
+        for (int a = 0; a < 5; ++a) {
+            if (f[a][i] <= lim[2 * a]) f[a][i] = lim[2 * a];
+            if (f[a][i] >= lim[2 * a + 1]) f[a][i] = lim[2 * a + 1];
+        }
+        for (int a = 0; a < 5; ++a) nd += x[(size_t)a * nc + i] * x[(size_t)a * nc + i];
+        for (int a = 0; a < 5; ++a) np_ += f[a][i] * f[a][i];
+    }
+    return sqrt(nd) / sqrt(np_) / 5.0;
+}

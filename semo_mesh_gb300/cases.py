@@ -21,7 +21,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .meshgen import PolyMesh, hex_box
+from .meshgen import PolyMesh, hex_box, tet_box
 
 # boundary-condition codes shared with the C-ABI (include/semo_gb300.h)
 BC_ZERO_GRADIENT = 0
@@ -151,3 +151,89 @@ def with_fields(case: Case, seed: int, p_scale: float = 1.0) -> Case:
     rng = np.random.default_rng(seed)
     case.P = p_scale * rng.uniform(-1.0, 1.0, size=case.mesh.n_cells)
     return case
+
+
+# ---------------------------------------------------------------------------
+# compressible coupled (p, U, T) cases
+# ---------------------------------------------------------------------------
+@dataclass
+class CoupledCase:
+    """Ideal-gas fields for the 5x5 block-coupled system.
+
+    ``bc_type`` per patch holds (type_p, type_u, type_T) with the codes above;
+    ``bc_value`` per patch (p, u, v, w, T).  ``old`` / ``old2`` are the
+    primitives (P, U, V, W, T) at steps n-1 and n-2, shape (5, n_cells).
+    """
+    name: str
+    mesh: PolyMesh
+    P: np.ndarray
+    U: np.ndarray
+    V: np.ndarray
+    W: np.ndarray
+    T: np.ndarray
+    old: np.ndarray
+    old2: np.ndarray
+    bc_type: np.ndarray
+    bc_value: np.ndarray
+    cv: float = 717.5               # R / (gamma - 1) with R = 287
+    gamma: float = 1.4
+    mu: float = 1.8e-5
+    dt: float = 1e-5
+    dt_old: float = 1e-5
+    dt_old2: float = 1e-5
+    gravity: tuple = (0.0, 0.0, 0.0)
+    urf: float = 1.0
+    # update clamps (min, max) for P, U, V, W, T
+    limits: np.ndarray = field(default_factory=lambda: np.array(
+        [1.0, 1e12, -1e6, 1e6, -1e6, 1e6, -1e6, 1e6, 1.0, 1e5], dtype=np.float64))
+
+    def history(self):
+        return (np.ascontiguousarray(self.old, dtype=np.float64).reshape(-1),
+                np.ascontiguousarray(self.old2, dtype=np.float64).reshape(-1))
+
+
+def _face_smooth(mesh: PolyMesh, phi: np.ndarray, passes: int) -> np.ndarray:
+    """``passes`` rounds of face-neighbour averaging: phi_i <- (phi_i + sum_j phi_j) / (1 + n_i)."""
+    o = mesh.owner[:mesh.n_internal].astype(np.int64)
+    q = mesh.neighbour.astype(np.int64)
+    cnt = np.ones(mesh.n_cells)
+    np.add.at(cnt, o, 1.0)
+    np.add.at(cnt, q, 1.0)
+    for _ in range(passes):
+        s = phi.copy()
+        np.add.at(s, o, phi[q])
+        np.add.at(s, q, phi[o])
+        phi = s / cnt
+    return phi
+
+
+def coupled_case(n: int, tets: bool = True, jitter: float = 0.2, mesh_seed: int = 1234,
+                 history_scale: float = 1e-3) -> CoupledCase:
+    """Ideal gas on a jittered box (6 tetrahedra per hex by default).
+
+    p = 1e5 + 1e3 * (N(0,1), seed 2, smoothed by 3 face-neighbour averaging
+    passes), T = 300 + uniform[-5, 5] (seed 4), velocity uniform[-50, 50] per
+    component (seed 3), dt = 1e-5.  Walls all round: p and T zeroGradient,
+    velocity noSlip.  The step n-1 and n-2 primitives are the current ones
+    scaled by 1 +- ``history_scale`` (seeds 5, 6), which exercises the
+    bounded BDF2.
+    """
+    mesh = tet_box(n, jitter=jitter, seed=mesh_seed) if tets else hex_box(n, jitter=jitter, seed=mesh_seed)
+    nc = mesh.n_cells
+    rng = np.random.default_rng(2)
+    P = 1e5 + 1e3 * _face_smooth(mesh, rng.standard_normal(nc), 3)
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-50.0, 50.0, size=(3, nc))
+    rng = np.random.default_rng(4)
+    T = 300.0 + rng.uniform(-5.0, 5.0, size=nc)
+    cur = np.stack([P, u[0], u[1], u[2], T])
+    hist = []
+    for sd in (5, 6):
+        r = np.random.default_rng(sd)
+        hist.append(cur * (1.0 + history_scale * r.uniform(-1.0, 1.0, size=cur.shape)))
+    npatch = len(mesh.patch_names)
+    bt = np.zeros((npatch, 3), dtype=np.int32)
+    bt[:, 1] = BC_NO_SLIP
+    bv = np.zeros((npatch, 5), dtype=np.float64)
+    return CoupledCase(name=("tet" if tets else "hex") + f"{n}c", mesh=mesh, P=P, U=u[0].copy(), V=u[1].copy(),
+                       W=u[2].copy(), T=T, old=hist[0], old2=hist[1], bc_type=bt, bc_value=bv)
