@@ -288,6 +288,62 @@ int64_t semo_kernel_launches(void);
 semo_status semo_residual_norm_static(const int32_t* ptr, const int32_t* col, const double* val, int n,
                                       const double* x, const double* b, double* out3, void* stream);
 
+/* ---------------------------------------------------------------------------
+   Compressible coupled system: one ideal-gas species, five unknowns per cell
+   (p, u, v, w, T), 5x5 blocks on the cell's scalar pattern.  Replaces
+   calcCompCoupledEq (src/solvers/build.h:210-214,
+   src/solvers/compressible/coupled.cpp:8-2711) with the face and EOS
+   helpers it calls (src/solvers/flux.cpp:924-949 M_func/pre_func,
+   src/solvers/eos.cpp:310-437 calcCellEOSMF, :805-844 eosIdeal) and its
+   solveAMGCL("coupled", mesh, B_n, ...) (src/solvers/solveAMGCL.cpp:
+   179-251, 485-520).  The reference's body of calcCompCoupledEq is commented
+   out; the formulas are those of its last live state, with zero-order face
+   values.  Boundary types per patch (p, u, T) use SEMO_BC_* codes.
+   --------------------------------------------------------------------------- */
+typedef struct {
+    double cv, gamma;            /* species cv [J/(kg K)] and gamma; cp = gamma cv */
+    double mu;                   /* dynamic viscosity */
+    double dt, dt_old, dt_old2;  /* controls.timeStep, oldTimeStep, old2TimeStep (bounded BDF2) */
+    double gravity[3];           /* controls.gravityAcceleration */
+    double urf;                  /* update relaxation of p, U, T (controls.momVelURF) */
+    double limits[10];           /* (min, max) clamps of P, U, V, W, T after the update */
+} semo_coupled_physics;
+
+/* Physics and per-patch boundary conditions: bc_type n_patches x 3
+   (p, u, T), bc_value n_patches x 5 (p, u, v, w, T). */
+semo_status semo_set_coupled_physics(semo_ctx* ctx, const semo_coupled_physics* phys, const int32_t* bc_type,
+                                     const double* bc_value);
+
+/* Cell fields in the caller's order; old / old2 are the primitives at steps
+   n-1 and n-2 as 5 planes (P, U, V, W, T) of n_cells, or NULL for "same as
+   the current fields". */
+semo_status semo_set_coupled_fields(semo_ctx* ctx, const double* P, const double* U, const double* V,
+                                    const double* W, const double* T, const double* old, const double* old2);
+
+/* Current primitives (after semo_coupled_pass) in the caller's order. */
+semo_status semo_get_coupled_fields(semo_ctx* ctx, double* P, double* U, double* V, double* W, double* T);
+
+/* Assembly only: 5x5 blocks and the field-split right-hand side on the GPU. */
+semo_status semo_assemble_coupled(semo_ctx* ctx);
+
+/* The assembled system in the caller's order: ptr/col as the scalar pattern
+   (row i: diagonal, then one entry per internal face of i in face order),
+   val 25 per entry, row-major (equation a = p, u, v, w, T; variable b),
+   b field-split: b[a * n_cells + i].  Blocks are kept whole: an entry the
+   reference would drop as |v| < DBL_MIN is stored as it is. */
+semo_status semo_get_coupled_system(semo_ctx* ctx, int32_t* ptr, int32_t* col, double* val, double* b,
+                                    int64_t* nnz);
+
+/* Solve the assembled system to params.tol (FP64 relative residual); x
+   field-split in the caller's order.  Mixed precision: block-Jacobi
+   BiCGStab in FP32 as the inner solve of FP64 defect correction; FP64: the
+   same BiCGStab in FP64. */
+semo_status semo_solve_coupled(semo_ctx* ctx, double* x, semo_solve_info* info);
+
+/* One calcCompCoupledEq: EOS, gradients, assembly, solve, update and the
+   reference's norm sqrt(sum dx^2) / sqrt(sum prim^2) / 5. */
+semo_status semo_coupled_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
+
 /* Mesh counts: out[0..6) = cells, faces, internal faces, boundary faces,
    vertex-stencil entries, matrix nonzeros. */
 semo_status semo_mesh_info(semo_ctx* ctx, int64_t* out6);

@@ -55,6 +55,12 @@ class Physics(C.Structure):
                 ("mu", C.c_double * 2), ("urf_mom", C.c_double), ("urf_vof", C.c_double)]
 
 
+class CoupledPhysics(C.Structure):
+    _fields_ = [("cv", C.c_double), ("gamma", C.c_double), ("mu", C.c_double), ("dt", C.c_double),
+                ("dt_old", C.c_double), ("dt_old2", C.c_double), ("gravity", C.c_double * 3),
+                ("urf", C.c_double), ("limits", C.c_double * 10)]
+
+
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("levels", C.c_int),
                 ("coarse_size", C.c_int), ("operator_complexity", C.c_double),
@@ -115,6 +121,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_assemble_vof.argtypes = [vp]
     L.semo_get_vof_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
     L.semo_solve_vof.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_set_coupled_physics.argtypes = [vp, C.POINTER(CoupledPhysics), i32p, f64p]
+    L.semo_set_coupled_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
+    L.semo_get_coupled_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p]
+    L.semo_assemble_coupled.argtypes = [vp]
+    L.semo_get_coupled_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
+    L.semo_solve_coupled.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_coupled_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     _lib = L
     return L
 
@@ -318,6 +331,67 @@ class Context:
         self._check(self.L.semo_solve_vof(self.h, x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
         return SolveResult(x=x, info=info.as_dict())
 
+    # ---- compressible coupled system (calcCompCoupledEq) --------------------
+    def set_coupled_case(self, case) -> None:
+        """Mesh (if new), physics, boundary conditions and fields of a CoupledCase."""
+        if self.mesh is not case.mesh:
+            self.upload_mesh(case.mesh)
+        ph = CoupledPhysics()
+        ph.cv, ph.gamma, ph.mu = case.cv, case.gamma, case.mu
+        ph.dt, ph.dt_old, ph.dt_old2 = case.dt, case.dt_old, case.dt_old2
+        for k in range(3):
+            ph.gravity[k] = case.gravity[k]
+        ph.urf = case.urf
+        for k in range(10):
+            ph.limits[k] = float(case.limits[k])
+        bt, btp = _i32(case.bc_type)
+        bv, bvp = _f64(case.bc_value)
+        self._check(self.L.semo_set_coupled_physics(self.h, C.byref(ph), btp, bvp))
+        self.set_coupled_fields(case.P, case.U, case.V, case.W, case.T, *case.history())
+
+    def set_coupled_fields(self, P, U, V, W, T, old=None, old2=None) -> None:
+        arrs = [_f64(a) for a in (P, U, V, W, T)]
+        o = _f64(old) if old is not None else (None, None)
+        o2 = _f64(old2) if old2 is not None else (None, None)
+        self._check(self.L.semo_set_coupled_fields(self.h, *[a[1] for a in arrs], o[1], o2[1]))
+
+    def coupled_fields(self) -> dict:
+        n = self.n_cells
+        out = {k: np.empty(n) for k in ("P", "U", "V", "W", "T")}
+        self._check(self.L.semo_get_coupled_fields(self.h, *[_f64(out[k])[1] for k in ("P", "U", "V", "W", "T")]))
+        return out
+
+    def assemble_coupled(self) -> None:
+        self._check(self.L.semo_assemble_coupled(self.h))
+
+    def coupled_system(self) -> dict:
+        """(ptr, col, val[nnz, 5, 5], b[5, n]) in the caller's numbering."""
+        n = self.n_cells
+        nnz = C.c_int64()
+        self._check(self.L.semo_get_coupled_system(self.h, None, None, None, None, C.byref(nnz)))
+        ptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz.value, dtype=np.int32)
+        val = np.empty(25 * nnz.value)
+        b = np.empty(5 * n)
+        self._check(self.L.semo_get_coupled_system(self.h, ptr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                   col.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                   val.ctypes.data_as(C.POINTER(C.c_double)),
+                                                   b.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nnz)))
+        return {"ptr": ptr, "col": col, "val": val.reshape(-1, 5, 5), "b": b.reshape(5, n)}
+
+    def solve_coupled(self) -> SolveResult:
+        x = np.empty(5 * self.n_cells)
+        info = SolveInfo()
+        self._check(self.L.semo_solve_coupled(self.h, x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+        return SolveResult(x=x, info=info.as_dict())
+
+    def calc_comp_coupled_eq(self) -> tuple:
+        """One calcCompCoupledEq: assemble, solve, update p, U, T; (norm, info)."""
+        norm = C.c_double()
+        info = SolveInfo()
+        self._check(self.L.semo_coupled_pass(self.h, C.byref(norm), C.byref(info)))
+        return norm.value, info.as_dict()
+
     def assemble_momentum(self) -> None:
         self._check(self.L.semo_assemble_momentum(self.h))
 
@@ -400,7 +474,7 @@ class Context:
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
               "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate", "mstacs", "vface",
-              "vsolve", "vupdate", "stencil_uvw", "mbface")
+              "vsolve", "vupdate", "stencil_uvw", "mbface", "cgrad", "cface", "ccell", "csolve", "cupdate")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

@@ -25,6 +25,7 @@ UNITS = [
     ("assemble.cu", []),
     ("momentum.cu", []),
     ("vof.cu", []),
+    ("coupled.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
     ("noalloc.cu", []),

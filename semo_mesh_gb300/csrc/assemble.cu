@@ -484,6 +484,14 @@ void stencil_pass(semo_ctx* c, bool full) {
     SEMO_CHECK_LAUNCH();
 }
 
+void lsq_gradients5(semo_ctx* c, const double* f0, const double* f1, const double* f2, const double* f3,
+                    const double* f4, const double* bf, double* grad, double* mm) {
+    k_stencil<true><<<blocks(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->nf, c->ni, c->nb, c->st_ptr, c->st_idx,
+                                                               c->stw, c->st_nnz, c->cf_ptr, c->cf_idx, c->bfw,
+                                                               c->minv, f0, f1, f2, f3, f4, bf, grad, mm);
+    SEMO_CHECK_LAUNCH();
+}
+
 void assemble_gravity_stencil(semo_ctx* c) {
     const bool keep = c->pvf_current;
     if (!keep) assemble_gravity(c);   // else the gravity source is kept

@@ -184,6 +184,7 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         c->amg64.clear();
         c->has_old = c->has_src = c->has_oldvf = false;
         c->pvf_current = c->sg_current = c->vof_assembled = false;
+        c->cpl_phys = c->cpl_fields = c->cpl_assembled = false;
         ++c->mesh_gen;
 
         // ---- cell -> faces, ascending face index (connectCelltoFaces, build.cpp:587-608) ----
@@ -1013,6 +1014,159 @@ semo_status semo_vjp_source(semo_ctx* c, const double* dJ_dx, double* lambda, do
     });
     if (st == SEMO_OK && conv != SEMO_OK) c->err = "adjoint solve did not reach the tolerance";
     return st != SEMO_OK ? st : conv;
+}
+
+// ---------------------------------------------------------------------------
+// compressible coupled system
+// ---------------------------------------------------------------------------
+semo_status semo_set_coupled_physics(semo_ctx* c, const semo_coupled_physics* phys, const int32_t* bc_type,
+                                     const double* bc_value) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(phys && bc_type && bc_value, SEMO_ERR_ARGUMENT, "null coupled physics or boundary arrays");
+        need(phys->cv > 0.0 && phys->gamma > 1.0 && phys->dt > 0.0 && phys->dt_old > 0.0 && phys->dt_old2 > 0.0,
+             SEMO_ERR_ARGUMENT, "coupled physics needs cv > 0, gamma > 1 and positive time steps");
+        for (int p = 0; p < c->npatch; ++p)
+            for (int q = 0; q < 3; ++q) {
+                const int t = bc_type[3 * p + q];
+                const bool ok = (q == 1) ? (t >= SEMO_BC_ZERO_GRADIENT && t <= SEMO_BC_SLIP)
+                                         : (t == SEMO_BC_ZERO_GRADIENT || t == SEMO_BC_FIXED_VALUE);
+                need(ok, SEMO_ERR_ARGUMENT, "bad coupled boundary type");
+            }
+        SEMO_CUDA(cudaSetDevice(c->device));
+        c->cphys = *phys;
+        c->cpl_bct.upload(bc_type, 3 * (size_t)c->npatch, c->stream);
+        c->cpl_bcv.upload(bc_value, 5 * (size_t)c->npatch, c->stream);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->cpl_phys = true;
+        c->cpl_assembled = false;
+    });
+}
+
+semo_status semo_set_coupled_fields(semo_ctx* c, const double* P, const double* U, const double* V, const double* W,
+                                    const double* T, const double* old, const double* old2) {
+    return guarded(c, [&] {
+        need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
+        need(P && U && V && W && T, SEMO_ERR_ARGUMENT, "null coupled field");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        c->cpl_f.alloc(15 * n, s);
+        c->cpl_fields = false;
+        c->cpl_assembled = false;
+        const double* cur[5] = {P, U, V, W, T};
+        for (int set = 0; set < 3; ++set) {
+            const double* h = (set == 0) ? nullptr : (set == 1 ? old : old2);
+            for (int q = 0; q < 5; ++q)
+                SEMO_CUDA(cudaMemcpyAsync(c->stage.p + q * n, h ? h + q * n : cur[q], sizeof(double) * n,
+                                          cudaMemcpyHostToDevice, s));
+            double* dst[5];
+            for (int q = 0; q < 5; ++q) dst[q] = c->cpl_f.p + (5 * set + q) * n;
+            if (!semo::fields_from_caller_order(c, c->stage.p, dst, 5))
+                throw Error(SEMO_ERR_NAN, "non-finite coupled field");
+        }
+        c->cpl_fields = true;
+    });
+}
+
+semo_status semo_get_coupled_fields(semo_ctx* c, double* P, double* U, double* V, double* W, double* T) {
+    return guarded(c, [&] {
+        need(c->cpl_fields, SEMO_ERR_STATE, "no coupled fields set");
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        c->stage.alloc(5 * n, s);
+        const double* src[5];
+        for (int q = 0; q < 5; ++q) src[q] = c->cpl_f.p + q * n;
+        semo::fields_to_caller_order(c, src, c->stage.p, 5);
+        double* dst[5] = {P, U, V, W, T};
+        for (int q = 0; q < 5; ++q)
+            if (dst[q])
+                SEMO_CUDA(cudaMemcpyAsync(dst[q], c->stage.p + q * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+semo_status semo_assemble_coupled(semo_ctx* c) {
+    return guarded(c, [&] {
+        need(c->mesh_ready && c->cpl_phys && c->cpl_fields, SEMO_ERR_STATE,
+             "mesh, coupled physics and coupled fields must be set before assembly");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::coupled_assemble(c);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+semo_status semo_get_coupled_system(semo_ctx* c, int32_t* ptr, int32_t* col, double* val, double* b, int64_t* nnz) {
+    return guarded(c, [&] {
+        need(c->cpl_assembled, SEMO_ERR_STATE, "coupled system not assembled");
+        cudaStream_t s = c->stream;
+        const int n = c->nc;
+        std::vector<int> hp(n + 1), hc(c->nnz);
+        std::vector<double> hv, hb;
+        SEMO_CUDA(cudaMemcpyAsync(hp.data(), c->A_ptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaMemcpyAsync(hc.data(), c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
+        if (val) {
+            hv.resize(25 * (size_t)c->nnz);
+            SEMO_CUDA(cudaMemcpyAsync(hv.data(), c->cpl_val.p, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost, s));
+        }
+        if (b) {
+            hb.resize(5 * (size_t)n);
+            SEMO_CUDA(cudaMemcpyAsync(hb.data(), c->cpl_b.p, sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, s));
+        }
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        int64_t k_out = 0;
+        if (ptr) ptr[0] = 0;
+        for (int i = 0; i < n; ++i) {
+            const int r = c->iperm[i];
+            for (int k = hp[r]; k < hp[r + 1]; ++k, ++k_out) {
+                if (col) col[k_out] = c->perm[hc[k]];
+                if (val) std::copy(hv.begin() + 25 * (size_t)k, hv.begin() + 25 * (size_t)k + 25, val + 25 * k_out);
+            }
+            if (ptr) ptr[i + 1] = (int32_t)k_out;
+        }
+        if (b)
+            for (int a = 0; a < 5; ++a)
+                for (int r = 0; r < n; ++r) b[(size_t)a * n + c->perm[r]] = hb[(size_t)a * n + r];
+        if (nnz) *nnz = k_out;
+    });
+}
+
+semo_status semo_solve_coupled(semo_ctx* c, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->cpl_assembled, SEMO_ERR_STATE, "coupled system not assembled");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        conv = semo::coupled_solve(c, info);
+        if (x) {
+            const size_t n = (size_t)c->nc;
+            cudaStream_t s = c->stream;
+            c->stage.alloc(5 * n, s);
+            const double* src[5];
+            for (int q = 0; q < 5; ++q) src[q] = c->cpl_x.p + q * n;
+            semo::fields_to_caller_order(c, src, c->stage.p, 5);
+            SEMO_CUDA(cudaMemcpyAsync(x, c->stage.p, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost, s));
+            SEMO_CUDA(cudaStreamSynchronize(s));
+        }
+    });
+    return finish(c, st, conv, "coupled solve did not reach the tolerance");
+}
+
+semo_status semo_coupled_pass(semo_ctx* c, double* norm, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->mesh_ready && c->cpl_phys && c->cpl_fields, SEMO_ERR_STATE,
+             "mesh, coupled physics and coupled fields must be set before the coupled pass");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::coupled_assemble(c);
+        conv = semo::coupled_solve(c, info);
+        // the reference updates after any solve; a breakdown leaves the fields as they are
+        if (conv == SEMO_OK || conv == SEMO_ERR_NOT_CONVERGED) {
+            const double nrm = semo::coupled_update(c);
+            if (norm) *norm = nrm;
+        }
+    });
+    return finish(c, st, conv, "coupled solve did not reach the tolerance");
 }
 
 }  // extern "C"

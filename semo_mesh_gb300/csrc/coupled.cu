@@ -1,0 +1,1082 @@
+// Compressible coupled system on the GPU: one ideal-gas species, five
+// unknowns per cell (p, u, v, w, T), 5x5 blocks on the scalar pattern.
+//
+// Replaces calcCompCoupledEq (src/solvers/compressible/coupled.cpp:8-2711).
+// The reference keeps that function's whole body commented out; the
+// formulas here are those of its last live state (the lines under one
+// comment level), with the mass-fraction row and column of its 6x6 form
+// dropped:
+//   k_ceos     calcCellEOSMF (nSp = 1) over eosIdeal   src/solvers/eos.cpp:310-437, :805-844
+//   k_cbstate  zero-order boundary right states      src/solvers/reconComp.cpp:1087-1131
+//   gradients  the LSQ stencil kernel of assemble.cu on P, U, V, W, T
+//   k_cface    internal faces: AUSM-type face velocity with Rhie-Chow, upwinded
+//              transport, Jacobian blocks, viscous fluxes
+//                                                     coupled.cpp:631-1936, src/solvers/flux.cpp:924-949
+//   k_cbface   boundary faces                         coupled.cpp:1945-2368
+//   k_ccell    time block, bounded BDF2, gravity; gathers the face terms
+//                                                     coupled.cpp:318-625
+//   k_cupdate  relaxation, clamps, norm               coupled.cpp:2494-2708
+// The solver (solveAMGCL("coupled"), src/solvers/solveAMGCL.cpp:485-520,
+// is FGMRES over ILU0 there) is BiCGStab preconditioned by the inverses of
+// the 5x5 diagonal blocks; in mixed mode it runs in FP32 on an FP32 copy of
+// the matrix as the inner solve of FP64 defect correction.
+//
+// Layout: cells in RCM order, faces in stored order; blocks are 25 doubles
+// per slot of the scalar CSR pattern (A_ptr/A_col), row-major (equation a,
+// variable b); right-hand side and solution are field-split planes
+// b[a * nc + i] as the reference orders its unknowns.  Every cell gathers
+// its face terms through the cell->face list in ascending face order, so
+// the diagonal blocks accumulate in the reference's order with no atomics.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "face_common.cuh"
+#include "semo_internal.h"
+
+namespace {
+
+using namespace semo::face;
+
+struct CplArgs {
+    int nc, nf, ni, nb;
+    const int *own, *nei, *lr, *rl, *dig, *cfp, *cfi, *bpatch, *bct;
+    const double *fn, *fa, *wc, *mpn, *alf, *epn, *skew, *vol;
+    const double* f;      // 15 planes of nc: P, U, V, W, T; the same at n-1; at n-2
+    const double* eos;    // 7 planes of nc: rho, C, Ht, drho/dp, drho/dT, dHt/dp, dHt/dT
+    const double* grad;   // 15 planes of nc: (P, U, V, W, T) x (x, y, z)
+    const double* bR;     // 12 planes of nb: boundary right primitives (5) and their EOS (7)
+    const double* bcv;    // per patch: p, u, v, w, T boundary values
+    double* val;          // 25 per slot
+    double* b;            // 5 planes of nc
+    double* flux;         // 5 planes of nf: convective minus viscous flux of each face
+    double* bblk;         // 27 planes of nb: boundary-face diagonal contributions
+    double cv, gam, mu, dt, dto, dto2, g0, g1, g2;
+};
+
+// eosIdeal (eos.cpp:805-844) folded through calcCellEOSMF with one species,
+// mass fraction 1 (eos.cpp:310-437)
+__device__ __forceinline__ void eos1(double cv, double gam, double P, double U, double V, double W, double T,
+                                     double* o) {
+    const double usqrt = U * U + V * V + W * W;
+    const double ri = 1.0 / ((gam - 1.0) * cv * T / P);
+    const double dri_p = ri * ri * (1.0 / ri) / P;
+    const double dri_t = -ri * ri * (1.0 / ri) / T;
+    const double dhi_t = gam * cv;
+    const double hti = gam * cv * T + 0.5 * usqrt;
+    const double rho = 1.0 / (1.0 / ri);
+    const double drdp = rho * rho * (1.0 / ri / ri * dri_p);
+    const double drdt = rho * rho * (1.0 / ri / ri * dri_t);
+    const double cc = drdp + 1.0 / rho * drdt / dhi_t;
+    o[0] = rho; o[1] = sqrt(1.0 / cc); o[2] = hti; o[3] = drdp; o[4] = drdt; o[5] = 0.0; o[6] = dhi_t;
+}
+
+__global__ void k_ceos(int nc, double cv, double gam, const double* __restrict__ f, double* __restrict__ eos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double o[7];
+    eos1(cv, gam, f[i], f[nc + i], f[2 * (size_t)nc + i], f[3 * (size_t)nc + i], f[4 * (size_t)nc + i], o);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) eos[q * (size_t)nc + i] = o[q];
+}
+
+// zero-order right state of boundary face b: the patch value, the owner's
+// value, zero (noSlip) or the owner's tangential velocity (slip)
+__global__ void k_cbstate(CplArgs a, double* __restrict__ bR) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.nb) return;
+    const int f = a.ni + b, o = a.own[f], p = a.bpatch[b];
+    const size_t nc = a.nc, nf = a.nf, nb = a.nb;
+    const int tp = a.bct[3 * p], tu = a.bct[3 * p + 1], tt = a.bct[3 * p + 2];
+    const double* bv = a.bcv;
+    const double P = a.f[o], U = a.f[nc + o], V = a.f[2 * nc + o], W = a.f[3 * nc + o], T = a.f[4 * nc + o];
+    const double n0 = a.fn[f], n1 = a.fn[nf + f], n2 = a.fn[2 * nf + f];
+    double r[5];
+    r[0] = (tp == SEMO_BC_FIXED_VALUE) ? bv[5 * p] : P;
+    if (tu == SEMO_BC_FIXED_VALUE) { r[1] = bv[5 * p + 1]; r[2] = bv[5 * p + 2]; r[3] = bv[5 * p + 3]; }
+    else if (tu == SEMO_BC_NO_SLIP) { r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; }
+    else if (tu == SEMO_BC_SLIP) {
+        const double un = U * n0 + V * n1 + W * n2;
+        r[1] = U - un * n0; r[2] = V - un * n1; r[3] = W - un * n2;
+    } else { r[1] = U; r[2] = V; r[3] = W; }
+    r[4] = (tt == SEMO_BC_FIXED_VALUE) ? bv[5 * p + 4] : T;
+    double e[7];
+    eos1(a.cv, a.gam, r[0], r[1], r[2], r[3], r[4], e);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) bR[q * nb + b] = r[q];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) bR[(5 + q) * nb + b] = e[q];
+}
+
+// AUSM split Mach number and pressure polynomials (flux.cpp:924-949)
+__device__ __forceinline__ double m_func(double M, double op, double alp) {
+    if (fabs(M) > 1.0) return 0.5 * (M + op * fabs(M));
+    return op * 0.25 * ((M + op) * (M + op)) + op * alp * ((M * M - 1.0) * (M * M - 1.0));
+}
+__device__ __forceinline__ double pre_func(double M, double op, double alp) {
+    if (fabs(M) > 1.0) return 0.5 * (1.0 + op * (M > 0.0 ? 1.0 : -1.0));
+    return 0.25 * ((M + op) * (M + op)) * (2.0 - op * M) + op * alp * M * ((M * M - 1.0) * (M * M - 1.0));
+}
+
+// Internal face f: the Jacobian blocks of the face flux with respect to the
+// owner's (cL) and the neighbour's (cR) primitives go to the off-diagonal
+// slots as cR (owner row) and -cL (neighbour row); the owner's diagonal
+// gathers +cL and the neighbour's -cR from there.  The six cross-momentum
+// entries are zero in the reference's last live state.
+__global__ void __launch_bounds__(128) k_cface(CplArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.ni) return;
+    const size_t nc = a.nc, nf = a.nf;
+    const int o = a.own[f], r = a.nei[f];
+    const double n0 = a.fn[f], n1 = a.fn[nf + f], n2 = a.fn[2 * nf + f];
+    const double nv[3] = {n0, n1, n2};
+    const double area = a.fa[f], wCL = a.wc[f], wCR = 1.0 - wCL;
+    const double PL = a.f[o], UL = a.f[nc + o], VL = a.f[2 * nc + o], WL = a.f[3 * nc + o];
+    const double PR = a.f[r], UR = a.f[nc + r], VR = a.f[2 * nc + r], WR = a.f[3 * nc + r];
+    const double RhoL = a.eos[o], CL = a.eos[nc + o], HtL = a.eos[2 * nc + o], dRhoDPL = a.eos[3 * nc + o];
+    const double dRhoDTL = a.eos[4 * nc + o], dHtDPL = a.eos[5 * nc + o], dHtDTL = a.eos[6 * nc + o];
+    const double RhoR = a.eos[r], CR = a.eos[nc + r], HtR = a.eos[2 * nc + r], dRhoDPR = a.eos[3 * nc + r];
+    const double dRhoDTR = a.eos[4 * nc + r], dHtDPR = a.eos[5 * nc + r], dHtDTR = a.eos[6 * nc + r];
+    const double UnL = UL * n0 + VL * n1 + WL * n2;
+    const double UnR = UR * n0 + VR * n1 + WR * n2;
+    const double muF = wCL * a.mu + wCR * a.mu;
+    const double Rho_star = 1.0 / (wCL / RhoL + wCR / RhoR);
+    const double tmp1 = a.dt / Rho_star;
+    const double dPN = a.mpn[f], alpha = a.alf[f];
+    const double ep[3] = {a.epn[f], a.epn[nf + f], a.epn[2 * nf + f]};
+    const double sk[3] = {a.skew[f], a.skew[nf + f], a.skew[2 * nf + f]};
+    const double* g = a.grad;
+    double UnF_RC = 0.0;
+    UnF_RC -= alpha * tmp1 * (PR - PL) / dPN;
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) {
+        UnF_RC += alpha * tmp1 * Rho_star * wCL / RhoL * g[ii * nc + o] * ep[ii];
+        UnF_RC += alpha * tmp1 * Rho_star * wCR / RhoR * g[ii * nc + r] * ep[ii];
+    }
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) UnF_RC -= alpha * tmp1 * (g[ii * nc + r] - g[ii * nc + o]) * sk[ii] / dPN;
+    const double Cbar = 0.5 * (CL + CR);
+    const double ML = UnL / Cbar, MR = UnR / Cbar;
+    const double MLP = m_func(ML, 1.0, 0.125), MRM = m_func(MR, -1.0, 0.125);
+    const double PLP = pre_func(ML, 1.0, 0.1875), PRM = pre_func(MR, -1.0, 0.1875);
+    const double KLR = sqrt(0.5 * (UL * UL + VL * VL + WL * WL + UR * UR + VR * VR + WR * WR));
+    const double Mdash = smin(1.0, KLR / Cbar);
+    const double chi = (1.0 - Mdash) * (1.0 - Mdash);
+    const double rhohat = 0.5 * (RhoL + RhoR);
+    const double UnF = (MLP + MRM) * Cbar + UnF_RC - 0.5 * chi / rhohat / Cbar * (PR - PL);
+    const bool up = UnF > 0.0;
+    const double weightL = up ? 1.0 : 0.0, weightR = 1.0 - weightL;
+    const double WUL = (fabs(ML) > 1.0) ? 0.5 * (1.0 + ((ML > 0.0) ? 1.0 : -1.0))
+                                        : 0.5 * (ML + 1.0) + 0.125 * 2.0 * 2.0 * (ML * ML - 1.0);
+    const double WUR = (fabs(MR) > 1.0) ? 0.5 * (1.0 - ((MR > 0.0) ? 1.0 : -1.0))
+                                        : -0.5 * (MR - 1.0) - 0.125 * 2.0 * 2.0 * (MR * MR - 1.0);
+    const double wp0 = 0.5 - 0.5 * Mdash * PLP * PRM * 0.5 / Cbar * (UnR - UnL) + 0.5 * Mdash * (PLP + PRM - 1.0);
+    const double WPL = wp0 + 0.5 * (PLP - PRM);
+    const double WPR = wp0 - 0.5 * (PLP - PRM);
+    const double diffDP = alpha * tmp1 / dPN + 0.5 * chi / rhohat / Cbar;
+    const double UF = up ? UL : UR, VF = up ? VL : VR, WF = up ? WL : WR;
+    const double RhoF = up ? RhoL : RhoR, HtF = up ? HtL : HtR;
+    const double PF = WPL * PL + WPR * PR;
+    // viscous terms: face-average gradients, non-orthogonal and skewness parts
+    double dU[3], dV[3], dW[3], dUdn = 0.0, dVdn = 0.0, dWdn = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) {
+        const double gUL = g[(3 + ii) * nc + o], gUR = g[(3 + ii) * nc + r];
+        const double gVL = g[(6 + ii) * nc + o], gVR = g[(6 + ii) * nc + r];
+        const double gWL = g[(9 + ii) * nc + o], gWR = g[(9 + ii) * nc + r];
+        dU[ii] = wCL * gUL + wCR * gUR;
+        dV[ii] = wCL * gVL + wCR * gVR;
+        dW[ii] = wCL * gWL + wCR * gWR;
+        const double tvec = nv[ii] - alpha * ep[ii];
+        dUdn += wCL * gUL * tvec; dUdn += wCR * gUR * tvec;
+        dVdn += wCL * gVL * tvec; dVdn += wCR * gVR * tvec;
+        dWdn += wCL * gWL * tvec; dWdn += wCR * gWR * tvec;
+        dUdn += alpha * (gUR - gUL) * sk[ii] / dPN;
+        dVdn += alpha * (gVR - gVL) * sk[ii] / dPN;
+        dWdn += alpha * (gWR - gWL) * sk[ii] / dPN;
+    }
+    dUdn += alpha * (UR - UL) / dPN; dVdn += alpha * (VR - VL) / dPN; dWdn += alpha * (WR - WL) / dPN;
+    const double dv3 = dU[0] + dV[1] + dW[2];
+    const double txx = dU[0] - 2.0 / 3.0 * dv3, txy = dV[0], txz = dW[0];
+    const double tyx = dU[1], tyy = dV[1] - 2.0 / 3.0 * dv3, tyz = dW[1];
+    const double tzx = dU[2], tzy = dV[2], tzz = dW[2] - 2.0 / 3.0 * dv3;
+    const double diff_viscous = muF * alpha / dPN;
+    const double visc1 = muF * (txx * n0 + txy * n1 + txz * n2 + dUdn) * area;
+    const double visc2 = muF * (tyx * n0 + tyy * n1 + tyz * n2 + dVdn) * area;
+    const double visc3 = muF * (tzx * n0 + tzy * n1 + tzz * n2 + dWdn) * area;
+    const double visc4 = muF * (txx * UF + txy * VF + txz * WF + dU[0] * UF + dU[1] * VF + dU[2] * WF) * n0 * area +
+                         muF * (tyx * UF + tyy * VF + tyz * WF + dV[0] * UF + dV[1] * VF + dV[2] * WF) * n1 * area +
+                         muF * (tzx * UF + tzy * VF + tzz * WF + dW[0] * UF + dW[1] * VF + dW[2] * WF) * n2 * area;
+    // blocks: LR = cR, RL = -cL
+    double* vLR = a.val + 25 * (size_t)a.lr[f];
+    double* vRL = a.val + 25 * (size_t)a.rl[f];
+    auto put = [&](int e, double cl, double cr) { vLR[e] = cr; vRL[e] = -cl; };
+    put(0, weightL * dRhoDPL * UnF * area + RhoF * diffDP * area, weightR * dRhoDPR * UnF * area - RhoF * diffDP * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) put(1 + k, RhoF * WUL * nv[k] * area, RhoF * WUR * nv[k] * area);
+    put(4, weightL * dRhoDTL * UnF * area, weightR * dRhoDTR * UnF * area);
+    const double phF[3] = {UF, VF, WF};
+#pragma unroll
+    for (int m = 1; m <= 3; ++m) {
+        const int k = m - 1;
+        const double ph = phF[k];
+        put(5 * m, weightL * dRhoDPL * UnF * ph * area + WPL * nv[k] * area + RhoF * diffDP * ph * area,
+            weightR * dRhoDPR * UnF * ph * area + WPR * nv[k] * area - RhoF * diffDP * ph * area);
+#pragma unroll
+        for (int q = 1; q <= 3; ++q)
+            if (q != m) put(5 * m + q, 0.0, 0.0);
+        put(5 * m + m, RhoF * WUL * nv[k] * ph * area + RhoF * UnF * weightL * area + diff_viscous * area,
+            RhoF * WUR * nv[k] * ph * area + RhoF * UnF * weightR * area - diff_viscous * area);
+        put(5 * m + 4, weightL * dRhoDTL * UnF * ph * area, weightR * dRhoDTR * UnF * ph * area);
+    }
+    const double velL[3] = {UL, VL, WL}, velR[3] = {UR, VR, WR};
+    put(20, weightL * dRhoDPL * HtF * UnF * area + RhoF * weightL * dHtDPL * UnF * area + RhoF * diffDP * HtF * area,
+        weightR * dRhoDPR * HtF * UnF * area + RhoF * weightR * dHtDPR * UnF * area - RhoF * diffDP * HtF * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        put(21 + k, RhoF * WUL * nv[k] * HtF * area + RhoF * UnF * weightL * velL[k] * area,
+            RhoF * WUR * nv[k] * HtF * area + RhoF * UnF * weightR * velR[k] * area);
+    put(24, weightL * dRhoDTL * UnF * HtF * area + RhoF * weightL * dHtDTL * UnF * area,
+        weightR * dRhoDTR * UnF * HtF * area + RhoF * weightR * dHtDTR * UnF * area);
+    // flux (the high-order face values equal the zero-order ones)
+    a.flux[f] = RhoF * UnF * area;
+    a.flux[nf + f] = (RhoF * UnF * UF * area + PF * n0 * area) - visc1;
+    a.flux[2 * nf + f] = (RhoF * UnF * VF * area + PF * n1 * area) - visc2;
+    a.flux[3 * nf + f] = (RhoF * UnF * WF * area + PF * n2 * area) - visc3;
+    a.flux[4 * nf + f] = RhoF * UnF * HtF * area - visc4;
+}
+
+// Boundary face b: its contributions to the owner's diagonal block (19
+// entries in planes 0..18, and in planes 19..26 the second terms of the 8
+// entries the reference touches twice), and its flux.
+__global__ void k_cbface(CplArgs a) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.nb) return;
+    const size_t nc = a.nc, nf = a.nf, nb = a.nb;
+    const int f = a.ni + b, o = a.own[f], p = a.bpatch[b];
+    const int tp = a.bct[3 * p], tu = a.bct[3 * p + 1], tt = a.bct[3 * p + 2];
+    const double cP = (tp == SEMO_BC_FIXED_VALUE) ? 0.0 : 1.0, cPd = 1.0 - cP;
+    const double cUVW = (tu == SEMO_BC_ZERO_GRADIENT) ? 1.0 : 0.0, cUVWd = 1.0 - cUVW;
+    const double cT = (tt == SEMO_BC_FIXED_VALUE) ? 0.0 : 1.0;
+    const double n0 = a.fn[f], n1 = a.fn[nf + f], n2 = a.fn[2 * nf + f];
+    const double nv[3] = {n0, n1, n2};
+    const double area = a.fa[f];
+    const double PL = a.f[o], UL = a.f[nc + o], VL = a.f[2 * nc + o], WL = a.f[3 * nc + o];
+    const double PR = a.bR[b], UR = a.bR[nb + b], VR = a.bR[2 * nb + b], WR = a.bR[3 * nb + b];
+    const double* eR = a.bR + 5 * nb + b;   // EOS plane q at eR[q * nb]
+    const double UnL = UL * n0 + VL * n1 + WL * n2;
+    const double UnR = UR * n0 + VR * n1 + WR * n2;
+    double UnF = 0.5 * UnL + 0.5 * UnR;
+    const double RhoF = 0.5 * a.eos[o] + 0.5 * eR[0];
+    const double UF = 0.5 * UL + 0.5 * UR, VF = 0.5 * VL + 0.5 * VR, WF = 0.5 * WL + 0.5 * WR;
+    const double PF = 0.5 * PL + 0.5 * PR;
+    const double dRhoDPF = 0.5 * a.eos[3 * nc + o] + 0.5 * eR[3 * nb];
+    const double dRhoDTF = 0.5 * a.eos[4 * nc + o] + 0.5 * eR[4 * nb];
+    const double dHtDPF = 0.5 * a.eos[5 * nc + o] + 0.5 * eR[5 * nb];
+    const double dHtDTF = 0.5 * a.eos[6 * nc + o] + 0.5 * eR[6 * nb];
+    const double HtF = 0.5 * a.eos[2 * nc + o] + 0.5 * eR[2 * nb];
+    const double dPN = 0.5 * a.mpn[f], alpha = a.alf[f];
+    const double tmp1 = 1.0 / a.eos[o] * a.dt;
+    const double ep[3] = {a.epn[f], a.epn[nf + f], a.epn[2 * nf + f]};
+    const double* g = a.grad;
+    UnF -= cPd * alpha * tmp1 * (PR - PL) / dPN;
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) UnF += cPd * alpha * tmp1 * g[ii * nc + o] * ep[ii];
+    const double muF = 0.5 * a.mu + 0.5 * a.mu;
+    double dU[3], dV[3], dW[3], dUdn = 0.0, dVdn = 0.0, dWdn = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 3; ++ii) {
+        dU[ii] = g[(3 + ii) * nc + o]; dV[ii] = g[(6 + ii) * nc + o]; dW[ii] = g[(9 + ii) * nc + o];
+        const double tvec = nv[ii] - alpha * ep[ii];
+        dUdn += dU[ii] * tvec; dVdn += dV[ii] * tvec; dWdn += dW[ii] * tvec;
+    }
+    dUdn += alpha * (UR - UL) / dPN; dVdn += alpha * (VR - VL) / dPN; dWdn += alpha * (WR - WL) / dPN;
+    const double dv3 = dU[0] + dV[1] + dW[2];
+    const double txx = dU[0] - 2.0 / 3.0 * dv3, txy = dV[0], txz = dW[0];
+    const double tyx = dU[1], tyy = dV[1] - 2.0 / 3.0 * dv3, tyz = dW[1];
+    const double tzx = dU[2], tzy = dV[2], tzz = dW[2] - 2.0 / 3.0 * dv3;
+    const double visc1 = muF * (txx * n0 + txy * n1 + txz * n2 + dUdn) * area;
+    const double visc2 = muF * (tyx * n0 + tyy * n1 + tyz * n2 + dVdn) * area;
+    const double visc3 = muF * (tzx * n0 + tzy * n1 + tzz * n2 + dWdn) * area;
+    const double visc4 = muF * (txx * UF + txy * VF + txz * WF + dU[0] * UF + dU[1] * VF + dU[2] * WF) * n0 * area +
+                         muF * (tyx * UF + tyy * VF + tyz * WF + dV[0] * UF + dV[1] * VF + dV[2] * WF) * n1 * area +
+                         muF * (tzx * UF + tzy * VF + tzz * WF + dW[0] * UF + dW[1] * VF + dW[2] * WF) * n2 * area;
+    const double phF[3] = {UF, VF, WF};
+    double* q = a.bblk + b;   // plane j at q[j * nb]
+    q[0] = cP * (dRhoDPF * UnF * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[(1 + k) * nb] = cUVW * (RhoF * nv[k] * area);
+    q[4 * nb] = cT * (dRhoDTF * UnF * area);
+    // momentum rows: entries (5, 6, 9), (10, 12, 14), (15, 18, 19) in planes 5..13
+#pragma unroll
+    for (int m = 1; m <= 3; ++m) {
+        const int k = m - 1, j = 5 + 3 * k;
+        const double ph = phF[k];
+        q[j * nb] = cP * (dRhoDPF * UnF * ph * area);
+        q[(j + 1) * nb] = cUVW * (RhoF * nv[k] * ph * area + RhoF * UnF * area);
+        q[(j + 2) * nb] = cT * (dRhoDTF * UnF * ph * area);
+    }
+    q[14 * nb] = cP * (dRhoDPF * UnF * HtF * area + RhoF * UnF * dHtDPF * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[(15 + k) * nb] = cUVW * (RhoF * nv[k] * HtF * area + RhoF * UnF * phF[k] * area);
+    q[18 * nb] = cT * (dRhoDTF * UnF * HtF * area + RhoF * UnF * dHtDTF * area);
+    // second terms: entry 0, then 5, 10, 15 (pressure diffusion), 6, 12, 18 (viscous), 20
+    q[19 * nb] = cPd * (RhoF * tmp1 / dPN * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[(20 + k) * nb] = cPd * (RhoF * alpha * tmp1 / dPN * phF[k] * area);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[(23 + k) * nb] = cUVWd * (alpha * muF / dPN * area);
+    q[26 * nb] = cPd * (RhoF * alpha * tmp1 / dPN * dHtDPF * area);
+    a.flux[f] = RhoF * UnF * area;
+    a.flux[nf + f] = (RhoF * UnF * UF * area + PF * n0 * area) - visc1;
+    a.flux[2 * nf + f] = (RhoF * UnF * VF * area + PF * n1 * area) - visc2;
+    a.flux[3 * nf + f] = (RhoF * UnF * WF * area + PF * n2 * area) - visc3;
+    a.flux[4 * nf + f] = RhoF * UnF * HtF * area - visc4;
+}
+
+// Cell i: the time block and the bounded BDF2 right-hand side
+// (coupled.cpp:318-625), then the face terms in ascending face order.
+__global__ void __launch_bounds__(128) k_ccell(CplArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nc) return;
+    const size_t nc = a.nc, nf = a.nf, nb = a.nb;
+    const double* F = a.f;
+    const double P = F[i], u = F[nc + i], v = F[2 * nc + i], w = F[3 * nc + i];
+    const double Rho = a.eos[i], Ht = a.eos[2 * nc + i], dRhoDP = a.eos[3 * nc + i], dRhoDT = a.eos[4 * nc + i];
+    const double dHtDP = a.eos[5 * nc + i], dHtDT = a.eos[6 * nc + i];
+    double eo[7], eo2[7];
+    eos1(a.cv, a.gam, F[5 * nc + i], F[6 * nc + i], F[7 * nc + i], F[8 * nc + i], F[9 * nc + i], eo);
+    eos1(a.cv, a.gam, F[10 * nc + i], F[11 * nc + i], F[12 * nc + i], F[13 * nc + i], F[14 * nc + i], eo2);
+    const double volume = a.vol[i], dt = a.dt;
+    const double gv[3] = {a.g0, a.g1, a.g2}, vel[3] = {u, v, w};
+    double d[25];
+#pragma unroll
+    for (int e = 0; e < 25; ++e) d[e] = 0.0;
+    d[0] = (dRhoDP) * volume / dt;
+    d[4] = (dRhoDT) * volume / dt;
+#pragma unroll
+    for (int m = 1; m <= 3; ++m) {
+        d[5 * m] = (dRhoDP * vel[m - 1]) * volume / dt;
+        d[5 * m] -= dRhoDP * gv[m - 1] * volume;
+        d[5 * m + m] = (Rho) * volume / dt;
+        d[5 * m + 4] = (dRhoDT * vel[m - 1]) * volume / dt;
+        d[5 * m + 4] -= dRhoDT * gv[m - 1] * volume;
+    }
+    const double gu = a.g0 * u + a.g1 * v + a.g2 * w;
+    d[20] = (dRhoDP * Ht + dHtDP * Rho - 1.0) * volume / dt;
+    d[20] -= dRhoDP * gu * volume;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        d[21 + k] = (Rho * vel[k]) * volume / dt;
+        d[21 + k] -= Rho * (gv[k]) * volume;
+    }
+    d[24] = (dRhoDT * Ht + dHtDT * Rho) * volume / dt;
+    d[24] -= dRhoDT * gu * volume;
+    // bounded BDF2 on the conservative variables
+    const double cn[5] = {Rho, Rho * u, Rho * v, Rho * w, Rho * Ht - P};
+    const double c1[5] = {eo[0], eo[0] * F[6 * nc + i], eo[0] * F[7 * nc + i], eo[0] * F[8 * nc + i],
+                          eo[0] * eo[2] - F[5 * nc + i]};
+    const double c2[5] = {eo2[0], eo2[0] * F[11 * nc + i], eo2[0] * F[12 * nc + i], eo2[0] * F[13 * nc + i],
+                          eo2[0] * eo2[2] - F[10 * nc + i]};
+    double beta = 1.0;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const double sou = (c1[q] - c2[q]) / (cn[q] - c2[q] + 1.e-200);
+        beta = (0.0 < sou && sou < 1.0) ? smin(beta, 0.0) : smin(beta, 1.0);
+    }
+    const double co1 = a.dto / (dt + a.dto), co2 = a.dto2 / (a.dto + a.dto2);
+    double B[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const double np12 = cn[q] + beta * co1 * (cn[q] - c1[q]);
+        const double nm12 = c1[q] + beta * co2 * (c1[q] - c2[q]);
+        B[q] = -(np12 - nm12) * volume / dt;
+    }
+    B[1] += Rho * a.g0 * volume;
+    B[2] += Rho * a.g1 * volume;
+    B[3] += Rho * a.g2 * volume;
+    B[4] += Rho * gu * volume;
+    // face terms
+    for (int k = a.cfp[i]; k < a.cfp[i + 1]; ++k) {
+        const int e = a.cfi[k];
+        const int f = e & kFaceMask;
+        if (f < a.ni) {
+            if (e >> 30) {   // neighbour side: -cR (stored in the owner-row slot)
+                const double* blk = a.val + 25 * (size_t)a.lr[f];
+#pragma unroll
+                for (int q = 0; q < 25; ++q)
+                    if (q != 7 && q != 8 && q != 11 && q != 13 && q != 16 && q != 17) d[q] -= blk[q];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) B[q] += a.flux[q * nf + f];
+            } else {         // owner side: +cL (stored negated in the neighbour-row slot)
+                const double* blk = a.val + 25 * (size_t)a.rl[f];
+#pragma unroll
+                for (int q = 0; q < 25; ++q)
+                    if (q != 7 && q != 8 && q != 11 && q != 13 && q != 16 && q != 17) d[q] += -blk[q];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) B[q] -= a.flux[q * nf + f];
+            }
+        } else {
+            // the 19 diagonal entries a boundary face touches (planes 0..18 of
+            // k_cbface), then the 8 it touches a second time (planes 19..26)
+            constexpr int kE[19] = {0, 1, 2, 3, 4, 5, 6, 9, 10, 12, 14, 15, 18, 19, 20, 21, 22, 23, 24};
+            constexpr int kE2[8] = {0, 5, 10, 15, 6, 12, 18, 20};
+            const int b = f - a.ni;
+            const double* qb = a.bblk + b;
+#pragma unroll
+            for (int j = 0; j < 19; ++j) d[kE[j]] += qb[j * nb];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) d[kE2[j]] += qb[(19 + j) * nb];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) B[q] -= a.flux[q * nf + f];
+        }
+    }
+    double* out = a.val + 25 * (size_t)a.dig[i];
+#pragma unroll
+    for (int q = 0; q < 25; ++q) out[q] = d[q];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) a.b[q * nc + i] = B[q];
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// solver: block SELL-32 copy of the matrix (values in V), BiCGStab with the
+// inverses of the 5x5 diagonal blocks.  Inner vectors are interleaved per
+// cell (v[5 i + a]) so one gather fetches a cell's five unknowns.
+// ---------------------------------------------------------------------------
+constexpr int kT = 256;
+
+// widest row of each chunk of 32 rows
+__global__ void k_bsell_width(int nc, const int* __restrict__ ptr, int* __restrict__ width) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nch = (nc + 31) / 32;
+    if (c >= nch) return;
+    int w = 0;
+    for (int l = 0; l < 32; ++l) {
+        const int i = 32 * c + l;
+        if (i < nc) w = max(w, ptr[i + 1] - ptr[i]);
+    }
+    width[c] = w;
+}
+
+// off32[c] = first slot row of chunk c; slot row s holds 32 columns
+// (col[32 s + lane]) and 25 x 32 values (val[(25 s + e) 32 + lane])
+template <class V>
+__global__ void k_bsell_fill(int nc, const int* __restrict__ ptr, const int* __restrict__ colA,
+                             const double* __restrict__ valA, const int* __restrict__ off32,
+                             const int* __restrict__ width, int* __restrict__ col, V* __restrict__ val,
+                             bool pattern) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const int c = i >> 5, l = i & 31;
+    const int s0 = off32[c], w = width[c], kb = ptr[i], len = ptr[i + 1] - kb;
+    for (int j = 0; j < w; ++j) {
+        const int64_t s = s0 + j;
+        if (pattern) col[32 * s + l] = (j < len) ? colA[kb + j] : -1;
+        const double* src = valA + 25 * (int64_t)(kb + j);
+#pragma unroll 5
+        for (int e = 0; e < 25; ++e) val[(25 * s + e) * 32 + l] = (j < len) ? (V)src[e] : (V)0;
+    }
+}
+
+// inverse of each diagonal block (Gauss-Jordan with partial pivoting, FP64)
+template <class V>
+__global__ void k_binv(int nc, const int* __restrict__ dig, const double* __restrict__ valA, V* __restrict__ minv,
+                       int* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double m[5][5], x[5][5];
+    const double* a = valA + 25 * (int64_t)dig[i];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) { m[r][q] = a[5 * r + q]; x[r][q] = (r == q) ? 1.0 : 0.0; }
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        int p = k;
+        double best = fabs(m[k][k]);
+#pragma unroll
+        for (int r = k + 1; r < 5; ++r)
+            if (fabs(m[r][k]) > best) { best = fabs(m[r][k]); p = r; }
+#pragma unroll
+        for (int r = k + 1; r < 5; ++r) {
+            const bool sw = (r == p);   // selects keep every index static (no local memory)
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                const double mk = m[k][q], mr = m[r][q], xk = x[k][q], xr = x[r][q];
+                m[k][q] = sw ? mr : mk; m[r][q] = sw ? mk : mr;
+                x[k][q] = sw ? xr : xk; x[r][q] = sw ? xk : xr;
+            }
+        }
+        if (!(fabs(m[k][k]) > 0.0) || !isfinite(m[k][k])) bad = true;
+        const double piv = 1.0 / m[k][k];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) { m[k][q] *= piv; x[k][q] *= piv; }
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+            if (r != k) {
+                const double fct = m[r][k];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) { m[r][q] -= fct * m[k][q]; x[r][q] -= fct * x[k][q]; }
+            }
+    }
+    if (bad) atomicExch(flag, 1);
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) minv[25 * (int64_t)i + 5 * r + q] = (V)x[r][q];
+}
+
+template <class V>
+__device__ __forceinline__ void bmv_row(int i, const int* __restrict__ off32, const int* __restrict__ width,
+                                        const int* __restrict__ col, const V* __restrict__ val,
+                                        const V* __restrict__ x, V* acc) {
+    const int c = i >> 5, l = i & 31;
+    const int s0 = off32[c], w = width[c];
+#pragma unroll
+    for (int a = 0; a < 5; ++a) acc[a] = (V)0;
+    for (int j = 0; j < w; ++j) {
+        const int64_t s = s0 + j;
+        const int jc = col[32 * s + l];
+        if (jc < 0) continue;
+        V xv[5];
+#pragma unroll
+        for (int b = 0; b < 5; ++b) xv[b] = x[5 * (int64_t)jc + b];
+        const V* vs = val + 25 * s * 32 + l;
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+#pragma unroll
+            for (int b = 0; b < 5; ++b) acc[a] += vs[(5 * a + b) * 32] * xv[b];
+    }
+}
+
+template <class V>
+__device__ __forceinline__ void bapply(const V* __restrict__ minv, int64_t i, const V* in, V* out) {
+    const V* m = minv + 25 * i;
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+        V t = (V)0;
+#pragma unroll
+        for (int b = 0; b < 5; ++b) t += m[5 * a + b] * in[b];
+        out[a] = t;
+    }
+}
+
+// device scalars: 0 rho, 1 alpha, 2 omega, 3 beta, 4 <r,r>, 5 <rh,r>,
+// 6 <b,b>, 7 breakdown; partials: 2 x kRedBlocks
+__global__ void k_bi_init_sc(double* __restrict__ sc) {
+    sc[0] = 1.0; sc[1] = 1.0; sc[2] = 1.0; sc[3] = 0.0; sc[7] = 0.0;
+}
+
+// r = rh = src (field-split FP64 in, interleaved V out), p = v = z = 0; partial <r,r>
+template <class V>
+__global__ void k_bi_start(int nc, const double* __restrict__ src, V* __restrict__ r, V* __restrict__ rh,
+                           V* __restrict__ p, V* __restrict__ v, V* __restrict__ z, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const V xv = (V)src[(int64_t)a * nc + i];
+            const int64_t q = 5 * (int64_t)i + a;
+            r[q] = xv; rh[q] = xv; p[q] = (V)0; v[q] = (V)0; z[q] = (V)0;
+            acc += (double)xv * (double)xv;
+        }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void k_bi_fin_start(const double* __restrict__ part, double* __restrict__ sc) {
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) a += part[i];
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) { sc[4] = a; sc[5] = a; sc[6] = a; }
+}
+
+// beta = (rho1 / rho)(alpha / omega), rho = rho1 (rho1 = <rh,r> in sc[5])
+__global__ void k_bi_beta(double* __restrict__ sc) {
+    const double rho1 = sc[5];
+    const double beta = (rho1 / sc[0]) * (sc[1] / sc[2]);
+    if (!isfinite(beta) || rho1 == 0.0) sc[7] = 1.0;
+    sc[3] = isfinite(beta) ? beta : 0.0;
+    sc[0] = rho1;
+}
+
+// p = r + beta (p - omega v); y = M^-1 p
+template <class V>
+__global__ void k_bi_p(int nc, const double* __restrict__ sc, const V* __restrict__ r, V* __restrict__ p,
+                       const V* __restrict__ v, const V* __restrict__ minv, V* __restrict__ y) {
+    const V beta = (V)sc[3], omega = (V)sc[2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        V pv[5], yv[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const int64_t q = 5 * (int64_t)i + a;
+            pv[a] = r[q] + beta * (p[q] - omega * v[q]);
+            p[q] = pv[a];
+        }
+        bapply(minv, i, pv, yv);
+#pragma unroll
+        for (int a = 0; a < 5; ++a) y[5 * (int64_t)i + a] = yv[a];
+    }
+}
+
+// out = A in; partial sums of <w1, out> (and <out, out> when kTwo)
+template <class V, bool kTwo>
+__global__ void k_bi_mv(int nc, const int* __restrict__ off32, const int* __restrict__ width,
+                        const int* __restrict__ col, const V* __restrict__ val, const V* __restrict__ in,
+                        V* __restrict__ out, const V* __restrict__ w1, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double d1 = 0.0, d2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        V acc[5];
+        bmv_row(i, off32, width, col, val, in, acc);
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const int64_t q = 5 * (int64_t)i + a;
+            out[q] = acc[a];
+            d1 += (double)w1[q] * (double)acc[a];
+            if (kTwo) d2 += (double)acc[a] * (double)acc[a];
+        }
+    }
+    d1 = block_sum(d1, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = d1;
+    if (kTwo) {
+        __syncthreads();
+        d2 = block_sum(d2, sh);
+        if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = d2;
+    }
+}
+
+// alpha = rho / <rh, v>
+__global__ void k_bi_alpha(const double* __restrict__ part, double* __restrict__ sc) {
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) a += part[i];
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) {
+        const double al = sc[0] / a;
+        if (!isfinite(al)) sc[7] = 1.0;
+        sc[1] = isfinite(al) ? al : 0.0;
+    }
+}
+
+// z += alpha y; s = r - alpha v; y = M^-1 s
+template <class V>
+__global__ void k_bi_s(int nc, const double* __restrict__ sc, const V* __restrict__ r, const V* __restrict__ v,
+                       V* __restrict__ s, V* __restrict__ z, V* __restrict__ y, const V* __restrict__ minv) {
+    const V alpha = (V)sc[1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        V sv[5], yv[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const int64_t q = 5 * (int64_t)i + a;
+            z[q] += alpha * y[q];
+            sv[a] = r[q] - alpha * v[q];
+            s[q] = sv[a];
+        }
+        bapply(minv, i, sv, yv);
+#pragma unroll
+        for (int a = 0; a < 5; ++a) y[5 * (int64_t)i + a] = yv[a];
+    }
+}
+
+// omega = <t, s> / <t, t>
+__global__ void k_bi_omega(const double* __restrict__ part, double* __restrict__ sc) {
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) { a += part[i]; b += part[kRedBlocks + i]; }
+    a = block_sum(a, sh);
+    __syncthreads();
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) sc[2] = (b > 0.0) ? a / b : 0.0;
+}
+
+// z += omega y; r = s - omega t; partials <r,r>, <rh,r>
+template <class V>
+__global__ void k_bi_r(int nc, const double* __restrict__ sc, const V* __restrict__ s, const V* __restrict__ t,
+                       const V* __restrict__ y, const V* __restrict__ rh, V* __restrict__ z, V* __restrict__ r,
+                       double* __restrict__ part) {
+    __shared__ double sh[32];
+    const V omega = (V)sc[2];
+    double d1 = 0.0, d2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const int64_t q = 5 * (int64_t)i + a;
+            z[q] += omega * y[q];
+            const V rv = s[q] - omega * t[q];
+            r[q] = rv;
+            d1 += (double)rv * (double)rv;
+            d2 += (double)rh[q] * (double)rv;
+        }
+    d1 = block_sum(d1, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = d1;
+    __syncthreads();
+    d2 = block_sum(d2, sh);
+    if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = d2;
+}
+
+__global__ void k_bi_fin_r(const double* __restrict__ part, double* __restrict__ sc) {
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) { a += part[i]; b += part[kRedBlocks + i]; }
+    a = block_sum(a, sh);
+    __syncthreads();
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) { sc[4] = a; sc[5] = b; }
+}
+
+// FP64 residual r = b - A x on the slot-major blocks (thread per row),
+// x and r field-split; partial <r,r>
+__global__ void k_bsr_res(int nc, const int* __restrict__ ptr, const int* __restrict__ colA,
+                          const double* __restrict__ valA, const double* __restrict__ x,
+                          const double* __restrict__ b, double* __restrict__ r, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        double acc[5] = {0, 0, 0, 0, 0};
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+            const int j = colA[k];
+            const double* blk = valA + 25 * (int64_t)k;
+            double xv[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) xv[q] = x[(int64_t)q * nc + j];
+#pragma unroll
+            for (int a = 0; a < 5; ++a)
+#pragma unroll
+                for (int q = 0; q < 5; ++q) acc[a] += blk[5 * a + q] * xv[q];
+        }
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            const double rv = b[(int64_t)a * nc + i] - acc[a];
+            r[(int64_t)a * nc + i] = rv;
+            acc2 += rv * rv;
+        }
+    }
+    acc2 = block_sum(acc2, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc2;
+}
+
+// x[a nc + i] += z[5 i + a]
+template <class V>
+__global__ void k_add_il(int nc, const V* __restrict__ z, double* __restrict__ x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
+#pragma unroll
+        for (int a = 0; a < 5; ++a) x[(int64_t)a * nc + i] += (double)z[5 * (int64_t)i + a];
+}
+
+__global__ void k_sum1(const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) a += part[i];
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) out[0] = a;
+}
+
+// primitives += urf x, clamps (coupled.cpp:2523-2556); partials of
+// sum x^2 and sum prim^2 (:2585-2593)
+__global__ void k_cupdate(int nc, double urf, const double* __restrict__ lim, const double* __restrict__ x,
+                          double* __restrict__ f, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double nd = 0.0, np = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        double v[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            double t = f[(int64_t)a * nc + i] + urf * x[(int64_t)a * nc + i];
+            if (t <= lim[2 * a]) t = lim[2 * a];
+            if (t >= lim[2 * a + 1]) t = lim[2 * a + 1];
+            f[(int64_t)a * nc + i] = t;
+            v[a] = t;
+        }
+#pragma unroll
+        for (int a = 0; a < 5; ++a) { const double xv = x[(int64_t)a * nc + i]; nd += xv * xv; }
+#pragma unroll
+        for (int a = 0; a < 5; ++a) np += v[a] * v[a];
+    }
+    nd = block_sum(nd, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = nd;
+    __syncthreads();
+    np = block_sum(np, sh);
+    if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = np;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct CplSolver {
+    int gen = -1;                  // mesh generation of the SELL layout
+    int nch = 0;
+    int64_t rows32 = 0;            // slot rows (of 32 lanes)
+    semo::DBuf<int> width, off32, col;
+    semo::DBuf<float> val32, minv32, v32;     // v32: 8 vectors of 5 nc
+    semo::DBuf<double> val64, minv64, v64;
+    semo::DBuf<double> part, sc, r64;
+};
+
+CplSolver& solver_state(semo_ctx* c) {
+    if (!c->cpl_solver) c->cpl_solver = std::make_shared<CplSolver>();
+    return *static_cast<CplSolver*>(c->cpl_solver.get());
+}
+
+CplArgs make_args(semo_ctx* c) {
+    CplArgs a{};
+    a.nc = c->nc; a.nf = c->nf; a.ni = c->ni; a.nb = c->nb;
+    a.own = c->own; a.nei = c->nei; a.lr = c->A_lr; a.rl = c->A_rl; a.dig = c->A_dig;
+    a.cfp = c->cf_ptr; a.cfi = c->cf_idx; a.bpatch = c->bpatch; a.bct = c->cpl_bct;
+    a.fn = c->fn; a.fa = c->fa; a.wc = c->wc; a.mpn = c->mpn; a.alf = c->alf; a.epn = c->epn; a.skew = c->skew;
+    a.vol = c->vol;
+    a.f = c->cpl_f; a.eos = c->cpl_eos; a.grad = c->cpl_grad; a.bR = c->cpl_bR; a.bcv = c->cpl_bcv;
+    a.val = c->cpl_val; a.b = c->cpl_b;
+    a.flux = c->cpl_scr; a.bblk = c->cpl_scr.p + 5 * (size_t)c->nf;
+    const semo_coupled_physics& p = c->cphys;
+    a.cv = p.cv; a.gam = p.gamma; a.mu = p.mu; a.dt = p.dt; a.dto = p.dt_old; a.dto2 = p.dt_old2;
+    a.g0 = p.gravity[0]; a.g1 = p.gravity[1]; a.g2 = p.gravity[2];
+    return a;
+}
+
+// BiCGStab on A z = src (src field-split FP64), right-preconditioned by the
+// block inverses, to rel_tol of ||src||; the solution is left in vec's 8th
+// vector (interleaved).  One host read of the residual per iteration.
+template <class V>
+int bicgstab_inner(semo_ctx* c, CplSolver& S, const V* val, const V* minv, V* vec, const double* src,
+                   double rtol, int maxit, double* rel_out, bool* breakdown) {
+    using namespace semo;
+    cudaStream_t s = c->stream;
+    const int nc = c->nc;
+    const size_t n5 = 5 * (size_t)nc;
+    V *r = vec, *rh = vec + n5, *p = vec + 2 * n5, *v = vec + 3 * n5, *sv = vec + 4 * n5, *t = vec + 5 * n5;
+    V *y = vec + 6 * n5, *z = vec + 7 * n5;
+    double* part = S.part;
+    double* sc = S.sc;
+    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
+    double* h = c->hpin;
+    k_bi_init_sc<<<1, 1, 0, s>>>(sc);
+    SEMO_CHECK_LAUNCH();
+    k_bi_start<V><<<kRedBlocks, kT, 0, s>>>(nc, src, r, rh, p, v, z, part);
+    SEMO_CHECK_LAUNCH();
+    k_bi_fin_start<<<1, kT, 0, s>>>(part, sc);
+    SEMO_CHECK_LAUNCH();
+    SEMO_CUDA(cudaMemcpyAsync(h, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    const double bn = std::sqrt(h[6]);
+    *breakdown = false;
+    if (bn == 0.0) { *rel_out = 0.0; return 0; }
+    int it = 0;
+    double rel = 1.0;
+    while (it < maxit) {
+        k_bi_beta<<<1, 1, 0, s>>>(sc);
+        SEMO_CHECK_LAUNCH();
+        k_bi_p<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, r, p, v, minv, y);
+        SEMO_CHECK_LAUNCH();
+        k_bi_mv<V, false><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, v, rh, part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_alpha<<<1, kT, 0, s>>>(part, sc);
+        SEMO_CHECK_LAUNCH();
+        k_bi_s<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, r, v, sv, z, y, minv);
+        SEMO_CHECK_LAUNCH();
+        k_bi_mv<V, true><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, t, sv, part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_omega<<<1, kT, 0, s>>>(part, sc);
+        SEMO_CHECK_LAUNCH();
+        k_bi_r<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, sv, t, y, rh, z, r, part);
+        SEMO_CHECK_LAUNCH();
+        k_bi_fin_r<<<1, kT, 0, s>>>(part, sc);
+        SEMO_CHECK_LAUNCH();
+        ++it;
+        SEMO_CUDA(cudaMemcpyAsync(h, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        rel = std::sqrt(h[4]) / bn;
+        if (h[7] != 0.0 || !std::isfinite(rel)) { *breakdown = true; break; }
+        if (rel <= rtol) break;
+    }
+    *rel_out = rel;
+    return it;
+}
+
+}  // namespace
+
+namespace semo {
+
+void coupled_assemble(semo_ctx* c) {
+    cudaStream_t s = c->stream;
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    c->cpl_eos.alloc(7 * (size_t)nc, s);
+    c->cpl_bR.alloc(12 * (size_t)std::max(nb, 1), s);
+    c->cpl_grad.alloc(15 * (size_t)nc, s);
+    c->cpl_mm.alloc(10 * (size_t)nc, s);
+    c->cpl_val.alloc(25 * (size_t)c->nnz, s);
+    c->cpl_b.alloc(5 * (size_t)nc, s);
+    c->cpl_scr.alloc(5 * (size_t)nf + 27 * (size_t)std::max(nb, 1), s);
+    CplArgs a = make_args(c);
+    {
+        StageScope sc(c, ST_CGRAD);
+        k_ceos<<<blocks(nc, kT), kT, 0, s>>>(nc, c->cphys.cv, c->cphys.gamma, c->cpl_f, c->cpl_eos);
+        SEMO_CHECK_LAUNCH();
+        if (nb > 0) {
+            k_cbstate<<<blocks(nb, kT), kT, 0, s>>>(a, c->cpl_bR);
+            SEMO_CHECK_LAUNCH();
+        }
+        const double* F = c->cpl_f;
+        const size_t n = nc;
+        lsq_gradients5(c, F, F + n, F + 2 * n, F + 3 * n, F + 4 * n, c->cpl_bR, c->cpl_grad, c->cpl_mm);
+    }
+    {
+        StageScope sc(c, ST_CFACE);
+        if (ni > 0) {
+            k_cface<<<blocks(ni, 128), 128, 0, s>>>(a);
+            SEMO_CHECK_LAUNCH();
+        }
+        if (nb > 0) {
+            k_cbface<<<blocks(nb, kT), kT, 0, s>>>(a);
+            SEMO_CHECK_LAUNCH();
+        }
+    }
+    {
+        StageScope sc(c, ST_CCELL);
+        k_ccell<<<blocks(nc, 128), 128, 0, s>>>(a);
+        SEMO_CHECK_LAUNCH();
+    }
+    c->cpl_assembled = true;
+}
+
+semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
+    cudaStream_t s = c->stream;
+    const int nc = c->nc;
+    CplSolver& S = solver_state(c);
+    const bool mixed = c->prm.precision == SEMO_PREC_MIXED;
+    cudaEvent_t e0 = take_event(c), e1 = take_event(c), e2 = take_event(c);
+    SEMO_CUDA(cudaEventRecord(e0, s));
+    StageScope stage(c, ST_CSOLVE);
+    S.part.alloc(2 * kRedBlocks, s);
+    S.sc.alloc(8, s);
+    // block SELL layout: the pattern once per mesh
+    if (S.gen != c->mesh_gen) {
+        S.nch = (nc + 31) / 32;
+        S.width.alloc(S.nch, s);
+        S.off32.alloc(S.nch + 1, s);
+        k_bsell_width<<<blocks(S.nch, kT), kT, 0, s>>>(nc, c->A_ptr, S.width);
+        SEMO_CHECK_LAUNCH();
+        SEMO_CUDA(cudaMemcpyAsync(S.off32.p, S.width.p, sizeof(int) * S.nch, cudaMemcpyDeviceToDevice, s));
+        SEMO_CUDA(cudaMemsetAsync(S.off32.p + S.nch, 0, sizeof(int), s));
+        S.rows32 = device_scan(s, S.off32.p, S.nch + 1);
+        S.col.alloc(32 * (size_t)S.rows32, s);
+        S.gen = c->mesh_gen;
+        S.val32.release(); S.val64.release();
+    }
+    SEMO_CUDA(cudaMemsetAsync(c->flag.p + 12, 0, sizeof(int), s));
+    const size_t n5 = 5 * (size_t)nc;
+    if (mixed) {
+        const bool pattern = S.val32.n == 0 && S.val64.n == 0;
+        S.val32.alloc(25 * 32 * (size_t)S.rows32, s);
+        S.minv32.alloc(25 * (size_t)nc, s);
+        S.v32.alloc(8 * n5, s);
+        k_bsell_fill<float><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, S.off32, S.width, S.col,
+                                                         S.val32, pattern);
+        SEMO_CHECK_LAUNCH();
+        k_binv<float><<<blocks(nc, 128), 128, 0, s>>>(nc, c->A_dig, c->cpl_val, S.minv32, c->flag.p + 12);
+        SEMO_CHECK_LAUNCH();
+    } else {
+        const bool pattern = S.val32.n == 0 && S.val64.n == 0;
+        S.val64.alloc(25 * 32 * (size_t)S.rows32, s);
+        S.minv64.alloc(25 * (size_t)nc, s);
+        S.v64.alloc(8 * n5, s);
+        k_bsell_fill<double><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, S.off32, S.width,
+                                                          S.col, S.val64, pattern);
+        SEMO_CHECK_LAUNCH();
+        k_binv<double><<<blocks(nc, 128), 128, 0, s>>>(nc, c->A_dig, c->cpl_val, S.minv64, c->flag.p + 12);
+        SEMO_CHECK_LAUNCH();
+    }
+    SEMO_CUDA(cudaEventRecord(e1, s));
+    int singular = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&singular, c->flag.p + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    if (singular) throw Error(SEMO_ERR_BREAKDOWN, "singular 5x5 diagonal block");
+    // defect correction: x = 0; r = b - A x; inner solve of A z = r; x += z
+    c->cpl_x.alloc(n5, s);
+    S.r64.alloc(n5, s);
+    c->cpl_x.zero();
+    const double tol = c->prm.tol;
+    const int maxit = c->prm.max_iter > 0 ? c->prm.max_iter : 1000;
+    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
+    double* h = c->hpin;
+    auto residual = [&]() {
+        k_bsr_res<<<kRedBlocks, kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, c->cpl_x, c->cpl_b, S.r64, S.part);
+        SEMO_CHECK_LAUNCH();
+        k_sum1<<<1, kT, 0, s>>>(S.part, S.sc.p + 6);
+        SEMO_CHECK_LAUNCH();
+        SEMO_CUDA(cudaMemcpyAsync(h + 8, S.sc.p + 6, sizeof(double), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        return std::sqrt(h[8]);
+    };
+    const double bn = residual();
+    int total = 0, outer = 0;
+    double rel = (bn > 0.0) ? 1.0 : 0.0;
+    bool brk = false;
+    while (rel > tol && total < maxit && outer < 30) {
+        double inner_rel = 0.0;
+        int it;
+        if (mixed) {
+            // FP32 reduces the defect by about 1e-3 per outer step
+            it = bicgstab_inner<float>(c, S, S.val32, S.minv32, S.v32, S.r64, std::max(1e-3, 0.5 * tol / rel),
+                                       maxit - total, &inner_rel, &brk);
+            k_add_il<float><<<kRedBlocks, kT, 0, s>>>(nc, S.v32.p + 7 * n5, c->cpl_x);
+        } else {
+            it = bicgstab_inner<double>(c, S, S.val64, S.minv64, S.v64, S.r64, 0.5 * tol / rel, maxit - total,
+                                        &inner_rel, &brk);
+            k_add_il<double><<<kRedBlocks, kT, 0, s>>>(nc, S.v64.p + 7 * n5, c->cpl_x);
+        }
+        SEMO_CHECK_LAUNCH();
+        total += it;
+        ++outer;
+        rel = residual() / bn;
+        if (brk || it == 0) break;
+    }
+    SEMO_CUDA(cudaEventRecord(e2, s));
+    SEMO_CUDA(cudaEventSynchronize(e2));
+    float t0 = 0.f, t1 = 0.f;
+    cudaEventElapsedTime(&t0, e0, e1);
+    cudaEventElapsedTime(&t1, e1, e2);
+    c->ev_pool.push_back(e0); c->ev_pool.push_back(e1); c->ev_pool.push_back(e2);
+    if (info) {
+        info->iterations = total;
+        info->rel_residual = rel;
+        info->levels = outer;
+        info->coarse_size = 0;
+        info->operator_complexity = 1.0;
+        info->setup_ms = t0;
+        info->solve_ms = t1;
+    }
+    if (!std::isfinite(rel)) return SEMO_ERR_NAN;
+    if (rel <= tol) return SEMO_OK;
+    return brk ? SEMO_ERR_BREAKDOWN : SEMO_ERR_NOT_CONVERGED;
+}
+
+double coupled_update(semo_ctx* c) {
+    cudaStream_t s = c->stream;
+    StageScope sc(c, ST_CUPDATE);
+    CplSolver& S = solver_state(c);
+    S.part.alloc(2 * kRedBlocks, s);
+    S.sc.alloc(8, s);
+    c->cpl_lim.upload(c->cphys.limits, 10, s);
+    k_cupdate<<<kRedBlocks, kT, 0, s>>>(c->nc, c->cphys.urf, c->cpl_lim, c->cpl_x, c->cpl_f, S.part);
+    SEMO_CHECK_LAUNCH();
+    k_finish2<<<1, kT, 0, s>>>(S.part, S.sc);
+    SEMO_CHECK_LAUNCH();
+    double h[2];
+    SEMO_CUDA(cudaMemcpyAsync(h, S.sc.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    c->cpl_assembled = false;
+    return std::sqrt(h[0]) / std::sqrt(h[1]) / 5.0;
+}
+
+}  // namespace semo

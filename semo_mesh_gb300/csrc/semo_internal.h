@@ -39,12 +39,13 @@ extern long long g_kernel_launches;
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
              ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_MSTACS, ST_VFACE, ST_VSOLVE, ST_VUPDATE,
-             ST_STENCIL_UVW, ST_MBFACE, ST_COUNT };
+             ST_STENCIL_UVW, ST_MBFACE, ST_CGRAD, ST_CFACE, ST_CCELL, ST_CSOLVE, ST_CUPDATE, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
                                                   "setup_level", "setup_coarse", "mface", "mcell", "msolve",
-                                                  "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw", "mbface"};
+                                                  "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw", "mbface",
+                                                  "cgrad", "cface", "ccell", "csolve", "cupdate"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -188,6 +189,21 @@ struct semo_ctx {
     semo::DBuf<double> fvf;                       // MSTACS face values: 2 planes of nf (left, right)
     semo::DBuf<double> co;                        // cell Courant number
     bool vof_assembled = false;
+
+    // ---- compressible coupled system (RCM order; 5x5 blocks on A_ptr/A_col) ----
+    semo_coupled_physics cphys{};
+    bool cpl_phys = false, cpl_fields = false, cpl_assembled = false;
+    semo::DBuf<int> cpl_bct;                      // npatch*3: type of p, u, T
+    semo::DBuf<double> cpl_bcv;                   // npatch*5: p, u, v, w, T
+    semo::DBuf<double> cpl_f;                     // 15 planes: P,U,V,W,T; at n-1; at n-2
+    semo::DBuf<double> cpl_eos;                   // 7 planes: rho, C, Ht, drho/dp, drho/dT, dHt/dp, dHt/dT
+    semo::DBuf<double> cpl_bR;                    // 12 planes of nb: boundary right primitives + EOS
+    semo::DBuf<double> cpl_grad, cpl_mm;          // 15 planes of gradients; 10 planes of stencil limits
+    semo::DBuf<double> cpl_val;                   // 25 per slot of the scalar pattern
+    semo::DBuf<double> cpl_b, cpl_x;              // 5 planes each (field-split)
+    semo::DBuf<double> cpl_scr;                   // 5 planes of nf face fluxes + 27 planes of nb
+    semo::DBuf<double> cpl_lim;                   // 10 update clamps
+    std::shared_ptr<void> cpl_solver;             // solver state (coupled.cu)
     std::shared_ptr<void> mom_apply;              // momentum Krylov state (cycle.cu)
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
@@ -282,6 +298,16 @@ bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst
 void fields_to_caller_order(semo_ctx* c, const double* const* src, double* dst, int planes);
 // out[i] = a[i] * b[i] over the cells (async)
 void cellwise_product(semo_ctx* c, const double* a, const double* b, double* out);
+
+// LSQ gradients (15 planes) and stencil limits (10 planes) of five cell
+// fields f0..f4 with boundary-face values bf (5 planes of nb)
+void lsq_gradients5(semo_ctx* c, const double* f0, const double* f1, const double* f2, const double* f3,
+                    const double* f4, const double* bf, double* grad, double* mm);
+
+// coupled.cu: compressible coupled 5x5 system
+void coupled_assemble(semo_ctx* c);
+semo_status coupled_solve(semo_ctx* c, semo_solve_info* info);   // c->cpl_b -> c->cpl_x
+double coupled_update(semo_ctx* c);
 
 // amg_setup.cu: smoothed-aggregation hierarchy (value type float or double)
 template <class V>
