@@ -335,9 +335,11 @@ semo_status semo_get_coupled_system(semo_ctx* ctx, int32_t* ptr, int32_t* col, d
                                     int64_t* nnz);
 
 /* Solve the assembled system to params.tol (FP64 relative residual); x
-   field-split in the caller's order.  Mixed precision: block-Jacobi
-   BiCGStab in FP32 as the inner solve of FP64 defect correction; FP64: the
-   same BiCGStab in FP64. */
+   field-split in the caller's order.  BiCGStab preconditioned by an AMG
+   V-cycle on a pressure equation formed from the blocks, followed by the
+   inverses of the 5x5 diagonal blocks; mixed precision multiplies by an
+   FP32 copy of the matrix and runs the preconditioner in FP32 inside FP64
+   defect correction. */
 semo_status semo_solve_coupled(semo_ctx* ctx, double* x, semo_solve_info* info);
 
 /* One calcCompCoupledEq: EOS, gradients, assembly, solve, update and the

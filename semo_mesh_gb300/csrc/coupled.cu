@@ -17,9 +17,12 @@
 //                                                     coupled.cpp:318-625
 //   k_cupdate  relaxation, clamps, norm               coupled.cpp:2494-2708
 // The solver (solveAMGCL("coupled"), src/solvers/solveAMGCL.cpp:485-520,
-// is FGMRES over ILU0 there) is BiCGStab preconditioned by the inverses of
-// the 5x5 diagonal blocks; in mixed mode it runs in FP32 on an FP32 copy of
-// the matrix as the inner solve of FP64 defect correction.
+// is FGMRES over ILU0 there) is FP64 BiCGStab with a two-stage
+// preconditioner: a smoothed-aggregation AMG V-cycle on a pressure equation
+// formed from the blocks, then the inverses of the 5x5 diagonal blocks on
+// the rest.  In mixed mode the matrix copy the iterations multiply by and
+// the preconditioner are FP32, inside FP64 defect correction against the
+// FP64 blocks.
 //
 // Layout: cells in RCM order, faces in stored order; blocks are 25 doubles
 // per slot of the scalar CSR pattern (A_ptr/A_col), row-major (equation a,
@@ -446,8 +449,9 @@ __global__ void __launch_bounds__(128) k_ccell(CplArgs a) {
 namespace {
 
 // ---------------------------------------------------------------------------
-// solver: block SELL-32 copy of the matrix (values in V), BiCGStab with the
-// inverses of the 5x5 diagonal blocks.  Inner vectors are interleaved per
+// solver: block SELL-32 copy of the matrix (values in M = float or double),
+// BiCGStab in FP64 preconditioned by AMG on a pressure equation and the
+// inverses of the 5x5 diagonal blocks.  Krylov vectors are interleaved per
 // cell (v[5 i + a]) so one gather fetches a cell's five unknowns.
 // ---------------------------------------------------------------------------
 constexpr int kT = 256;
@@ -467,10 +471,10 @@ __global__ void k_bsell_width(int nc, const int* __restrict__ ptr, int* __restri
 
 // off32[c] = first slot row of chunk c; slot row s holds 32 columns
 // (col[32 s + lane]) and 25 x 32 values (val[(25 s + e) 32 + lane])
-template <class V>
+template <class M>
 __global__ void k_bsell_fill(int nc, const int* __restrict__ ptr, const int* __restrict__ colA,
                              const double* __restrict__ valA, const int* __restrict__ off32,
-                             const int* __restrict__ width, int* __restrict__ col, V* __restrict__ val,
+                             const int* __restrict__ width, int* __restrict__ col, M* __restrict__ val,
                              bool pattern) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
@@ -481,13 +485,13 @@ __global__ void k_bsell_fill(int nc, const int* __restrict__ ptr, const int* __r
         if (pattern) col[32 * s + l] = (j < len) ? colA[kb + j] : -1;
         const double* src = valA + 25 * (int64_t)(kb + j);
 #pragma unroll 5
-        for (int e = 0; e < 25; ++e) val[(25 * s + e) * 32 + l] = (j < len) ? (V)src[e] : (V)0;
+        for (int e = 0; e < 25; ++e) val[(25 * s + e) * 32 + l] = (j < len) ? (M)src[e] : (M)0;
     }
 }
 
 // inverse of each diagonal block (Gauss-Jordan with partial pivoting, FP64)
-template <class V>
-__global__ void k_binv(int nc, const int* __restrict__ dig, const double* __restrict__ valA, V* __restrict__ minv,
+template <class M>
+__global__ void k_binv(int nc, const int* __restrict__ dig, const double* __restrict__ valA, M* __restrict__ minv,
                        int* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
@@ -531,41 +535,53 @@ __global__ void k_binv(int nc, const int* __restrict__ dig, const double* __rest
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
-        for (int q = 0; q < 5; ++q) minv[25 * (int64_t)i + 5 * r + q] = (V)x[r][q];
+        for (int q = 0; q < 5; ++q) minv[25 * (int64_t)i + 5 * r + q] = (M)x[r][q];
 }
 
-template <class V>
+// Krylov vectors are FP64; the matrix copy and the preconditioner are M
+// (float in mixed mode, double in FP64 mode).  The block products run in M
+// too: a 5x5 block costs 25 fused multiply-adds against 100-200 bytes, which
+// at this part's FP64 issue rate (1/58 of FP32) would bound the product
+// below the HBM rate; in mixed mode the gathered x is rounded to FP32 and
+// only the row sums go back to FP64.
+template <class M>
 __device__ __forceinline__ void bmv_row(int i, const int* __restrict__ off32, const int* __restrict__ width,
-                                        const int* __restrict__ col, const V* __restrict__ val,
-                                        const V* __restrict__ x, V* acc) {
+                                        const int* __restrict__ col, const M* __restrict__ val,
+                                        const double* __restrict__ x, double* out) {
     const int c = i >> 5, l = i & 31;
     const int s0 = off32[c], w = width[c];
+    M acc[5];
 #pragma unroll
-    for (int a = 0; a < 5; ++a) acc[a] = (V)0;
+    for (int a = 0; a < 5; ++a) acc[a] = (M)0;
     for (int j = 0; j < w; ++j) {
         const int64_t s = s0 + j;
         const int jc = col[32 * s + l];
         if (jc < 0) continue;
-        V xv[5];
+        M xv[5];
 #pragma unroll
-        for (int b = 0; b < 5; ++b) xv[b] = x[5 * (int64_t)jc + b];
-        const V* vs = val + 25 * s * 32 + l;
+        for (int b = 0; b < 5; ++b) xv[b] = (M)x[5 * (int64_t)jc + b];
+        const M* vs = val + 25 * s * 32 + l;
 #pragma unroll
         for (int a = 0; a < 5; ++a)
 #pragma unroll
             for (int b = 0; b < 5; ++b) acc[a] += vs[(5 * a + b) * 32] * xv[b];
     }
+#pragma unroll
+    for (int a = 0; a < 5; ++a) out[a] = (double)acc[a];
 }
 
-template <class V>
-__device__ __forceinline__ void bapply(const V* __restrict__ minv, int64_t i, const V* in, V* out) {
-    const V* m = minv + 25 * i;
+template <class M>
+__device__ __forceinline__ void bapply(const M* __restrict__ minv, int64_t i, const double* in, double* out) {
+    const M* m = minv + 25 * i;
+    M v[5];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) v[b] = (M)in[b];
 #pragma unroll
     for (int a = 0; a < 5; ++a) {
-        V t = (V)0;
+        M t = (M)0;
 #pragma unroll
-        for (int b = 0; b < 5; ++b) t += m[5 * a + b] * in[b];
-        out[a] = t;
+        for (int b = 0; b < 5; ++b) t += m[5 * a + b] * v[b];
+        out[a] = (double)t;
     }
 }
 
@@ -575,19 +591,19 @@ __global__ void k_bi_init_sc(double* __restrict__ sc) {
     sc[0] = 1.0; sc[1] = 1.0; sc[2] = 1.0; sc[3] = 0.0; sc[7] = 0.0;
 }
 
-// r = rh = src (field-split FP64 in, interleaved V out), p = v = z = 0; partial <r,r>
-template <class V>
-__global__ void k_bi_start(int nc, const double* __restrict__ src, V* __restrict__ r, V* __restrict__ rh,
-                           V* __restrict__ p, V* __restrict__ v, V* __restrict__ z, double* __restrict__ part) {
+// r = rh = src (field-split in, interleaved out), p = v = z = 0; partial <r,r>
+__global__ void k_bi_start(int nc, const double* __restrict__ src, double* __restrict__ r, double* __restrict__ rh,
+                           double* __restrict__ p, double* __restrict__ v, double* __restrict__ z,
+                           double* __restrict__ part) {
     __shared__ double sh[32];
     double acc = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
 #pragma unroll
         for (int a = 0; a < 5; ++a) {
-            const V xv = (V)src[(int64_t)a * nc + i];
+            const double xv = src[(int64_t)a * nc + i];
             const int64_t q = 5 * (int64_t)i + a;
-            r[q] = xv; rh[q] = xv; p[q] = (V)0; v[q] = (V)0; z[q] = (V)0;
-            acc += (double)xv * (double)xv;
+            r[q] = xv; rh[q] = xv; p[q] = 0.0; v[q] = 0.0; z[q] = 0.0;
+            acc += xv * xv;
         }
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
@@ -610,41 +626,31 @@ __global__ void k_bi_beta(double* __restrict__ sc) {
     sc[0] = rho1;
 }
 
-// p = r + beta (p - omega v); y = M^-1 p
-template <class V>
-__global__ void k_bi_p(int nc, const double* __restrict__ sc, const V* __restrict__ r, V* __restrict__ p,
-                       const V* __restrict__ v, const V* __restrict__ minv, V* __restrict__ y) {
-    const V beta = (V)sc[3], omega = (V)sc[2];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
-        V pv[5], yv[5];
-#pragma unroll
-        for (int a = 0; a < 5; ++a) {
-            const int64_t q = 5 * (int64_t)i + a;
-            pv[a] = r[q] + beta * (p[q] - omega * v[q]);
-            p[q] = pv[a];
-        }
-        bapply(minv, i, pv, yv);
-#pragma unroll
-        for (int a = 0; a < 5; ++a) y[5 * (int64_t)i + a] = yv[a];
-    }
+// p = r + beta (p - omega v)
+__global__ void k_bi_p(int nc, const double* __restrict__ sc, const double* __restrict__ r, double* __restrict__ p,
+                       const double* __restrict__ v) {
+    const double beta = sc[3], omega = sc[2];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 5 * (int64_t)nc;
+         q += (int64_t)gridDim.x * blockDim.x)
+        p[q] = r[q] + beta * (p[q] - omega * v[q]);
 }
 
 // out = A in; partial sums of <w1, out> (and <out, out> when kTwo)
-template <class V, bool kTwo>
+template <class M, bool kTwo>
 __global__ void k_bi_mv(int nc, const int* __restrict__ off32, const int* __restrict__ width,
-                        const int* __restrict__ col, const V* __restrict__ val, const V* __restrict__ in,
-                        V* __restrict__ out, const V* __restrict__ w1, double* __restrict__ part) {
+                        const int* __restrict__ col, const M* __restrict__ val, const double* __restrict__ in,
+                        double* __restrict__ out, const double* __restrict__ w1, double* __restrict__ part) {
     __shared__ double sh[32];
     double d1 = 0.0, d2 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
-        V acc[5];
+        double acc[5];
         bmv_row(i, off32, width, col, val, in, acc);
 #pragma unroll
         for (int a = 0; a < 5; ++a) {
             const int64_t q = 5 * (int64_t)i + a;
             out[q] = acc[a];
-            d1 += (double)w1[q] * (double)acc[a];
-            if (kTwo) d2 += (double)acc[a] * (double)acc[a];
+            d1 += w1[q] * acc[a];
+            if (kTwo) d2 += acc[a] * acc[a];
         }
     }
     d1 = block_sum(d1, sh);
@@ -669,23 +675,15 @@ __global__ void k_bi_alpha(const double* __restrict__ part, double* __restrict__
     }
 }
 
-// z += alpha y; s = r - alpha v; y = M^-1 s
-template <class V>
-__global__ void k_bi_s(int nc, const double* __restrict__ sc, const V* __restrict__ r, const V* __restrict__ v,
-                       V* __restrict__ s, V* __restrict__ z, V* __restrict__ y, const V* __restrict__ minv) {
-    const V alpha = (V)sc[1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
-        V sv[5], yv[5];
-#pragma unroll
-        for (int a = 0; a < 5; ++a) {
-            const int64_t q = 5 * (int64_t)i + a;
-            z[q] += alpha * y[q];
-            sv[a] = r[q] - alpha * v[q];
-            s[q] = sv[a];
-        }
-        bapply(minv, i, sv, yv);
-#pragma unroll
-        for (int a = 0; a < 5; ++a) y[5 * (int64_t)i + a] = yv[a];
+// z += alpha y; s = r - alpha v
+__global__ void k_bi_s(int nc, const double* __restrict__ sc, const double* __restrict__ r,
+                       const double* __restrict__ v, double* __restrict__ s, double* __restrict__ z,
+                       const double* __restrict__ y) {
+    const double alpha = sc[1];
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 5 * (int64_t)nc;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        z[q] += alpha * y[q];
+        s[q] = r[q] - alpha * v[q];
     }
 }
 
@@ -701,23 +699,20 @@ __global__ void k_bi_omega(const double* __restrict__ part, double* __restrict__
 }
 
 // z += omega y; r = s - omega t; partials <r,r>, <rh,r>
-template <class V>
-__global__ void k_bi_r(int nc, const double* __restrict__ sc, const V* __restrict__ s, const V* __restrict__ t,
-                       const V* __restrict__ y, const V* __restrict__ rh, V* __restrict__ z, V* __restrict__ r,
-                       double* __restrict__ part) {
+__global__ void k_bi_r(int nc, const double* __restrict__ sc, const double* __restrict__ s,
+                       const double* __restrict__ t, const double* __restrict__ y, const double* __restrict__ rh,
+                       double* __restrict__ z, double* __restrict__ r, double* __restrict__ part) {
     __shared__ double sh[32];
-    const V omega = (V)sc[2];
+    const double omega = sc[2];
     double d1 = 0.0, d2 = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
-#pragma unroll
-        for (int a = 0; a < 5; ++a) {
-            const int64_t q = 5 * (int64_t)i + a;
-            z[q] += omega * y[q];
-            const V rv = s[q] - omega * t[q];
-            r[q] = rv;
-            d1 += (double)rv * (double)rv;
-            d2 += (double)rh[q] * (double)rv;
-        }
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 5 * (int64_t)nc;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        z[q] += omega * y[q];
+        const double rv = s[q] - omega * t[q];
+        r[q] = rv;
+        d1 += rv * rv;
+        d2 += rh[q] * rv;
+    }
     d1 = block_sum(d1, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = d1;
     __syncthreads();
@@ -733,6 +728,70 @@ __global__ void k_bi_fin_r(const double* __restrict__ part, double* __restrict__
     __syncthreads();
     b = block_sum(b, sh);
     if (threadIdx.x == 0) { sc[4] = a; sc[5] = b; }
+}
+
+// ---- two-stage preconditioner: AMG on a pressure equation, then the
+// block-Jacobi on what is left.  The pressure equation of row i combines the
+// five equations with the weights w = first row of D_i^-1 (D_i the diagonal
+// block), so its diagonal is 1 and it carries the velocity and temperature
+// couplings of the continuity row through D_i ("quasi-IMPES").
+// app[k] = sum_a w_a(i) A_k[a][0] over the slots k of row i
+template <class M>
+__global__ void k_cpr_pp(int nc, const int* __restrict__ ptr, const double* __restrict__ valA,
+                         const M* __restrict__ minv, double* __restrict__ app) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double w[5];
+#pragma unroll
+    for (int a = 0; a < 5; ++a) w[a] = (double)minv[25 * (int64_t)i + a];
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+        const double* blk = valA + 25 * (int64_t)k;
+        double t = 0.0;
+#pragma unroll
+        for (int a = 0; a < 5; ++a) t += w[a] * blk[5 * a];
+        app[k] = t;
+    }
+}
+// bp[i] = sum_a w_a(i) in[5 i + a]
+template <class M>
+__global__ void k_cpr_restrict(int nc, const M* __restrict__ minv, const double* __restrict__ in,
+                               M* __restrict__ bp) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        M t = (M)0;
+#pragma unroll
+        for (int a = 0; a < 5; ++a) t += minv[25 * (int64_t)i + a] * (M)in[5 * (int64_t)i + a];
+        bp[i] = t;
+    }
+}
+// out = D^-1 (in - A (zp e_p)) + zp e_p: the pressure correction zp enters
+// through the pressure column of every block (5 of the 25 value planes)
+template <class M>
+__global__ void k_cpr_second(int nc, const int* __restrict__ off32, const int* __restrict__ width,
+                             const int* __restrict__ col, const M* __restrict__ val, const M* __restrict__ minv,
+                             const double* __restrict__ in, const M* __restrict__ zp, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+        const int c = i >> 5, l = i & 31;
+        const int s0 = off32[c], w = width[c];
+        M acc[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) acc[a] = (M)0;
+        for (int j = 0; j < w; ++j) {
+            const int64_t s = s0 + j;
+            const int jc = col[32 * s + l];
+            if (jc < 0) continue;
+            const M z = zp[jc];
+            const M* vs = val + 25 * s * 32 + l;
+#pragma unroll
+            for (int a = 0; a < 5; ++a) acc[a] += vs[(5 * a) * 32] * z;
+        }
+        double rem[5], y[5];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) rem[a] = in[5 * (int64_t)i + a] - (double)acc[a];
+        bapply(minv, i, rem, y);
+        y[0] += (double)zp[i];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) out[5 * (int64_t)i + a] = y[a];
+    }
 }
 
 // FP64 residual r = b - A x on the slot-major blocks (thread per row),
@@ -767,11 +826,10 @@ __global__ void k_bsr_res(int nc, const int* __restrict__ ptr, const int* __rest
 }
 
 // x[a nc + i] += z[5 i + a]
-template <class V>
-__global__ void k_add_il(int nc, const V* __restrict__ z, double* __restrict__ x) {
+__global__ void k_add_il(int nc, const double* __restrict__ z, double* __restrict__ x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
 #pragma unroll
-        for (int a = 0; a < 5; ++a) x[(int64_t)a * nc + i] += (double)z[5 * (int64_t)i + a];
+        for (int a = 0; a < 5; ++a) x[(int64_t)a * nc + i] += z[5 * (int64_t)i + a];
 }
 
 __global__ void k_sum1(const double* __restrict__ part, double* __restrict__ out) {
@@ -818,9 +876,10 @@ struct CplSolver {
     int nch = 0;
     int64_t rows32 = 0;            // slot rows (of 32 lanes)
     semo::DBuf<int> width, off32, col;
-    semo::DBuf<float> val32, minv32, v32;     // v32: 8 vectors of 5 nc
-    semo::DBuf<double> val64, minv64, v64;
-    semo::DBuf<double> part, sc, r64;
+    semo::DBuf<float> val32, minv32, cp32;    // cp: restricted residual and pressure correction (2 nc)
+    semo::DBuf<double> val64, minv64, cp64;
+    semo::DBuf<double> vec;                   // 8 Krylov vectors of 5 nc
+    semo::DBuf<double> part, sc, r64, app;    // app: pressure-equation values on the scalar pattern
 };
 
 CplSolver& solver_state(semo_ctx* c) {
@@ -844,25 +903,36 @@ CplArgs make_args(semo_ctx* c) {
     return a;
 }
 
-// BiCGStab on A z = src (src field-split FP64), right-preconditioned by the
-// block inverses, to rel_tol of ||src||; the solution is left in vec's 8th
-// vector (interleaved).  One host read of the residual per iteration.
-template <class V>
-int bicgstab_inner(semo_ctx* c, CplSolver& S, const V* val, const V* minv, V* vec, const double* src,
+// BiCGStab on A z = src (src field-split FP64) with the two-stage
+// preconditioner, to rtol of ||src||; z is left in the 8th Krylov vector
+// (interleaved).  One host read of the residual per iteration.
+template <class M>
+int bicgstab_inner(semo_ctx* c, CplSolver& S, const M* val, const M* minv, M* cpbuf, const double* src,
                    double rtol, int maxit, double* rel_out, bool* breakdown) {
     using namespace semo;
     cudaStream_t s = c->stream;
     const int nc = c->nc;
     const size_t n5 = 5 * (size_t)nc;
-    V *r = vec, *rh = vec + n5, *p = vec + 2 * n5, *v = vec + 3 * n5, *sv = vec + 4 * n5, *t = vec + 5 * n5;
-    V *y = vec + 6 * n5, *z = vec + 7 * n5;
+    double* vec = S.vec;
+    double *r = vec, *rh = vec + n5, *p = vec + 2 * n5, *v = vec + 3 * n5, *sv = vec + 4 * n5, *t = vec + 5 * n5;
+    double *y = vec + 6 * n5, *z = vec + 7 * n5;
     double* part = S.part;
     double* sc = S.sc;
     if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* h = c->hpin;
+    // y = M^-1 in
+    auto precond = [&](const double* in) {
+        M* bp = cpbuf;
+        M* zp = cpbuf + nc;
+        k_cpr_restrict<M><<<kRedBlocks, kT, 0, s>>>(nc, minv, in, bp);
+        SEMO_CHECK_LAUNCH();
+        cpr_vcycle<M>(c, bp, zp);
+        k_cpr_second<M><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, minv, in, zp, y);
+        SEMO_CHECK_LAUNCH();
+    };
     k_bi_init_sc<<<1, 1, 0, s>>>(sc);
     SEMO_CHECK_LAUNCH();
-    k_bi_start<V><<<kRedBlocks, kT, 0, s>>>(nc, src, r, rh, p, v, z, part);
+    k_bi_start<<<kRedBlocks, kT, 0, s>>>(nc, src, r, rh, p, v, z, part);
     SEMO_CHECK_LAUNCH();
     k_bi_fin_start<<<1, kT, 0, s>>>(part, sc);
     SEMO_CHECK_LAUNCH();
@@ -873,22 +943,25 @@ int bicgstab_inner(semo_ctx* c, CplSolver& S, const V* val, const V* minv, V* ve
     if (bn == 0.0) { *rel_out = 0.0; return 0; }
     int it = 0;
     double rel = 1.0;
+    std::vector<double> hist;
     while (it < maxit) {
         k_bi_beta<<<1, 1, 0, s>>>(sc);
         SEMO_CHECK_LAUNCH();
-        k_bi_p<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, r, p, v, minv, y);
+        k_bi_p<<<kRedBlocks, kT, 0, s>>>(nc, sc, r, p, v);
         SEMO_CHECK_LAUNCH();
-        k_bi_mv<V, false><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, v, rh, part);
+        precond(p);
+        k_bi_mv<M, false><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, v, rh, part);
         SEMO_CHECK_LAUNCH();
         k_bi_alpha<<<1, kT, 0, s>>>(part, sc);
         SEMO_CHECK_LAUNCH();
-        k_bi_s<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, r, v, sv, z, y, minv);
+        k_bi_s<<<kRedBlocks, kT, 0, s>>>(nc, sc, r, v, sv, z, y);
         SEMO_CHECK_LAUNCH();
-        k_bi_mv<V, true><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, t, sv, part);
+        precond(sv);
+        k_bi_mv<M, true><<<kRedBlocks, kT, 0, s>>>(nc, S.off32, S.width, S.col, val, y, t, sv, part);
         SEMO_CHECK_LAUNCH();
         k_bi_omega<<<1, kT, 0, s>>>(part, sc);
         SEMO_CHECK_LAUNCH();
-        k_bi_r<V><<<kRedBlocks, kT, 0, s>>>(nc, sc, sv, t, y, rh, z, r, part);
+        k_bi_r<<<kRedBlocks, kT, 0, s>>>(nc, sc, sv, t, y, rh, z, r, part);
         SEMO_CHECK_LAUNCH();
         k_bi_fin_r<<<1, kT, 0, s>>>(part, sc);
         SEMO_CHECK_LAUNCH();
@@ -898,6 +971,10 @@ int bicgstab_inner(semo_ctx* c, CplSolver& S, const V* val, const V* minv, V* ve
         rel = std::sqrt(h[4]) / bn;
         if (h[7] != 0.0 || !std::isfinite(rel)) { *breakdown = true; break; }
         if (rel <= rtol) break;
+        // stagnation (an FP32 matrix copy limits the attainable accuracy):
+        // less than 10 % progress over the last 20 iterations ends the inner solve
+        hist.push_back(rel);
+        if (hist.size() > 20 && rel > 0.9 * hist[hist.size() - 21]) break;
     }
     *rel_out = rel;
     return it;
@@ -949,6 +1026,26 @@ void coupled_assemble(semo_ctx* c) {
     c->cpl_assembled = true;
 }
 
+template <class M>
+void prepare_blocks(semo_ctx* c, CplSolver& S, DBuf<M>& val, DBuf<M>& minv, DBuf<M>& cp) {
+    cudaStream_t s = c->stream;
+    const int nc = c->nc;
+    const bool pattern = S.val32.n == 0 && S.val64.n == 0;
+    val.alloc(25 * 32 * (size_t)S.rows32, s);
+    minv.alloc(25 * (size_t)nc, s);
+    cp.alloc(2 * (size_t)nc, s);
+    k_bsell_fill<M><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, S.off32, S.width, S.col, val,
+                                                 pattern);
+    SEMO_CHECK_LAUNCH();
+    k_binv<M><<<blocks(nc, 128), 128, 0, s>>>(nc, c->A_dig, c->cpl_val, minv, c->flag.p + 12);
+    SEMO_CHECK_LAUNCH();
+    // pressure equation and its AMG hierarchy
+    S.app.alloc((size_t)c->nnz, s);
+    k_cpr_pp<M><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->cpl_val, minv, S.app);
+    SEMO_CHECK_LAUNCH();
+    cpr_setup<M>(c, c->A_ptr, c->A_col, S.app, nc, c->nnz);
+}
+
 semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     cudaStream_t s = c->stream;
     const int nc = c->nc;
@@ -975,27 +1072,8 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     }
     SEMO_CUDA(cudaMemsetAsync(c->flag.p + 12, 0, sizeof(int), s));
     const size_t n5 = 5 * (size_t)nc;
-    if (mixed) {
-        const bool pattern = S.val32.n == 0 && S.val64.n == 0;
-        S.val32.alloc(25 * 32 * (size_t)S.rows32, s);
-        S.minv32.alloc(25 * (size_t)nc, s);
-        S.v32.alloc(8 * n5, s);
-        k_bsell_fill<float><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, S.off32, S.width, S.col,
-                                                         S.val32, pattern);
-        SEMO_CHECK_LAUNCH();
-        k_binv<float><<<blocks(nc, 128), 128, 0, s>>>(nc, c->A_dig, c->cpl_val, S.minv32, c->flag.p + 12);
-        SEMO_CHECK_LAUNCH();
-    } else {
-        const bool pattern = S.val32.n == 0 && S.val64.n == 0;
-        S.val64.alloc(25 * 32 * (size_t)S.rows32, s);
-        S.minv64.alloc(25 * (size_t)nc, s);
-        S.v64.alloc(8 * n5, s);
-        k_bsell_fill<double><<<blocks(nc, kT), kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, S.off32, S.width,
-                                                          S.col, S.val64, pattern);
-        SEMO_CHECK_LAUNCH();
-        k_binv<double><<<blocks(nc, 128), 128, 0, s>>>(nc, c->A_dig, c->cpl_val, S.minv64, c->flag.p + 12);
-        SEMO_CHECK_LAUNCH();
-    }
+    if (mixed) prepare_blocks<float>(c, S, S.val32, S.minv32, S.cp32);
+    else prepare_blocks<double>(c, S, S.val64, S.minv64, S.cp64);
     SEMO_CUDA(cudaEventRecord(e1, s));
     int singular = 0;
     SEMO_CUDA(cudaMemcpyAsync(&singular, c->flag.p + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1004,6 +1082,7 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     // defect correction: x = 0; r = b - A x; inner solve of A z = r; x += z
     c->cpl_x.alloc(n5, s);
     S.r64.alloc(n5, s);
+    S.vec.alloc(8 * n5, s);
     c->cpl_x.zero();
     const double tol = c->prm.tol;
     const int maxit = c->prm.max_iter > 0 ? c->prm.max_iter : 1000;
@@ -1026,15 +1105,16 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
         double inner_rel = 0.0;
         int it;
         if (mixed) {
-            // FP32 reduces the defect by about 1e-3 per outer step
-            it = bicgstab_inner<float>(c, S, S.val32, S.minv32, S.v32, S.r64, std::max(1e-3, 0.5 * tol / rel),
+            // the inner solve multiplies by the FP32 copy, whose solution is
+            // within ~1e-6 of the FP64 one: each step reduces the defect by up
+            // to 1e-5, two steps reach 1e-8
+            it = bicgstab_inner<float>(c, S, S.val32, S.minv32, S.cp32, S.r64, std::max(1e-5, 0.5 * tol / rel),
                                        maxit - total, &inner_rel, &brk);
-            k_add_il<float><<<kRedBlocks, kT, 0, s>>>(nc, S.v32.p + 7 * n5, c->cpl_x);
         } else {
-            it = bicgstab_inner<double>(c, S, S.val64, S.minv64, S.v64, S.r64, 0.5 * tol / rel, maxit - total,
+            it = bicgstab_inner<double>(c, S, S.val64, S.minv64, S.cp64, S.r64, 0.5 * tol / rel, maxit - total,
                                         &inner_rel, &brk);
-            k_add_il<double><<<kRedBlocks, kT, 0, s>>>(nc, S.v64.p + 7 * n5, c->cpl_x);
         }
+        k_add_il<<<kRedBlocks, kT, 0, s>>>(nc, S.vec.p + 7 * n5, c->cpl_x);
         SEMO_CHECK_LAUNCH();
         total += it;
         ++outer;

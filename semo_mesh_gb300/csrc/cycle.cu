@@ -1390,4 +1390,57 @@ void solve_transpose_reuse(semo_ctx* c, const double* g, double* lam, semo_solve
     info->solve_ms = t1;
 }
 
+// ---- AMG on the pressure equation of the coupled system (first stage of its
+// two-stage preconditioner).  A hierarchy of its own, so the pressure
+// equation's hierarchy is left as it is.
+struct CprState {
+    Amg<float> h32;
+    Cycle<float> cy32;
+    Amg<double> h64;
+    Cycle<double> cy64;
+};
+CprState& cpr_state(semo_ctx* c) {
+    if (!c->cpr) c->cpr = std::shared_ptr<void>(new CprState(), [](void* p) { delete (CprState*)p; });
+    return *(CprState*)c->cpr.get();
+}
+template <class V> Amg<V>& cpr_h(CprState& S);
+template <> Amg<float>& cpr_h<float>(CprState& S) { return S.h32; }
+template <> Amg<double>& cpr_h<double>(CprState& S) { return S.h64; }
+template <class V> Cycle<V>& cpr_cy(CprState& S);
+template <> Cycle<float>& cpr_cy<float>(CprState& S) { return S.cy32; }
+template <> Cycle<double>& cpr_cy<double>(CprState& S) { return S.cy64; }
+
+template <class V>
+void cpr_setup(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz) {
+    CprState& S = cpr_state(c);
+    build_hierarchy<V>(c, cpr_h<V>(S), ptr, col, val, n, nnz);
+    prepare_cycle(c, cpr_h<V>(S), cpr_cy<V>(S));
+}
+
+// x = one V-cycle (zero start, both smoothing sweeps on every level) applied to b
+template <class V>
+void cpr_vcycle(semo_ctx* c, const V* b, V* x) {
+    CprState& S = cpr_state(c);
+    Amg<V>& h = cpr_h<V>(S);
+    Cycle<V>& cy = cpr_cy<V>(S);
+    cudaStream_t s = c->stream;
+    AmgLevel<V>& L = h.lev[0];
+    const int n = L.A.n;
+    SEMO_CUDA(cudaMemcpyAsync(L.b.p, b, sizeof(V) * n, cudaMemcpyDeviceToDevice, s));
+    vcycle_from(c, h, cy, 0);
+    if (h.lev.size() > 1 && c->prm.cheb_degree == 2) {
+        // the last step vcycle_from leaves to the fused CG kernels on the finest level
+        const ChebCoef cc = cheb2(L.lam_max);
+        with_A(cy.lev[0], L.A, [&](auto A) {
+            k_post1<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
+        });
+        SEMO_CHECK_LAUNCH();
+    }
+    SEMO_CUDA(cudaMemcpyAsync(x, L.x.p, sizeof(V) * n, cudaMemcpyDeviceToDevice, s));
+}
+template void cpr_setup<float>(semo_ctx*, const int*, const int*, const double*, int, int64_t);
+template void cpr_setup<double>(semo_ctx*, const int*, const int*, const double*, int, int64_t);
+template void cpr_vcycle<float>(semo_ctx*, const float*, float*);
+template void cpr_vcycle<double>(semo_ctx*, const double*, double*);
+
 }  // namespace semo

@@ -204,6 +204,7 @@ struct semo_ctx {
     semo::DBuf<double> cpl_scr;                   // 5 planes of nf face fluxes + 27 planes of nb
     semo::DBuf<double> cpl_lim;                   // 10 update clamps
     std::shared_ptr<void> cpl_solver;             // solver state (coupled.cu)
+    std::shared_ptr<void> cpr;                    // AMG on the coupled pressure equation (cycle.cu)
     std::shared_ptr<void> mom_apply;              // momentum Krylov state (cycle.cu)
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
@@ -303,6 +304,13 @@ void cellwise_product(semo_ctx* c, const double* a, const double* b, double* out
 // fields f0..f4 with boundary-face values bf (5 planes of nb)
 void lsq_gradients5(semo_ctx* c, const double* f0, const double* f1, const double* f2, const double* f3,
                     const double* f4, const double* bf, double* grad, double* mm);
+
+// cycle.cu: AMG on the pressure equation of the coupled system (value type float or double)
+template <class V>
+void cpr_setup(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz);
+// x = one V-cycle on b (device arrays of n)
+template <class V>
+void cpr_vcycle(semo_ctx* c, const V* b, V* x);
 
 // coupled.cu: compressible coupled 5x5 system
 void coupled_assemble(semo_ctx* c);
