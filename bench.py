@@ -339,7 +339,12 @@ def run_gpu_arm(args, rank, world, local) -> None:
     ctx64.close()
 
     # ---- compressible coupled 5x5 system (6 tetrahedra per hex) -------------
-    coupled = coupled_bench(args, S, torch, local) if args.coupled_n > 0 else None
+    coupled = None
+    if args.coupled_n > 0:
+        try:
+            coupled = coupled_bench(args, S, torch, local)
+        except S.SemoError as e:   # reported, never allowed to take the headline down
+            coupled = {"error": str(e)}
 
     if rank != 0:
         if world > 1:
@@ -432,9 +437,10 @@ def coupled_bench(args, S, torch, local) -> dict:
     """calcCompCoupledEq on the tetrahedral ideal-gas case, FP64 and mixed.
 
     A step is one coupled pass (EOS, gradients, 5x5 block assembly, solve to
-    a 1e-8 FP64 relative residual, update); successive steps continue from
-    the updated fields.  Fields resident in HBM; CUDA events on the
-    context's stream."""
+    a 1e-8 FP64 relative residual, update) from the case's fields: the
+    fields are put back between steps (outside the timed region; each pass
+    is timed with CUDA events on the context's stream), so every step solves
+    the same system."""
     from semo_mesh_gb300.cases import coupled_case
     case = coupled_case(args.coupled_n)
     m = case.mesh
@@ -448,19 +454,23 @@ def coupled_bench(args, S, torch, local) -> dict:
         ctx = S.Context(precision=prec, tol=1e-8, max_iter=3000, device=local)
         ctx.set_coupled_case(case)
         strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
+        fields = (case.P, case.U, case.V, case.W, case.T, *case.history())
         for _ in range(args.warmup):
+            ctx.set_coupled_fields(*fields)
             ctx.calc_comp_coupled_eq()
         ctx.set_profiling(True)
         ctx.reset_stats()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        infos = []
-        e0.record(strm)
+        infos, total = [], 0.0
         for _ in range(steps):
+            ctx.set_coupled_fields(*fields)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(strm)
             infos.append(ctx.calc_comp_coupled_eq()[1])
-        e1.record(strm)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / steps
+            e1.record(strm)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        ms = total / steps
         st = ctx.stage_times()
         free_b, total_b = torch.cuda.mem_get_info()
         out[prec] = {"value": round(m.n_cells / (ms * 1e-3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms, 3),
