@@ -121,6 +121,27 @@ semo_status semo_mesh_upload(semo_ctx* ctx, int n_points, const double* points /
                              const int32_t* owner /*n_faces*/, const int32_t* neighbour /*n_internal*/,
                              int n_patches, const int32_t* patch_start, const int32_t* patch_size);
 
+/* OpenFOAM polyMesh directories (ASCII points, faces, owner, neighbour,
+   boundary), read as SEMO_Mesh_Load::OpenFoam reads them
+   (src/load/loadOpenFoam.cpp:16-350: coordinates parsed to long double and
+   rounded to double, faces "n(p0 ... )", the neighbour list ending at ')' or
+   a negative label, patches "name { nFaces N; startFace S; }").  These two
+   need no context and no GPU; on failure semo_foam_last_error() gives the
+   message (per thread).
+   semo_foam_sizes: out6 = points, faces, internal faces, cells, face-point
+   entries, patches.
+   semo_foam_read: fills caller arrays of those sizes (points 3 per point,
+   face_ptr n_faces+1); patch_names n_patches x 64 chars, NUL-terminated. */
+semo_status semo_foam_sizes(const char* dir, int64_t* out6);
+semo_status semo_foam_read(const char* dir, double* points, int32_t* face_ptr, int32_t* face_pts, int32_t* owner,
+                           int32_t* neighbour, int32_t* patch_start, int32_t* patch_size, char* patch_names);
+const char* semo_foam_last_error(void);
+
+/* Read an OpenFOAM polyMesh directory and upload it (semo_mesh_upload on the
+   arrays read).  Replaces: SEMO_Mesh_Load::OpenFoam (src/load/load.h:58,
+   src/load/loadOpenFoam.cpp:8-383) with its post-load sequence. */
+semo_status semo_mesh_load_foam(semo_ctx* ctx, const char* dir);
+
 /* RCM permutation, bit-exact with SEMO_Utility_Math::lib_RCM
    (src/math/RCM.cpp:199-201): perm[r] = original cell at RCM position r
    (cells[r].RCM), iperm[c] = RCM position of original cell c (cells[c].invRCM). */

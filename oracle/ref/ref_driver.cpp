@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../solvers/build.h"
+#include "../load/load.h"
 #include "../mesh/geometric.h"
 #include "../math/math.h"
 
@@ -85,8 +86,41 @@ template <class T> static void rd(FILE* f, T* p, size_t n) {
     if (n && fread(p, sizeof(T), n, f) != n) { fprintf(stderr, "short read\n"); exit(2); }
 }
 
+// "foam <dir> <out.bin>": load an OpenFOAM polyMesh directory with the
+// reference's own loader (src/load/loadOpenFoam.cpp:8-383) and dump what it
+// read: points, face point lists, owner, neighbour (internal faces), patches.
+static int dump_foam(const char* dir, const char* out) {
+    SEMO_Mesh_Builder mesh;
+    SEMO_Mesh_Load load;
+    load.OpenFoam(mesh, dir);
+    FILE* o = fopen(out, "wb");
+    if (!o) { perror(out); return 2; }
+    auto w32 = [&](int32_t v) { fwrite(&v, 4, 1, o); };
+    w32((int32_t)mesh.points.size());
+    for (auto& p : mesh.points) { double x[3] = {p.x, p.y, p.z}; fwrite(x, 8, 3, o); }
+    w32((int32_t)mesh.faces.size());
+    for (auto& f : mesh.faces) {
+        w32((int32_t)f.points.size());
+        for (int q : f.points) w32(q);
+    }
+    for (auto& f : mesh.faces) w32(f.owner);
+    int32_t ni = 0;
+    for (auto& f : mesh.faces) ni += f.neighbour >= 0;
+    w32(ni);
+    for (auto& f : mesh.faces) if (f.neighbour >= 0) w32(f.neighbour);
+    w32((int32_t)mesh.boundary.size());
+    for (auto& b : mesh.boundary) {
+        w32((int32_t)b.name.size());
+        fwrite(b.name.data(), 1, b.name.size(), o);
+        w32(b.startFace); w32(b.nFaces);
+    }
+    fclose(o);
+    return 0;
+}
+
 int main(int argc, char** argv) {
-    if (argc < 3) { fprintf(stderr, "usage: %s case.bin out.bin\n", argv[0]); return 2; }
+    if (argc >= 4 && !strcmp(argv[1], "foam")) return dump_foam(argv[2], argv[3]);
+    if (argc < 3) { fprintf(stderr, "usage: %s case.bin out.bin | foam <dir> <out.bin>\n", argv[0]); return 2; }
     FILE* f = fopen(argv[1], "rb");
     if (!f) { perror(argv[1]); return 2; }
     int32_t hdr[8]; rd(f, hdr, 8);

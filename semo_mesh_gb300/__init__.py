@@ -121,6 +121,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_assemble_vof.argtypes = [vp]
     L.semo_get_vof_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
     L.semo_solve_vof.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
+    L.semo_foam_sizes.argtypes = [C.c_char_p, C.POINTER(C.c_int64)]
+    L.semo_foam_read.argtypes = [C.c_char_p, f64p, i32p, i32p, i32p, i32p, i32p, i32p, C.c_char_p]
+    L.semo_foam_last_error.restype = C.c_char_p
+    L.semo_mesh_load_foam.argtypes = [vp, C.c_char_p]
     L.semo_set_coupled_physics.argtypes = [vp, C.POINTER(CoupledPhysics), i32p, f64p]
     L.semo_set_coupled_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
     L.semo_get_coupled_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p]
@@ -206,6 +210,17 @@ class Context:
                                             len(mesh.patch_names), keep[4][1], keep[5][1]))
         self.mesh = mesh
         self.n_cells = mesh.n_cells
+
+    def load_foam(self, directory: str, mesh=None) -> None:
+        """Read an OpenFOAM polyMesh directory and upload it (semo_mesh_load_foam).
+
+        ``mesh`` (a PolyMesh of the same directory, e.g. from
+        ``foam.read_polymesh``) is kept for the case helpers that need the
+        patch layout."""
+        from .foam import read_polymesh
+        self._check(self.L.semo_mesh_load_foam(self.h, directory.encode()))
+        self.mesh = mesh if mesh is not None else read_polymesh(directory)
+        self.n_cells = self.mesh.n_cells
 
     def set_physics(self, case) -> None:
         ph = Physics()

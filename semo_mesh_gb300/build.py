@@ -30,6 +30,7 @@ UNITS = [
     ("cycle.cu", []),
     ("noalloc.cu", []),
     ("capi.cpp", []),
+    ("foam.cpp", []),
     ("rcm.cpp", []),
 ]
 

@@ -7,9 +7,11 @@ reference tree nor its build.  Fixtures named outer_* hold a whole outer
 iteration (momentum equation, then the pressure correction) with seeded old
 and second-old velocities for the BDF2 term; fixtures named vofeq_* hold one
 volume-fraction sub-iteration (MSTACS reconstruction + calcVolfracEq) with
-seeded old and second-old volume fractions.
+seeded old and second-old volume fractions.  foam_* are OpenFOAM polyMesh
+directories written from seeded meshes, with foam_*_ref.npz holding what the
+reference's own loader (SEMO_Mesh_Load::OpenFoam) read from them.
 
-    python tests/golden/make_golden.py [REF_DIR]
+    python tests/golden/make_golden.py [REF_DIR] [--foam-only]
 """
 from __future__ import annotations
 
@@ -98,10 +100,69 @@ def save(name: str, case, ref: dict, momentum: bool = False, vof: bool = False) 
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
+def foam_cases():
+    """Meshes written as OpenFOAM polyMesh directories (tests/golden/foam_*)."""
+    from semo_mesh_gb300.meshgen import hex_box, tet_box
+    yield "foam_hex4j", hex_box(4, jitter=0.2, seed=7)
+    yield "foam_tet2j", tet_box(2, jitter=0.2, seed=8)
+
+
+def parse_foam_dump(path: str) -> dict:
+    """The binary dump of `semo_ref foam` (oracle/ref/ref_driver.cpp)."""
+    raw = open(path, "rb").read()
+    pos = 0
+
+    def i32(k=1):
+        nonlocal pos
+        v = np.frombuffer(raw, dtype=np.int32, count=k, offset=pos)
+        pos += 4 * k
+        return v
+
+    np_ = int(i32()[0])
+    pts = np.frombuffer(raw, dtype=np.float64, count=3 * np_, offset=pos).copy()
+    pos += 24 * np_
+    nf = int(i32()[0])
+    fptr, fpts = [0], []
+    for _ in range(nf):
+        n = int(i32()[0])
+        fpts.extend(i32(n).tolist())
+        fptr.append(len(fpts))
+    owner = i32(nf).copy()
+    ni = int(i32()[0])
+    neighbour = i32(ni).copy()
+    npatch = int(i32()[0])
+    names, start, size = [], [], []
+    for _ in range(npatch):
+        ln = int(i32()[0])
+        names.append(raw[pos:pos + ln].decode())
+        pos += ln
+        start.append(int(i32()[0]))
+        size.append(int(i32()[0]))
+    return {"points": pts, "face_ptr": np.array(fptr, dtype=np.int32), "face_pts": np.array(fpts, dtype=np.int32),
+            "owner": owner, "neighbour": neighbour, "patch_names": np.array(names),
+            "patch_start": np.array(start, dtype=np.int32), "patch_size": np.array(size, dtype=np.int32)}
+
+
+def make_foam() -> None:
+    from semo_mesh_gb300.foam import write_polymesh
+    exe = os.path.join(ROOT, "oracle", "_ref", "semo_ref")
+    for name, mesh in foam_cases():
+        d = os.path.join(HERE, name)
+        write_polymesh(mesh, d)
+        out = os.path.join(HERE, name + ".bin")
+        subprocess.run([exe, "foam", d, out], check=True, stdout=subprocess.DEVNULL)
+        np.savez_compressed(os.path.join(HERE, f"{name}_ref.npz"), **parse_foam_dump(out))
+        os.remove(out)
+        print(name, mesh.n_cells, "cells (OpenFOAM loader)")
+
+
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference"
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref_dir}", "-j8"],
                    check=True, stdout=subprocess.DEVNULL)
+    make_foam()
+    if "--foam-only" in sys.argv:
+        return
     for name, case in golden_cases():
         ref = run_reference(case, threads=1)
         save(name, case, ref)
