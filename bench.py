@@ -535,11 +535,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--coupled-n", type=int, default=96,
                     help="hexes per edge of the tetrahedral coupled case (0 skips it)")
+    ap.add_argument("--coupled-only", action="store_true",
+                    help="run only the coupled case and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+    elif args.coupled_only:
+        import torch
+        import semo_mesh_gb300 as S
+        from semo_mesh_gb300.build import build
+        build()
+        torch.cuda.set_device(local)
+        print(json.dumps({"coupled": coupled_bench(args, S, torch, local)}), flush=True)
     else:
         run_gpu_arm(args, rank, world, local)
 

@@ -61,7 +61,7 @@ typedef struct {
     double tol;                  /* relative residual ||b-Ax||/||b|| (FP64), default 1e-8 */
     int max_iter;                /* Krylov iteration cap, default 500 */
     /* smoothed aggregation (AMGCL smoothed_aggregation semantics) */
-    double eps_strong;           /* strength threshold, halved per level; default 0.08 */
+    double eps_strong;           /* strength threshold, halved per level; default 0.03 (AMGCL: 0.08) */
     int coarse_enough;           /* direct solve at or below this size; default 64 */
     int max_levels;              /* default 24 */
     int cheb_degree;             /* Chebyshev pre/post smoothing degree; default 2 */

@@ -795,7 +795,7 @@ void orc_permute_csr(orc_ctx* c) {
 
 /* ------------------------------------------------------------------------ */
 /* Solver: smoothed-aggregation AMG (AMGCL coarsening/smoothed_aggregation   */
-/* .hpp:130-215 semantics: strength eps^2 d_i d_j < a_ij^2 with eps 0.08      */
+/* .hpp:130-215 semantics: strength eps^2 d_i d_j < a_ij^2 (eps 0.03 here)    */
 /* halved per level, filtered diagonal, omega 2/3) with MIS(2) aggregation,  */
 /* Chebyshev smoothing, dense Cholesky on the coarsest level, inside CG.     */
 /* ------------------------------------------------------------------------ */
@@ -1125,7 +1125,7 @@ int orc_solve(orc_ctx* c, int use_rcm, double tol, int maxiter, double* out_info
     A.nnz = A.ptr[A.n];
     double* b = dget(c, use_rcm ? "rcm_B" : "B");
     int n = A.n;
-    amg_t h; amg_prm prm = {0.08, 64, 24, 2};
+    amg_t h; amg_prm prm = {0.03, 64, 24, 2};
     if (amg_setup(&h, &A, &prm) != 0) { amg_free(&h); return -2; }
     double* x = dreg(c, use_rcm ? "rcm_x_orc" : "x_orc", n);
     double *r = (double*)malloc(sizeof(double) * n), *z = (double*)malloc(sizeof(double) * n);

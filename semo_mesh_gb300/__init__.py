@@ -156,7 +156,7 @@ class Context:
     """One GPU context (semo_ctx) holding a mesh, its fields and the solver."""
 
     def __init__(self, precision: str = "mixed", tol: float = 1e-8, max_iter: int = 500, device: int = 0,
-                 eps_strong: float = 0.08, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24,
+                 eps_strong: float = 0.03, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24,
                  mom_tol: float = 1e-9, mom_max_iter: int = 1000, reuse_hierarchy: bool = True):
         self.L = load_library()
         p = Params()

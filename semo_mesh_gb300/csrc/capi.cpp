@@ -54,7 +54,7 @@ void semo_params_default(semo_params* p) {
     p->precision = SEMO_PREC_MIXED;
     p->tol = 1e-8;
     p->max_iter = 500;
-    p->eps_strong = 0.08;
+    p->eps_strong = 0.03;
     p->coarse_enough = 64;
     p->max_levels = 24;
     p->cheb_degree = 2;
