@@ -16,7 +16,7 @@ def _all():
 
 def names():
     """Fixtures of one pressure-correction pass."""
-    return [n for n in _all() if not n.startswith(("outer_", "vofeq_"))]
+    return [n for n in _all() if not n.startswith(("outer_", "vofeq_", "foam_"))]
 
 
 def outer_names():
