@@ -61,6 +61,8 @@ def lib():
         L.orc_update_vof.argtypes = [vp, vp]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_coupled.argtypes = [vp, vp, vp, vp]
+        L.orc_curvature.argtypes = [vp]
+        L.orc_surface_tension.argtypes = [vp, C.c_double]
         L.orc_coupled_terms.argtypes = [C.c_int]
         L.orc_assemble_coupled.argtypes = [vp]
         L.orc_coupled_bsr.argtypes = [vp, vp]
@@ -131,6 +133,10 @@ class Oracle:
             self.set(nm, a)
         for nm, a in zip(("oldVF", "old2VF"), case.vf_history()):
             self.set(nm, a)
+        if case.sigma != 0.0:
+            # curvature and source from the case's fields, once per pass
+            # (src/solvers/pressureBased.cpp:142)
+            self.surface_tension(case.sigma)
 
     def assemble(self) -> None:
         lib().orc_assemble_pressure(self.h)
@@ -208,6 +214,10 @@ class Oracle:
         norm = self.update(sol["x"])
         sol["norm"] = norm
         return sol
+
+    def surface_tension(self, sigma: float) -> None:
+        """Curvature (kappa, ls) and the surface-tension source (src_sft, 4 per cell)."""
+        lib().orc_surface_tension(self.h, float(sigma))
 
     # ---- compressible coupled 5x5 block system --------------------------------
     def set_coupled(self, case) -> None:

@@ -13,6 +13,8 @@
 // with old and second-old velocities read from the case.  With case flag 4 the
 // pass is one volume-fraction sub-iteration instead (:104-112): MSTACS face
 // reconstruction and calcVolfracEq, with old and second-old VF from the case.
+// With case flag 8 the curvature and the surface-tension source are computed
+// after the gravity source (:142) and dumped.
 //
 // usage: semo_ref <case.bin> <out.bin>
 #include <chrono>
@@ -227,6 +229,7 @@ int main(int argc, char** argv) {
     solver.setIncomValuesLeftRightFace(mesh, controls, species);
     solver.setCellVarMinMax(mesh, controls.VF[0], controls.maximumVF[0], controls.minimumVF[0]);
     if (flags & 1) solver.calcSourceGravity(mesh, controls, species);
+    if (flags & 8) solver.calcSourceSurfaceTension(mesh, controls, species);
     auto t1 = chrono::steady_clock::now();
 
     g_out = fopen(argv[2], "wb");
@@ -263,6 +266,15 @@ int main(int argc, char** argv) {
         put("cell_vol", vol); put("cell_c", cc); put("lsq_minv", minv);
         put("stencil_ptr", sptr); put("stencil_idx", sidx);
         put("rho", rho); put("src_grav", sg); put("max_vf", mxvf); put("min_vf", mnvf);
+        if (flags & 8) {   // curvature and surface-tension source (pressureBased.cpp:142)
+            vector<double> kap(nc), ls(nc), sst(4 * nc);
+            for (int i = 0; i < nc; ++i) {
+                auto& c = mesh.cells[i];
+                kap[i] = c.var[controls.kappa]; ls[i] = c.var[controls.LS];
+                for (int k = 0; k < 4; ++k) sst[4 * i + k] = c.var[controls.sourceSurfaceTension[k]];
+            }
+            put("kappa", kap); put("ls", ls); put("src_sft", sst);
+        }
         vector<double> frl(nf), frr(nf), fpl(nf), fpr(nf), ful(3 * nf), fur(3 * nf);
         for (int i = 0; i < nf; ++i) {
             auto& fc = mesh.faces[i];

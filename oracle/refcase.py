@@ -20,10 +20,12 @@ MAGIC = 0x53454D4F
 
 def write_case(case, path: str, flags: int | None = None, momentum: bool = False, vof: bool = False) -> None:
     """flags bit 0: gravity source; bit 1: whole outer iteration (momentum, then
-    pressure); bit 2: one volume-fraction sub-iteration instead."""
+    pressure); bit 2: one volume-fraction sub-iteration instead; bit 3:
+    curvature and surface-tension source (set when the case has sigma != 0)."""
     m = case.mesh
     if flags is None:
-        flags = (1 if case.use_gravity else 0) | (2 if momentum else 0) | (4 if vof else 0)
+        flags = ((1 if case.use_gravity else 0) | (2 if momentum else 0) | (4 if vof else 0)
+                 | (8 if case.sigma != 0.0 else 0))
     with open(path, "wb") as f:
         f.write(struct.pack("<8i", MAGIC, m.n_points, m.n_faces, m.n_internal, m.n_cells,
                             len(m.patch_names), int(m.face_pts.shape[0]), flags))

@@ -43,7 +43,7 @@ typedef struct {
     /* bc per patch: type p/u/vf and values p,u,v,w,vf */
     int* bct; double* bcv;
     /* parameters */
-    double dt, rho0, rho1, mu0, mu1, urf_p, urf_u, urf_mom, urf_vof, g[3];
+    double dt, rho0, rho1, mu0, mu1, urf_p, urf_u, urf_mom, urf_vof, g[3], sigma;
     int use_gravity;
     double minP, maxP, minU, maxU, minV, maxV, minW, maxW;
     /* registry of named arrays (owned) */
@@ -507,7 +507,7 @@ void orc_destroy(orc_ctx* c) {
 void orc_set_case(orc_ctx* c, const int* bct, const double* bcv, const double* prm) {
     memcpy(c->bct, bct, sizeof(int) * 3 * c->npatch);
     memcpy(c->bcv, bcv, sizeof(double) * 5 * c->npatch);
-    c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2]; c->mu0 = prm[3]; c->mu1 = prm[4];
+    c->dt = prm[0]; c->rho0 = prm[1]; c->rho1 = prm[2]; c->mu0 = prm[3]; c->mu1 = prm[4]; c->sigma = prm[5];
     c->urf_mom = prm[12]; c->urf_vof = prm[13];
     c->g[0] = prm[6]; c->g[1] = prm[7]; c->g[2] = prm[8];
     c->urf_p = prm[9]; c->urf_u = prm[10]; c->use_gravity = prm[11] != 0.0;
@@ -654,6 +654,29 @@ static void lsq_grad(orc_ctx* c, const double* phi, const double* phiR, double* 
 /* src/solvers/surfaceNormalVelocity.cpp:125-221 Rhie-Chow terms), :570-673  */
 /* (boundary loop).  COO order: N diagonals, then (LR, RL) per internal face */
 /* ------------------------------------------------------------------------ */
+/* surfaceNormalVelocity.cpp:190-221 (calcInterpolVelSurfTens), with kappa
+   and src_sft from orc_surface_tension and the cell volume fractions; all
+   its terms carry sigma, so with sigma = 0 (or no curvature computed) UnF is
+   left as it is */
+static double sft_unf(orc_ctx* c, double UnF, int o, int q, double RhoL, double RhoR, double wCL, double wCR,
+                      double alpha, double dPN, const double* n, const double* e) {
+    double* kap = dget(c, "kappa"); double* ss = dget(c, "src_sft");
+    if (c->sigma == 0.0 || !kap || !ss) return UnF;
+    double* VF = dget(c, "VF");
+    double rs = 1.0 / (wCL / RhoL + wCR / RhoR);
+    double tt = c->dt / rs;
+    UnF += alpha * tt * c->sigma * (wCL * kap[o] + wCR * kap[q]) * (VF[q] - VF[o]) / dPN;
+    for (int k = 0; k < 3; ++k) {
+        UnF += tt * rs * wCL / RhoL * ss[4 * o + k] * (n[k] - alpha * e[k]);
+        UnF += tt * rs * wCR / RhoR * ss[4 * q + k] * (n[k] - alpha * e[k]);
+    }
+    for (int k = 0; k < 3; ++k) {
+        UnF -= alpha * tt * rs * wCL / RhoL * ss[4 * o + k] * n[k];
+        UnF -= alpha * tt * rs * wCR / RhoR * ss[4 * q + k] * n[k];
+    }
+    return UnF;
+}
+
 void orc_assemble_pressure(orc_ctx* c) {
     int nc = c->nc, nf = c->nf, ni = c->ni;
     face_values(c);
@@ -731,6 +754,7 @@ void orc_assemble_pressure(orc_ctx* c) {
             UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
             UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
         }
+        UnF = sft_unf(c, UnF, o, q, RhoL, RhoR, wCL, wCR, alpha, dPN, n, e);
         unf[f] = UnF;
         double coef = alpha * tmp1 / dPN * area;
         av[o] += (+coef);
@@ -1292,7 +1316,12 @@ void orc_assemble_momentum(orc_ctx* c) {
         B1[i] = -Rho * (1.5 * V[i] - 2.0 * oV[i] + 0.5 * o2V[i]) * volume / dt;
         B2[i] = -Rho * (1.5 * W[i] - 2.0 * oW[i] + 0.5 * o2W[i]) * volume / dt;
         B0[i] += volume * sg[4 * i]; B1[i] += volume * sg[4 * i + 1]; B2[i] += volume * sg[4 * i + 2];
-        B0[i] += volume * 0.0; B1[i] += volume * 0.0; B2[i] += volume * 0.0;   /* surface tension, sigma = 0 */
+        {   /* surface-tension source (eqMomentum.cpp:320-322) */
+            double* ss = dget(c, "src_sft");
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+            if (ss && c->sigma != 0.0) { s0 = ss[4 * i]; s1 = ss[4 * i + 1]; s2 = ss[4 * i + 2]; }
+            B0[i] += volume * s0; B1[i] += volume * s1; B2[i] += volume * s2;
+        }
     }
     double *fn = dget(c, "face_n"), *fa = dget(c, "face_area"), *wc = dget(c, "face_wC");
     double *mpn = dget(c, "face_magPN"), *al = dget(c, "face_alphaF"), *epn = dget(c, "face_ePN");
@@ -1332,7 +1361,7 @@ void orc_assemble_momentum(orc_ctx* c) {
             UnF += tt * rs * wCL / RhoL * gP[3 * o + k] * n[k];
             UnF += tt * rs * wCR / RhoR * gP[3 * q + k] * n[k];
         }
-        /* surfaceNormalVelocity.cpp:156-187 (gravity); surface tension vanishes with sigma = 0 */
+        /* surfaceNormalVelocity.cpp:156-187 (gravity), then :190-221 (surface tension) */
         for (int k = 0; k < 3; ++k) UnF += alpha * tt * rs * c->g[k] * alpha * e[k];
         for (int k = 0; k < 3; ++k) {
             UnF += tt * rs * wCL / RhoL * sg[4 * o + k] * (n[k] - alpha * e[k]);
@@ -1342,6 +1371,7 @@ void orc_assemble_momentum(orc_ctx* c) {
             UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
             UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
         }
+        UnF = sft_unf(c, UnF, o, q, RhoL, RhoR, wCL, wCR, alpha, dPN, n, e);
         unf[f] = UnF;
         double weightL = (UnF > 0.0) ? 1.0 : 0.0;
         double weightR = 1.0 - weightL;
@@ -1711,6 +1741,7 @@ void orc_assemble_vof(orc_ctx* c) {
             UnF -= alpha * tt * rs * wCL / RhoL * sg[4 * o + k] * n[k];
             UnF -= alpha * tt * rs * wCR / RhoR * sg[4 * q + k] * n[k];
         }
+        UnF = sft_unf(c, UnF, o, q, RhoL, RhoR, wCL, wCR, alpha, dPN, n, e);
         unf[f] = UnF;
         double weightL = (UnF > 0.0) ? 1.0 : 0.0;
         double weightR = 1.0 - weightL;
@@ -2271,4 +2302,418 @@ double orc_update_coupled(orc_ctx* c, const double* x, const double* lim) {
         for (int a = 0; a < 5; ++a) np_ += f[a][i] * f[a][i];
     }
     return sqrt(nd) / sqrt(np_) / 5.0;
+}
+
+/* ======================================================================== */
+/* Curvature and surface-tension source (once per time step):               */
+/* src/solvers/source/curvature.cpp:7-3537 (calcCurvature, the live lines:  */
+/* 0.5-shifted level set, interface cells, gradient-normalisation, 4 sweeps */
+/* of upwind least-squares re-initialisation, normals, divergence of the    */
+/* normals; both smoothing loops run 0 times), and                          */
+/* src/solvers/source/surfaceTension.cpp:7-120 (calcSourceSurfaceTension:   */
+/* LSQ then Gauss-Green gradient of VF, src = sigma kappa grad VF, and      */
+/* sigma kappa grad VF . U).  Arrays: kappa, ls, src_sft[4 i + k].          */
+/* ======================================================================== */
+
+/* Singular value decomposition A = U W V^T of a 3x3 matrix by Householder
+   bidiagonalisation and implicit-shift QR (Golub & Reinsch 1970, in the
+   formulation of Numerical Recipes' svdcmp, which src/math/math.cpp:372-585
+   follows); a is replaced by U. */
+static double hyp2(double a, double b) {
+    double x = fabs(a), y = fabs(b);
+    if (x > y) return x * sqrt(1.0 + (y / x) * (y / x));
+    return (y == 0.0) ? 0.0 : y * sqrt(1.0 + (x / y) * (x / y));
+}
+static double signed_sqrt(double s, double f) { return -(f > 0.0 ? fabs(sqrt(s)) : -fabs(sqrt(s))); }
+static void svd3(double a[3][3], double w[3], double v[3][3]) {
+    const int n = 3;
+    double rv1[3] = {0, 0, 0};
+    double g = 0.0, scale = 0.0, anorm = 0.0, s, f, h, c, x, y, z;
+    int l = 0, i, j, k, nm = 0;
+    for (i = 0; i < n; i++) {                       /* bidiagonalisation */
+        l = i + 1;
+        rv1[i] = scale * g;
+        g = s = scale = 0.0;
+        for (k = i; k < n; k++) scale += fabs(a[k][i]);
+        if (scale != 0.0) {
+            for (k = i; k < n; k++) { a[k][i] /= scale; s += a[k][i] * a[k][i]; }
+            f = a[i][i];
+            g = signed_sqrt(s, f);
+            h = f * g - s;
+            a[i][i] = f - g;
+            for (j = l; j < n; j++) {
+                for (s = 0.0, k = i; k < n; k++) s += a[k][i] * a[k][j];
+                f = s / h;
+                for (k = i; k < n; k++) a[k][j] += f * a[k][i];
+            }
+            for (k = i; k < n; k++) a[k][i] *= scale;
+        }
+        w[i] = scale * g;
+        g = s = scale = 0.0;
+        if (i != n - 1) {
+            for (k = l; k < n; k++) scale += fabs(a[i][k]);
+            if (scale != 0.0) {
+                for (k = l; k < n; k++) { a[i][k] /= scale; s += a[i][k] * a[i][k]; }
+                f = a[i][l];
+                g = signed_sqrt(s, f);
+                h = f * g - s;
+                a[i][l] = f - g;
+                for (k = l; k < n; k++) rv1[k] = a[i][k] / h;
+                for (j = l; j < n; j++) {
+                    for (s = 0.0, k = l; k < n; k++) s += a[j][k] * a[i][k];
+                    for (k = l; k < n; k++) a[j][k] += s * rv1[k];
+                }
+                for (k = l; k < n; k++) a[i][k] *= scale;
+            }
+        }
+        anorm = smax(anorm, (fabs(w[i]) + fabs(rv1[i])));
+    }
+    for (i = n - 1; i >= 0; i--) {                  /* right transformations */
+        if (i < n - 1) {
+            if (g != 0.0) {
+                for (j = l; j < n; j++) v[j][i] = (a[i][j] / a[i][l]) / g;
+                for (j = l; j < n; j++) {
+                    for (s = 0.0, k = l; k < n; k++) s += a[i][k] * v[k][j];
+                    for (k = l; k < n; k++) v[k][j] += s * v[k][i];
+                }
+            }
+            for (j = l; j < n; j++) v[i][j] = v[j][i] = 0.0;
+        }
+        v[i][i] = 1.0;
+        g = rv1[i];
+        l = i;
+    }
+    for (i = n - 1; i >= 0; i--) {                  /* left transformations */
+        l = i + 1;
+        g = w[i];
+        for (j = l; j < n; j++) a[i][j] = 0.0;
+        if (g != 0.0) {
+            g = 1.0 / g;
+            for (j = l; j < n; j++) {
+                for (s = 0.0, k = l; k < n; k++) s += a[k][i] * a[k][j];
+                f = (s / a[i][i]) * g;
+                for (k = i; k < n; k++) a[k][j] += f * a[k][i];
+            }
+            for (j = i; j < n; j++) a[j][i] *= g;
+        } else {
+            for (j = i; j < n; j++) a[j][i] = 0.0;
+        }
+        ++a[i][i];
+    }
+    for (k = n - 1; k >= 0; k--) {                  /* diagonalisation */
+        for (int its = 0; its < 30; its++) {
+            int flag = 1;
+            for (l = k; l >= 0; l--) {
+                nm = l - 1;
+                if ((fabs(rv1[l]) + anorm) == anorm) { flag = 0; break; }
+                if ((fabs(w[nm]) + anorm) == anorm) break;
+            }
+            if (flag) {
+                c = 0.0; s = 1.0;
+                for (i = l; i <= k; i++) {
+                    f = s * rv1[i];
+                    rv1[i] = c * rv1[i];
+                    if ((fabs(f) + anorm) == anorm) break;
+                    g = w[i];
+                    h = hyp2(f, g);
+                    w[i] = h;
+                    h = 1.0 / h;
+                    c = g * h;
+                    s = -f * h;
+                    for (j = 0; j < n; j++) {
+                        y = a[j][nm]; z = a[j][i];
+                        a[j][nm] = y * c + z * s;
+                        a[j][i] = z * c - y * s;
+                    }
+                }
+            }
+            z = w[k];
+            if (l == k) {
+                if (z < 0.0) { w[k] = -z; for (j = 0; j < n; j++) v[j][k] = -v[j][k]; }
+                break;
+            }
+            x = w[l];
+            nm = k - 1;
+            y = w[nm];
+            g = rv1[nm];
+            h = rv1[k];
+            f = ((y - z) * (y + z) + (g - h) * (g + h)) / (2.0 * h * y);
+            g = hyp2(f, 1.0);
+            f = ((x - z) * (x + z) + h * ((y / (f + (f > 0.0 ? fabs(g) : -fabs(g)))) - h)) / x;
+            c = s = 1.0;
+            for (j = l; j <= nm; j++) {
+                i = j + 1;
+                g = rv1[i]; y = w[i];
+                h = s * g; g = c * g;
+                z = hyp2(f, h);
+                rv1[j] = z;
+                c = f / z; s = h / z;
+                f = x * c + g * s;
+                g = g * c - x * s;
+                h = y * s;
+                y *= c;
+                for (int jj = 0; jj < n; jj++) {
+                    x = v[jj][j]; z = v[jj][i];
+                    v[jj][j] = x * c + z * s;
+                    v[jj][i] = z * c - x * s;
+                }
+                z = hyp2(f, h);
+                w[j] = z;
+                if (z != 0.0) { z = 1.0 / z; c = f * z; s = h * z; }
+                f = c * g + s * y;
+                x = c * y - s * g;
+                for (int jj = 0; jj < n; jj++) {
+                    y = a[jj][j]; z = a[jj][i];
+                    a[jj][j] = y * c + z * s;
+                    a[jj][i] = z * c - y * s;
+                }
+            }
+            rv1[l] = 0.0;
+            rv1[k] = f;
+            w[k] = x;
+        }
+    }
+}
+/* out = a b for 3x3 (row i, column j, sum over m in order) */
+static void mm3(double a[3][3], double b[3][3], double out[3][3]) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double t = 0.0;
+            for (int m = 0; m < 3; ++m) t += a[i][m] * b[m][j];
+            out[i][j] = t;
+        }
+}
+
+/* upwind weight of face f for cell side (owner: sign -1 on the distance) */
+static double reinit_weight(double vel0, const double* nv, const double* d, double side) {
+    double sgn = (vel0 > 0.0 ? 1.0 : -1.0);
+    double wk = 0.0;
+    wk += sgn * nv[0] * (side * d[0]);
+    wk += sgn * nv[1] * (side * d[1]);
+    wk += sgn * nv[2] * (side * d[2]);
+    wk = pow(1.0 * wk, 1.0);
+    return smax(1.e-5, wk);
+}
+
+void orc_curvature(orc_ctx* c) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    double* VF = dget(c, "VF");
+    double *wc = dget(c, "face_wC"), *fa = dget(c, "face_area"), *dist = dget(c, "face_dist");
+    double *vol = dget(c, "cell_vol"), *cc = dget(c, "cell_c"), *fc = dget(c, "face_c");
+    int *cfp = iget(c, "cf_ptr"), *cfi = iget(c, "cf_idx");
+    int *sp = iget(c, "stencil_ptr"), *si = iget(c, "stencil_idx");
+    double* sa = (double*)malloc(sizeof(double) * nc);        /* smoothAi */
+    for (int i = 0; i < nc; ++i) sa[i] = VF[i];
+    /* interface cells: the 0.5 level crosses between a cell and one of its faces */
+    double* fsa = (double*)malloc(sizeof(double) * nf);
+    for (int f = 0; f < nf; ++f) {
+        double wL = wc[f], wR = 1.0 - wL;
+        fsa[f] = (f < ni) ? wL * sa[c->own[f]] + wR * sa[c->nei[f]] : sa[c->own[f]];
+    }
+    char* iface = (char*)calloc(nc, 1);
+    for (int f = 0; f < nf; ++f) {
+        if ((sa[c->own[f]] - 0.5) * (fsa[f] - 0.5) <= 0.0) iface[c->own[f]] = 1;
+        if (f < ni && (sa[c->nei[f]] - 0.5) * (fsa[f] - 0.5) <= 0.0) iface[c->nei[f]] = 1;
+    }
+    for (int i = 0; i < nc; ++i) sa[i] = sa[i] - 0.5;
+    double* phiR = (double*)malloc(sizeof(double) * nf);
+    double* g = (double*)malloc(sizeof(double) * 3 * nc);
+#define LSQ_INPUT(phi, out)                                                    \
+    do {                                                                       \
+        for (int f_ = ni; f_ < nf; ++f_) phiR[f_] = (phi)[c->own[f_]];         \
+        lsq_grad(c, (phi), phiR, (out));                                       \
+    } while (0)
+    LSQ_INPUT(sa, g);
+    for (int i = 0; i < nc; ++i)
+        if (iface[i]) {
+            double mg = 0.0;
+            mg += g[3 * i] * g[3 * i]; mg += g[3 * i + 1] * g[3 * i + 1]; mg += g[3 * i + 2] * g[3 * i + 2];
+            if (mg > 1.0) sa[i] = sa[i] / mg;
+        }
+    double* tau = (double*)malloc(sizeof(double) * nc);
+    for (int i = 0; i < nc; ++i) {
+        double maxA = 0.0;
+        for (int k = cfp[i]; k < cfp[i + 1]; ++k) maxA = smax(maxA, fa[cfi[k]]);
+        tau[i] = vol[i] / maxA / 1.0;
+        tau[i] = smin(tau[i], pow(vol[i], 0.3));
+    }
+    double* vel0 = (double*)malloc(sizeof(double) * nc);
+    for (int i = 0; i < nc; ++i) {
+        double var = sa[i];
+        vel0[i] = var / sqrt(var * var + (fabs(var) * pow(vol[i], 0.333)) * (fabs(var) * pow(vol[i], 0.333)));
+    }
+    double* nrm = (double*)malloc(sizeof(double) * 3 * nc);
+    double* vs = (double*)malloc(sizeof(double) * 6 * nc);
+    double* gt = (double*)malloc(sizeof(double) * 3 * nc);
+    for (int iter = 0; iter < 4; ++iter) {
+        LSQ_INPUT(sa, g);
+        for (int i = 0; i < nc; ++i) {
+            double m = sqrt(g[3 * i] * g[3 * i] + g[3 * i + 1] * g[3 * i + 1] + g[3 * i + 2] * g[3 * i + 2]);
+            for (int q = 0; q < 3; ++q) nrm[3 * i + q] = (m != 0.0) ? g[3 * i + q] / m : 0.0;
+        }
+        memset(vs, 0, sizeof(double) * 6 * nc);
+        for (int f = 0; f < nf; ++f) {
+            const double* d = dist + 3 * f;
+            int o = c->own[f];
+            double wk = reinit_weight(vel0[o], nrm + 3 * o, d, -1.0);
+            for (int ii = 0, num = 0; ii < 3; ++ii)
+                for (int jj = ii; jj < 3; ++jj) vs[6 * o + num++] += wk * d[ii] * d[jj];
+            if (f < ni) {
+                int q = c->nei[f];
+                wk = reinit_weight(vel0[q], nrm + 3 * q, d, 1.0);
+                for (int ii = 0, num = 0; ii < 3; ++ii)
+                    for (int jj = ii; jj < 3; ++jj) vs[6 * q + num++] += wk * d[ii] * d[jj];
+            }
+        }
+        for (int i = 0; i < nc; ++i) {
+            double* v6 = vs + 6 * i;
+            double U[3][3] = {{v6[0], v6[1], v6[2]}, {v6[1], v6[3], v6[4]}, {v6[2], v6[4], v6[5]}};
+            double D[3], V[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            svd3(U, D, V);
+            double iD[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int q = 0; q < 3; ++q) if (fabs(D[q]) > 1.e-25) iD[q][q] = 1.0 / D[q];
+            double Ut[3][3], o3[3][3], P[3][3];
+            for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) Ut[a][b] = U[b][a];
+            mm3(iD, Ut, o3);
+            mm3(V, o3, P);
+            v6[0] = P[0][0]; v6[1] = P[0][1]; v6[2] = P[0][2]; v6[3] = P[1][1]; v6[4] = P[1][2]; v6[5] = P[2][2];
+        }
+        memset(gt, 0, sizeof(double) * 3 * nc);
+        for (int f = 0; f < nf; ++f) {
+            const double* d = dist + 3 * f;
+            int o = c->own[f];
+            double L = sa[o], R = (f < ni) ? sa[c->nei[f]] : L;
+            double DV = R - L;
+            double wk = reinit_weight(vel0[o], nrm + 3 * o, d, -1.0);
+            for (int q = 0; q < 3; ++q) gt[3 * o + q] += wk * d[q] * DV;
+            if (f < ni) {
+                int r = c->nei[f];
+                wk = reinit_weight(vel0[r], nrm + 3 * r, d, 1.0);
+                for (int q = 0; q < 3; ++q) gt[3 * r + q] += wk * d[q] * DV;
+            }
+        }
+        for (int i = 0; i < nc; ++i) {
+            const double* v6 = vs + 6 * i; double* t = gt + 3 * i;
+            double t0 = v6[0] * t[0] + v6[1] * t[1] + v6[2] * t[2];
+            double t1 = v6[1] * t[0] + v6[3] * t[1] + v6[4] * t[2];
+            double t2 = v6[2] * t[0] + v6[4] * t[1] + v6[5] * t[2];
+            t[0] = t0; t[1] = t1; t[2] = t2;
+        }
+        for (int i = 0; i < nc; ++i)
+            if (!iface[i]) {
+                double* t = gt + 3 * i;
+                double mg = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+                double resi = 0.1 * tau[i] * vel0[i] * (1.0 - mg);
+                sa[i] += resi;
+            }
+    }
+    double* ls = dreg(c, "ls", nc);
+    memcpy(ls, sa, sizeof(double) * nc);
+    /* normals of the re-initialised level set, then the divergence */
+    LSQ_INPUT(sa, g);
+    for (int i = 0; i < nc; ++i) {
+        double m = 0.0;
+        for (int q = 0; q < 3; ++q) m += g[3 * i + q] * g[3 * i + q];
+        m = sqrt(m);
+        for (int q = 0; q < 3; ++q) nrm[3 * i + q] = (m > 1.e-15) ? g[3 * i + q] / m : 0.0;
+    }
+    memset(vs, 0, sizeof(double) * 6 * nc);
+    memset(gt, 0, sizeof(double) * 3 * nc);
+    for (int i = 0; i < nc; ++i)
+        for (int k = sp[i]; k < sp[i + 1]; ++k) {
+            int j = si[k];
+            double d[3] = {cc[3 * j] - cc[3 * i], cc[3 * j + 1] - cc[3 * i + 1], cc[3 * j + 2] - cc[3 * i + 2]};
+            for (int ii = 0, num = 0; ii < 3; ++ii)
+                for (int jj = ii; jj < 3; ++jj) vs[6 * i + num++] += 1.0 * d[ii] * d[jj];
+        }
+    for (int p = 0; p < c->npatch; ++p)
+        for (int f = c->pstart[p]; f < c->pstart[p] + c->psize[p]; ++f) {
+            int o = c->own[f];
+            double d[3] = {fc[3 * f] - cc[3 * o], fc[3 * f + 1] - cc[3 * o + 1], fc[3 * f + 2] - cc[3 * o + 2]};
+            for (int ii = 0, num = 0; ii < 3; ++ii)
+                for (int jj = ii; jj < 3; ++jj) vs[6 * o + num++] += 1.0 * d[ii] * d[jj];
+        }
+    for (int i = 0; i < nc; ++i) {
+        double* v = vs + 6 * i;
+        double det = v[0] * v[3] * v[5] + v[1] * v[4] * v[2] + v[2] * v[1] * v[4] - v[0] * v[4] * v[4] -
+                     v[2] * v[3] * v[2] - v[1] * v[1] * v[5];
+        double t[6];
+        t[0] = (v[3] * v[5] - v[4] * v[4]) / det;
+        t[1] = (v[2] * v[4] - v[1] * v[5]) / det;
+        t[2] = (v[1] * v[4] - v[2] * v[3]) / det;
+        t[3] = (v[0] * v[5] - v[2] * v[2]) / det;
+        t[4] = (v[2] * v[1] - v[0] * v[4]) / det;
+        t[5] = (v[0] * v[3] - v[1] * v[1]) / det;
+        memcpy(v, t, sizeof t);
+    }
+    for (int i = 0; i < nc; ++i)
+        for (int k = sp[i]; k < sp[i + 1]; ++k) {
+            int j = si[k];
+            double d[3] = {cc[3 * j] - cc[3 * i], cc[3 * j + 1] - cc[3 * i + 1], cc[3 * j + 2] - cc[3 * i + 2]};
+            for (int q = 0; q < 3; ++q) gt[3 * i + q] += 1.0 * d[q] * (nrm[3 * j + q] - nrm[3 * i + q]);
+        }
+    double* kappa = dreg(c, "kappa", nc);
+    for (int i = 0; i < nc; ++i) {
+        const double* v = vs + 6 * i; const double* t = gt + 3 * i;
+        double t0 = v[0] * t[0] + v[1] * t[1] + v[2] * t[2];
+        double t1 = v[1] * t[0] + v[3] * t[1] + v[4] * t[2];
+        double t2 = v[2] * t[0] + v[4] * t[1] + v[5] * t[2];
+        kappa[i] = -(t0 + t1 + t2);
+    }
+#undef LSQ_INPUT
+    free(sa); free(fsa); free(iface); free(phiR); free(g); free(tau); free(vel0); free(nrm); free(vs); free(gt);
+}
+
+/* calcSourceSurfaceTension (surfaceTension.cpp:7-120) after calcCurvature;
+   needs the face values of the pressure pass (face_vfR) */
+void orc_surface_tension(orc_ctx* c, double sigma) {
+    int nc = c->nc, nf = c->nf, ni = c->ni;
+    face_values(c);
+    orc_curvature(c);
+    double *VF = dget(c, "VF"), *U = dget(c, "U"), *V = dget(c, "V"), *W = dget(c, "W");
+    double* kappa = dget(c, "kappa");
+    double* g = (double*)malloc(sizeof(double) * 3 * nc);
+    lsq_grad(c, VF, dget(c, "face_vfR"), g);
+    /* Gauss-Green (gradient.cpp:1778-1975) with the LSQ gradient for the
+       skewness correction and the zeroGradient extrapolation */
+    double *wc = dget(c, "face_wC"), *fn = dget(c, "face_n"), *fa = dget(c, "face_area");
+    double *sk = dget(c, "face_skew"), *vol = dget(c, "cell_vol"), *cc = dget(c, "cell_c"), *fc = dget(c, "face_c");
+    double* vr = dget(c, "face_vfR");
+    double* gg = (double*)calloc(3 * (size_t)nc, sizeof(double));
+    for (int f = 0; f < ni; ++f) {
+        int o = c->own[f], q = c->nei[f];
+        double wL = wc[f], wR = 1.0 - wL;
+        double vf = wL * VF[o] + wR * VF[q];
+        vf += wL * g[3 * o] * sk[3 * f]; vf += wL * g[3 * o + 1] * sk[3 * f + 1]; vf += wL * g[3 * o + 2] * sk[3 * f + 2];
+        vf += wR * g[3 * q] * sk[3 * f]; vf += wR * g[3 * q + 1] * sk[3 * f + 1]; vf += wR * g[3 * q + 2] * sk[3 * f + 2];
+        for (int j = 0; j < 3; ++j) {
+            gg[3 * o + j] += vf * fn[3 * f + j] * fa[f] / vol[o];
+            gg[3 * q + j] -= vf * fn[3 * f + j] * fa[f] / vol[q];
+        }
+    }
+    for (int p = 0; p < c->npatch; ++p) {
+        int t = c->bct[3 * p + 2];
+        for (int f = c->pstart[p]; f < c->pstart[p] + c->psize[p]; ++f) {
+            int o = c->own[f];
+            double vf = VF[o];
+            if (t == 1) vf = c->bcv[5 * p + 4];
+            else if (t == 0) {
+                vf += g[3 * o] * (fc[3 * f] - cc[3 * o]);
+                vf += g[3 * o + 1] * (fc[3 * f + 1] - cc[3 * o + 1]);
+                vf += g[3 * o + 2] * (fc[3 * f + 2] - cc[3 * o + 2]);
+            } else vf = 0.5 * (VF[o] + vr[f]);
+            for (int j = 0; j < 3; ++j) gg[3 * o + j] += vf * fn[3 * f + j] * fa[f] / vol[o];
+        }
+    }
+    double* gvf = dreg(c, "sft_grad_VF", 3LL * nc);
+    memcpy(gvf, gg, sizeof(double) * 3 * nc);
+    double* src = dreg(c, "src_sft", 4LL * nc);
+    for (int i = 0; i < nc; ++i) {
+        src[4 * i] = (sigma * kappa[i] * gg[3 * i]);
+        src[4 * i + 1] = (sigma * kappa[i] * gg[3 * i + 1]);
+        src[4 * i + 2] = (sigma * kappa[i] * gg[3 * i + 2]);
+        src[4 * i + 3] = sigma * kappa[i] * (gg[3 * i] * U[i] + gg[3 * i + 1] * V[i] + gg[3 * i + 2] * W[i]);
+    }
+    free(g); free(gg);
+    (void)nf;
 }

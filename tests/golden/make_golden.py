@@ -7,11 +7,14 @@ reference tree nor its build.  Fixtures named outer_* hold a whole outer
 iteration (momentum equation, then the pressure correction) with seeded old
 and second-old velocities for the BDF2 term; fixtures named vofeq_* hold one
 volume-fraction sub-iteration (MSTACS reconstruction + calcVolfracEq) with
-seeded old and second-old volume fractions.  foam_* are OpenFOAM polyMesh
+seeded old and second-old volume fractions.  Names ending in "s" carry a
+surface tension (sigma != 0): the reference then computes the curvature and
+the surface-tension source first and every face velocity takes its terms.
+foam_* are OpenFOAM polyMesh
 directories written from seeded meshes, with foam_*_ref.npz holding what the
 reference's own loader (SEMO_Mesh_Load::OpenFoam) read from them.
 
-    python tests/golden/make_golden.py [REF_DIR] [--foam-only]
+    python tests/golden/make_golden.py [REF_DIR] [--foam-only | --only NAME ...]
 """
 from __future__ import annotations
 
@@ -45,6 +48,11 @@ def golden_cases():
     c.name = "box7j"
     c.P = np.random.default_rng(5).uniform(-2, 2, c.mesh.n_cells)
     cs.append(("box7j", c))
+    # surface tension: curvature, source and the face-velocity terms
+    c = with_fields(vof_case(6, jitter=0.2), seed=3, p_scale=50.0)
+    c.sigma = 0.07
+    c.name = "vof6js"
+    cs.append(("vof6js", c))
     return cs
 
 
@@ -64,6 +72,10 @@ def outer_cases():
     c.mom_u_urf = 0.7
     c.name = "outer_box7j"
     cs.append(("outer_box7j", c))
+    c = with_history(with_fields(vof_case(6, jitter=0.2), seed=11, p_scale=80.0), seed=12)
+    c.sigma = 0.07
+    c.name = "outer_vof6js"
+    cs.append(("outer_vof6js", c))
     return cs
 
 
@@ -79,6 +91,10 @@ def vofeq_cases():
     c.vof_urf = 0.5
     c.name = "vofeq_vof7"
     cs.append(("vofeq_vof7", c))
+    c = with_vf_history(with_fields(vof_case(7, jitter=0.25), seed=5, p_scale=100.0), seed=9)
+    c.sigma = 0.07
+    c.name = "vofeq_vof7js"
+    cs.append(("vofeq_vof7js", c))
     return cs
 
 
@@ -160,18 +176,28 @@ def main():
     ref_dir = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference"
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref_dir}", "-j8"],
                    check=True, stdout=subprocess.DEVNULL)
-    make_foam()
+    # --only NAME [NAME ...]: regenerate just those fixtures
+    only = set(sys.argv[sys.argv.index("--only") + 1:]) if "--only" in sys.argv else None
+    pick = (lambda n: only is None or n in only)
+    if only is None or any(n.startswith("foam_") for n in only):
+        make_foam()
     if "--foam-only" in sys.argv:
         return
     for name, case in golden_cases():
+        if not pick(name):
+            continue
         ref = run_reference(case, threads=1)
         save(name, case, ref)
         print(name, case.mesh.n_cells, "cells")
     for name, case in outer_cases():
+        if not pick(name):
+            continue
         ref = run_reference(case, threads=1, momentum=True)
         save(name, case, ref, momentum=True)
         print(name, case.mesh.n_cells, "cells (outer iteration)")
     for name, case in vofeq_cases():
+        if not pick(name):
+            continue
         ref = run_reference(case, threads=1, vof=True)
         save(name, case, ref, vof=True)
         print(name, case.mesh.n_cells, "cells (volume-fraction sub-iteration)")
