@@ -84,6 +84,9 @@ typedef struct {
     double mu[2];                /* phase viscosities (species[].mu), laminar */
     double urf_mom;              /* controls.momVelURF */
     double urf_vof;              /* controls.vofVofURF */
+    double sigma;                /* species[0].sigma, surface tension; 0 (default) leaves out the curvature,
+                                    the source and the face-velocity terms (calcSourceSurfaceTension,
+                                    calcInterpolVelSurfTens) */
 } semo_physics;
 
 typedef struct {
@@ -232,6 +235,23 @@ semo_status semo_vof_pass(semo_ctx* ctx, double* norm, semo_solve_info* info);
 
 /* Volume-fraction assembly only. */
 semo_status semo_assemble_vof(semo_ctx* ctx);
+
+/* Curvature and surface-tension source from the current fields (needs
+   phys.sigma != 0).  The passes compute it themselves with the gravity
+   source, once per change of fields or physics, as SEMO does once per time
+   step before its outer loop (src/solvers/pressureBased.cpp:142); every face
+   velocity then takes calcInterpolVelSurfTens' terms
+   (src/solvers/surfaceNormalVelocity.cpp:190-221) and the momentum right-hand
+   side the source (src/solvers/eqMomentum.cpp:320-322).  Replaces:
+   SEMO_Solvers_Builder::calcSourceSurfaceTension
+   (src/solvers/source/surfaceTension.cpp:7-120) with calcCurvature
+   (src/solvers/source/curvature.cpp). */
+semo_status semo_source_surface_tension(semo_ctx* ctx);
+/* Its results in the caller's cell order: kappa (controls.kappa), ls
+   (controls.LS, the re-initialised level set) and src, 4 per cell
+   (controls.sourceSurfaceTension[0..3]: sigma kappa grad VF, and its dot
+   product with U).  Any pointer may be null. */
+semo_status semo_get_surface_tension(semo_ctx* ctx, double* kappa, double* ls, double* src);
 
 /* The assembled volume-fraction system in SEMO's layout (as
    semo_get_momentum_system; b is n_cells). */

@@ -52,7 +52,8 @@ class Physics(C.Structure):
                 ("use_gravity", C.c_int), ("urf_p", C.c_double), ("urf_u", C.c_double),
                 ("p_min", C.c_double), ("p_max", C.c_double), ("u_min", C.c_double), ("u_max", C.c_double),
                 ("v_min", C.c_double), ("v_max", C.c_double), ("w_min", C.c_double), ("w_max", C.c_double),
-                ("mu", C.c_double * 2), ("urf_mom", C.c_double), ("urf_vof", C.c_double)]
+                ("mu", C.c_double * 2), ("urf_mom", C.c_double), ("urf_vof", C.c_double),
+                ("sigma", C.c_double)]
 
 
 class CoupledPhysics(C.Structure):
@@ -119,6 +120,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_set_old_vf.argtypes = [vp, f64p, f64p]
     L.semo_vof_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_assemble_vof.argtypes = [vp]
+    L.semo_source_surface_tension.argtypes = [vp]
+    L.semo_get_surface_tension.argtypes = [vp, f64p, f64p, f64p]
     L.semo_get_vof_system.argtypes = [vp, i32p, i32p, f64p, f64p, C.POINTER(C.c_int64)]
     L.semo_solve_vof.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_foam_sizes.argtypes = [C.c_char_p, C.POINTER(C.c_int64)]
@@ -234,6 +237,7 @@ class Context:
         ph.mu[0], ph.mu[1] = case.mu
         ph.urf_mom = case.mom_u_urf
         ph.urf_vof = case.vof_urf
+        ph.sigma = case.sigma
         bt, btp = _i32(case.bc_type.reshape(-1))
         bv, bvp = _f64(case.bc_value.reshape(-1))
         self._check(self.L.semo_set_physics(self.h, C.byref(ph), btp, bvp))
@@ -324,6 +328,18 @@ class Context:
 
     def assemble_vof(self) -> None:
         self._check(self.L.semo_assemble_vof(self.h))
+
+    def calc_source_surface_tension(self) -> None:
+        """Curvature and surface-tension source from the current fields (sigma != 0)."""
+        self._check(self.L.semo_source_surface_tension(self.h))
+
+    def surface_tension(self) -> dict:
+        """The last curvature / source: kappa, ls (n_cells each), src (n_cells x 4)."""
+        n = self.n_cells
+        kap, ls, src = np.empty(n), np.empty(n), np.empty(4 * n)
+        p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        self._check(self.L.semo_get_surface_tension(self.h, p(kap), p(ls), p(src)))
+        return {"kappa": kap, "ls": ls, "src": src.reshape(n, 4)}
 
     def vof_system(self) -> dict:
         """The volume-fraction system in SEMO's layout (caller numbering, COO-scatter rows)."""
@@ -489,7 +505,8 @@ class Context:
     STAGES = ("face_values", "gravity", "stencil", "pface", "pbface", "pcell", "amg_setup", "pcg",
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
               "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate", "mstacs", "vface",
-              "vsolve", "vupdate", "stencil_uvw", "mbface", "cgrad", "cface", "ccell", "csolve", "cupdate")
+              "vsolve", "vupdate", "stencil_uvw", "mbface", "cgrad", "cface", "ccell", "csolve", "cupdate",
+              "surface_tension")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

@@ -26,6 +26,7 @@ UNITS = [
     ("momentum.cu", []),
     ("vof.cu", []),
     ("coupled.cu", []),
+    ("surftens.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
     ("noalloc.cu", []),

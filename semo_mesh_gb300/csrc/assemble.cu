@@ -496,6 +496,8 @@ void assemble_gravity_stencil(semo_ctx* c) {
     const bool keep = c->pvf_current;
     if (!keep) assemble_gravity(c);   // else the gravity source is kept
     stencil_pass(c, !keep);
+    // the surface-tension source is kept with the gravity source
+    if (!keep || (c->phys.sigma != 0.0 && !c->sft_current)) assemble_surface_tension(c);
 }
 
 void assemble_pressure(semo_ctx* c) {
@@ -514,6 +516,7 @@ void assemble_pressure(semo_ctx* c) {
         a.P = c->P; a.U = c->U; a.V = c->V; a.W = c->W; a.irho = c->irho; a.grad = c->grad; a.mm = c->mm; a.sg = c->sg;
         a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
         a.use_gravity = c->phys.use_gravity;
+        set_sft_args(c, a);
         a.val = c->A_val; a.coef = coef; a.flux = flux; a.unf = c->unf;
         StageScope sc(c, ST_PFACE);
         k_pface<<<blocks(ni, 256), 256, 0, s>>>(a);

@@ -183,7 +183,7 @@ semo_status semo_mesh_upload(semo_ctx* c, int n_points, const double* points, in
         c->amg32.clear();
         c->amg64.clear();
         c->has_old = c->has_src = c->has_oldvf = false;
-        c->pvf_current = c->sg_current = c->vof_assembled = false;
+        c->pvf_current = c->sg_current = c->sft_current = c->vof_assembled = false;
         c->cpl_phys = c->cpl_fields = c->cpl_assembled = false;
         ++c->mesh_gen;
 
@@ -444,6 +444,7 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         need(std::isfinite(phys->dt) && phys->dt > 0.0, SEMO_ERR_ARGUMENT, "dt must be positive");
         need(phys->rho[0] > 0.0 && phys->rho[1] > 0.0, SEMO_ERR_ARGUMENT, "densities must be positive");
         need(phys->mu[0] >= 0.0 && phys->mu[1] >= 0.0, SEMO_ERR_ARGUMENT, "viscosities must be non-negative");
+        need(std::isfinite(phys->sigma), SEMO_ERR_ARGUMENT, "sigma must be finite");
         for (int p = 0; p < c->npatch; ++p) {
             need(bc_type[3 * p] == SEMO_BC_ZERO_GRADIENT || bc_type[3 * p] == SEMO_BC_FIXED_VALUE, SEMO_ERR_ARGUMENT,
                  "pressure BC must be zeroGradient or fixedValue");
@@ -463,6 +464,7 @@ semo_status semo_set_physics(semo_ctx* c, const semo_physics* phys, const int32_
         c->vof_assembled = false;
         c->pvf_current = false;
         c->sg_current = false;
+        c->sft_current = false;
     });
 }
 
@@ -501,6 +503,7 @@ semo_status semo_set_fields(semo_ctx* c, const double* P, const double* U, const
         c->vof_assembled = false;
         c->pvf_current = false;
         c->sg_current = false;
+        c->sft_current = false;
     });
 }
 
@@ -517,6 +520,31 @@ semo_status semo_get_fields(semo_ctx* c, double* P, double* U, double* V, double
             if (dst[q])
                 SEMO_CUDA(cudaMemcpyAsync(dst[q], c->stage.p + q * n, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+semo_status semo_source_surface_tension(semo_ctx* c) {
+    return guarded(c, [&] {
+        need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
+             "mesh, physics and fields must be set first");
+        need(c->phys.sigma != 0.0, SEMO_ERR_STATE, "sigma is 0: no surface tension");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        semo::assemble_face_values(c, false);
+        semo::assemble_gravity(c);
+        semo::stencil_pass(c, true);
+        semo::assemble_surface_tension(c);
+        SEMO_CUDA(cudaStreamSynchronize(c->stream));
+        c->pvf_current = false;
+    });
+}
+
+semo_status semo_get_surface_tension(semo_ctx* c, double* kappa, double* ls, double* src) {
+    return guarded(c, [&] {
+        need(c->sft_current, SEMO_ERR_STATE, "no surface-tension source computed for the current fields");
+        const size_t n = (size_t)c->nc;
+        if (kappa) download_permuted(c, c->sft.p, kappa);
+        if (ls) download_permuted(c, c->sft.p + n, ls);
+        if (src) download_permuted(c, c->sft.p + 2 * n, src, 4, true);
     });
 }
 

@@ -70,10 +70,22 @@ struct FaceArgs {
     const int *own, *nei, *lr, *rl;
     const double *fn, *epn, *skew, *alf, *fk;
     const double *P, *U, *V, *W, *irho, *grad, *mm, *sg;
-    double dt, g0, g1, g2;
-    int use_gravity;
+    const double *VF, *kap, *ss;   // surface tension: cell VF, curvature, source (4 planes of nc)
+    double dt, g0, g1, g2, sigma;
+    int use_gravity, use_sft;
     double *val, *coef, *flux, *unf;
 };
+
+// Surface-tension inputs of the face velocity from a context (semo_ctx):
+// cell VF, curvature and source planes, used when sigma != 0.
+template <class Ctx>
+inline void set_sft_args(const Ctx* c, FaceArgs& a) {
+    a.sigma = c->phys.sigma;
+    a.use_sft = (c->phys.sigma != 0.0 && c->sft_current) ? 1 : 0;
+    a.VF = c->VF.p;
+    a.kap = a.use_sft ? c->sft.p : nullptr;
+    a.ss = a.use_sft ? c->sft.p + 2 * (size_t)c->nc : nullptr;
+}
 
 struct FaceGeo {
     double n0, n1, n2, s0, s1, s2, alpha, ae0, ae1, ae2, kA, kP, area, wL, wR;
@@ -97,8 +109,10 @@ __device__ __forceinline__ FaceGeo load_geo(const FaceArgs& a, int f) {
 // (:156-187) Rhie-Chow terms.  Those are evaluated in reduced form:
 // (dt/rho*)*rho* = dt, and the (n - alpha e) and n pieces of the
 // non-orthogonal correction combine to alpha e; agreement with SEMO's
-// operation order is to rounding (a few ulp), not bit-for-bit.  Surface
-// tension (:188-221) vanishes with sigma = 0.
+// operation order is to rounding (a few ulp), not bit-for-bit.  With sigma
+// != 0 the surface-tension terms (:190-221) follow, reduced the same way:
+// alpha (dt/rho*) sigma (wL kL + wR kR) (VF_R - VF_L)/|PN| and the source's
+// non-orthogonal part.
 __device__ __forceinline__ double face_unf(const FaceArgs& a, const FaceGeo& g, int o, int q) {
     const size_t N = a.nc;
     const double* G = a.grad;
@@ -124,11 +138,18 @@ __device__ __forceinline__ double face_unf(const FaceArgs& a, const FaceGeo& g, 
     const double aL = a.dt * g.wL * iRL, aR = a.dt * g.wR * iRR;
     UnF += aL * (__ldg(G + o) * g.ae0 + __ldg(G + N + o) * g.ae1 + __ldg(G + 2 * N + o) * g.ae2);
     UnF += aR * (__ldg(G + q) * g.ae0 + __ldg(G + N + q) * g.ae1 + __ldg(G + 2 * N + q) * g.ae2);
+    const double t0 = g.n0 - g.ae0 - g.alpha * g.n0, t1 = g.n1 - g.ae1 - g.alpha * g.n1;
+    const double t2 = g.n2 - g.ae2 - g.alpha * g.n2;
     if (a.use_gravity) {
         UnF += a.dt * g.alpha * (a.g0 * g.ae0 + a.g1 * g.ae1 + a.g2 * g.ae2);
-        const double t0 = g.n0 - g.ae0 - g.alpha * g.n0, t1 = g.n1 - g.ae1 - g.alpha * g.n1;
-        const double t2 = g.n2 - g.ae2 - g.alpha * g.n2;
         const double* S = a.sg;
+        UnF += aL * (__ldg(S + o) * t0 + __ldg(S + N + o) * t1 + __ldg(S + 2 * N + o) * t2);
+        UnF += aR * (__ldg(S + q) * t0 + __ldg(S + N + q) * t1 + __ldg(S + 2 * N + q) * t2);
+    }
+    if (a.use_sft) {
+        const double kf = g.wL * __ldg(a.kap + o) + g.wR * __ldg(a.kap + q);
+        UnF += tt * g.kP * a.sigma * kf * (__ldg(a.VF + q) - __ldg(a.VF + o));
+        const double* S = a.ss;
         UnF += aL * (__ldg(S + o) * t0 + __ldg(S + N + o) * t1 + __ldg(S + 2 * N + o) * t2);
         UnF += aR * (__ldg(S + q) * t0 + __ldg(S + N + q) * t1 + __ldg(S + 2 * N + q) * t2);
     }

@@ -153,7 +153,8 @@ __global__ void k_mcell(int nc, int ni, int nf, double dt, const int* __restrict
                         const int* __restrict__ dig, const double* __restrict__ rho, const double* __restrict__ vol,
                         const double* __restrict__ U, const double* __restrict__ V, const double* __restrict__ W,
                         const double* __restrict__ old, int has_old, const double* __restrict__ sg,
-                        const double* __restrict__ sc, double* __restrict__ val, double* __restrict__ bm) {
+                        const double* __restrict__ sft, const double* __restrict__ sc, double* __restrict__ val,
+                        double* __restrict__ bm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     const size_t N = nc, NF = nf;
@@ -167,6 +168,7 @@ __global__ void k_mcell(int nc, int ni, int nf, double dt, const int* __restrict
         const double o2 = has_old ? old[(3 + c) * N + i] : cur[c];
         b[c] = -r * (1.5 * cur[c] - 2.0 * o1 + 0.5 * o2) * v / dt;
         b[c] += v * sg[c * N + i];
+        if (sft) b[c] += v * sft[c * N + i];   // surface tension (eqMomentum.cpp:320-322)
     }
     for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
         const int e = cfi[k], f = e & kFaceMask;
@@ -238,6 +240,7 @@ void assemble_momentum(semo_ctx* c) {
         a.P = c->P; a.U = c->U; a.V = c->V; a.W = c->W; a.irho = c->irho; a.grad = c->grad; a.mm = c->mm; a.sg = c->sg;
         a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
         a.use_gravity = c->phys.use_gravity;
+        set_sft_args(c, a);
         a.val = c->Am_val; a.coef = nullptr; a.flux = nullptr; a.unf = nullptr;
         m.rho = c->rho; m.mu = c->mu; m.sc = c->msc;
         StageScope sc(c, ST_MFACE);
@@ -254,7 +257,8 @@ void assemble_momentum(semo_ctx* c) {
     StageScope sc(c, ST_MCELL);
     k_mcell<<<blocks(nc, T), T, 0, s>>>(nc, ni, nf, c->phys.dt, c->cf_ptr, c->cf_idx, c->A_dig, c->rho, c->vol,
                                          c->U, c->V, c->W, c->has_old ? c->old.p : nullptr, c->has_old ? 1 : 0,
-                                         c->sg, c->msc, c->Am_val, c->bm);
+                                         c->sg, (c->phys.sigma != 0.0 && c->sft_current) ? c->sft.p + 2 * (size_t)nc : nullptr,
+                                         c->msc, c->Am_val, c->bm);
     SEMO_CHECK_LAUNCH();
 }
 

@@ -39,13 +39,13 @@ extern long long g_kernel_launches;
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
              ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_MSTACS, ST_VFACE, ST_VSOLVE, ST_VUPDATE,
-             ST_STENCIL_UVW, ST_MBFACE, ST_CGRAD, ST_CFACE, ST_CCELL, ST_CSOLVE, ST_CUPDATE, ST_COUNT };
+             ST_STENCIL_UVW, ST_MBFACE, ST_CGRAD, ST_CFACE, ST_CCELL, ST_CSOLVE, ST_CUPDATE, ST_SFT, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
                                                   "setup_level", "setup_coarse", "mface", "mcell", "msolve",
                                                   "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw", "mbface",
-                                                  "cgrad", "cface", "ccell", "csolve", "cupdate"};
+                                                  "cgrad", "cface", "ccell", "csolve", "cupdate", "surface_tension"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -180,6 +180,12 @@ struct semo_ctx {
     // the gravity source was computed since the last change of fields or physics
     // (the VOF sub-iterations keep it, as SEMO keeps its per-time-step source)
     bool sg_current = false;
+    // curvature and surface-tension source (phys.sigma != 0): planes of nc
+    // 0 kappa, 1 ls, 2-5 src (x, y, z, .U), 6-11 scratch; computed with the
+    // gravity source and kept with it
+    semo::DBuf<double> sft;
+    semo::DBuf<int> sft_iface;
+    bool sft_current = false;
 
     // ---- volume fraction (RCM order; matrix on the A_ptr/A_col pattern) ----
     semo::DBuf<double> oldvf;                     // 2 planes: oldVF, old2VF
@@ -293,6 +299,9 @@ void assemble_gravity_stencil(semo_ctx* c);
 void assemble_gravity(semo_ctx* c);
 // full: all five fields; else U, V, W only (P and VF planes left as they are)
 void stencil_pass(semo_ctx* c, bool full);
+// surftens.cu: curvature and surface-tension source (no-op when sigma == 0);
+// after assemble_face_values and a full stencil_pass
+void assemble_surface_tension(semo_ctx* c);
 // dst[q][r] = src[q*n + perm[r]] for q < planes; false if any value is not finite (syncs)
 bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst, int planes);
 // dst[q*n + perm[r]] = src[q][r] for q < planes (async)

@@ -225,9 +225,12 @@ void assemble_vof(semo_ctx* c) {
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
     assemble_face_values(c, false);
-    // the gravity source is the one of the time step (computed once, as SEMO does before its outer loop)
-    if (!c->sg_current) assemble_gravity(c);
+    // the gravity and surface-tension sources are the time step's (computed
+    // once, as SEMO does before its outer loop)
+    const bool fresh = !c->sg_current;
+    if (fresh) assemble_gravity(c);
     stencil_pass(c, true);
+    if (fresh || (c->phys.sigma != 0.0 && !c->sft_current)) assemble_surface_tension(c);
     c->co.alloc(nc, s);
     c->fvf.alloc(2 * (size_t)std::max(ni, 1), s);
     c->Av_val.alloc(c->nnz, s);
@@ -254,6 +257,7 @@ void assemble_vof(semo_ctx* c) {
         a.P = c->P; a.U = c->U; a.V = c->V; a.W = c->W; a.irho = c->irho; a.grad = c->grad; a.mm = c->mm; a.sg = c->sg;
         a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
         a.use_gravity = c->phys.use_gravity;
+        set_sft_args(c, a);
         a.val = c->Av_val; a.coef = nullptr; a.flux = nullptr; a.unf = nullptr;
         m.fvf = c->fvf; m.sc = c->vsc;
         k_vface<<<blocks(ni, 256), 256, 0, s>>>(m);
