@@ -70,6 +70,9 @@ typedef struct {
     /* momentum solve (BiCGStab, Jacobi preconditioner, per right-hand side) */
     double mom_tol;              /* relative residual, default 1e-9 (SEMO's momentum tolerance) */
     int mom_max_iter;            /* default 1000 */
+    int overlap_setup;           /* semo_outer_iteration assembles the pressure matrix (which depends only on
+                                    geometry, dt and the densities) and builds its hierarchy on a second stream
+                                    while the momentum pass runs; same results bit for bit; default 1 */
 } semo_params;
 
 /* Physics of one outer iteration (calcMomentumEqs / calcPressureEq inputs). */

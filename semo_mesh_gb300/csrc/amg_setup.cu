@@ -112,17 +112,20 @@ __global__ void k_diag(int n, const int* __restrict__ ptr, const int* __restrict
                        V* __restrict__ dia, V* __restrict__ dinv, double* __restrict__ ratio, int* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double d = 0.0, rs = 0.0;
+    // in the value type: an FP32 hierarchy takes its reciprocals and the
+    // Gershgorin ratio (an estimate for the Chebyshev interval) in FP32, with
+    // no FP64 conversions or divisions (slow on this part) per row
+    V d = V(0), rs = V(0);
     for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
-        const double v = (double)val[k];
+        const V v = val[k];
         if (col[k] == i) d = v;
         rs += fabs(v);
     }
-    if (!(d > 0.0) && !(d < 0.0)) atomicExch(flag + 2, 1);   // zero diagonal
+    if (!(d > V(0)) && !(d < V(0))) atomicExch(flag + 2, 1);   // zero diagonal
     if (!isfinite(d) || !isfinite(rs)) atomicExch(flag + 3, 1);
-    dia[i] = (V)d;
-    dinv[i] = (V)(1.0 / d);
-    ratio[i] = rs / fabs(d);
+    dia[i] = d;
+    dinv[i] = V(1) / d;
+    ratio[i] = (double)(rs / fabs(d));
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_max(int n, const double* __restrict__ a, double* __restrict__ part) {
@@ -756,11 +759,15 @@ __global__ void k_gauss_jordan(int n, double* __restrict__ a, double* __restrict
 
 // ------------------------------------------------------------- host helpers
 // lanes per row for the per-row setup kernels, from the average row length
+inline int row_lanes(int64_t nnz, int n) {
+    const double avg = n ? (double)nnz / n : 1.0;
+    return avg <= 12.0 ? 1 : (avg <= 48.0 ? 8 : 32);
+}
 template <class F>
 void with_row_lanes(int64_t nnz, int n, F&& f) {
-    const double avg = n ? (double)nnz / n : 1.0;
-    if (avg <= 12.0) f(std::integral_constant<int, 1>{});
-    else if (avg <= 48.0) f(std::integral_constant<int, 8>{});
+    const int vs = row_lanes(nnz, n);
+    if (vs == 1) f(std::integral_constant<int, 1>{});
+    else if (vs == 8) f(std::integral_constant<int, 8>{});
     else f(std::integral_constant<int, 32>{});
 }
 
@@ -889,14 +896,14 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
 
 template <class V>
 void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia) {
-    cudaStream_t s = c->stream;
+    cudaStream_t s = setup_stream(c);
     const int n = L.A.n;
     L.dinv.alloc(n, s);
     dia.alloc(n, s);
     DBuf<double> ratio, part;
     ratio.alloc(n, s);
     part.alloc(kRedBlocks, s);
-    k_diag<V><<<blocks(n, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, dia, L.dinv, ratio, c->flag);
+    k_diag<V><<<blocks(n, 256), 256, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, dia, L.dinv, ratio, c->sflag);
     SEMO_CHECK_LAUNCH();
     k_max<<<kRedBlocks, kRedThreads, 0, s>>>(n, ratio, part);
     SEMO_CHECK_LAUNCH();
@@ -911,7 +918,9 @@ void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia) {
 
 template <class V>
 void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val64, int n, int64_t nnz) {
-    cudaStream_t s = c->stream;
+    cudaStream_t s = setup_stream(c);
+    c->sflag.alloc(16, s);
+    SEMO_CUDA(cudaMemsetAsync(c->sflag.p, 0, 16 * sizeof(int), s));
     h.clear();
     h.lev.reserve(c->prm.max_levels + 1);
     h.lev.emplace_back();
@@ -1020,26 +1029,37 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         L.P.ptr.alloc(nl + 1, s);
         SEMO_CUDA(cudaMemsetAsync(L.P.ptr.p + nl, 0, sizeof(int), s));
         DBuf<unsigned char> first;
-        // one thread a row costs O(row length x aggregates in the row), the
-        // lane version O(row length^2 / lanes): lanes only for the longest rows
-        const int lanes = ((double)L.A.nnz > 48.0 * (double)nl) ? 32 : 1;
+        // counting: one thread a row costs O(row length x aggregates in the
+        // row), the lane version O(row length^2 / lanes): a thread a row for
+        // the finest level's short rows, lanes for the coarse levels' long ones
+        const int lanes = row_lanes(L.A.nnz, nl);
         if (lanes == 1) {
             k_prolong_count<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg, L.P.ptr);
         } else {
             first.alloc(std::max<int64_t>(L.A.nnz, 1), s);
-            k_prolong_count_vs<32><<<blocks((int64_t)nl * 32, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, strong, agg,
-                                                                                 first, L.P.ptr);
+            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                constexpr int VS = decltype(vs)::value;
+                if constexpr (VS > 1)
+                    k_prolong_count_vs<VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col,
+                                                                                         strong, agg, first, L.P.ptr);
+            });
         }
         SEMO_CHECK_LAUNCH();
         L.P.nnz = scan_exclusive(s, L.P.ptr.p, nl + 1);
         L.P.col.alloc(std::max<int64_t>(L.P.nnz, 1), s);
         L.P.val.alloc(std::max<int64_t>(L.P.nnz, 1), s);
-        if (lanes == 1) {
+        // filling: the lane version rescans the row per output entry, which
+        // only pays for the longest rows; both give the same values and order
+        if (lanes < 32) {
             k_prolong_fill<V><<<blocks(nl, 256), 256, 0, s>>>(nl, L.A.ptr, L.A.col, L.A.val, strong, agg, omega,
                                                               L.P.ptr, L.P.col, L.P.val);
         } else {
-            k_prolong_fill_vs<V, 32><<<blocks((int64_t)nl * 32, 256), 256, 0, s>>>(
-                nl, L.A.ptr, L.A.col, L.A.val, strong, agg, first, omega, L.P.ptr, L.P.col, L.P.val);
+            with_row_lanes(L.A.nnz, nl, [&](auto vs) {
+                constexpr int VS = decltype(vs)::value;
+                if constexpr (VS > 1)
+                    k_prolong_fill_vs<V, VS><<<blocks((int64_t)nl * VS, 256), 256, 0, s>>>(
+                        nl, L.A.ptr, L.A.col, L.A.val, strong, agg, first, omega, L.P.ptr, L.P.col, L.P.val);
+            });
         }
         SEMO_CHECK_LAUNCH();
         transpose(s, L.P, L.R);
@@ -1064,10 +1084,10 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     h.cinv.alloc((size_t)m * m, s);
     k_dense<V><<<1, 1024, 0, s>>>(m, Lc.A.ptr, Lc.A.col, Lc.A.val, dense);
     SEMO_CHECK_LAUNCH();
-    k_gauss_jordan<<<1, 1024, 0, s>>>(m, dense, h.cinv, c->flag);
+    k_gauss_jordan<<<1, 1024, 0, s>>>(m, dense, h.cinv, c->sflag);
     SEMO_CHECK_LAUNCH();
     int hf[5] = {0, 0, 0, 0, 0};
-    SEMO_CUDA(cudaMemcpyAsync(hf, c->flag.p, sizeof(hf), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hf, c->sflag.p, sizeof(hf), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
     if (hf[2]) throw Error(SEMO_ERR_ARGUMENT, "matrix has a zero diagonal entry");
     if (hf[3]) throw Error(SEMO_ERR_NAN, "non-finite matrix entry");

@@ -220,7 +220,22 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
     }
 }
 
-// Internal faces of calcPressureEq (UnF as face_unf).
+// Pressure-matrix coefficients, written with explicit roundings so that the
+// early matrix (pressure_matrix) and the pass's own assembly agree bit for bit.
+// Internal face: kA dt (wR/rhoL + wR/rhoR), SEMO's rho* = 1/(wCR/rhoL + wCR/rhoR)
+// (wCR twice, eqPressure.cpp:396).
+__device__ __forceinline__ double pcoef_face(double kA, double dt, double wR, double iRL, double iRR) {
+    return __dmul_rn(kA, __dmul_rn(dt, __dadd_rn(__dmul_rn(wR, iRL), __dmul_rn(wR, iRR))));
+}
+// Boundary face (eqPressure.cpp:570-673): fixedValue pressure alpha tmp1/dPN
+// area with tmp1 = dt/rhoF; zeroGradient 0 x the same
+__device__ __forceinline__ double pcoef_bface(bool fixed, double alpha, double tmp1, double dPN, double area) {
+    const double t = alpha * tmp1 / dPN * area;
+    return fixed ? 1.0 * t : 0.0 * t;
+}
+
+// Internal faces of calcPressureEq (UnF as face_unf).  With a.val null the
+// matrix values are left as they are (built beforehand by pressure_matrix).
 __global__ void __launch_bounds__(256) k_pface(FaceArgs a) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= a.ni) return;
@@ -229,10 +244,11 @@ __global__ void __launch_bounds__(256) k_pface(FaceArgs a) {
     const double UnF = face_unf(a, g, o, q);
     const double iRL = __ldg(a.irho + o), iRR = __ldg(a.irho + q);
     const double area = g.area;
-    // off-diagonal coefficient, with SEMO's rho* = 1/(wCR/rhoL + wCR/rhoR) (eqPressure.cpp:396)
-    const double coef = g.kA * (a.dt * (g.wR * iRL + g.wR * iRR));
-    a.val[a.lr[f]] = -coef;
-    a.val[a.rl[f]] = -coef;
+    const double coef = pcoef_face(g.kA, a.dt, g.wR, iRL, iRR);
+    if (a.val) {
+        a.val[a.lr[f]] = -coef;
+        a.val[a.rl[f]] = -coef;
+    }
     a.coef[f] = coef;
     a.flux[f] = UnF * area;
     a.unf[f] = UnF;
@@ -254,17 +270,13 @@ __global__ void k_pbface(int nb, int ni, int nf, int nc, const int* __restrict__
     const double tmp1 = 1.0 / bf[5 * nb + b] * dt;
     const bool fixed = bct[3 * bpatch[b]] == SEMO_BC_FIXED_VALUE;
     const double dPN = 0.5 * mpn[f], alpha = alf[f];
-    double d = 0.0;
     if (fixed) {
         UnF -= alpha * tmp1 * (bf[b] - P[o]) / dPN;
         UnF += alpha * tmp1 * grad[o] * epn[f];
         UnF += alpha * tmp1 * grad[nc + o] * epn[nf + f];
         UnF += alpha * tmp1 * grad[2 * (size_t)nc + o] * epn[2 * nf + f];
-        d = 1.0 * (alpha * tmp1 / dPN * area);
-    } else {
-        d = 0.0 * (alpha * tmp1 / dPN * area);
     }
-    coef[f] = d;
+    coef[f] = pcoef_bface(fixed, alpha, tmp1, dPN, area);
     flux[f] = UnF * area;
     unf[f] = UnF;
 }
@@ -282,8 +294,42 @@ __global__ void k_pcell(int nc, int ni, const int* __restrict__ cfp, const int* 
         if (e >> 30) s += flux[f]; else s -= flux[f];
     }
     if (src) s += src[i] * vol[i];
-    val[dig[i]] = d;
+    if (val) val[dig[i]] = d;
     b[i] = s;
+}
+
+// The matrix part of the three kernels above alone (values only, the same
+// roundings): face coefficients, off-diagonals, then the diagonal gather.
+__global__ void k_pmat_face(int nf, int ni, int nb, const int* __restrict__ own, const int* __restrict__ nei,
+                            const int* __restrict__ lr, const int* __restrict__ rl, const double* __restrict__ fk,
+                            const double* __restrict__ irho, const int* __restrict__ bpatch,
+                            const int* __restrict__ bct, const double* __restrict__ mpn,
+                            const double* __restrict__ alf, const double* __restrict__ fa,
+                            const double* __restrict__ bf, double dt, double* __restrict__ coef,
+                            double* __restrict__ val) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    if (f < ni) {
+        const double kA = fk[f], wR = 1.0 - fk[3 * ni + f];
+        const double c = pcoef_face(kA, dt, wR, __ldg(irho + own[f]), __ldg(irho + nei[f]));
+        val[lr[f]] = -c;
+        val[rl[f]] = -c;
+        coef[f] = c;
+    } else {
+        const int b = f - ni;
+        const double tmp1 = 1.0 / bf[5 * nb + b] * dt;
+        const bool fixed = bct[3 * bpatch[b]] == SEMO_BC_FIXED_VALUE;
+        coef[f] = pcoef_bface(fixed, alf[f], tmp1, 0.5 * mpn[f], fa[f]);
+    }
+}
+
+__global__ void k_pmat_cell(int nc, const int* __restrict__ cfp, const int* __restrict__ cfi,
+                            const int* __restrict__ dig, const double* __restrict__ coef, double* __restrict__ val) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    double d = 0.0;
+    for (int k = cfp[i]; k < cfp[i + 1]; ++k) d += coef[cfi[k] & kFaceMask];
+    val[dig[i]] = d;
 }
 
 // Gauss-Green sweep, face part: interpolated p' with skewness correction
@@ -517,7 +563,8 @@ void assemble_pressure(semo_ctx* c) {
         a.dt = c->phys.dt; a.g0 = c->phys.gravity[0]; a.g1 = c->phys.gravity[1]; a.g2 = c->phys.gravity[2];
         a.use_gravity = c->phys.use_gravity;
         set_sft_args(c, a);
-        a.val = c->A_val; a.coef = coef; a.flux = flux; a.unf = c->unf;
+        a.val = c->matrix_prebuilt ? nullptr : c->A_val.p;
+        a.coef = coef; a.flux = flux; a.unf = c->unf;
         StageScope sc(c, ST_PFACE);
         k_pface<<<blocks(ni, 256), 256, 0, s>>>(a);
         SEMO_CHECK_LAUNCH();
@@ -530,7 +577,22 @@ void assemble_pressure(semo_ctx* c) {
     }
     StageScope sc(c, ST_PCELL);
     k_pcell<<<blocks(nc, T), T, 0, s>>>(nc, ni, c->cf_ptr, c->cf_idx, c->A_dig, coef, flux,
-                                         c->has_src ? c->src.p : nullptr, c->vol, c->A_val, c->b);
+                                         c->has_src ? c->src.p : nullptr, c->vol,
+                                         c->matrix_prebuilt ? nullptr : c->A_val.p, c->b);
+    SEMO_CHECK_LAUNCH();
+}
+
+void pressure_matrix(semo_ctx* c, cudaStream_t s) {
+    const int T = 256;
+    const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
+    c->pm_coef.alloc(std::max(nf, 1), s);
+    if (nf > 0) {
+        k_pmat_face<<<blocks(nf, T), T, 0, s>>>(nf, ni, nb, c->own, c->nei, c->A_lr, c->A_rl, c->fk, c->irho,
+                                                 c->bpatch, c->bc_type, c->mpn, c->alf, c->fa, c->bface,
+                                                 c->phys.dt, c->pm_coef, c->A_val);
+        SEMO_CHECK_LAUNCH();
+    }
+    k_pmat_cell<<<blocks(nc, T), T, 0, s>>>(nc, c->cf_ptr, c->cf_idx, c->A_dig, c->pm_coef, c->A_val);
     SEMO_CHECK_LAUNCH();
 }
 

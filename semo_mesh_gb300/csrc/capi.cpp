@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <exception>
+#include <thread>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -61,6 +63,7 @@ void semo_params_default(semo_params* p) {
     p->reuse_hierarchy = 1;
     p->mom_tol = 1e-9;
     p->mom_max_iter = 1000;
+    p->overlap_setup = 1;
 }
 
 void semo_physics_default(semo_physics* p) {
@@ -101,11 +104,17 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
             throw Error(SEMO_ERR_NO_DEVICE, "library built for sm_103a, device is sm_" +
                                                 std::to_string(dp.major) + std::to_string(dp.minor));
         SEMO_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->setup_s = c->stream;
         // keep freed blocks in the stream-ordered pool instead of returning them
         cudaMemPool_t pool;
         SEMO_CUDA(cudaDeviceGetDefaultMemPool(&pool, c->device));
         uint64_t thr = UINT64_MAX;
         SEMO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        // a block freed on one stream is not handed to another stream by making
+        // that stream wait for the first (the pressure setup runs on a second
+        // stream beside the momentum pass and must not be serialised behind it)
+        int no_deps = 0;
+        SEMO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no_deps));
         for (auto& e : c->ev) SEMO_CUDA(cudaEventCreate(&e));
         c->flag.alloc(16, c->stream);
         c->flag.zero();
@@ -124,6 +133,8 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
         cudaSetDevice(c->device);
         cudaStreamSynchronize(c->stream);
     }
+    if (c->aux_stream) cudaStreamSynchronize(c->aux_stream);
+    for (auto& e : c->ov_ev) if (e) cudaEventDestroy(e);
     c->amg64.clear();
     c->amg32.clear();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
@@ -132,8 +143,9 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     for (auto& e : c->sync_ev) if (e) cudaEventDestroy(e);
     if (c->hpin) cudaFreeHost(c->hpin);
     if (c->hpin_int) cudaFreeHost(c->hpin_int);
-    cudaStream_t s = c->stream;
-    delete c;  // DBuf destructors enqueue frees on the (still valid) stream
+    cudaStream_t s = c->stream, aux = c->aux_stream;
+    delete c;  // DBuf destructors enqueue frees on the (still valid) streams
+    if (aux) { cudaStreamSynchronize(aux); cudaStreamDestroy(aux); }
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
     return SEMO_OK;
 }
@@ -679,11 +691,11 @@ semo_status pressure_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info)
 }
 
 // calcMomentumEqs: assemble, three solves, update (skipped after a breakdown).
-semo_status momentum_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info) {
+semo_status momentum_pass_impl(semo_ctx* c, double* norm, semo_solve_info* info, bool face_values_done = false) {
     need(c->mesh_ready && c->phys_ready && c->fields_ready, SEMO_ERR_STATE,
          "mesh, physics and fields must be set before a pass");
     SEMO_CUDA(cudaSetDevice(c->device));
-    semo::assemble_momentum(c);
+    semo::assemble_momentum(c, face_values_done);
     c->mom_assembled = true;
     semo_solve_info inf[3] = {};
     semo_status conv = semo::solve_momentum(c, inf);
@@ -774,16 +786,105 @@ semo_status semo_solve_momentum(semo_ctx* c, double* x, semo_solve_info* info) {
     return finish(c, st, conv, "momentum solve did not reach the tolerance");
 }
 
+namespace {
+// The pressure matrix and its AMG hierarchy built on the second stream, the
+// hierarchy from a second host thread, while this thread runs the momentum
+// pass and the pressure assembly on the context's stream.  The pressure
+// matrix reads only geometry, dt, the cell densities and the boundary
+// densities of the face values, which neither of those changes, so it equals
+// the one the pressure pass would assemble (the same kernels' roundings) and
+// so does its hierarchy.  The destructor joins the thread (also when a pass
+// throws) and puts the setup back on the context's stream.
+struct SideSetup {
+    semo_ctx* c;
+    std::thread th;
+    std::exception_ptr err;
+    explicit SideSetup(semo_ctx* ctx) : c(ctx) {
+        if (!c->aux_stream) {
+            // high priority: the setup is a chain of short dependent launches and
+            // host round trips, so its blocks go first whenever the momentum
+            // pass's kernels would otherwise hold every SM
+            int least = 0, greatest = 0;
+            SEMO_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            SEMO_CUDA(cudaStreamCreateWithPriority(&c->aux_stream, cudaStreamNonBlocking, greatest));
+        }
+        for (auto& e : c->ov_ev)
+            if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        // host resources the setup creates on first use, made here on this thread
+        if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
+        for (auto& e : c->sync_ev)
+            if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        SEMO_CUDA(cudaEventRecord(c->ov_ev[0], c->stream));   // face values (densities) are on the stream
+        SEMO_CUDA(cudaStreamWaitEvent(c->aux_stream, c->ov_ev[0], 0));
+        semo::pressure_matrix(c, c->aux_stream);
+        SEMO_CUDA(cudaEventRecord(c->ov_ev[2], c->aux_stream));   // the face values may be rewritten after this
+        c->setup_s = c->aux_stream;
+        th = std::thread([this] {
+            try {
+                SEMO_CUDA(cudaSetDevice(c->device));
+                semo::pressure_setup(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, true, nullptr);
+                SEMO_CUDA(cudaEventRecord(c->ov_ev[1], c->aux_stream));
+            } catch (...) {
+                err = std::current_exception();
+            }
+        });
+    }
+    // join; rethrow a setup failure; the context's stream then waits for the hierarchy
+    void finish() {
+        th.join();
+        c->setup_s = c->stream;
+        if (err) std::rethrow_exception(err);
+        SEMO_CUDA(cudaStreamWaitEvent(c->stream, c->ov_ev[1], 0));
+    }
+    ~SideSetup() {
+        if (th.joinable()) th.join();
+        c->setup_s = c->stream;
+    }
+};
+
+// the pressure pass with the side setup: its assembly leaves A_val alone and
+// its solve first joins the setup (solve_system calls before_solve)
+struct PrebuiltFlag {
+    semo_ctx* c;
+    PrebuiltFlag(semo_ctx* ctx, SideSetup& ss) : c(ctx) {
+        c->matrix_prebuilt = true;
+        c->before_solve = [&ss] { ss.finish(); };
+    }
+    ~PrebuiltFlag() {
+        c->matrix_prebuilt = false;
+        c->before_solve = nullptr;
+    }
+};
+}  // namespace
+
 semo_status semo_outer_iteration(semo_ctx* c, double* norms, semo_solve_info* info) {
     semo_status conv = SEMO_OK;
     semo_status st = guarded(c, [&] {
         semo_solve_info inf[4] = {};
         double nm[2] = {0.0, 0.0};
-        semo_status cm = momentum_pass_impl(c, &nm[0], inf);
-        if (cm == SEMO_ERR_BREAKDOWN) { conv = cm; }
-        else {
-            semo_status cp = pressure_pass_impl(c, &nm[1], &inf[3]);
-            conv = (cp != SEMO_OK) ? cp : cm;
+        if (c->prm.overlap_setup && c->mesh_ready && c->phys_ready && c->fields_ready) {
+            SEMO_CUDA(cudaSetDevice(c->device));
+            semo::assemble_face_values(c, true);
+            SideSetup ss(c);
+            const semo_status cm = momentum_pass_impl(c, &nm[0], inf, true);
+            if (cm == SEMO_ERR_BREAKDOWN) {
+                ss.finish();
+                conv = cm;
+            } else {
+                // the pressure pass rewrites the face values the early matrix read
+                SEMO_CUDA(cudaStreamWaitEvent(c->stream, c->ov_ev[2], 0));
+                PrebuiltFlag pb(c, ss);
+                const semo_status cp = pressure_pass_impl(c, &nm[1], &inf[3]);
+                conv = (cp != SEMO_OK) ? cp : cm;
+            }
+        } else {
+            const semo_status cm = momentum_pass_impl(c, &nm[0], inf);
+            if (cm == SEMO_ERR_BREAKDOWN) {
+                conv = cm;
+            } else {
+                const semo_status cp = pressure_pass_impl(c, &nm[1], &inf[3]);
+                conv = (cp != SEMO_OK) ? cp : cm;
+            }
         }
         if (norms) { norms[0] = nm[0]; norms[1] = nm[1]; }
         if (info) for (int j = 0; j < 4; ++j) info[j] = inf[j];

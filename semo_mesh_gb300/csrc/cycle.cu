@@ -862,7 +862,7 @@ ApplyState& apply_state(semo_ctx* c) {
 
 template <class V>
 void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
-    cudaStream_t s = c->stream;
+    cudaStream_t s = setup_stream(c);
     const int nl = (int)h.lev.size();
     cy.lev.resize(std::max(nl - 1, 0));
     for (int l = 0; l + 1 < nl; ++l) {
@@ -871,7 +871,7 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
         M.a = sell_pays(L.A);
         M.p = sell_pays(L.P);
         M.r = sell_pays(L.R);
-        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, c->flag.p + 11);
+        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, c->sflag.p + 11);
         if (M.a16) M.a = false;
         if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
         if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
@@ -1144,11 +1144,12 @@ MomState& mom_state(semo_ctx* c) {
 
 }  // namespace
 
-void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
-                  const double* b, double* x, semo_solve_info* info, bool zero_guess, bool may_reuse) {
-    cudaStream_t s = c->stream;
+void pressure_setup(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
+                    bool may_reuse, semo_solve_info* info) {
+    cudaStream_t s = setup_stream(c);
     ApplyState& st = apply_state(c);
-    c->flag.zero();
+    c->sflag.alloc(16, s);
+    SEMO_CUDA(cudaMemsetAsync(c->sflag.p, 0, 16 * sizeof(int), s));
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
     {
         StageScope sc(c, ST_AMG_SETUP);
@@ -1163,10 +1164,10 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
         const bool have = (c->prm.precision == SEMO_PREC_MIXED) ? h32.ready : h64.ready;
         if (may_reuse && c->prm.reuse_hierarchy && have && st.src_prec == c->prm.precision && st.src_n == n &&
             st.src_nnz == nnz) {
-            k_differs<<<kRedBlocks, kRedThreads, 0, s>>>(nnz, val, st.src_val, c->flag.p + 10);
+            k_differs<<<kRedBlocks, kRedThreads, 0, s>>>(nnz, val, st.src_val, c->sflag.p + 10);
             SEMO_CHECK_LAUNCH();
             int differs = 1;
-            SEMO_CUDA(cudaMemcpyAsync(&differs, c->flag.p + 10, sizeof(int), cudaMemcpyDeviceToHost, s));
+            SEMO_CUDA(cudaMemcpyAsync(&differs, c->sflag.p + 10, sizeof(int), cudaMemcpyDeviceToHost, s));
             SEMO_CUDA(cudaStreamSynchronize(s));
             reuse = differs == 0;
         }
@@ -1180,7 +1181,7 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
                 build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
                 prepare_cycle(c, c->amg64, st.cy64);
             }
-            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->flag.p + 11);
+            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->sflag.p + 11);
             if (!st.outer.use16) build_sell<double, double>(s, ptr, col, val, n, st.outer.s32);
             st.src_prec = -1;
             if (may_reuse && c->prm.reuse_hierarchy) {
@@ -1192,7 +1193,24 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
             }
         }
     }
-    SEMO_CUDA(cudaEventRecord(c->ev[1], s));
+    SEMO_CUDA(cudaEventRecord(c->ev[1], s));   // setup_ms is read from ev[0..1] after the solve
+    (void)info;
+}
+
+void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val, int n, int64_t nnz,
+                  const double* b, double* x, semo_solve_info* info, bool zero_guess, bool may_reuse) {
+    cudaStream_t s = c->stream;
+    // with matrix_prebuilt the hierarchy is being built beside this thread's
+    // work; before_solve joins that setup and makes this stream wait for it
+    if (c->before_solve) {
+        auto f = std::move(c->before_solve);
+        c->before_solve = nullptr;
+        f();
+    }
+    ApplyState& st = apply_state(c);
+    c->flag.zero();
+    if (!c->matrix_prebuilt) pressure_setup(c, ptr, col, val, n, nnz, may_reuse, info);
+    SEMO_CUDA(cudaEventRecord(c->ev[2], s));
     {
         StageScope sc(c, ST_PCG);
         if (c->prm.precision == SEMO_PREC_MIXED) {
@@ -1203,11 +1221,14 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
             fill_info(c->amg64, nnz, info);
         }
     }
-    SEMO_CUDA(cudaEventRecord(c->ev[2], s));
-    SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
+    SEMO_CUDA(cudaEventRecord(c->ev[3], s));
+    SEMO_CUDA(cudaEventSynchronize(c->ev[3]));
+    // the setup events may be on the other stream: their completion is
+    // observed explicitly before their elapsed time is read
+    SEMO_CUDA(cudaEventSynchronize(c->ev[1]));
     float t0 = 0, t1 = 0;
     SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
-    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
+    SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[2], c->ev[3]));
     info->setup_ms = t0;
     info->solve_ms = t1;
 }

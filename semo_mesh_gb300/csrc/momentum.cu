@@ -220,11 +220,11 @@ __global__ void __launch_bounds__(kRedThreads) k_mupdate(int nc, double urf, con
 
 namespace semo {
 
-void assemble_momentum(semo_ctx* c) {
+void assemble_momentum(semo_ctx* c, bool face_values_done) {
     const int T = 256;
     cudaStream_t s = c->stream;
     const int nc = c->nc, nf = c->nf, ni = c->ni, nb = c->nb;
-    assemble_face_values(c, true);
+    if (!face_values_done) assemble_face_values(c, true);
     c->pvf_current = false;
     assemble_gravity_stencil(c);
     c->pvf_current = true;

@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -215,6 +217,22 @@ struct semo_ctx {
     semo::DBuf<double> red;                       // reduction partials
     semo::DBuf<int> flag;                         // device error flags
 
+    // ---- pressure hierarchy built beside the momentum pass ----
+    // The pressure matrix depends only on geometry, dt and the densities, so
+    // semo_outer_iteration assembles it and builds its AMG hierarchy on a
+    // second stream (from a second host thread) while the momentum pass runs.
+    // The setup functions launch on setup_s (the context's stream otherwise)
+    // and report through sflag; the pressure pass then leaves A_val alone.
+    cudaStream_t aux_stream = nullptr;
+    cudaStream_t setup_s = nullptr;
+    semo::DBuf<int> sflag;                        // setup error flags (16)
+    semo::DBuf<double> pm_coef;                   // face coefficients of the early matrix (nf)
+    bool matrix_prebuilt = false;
+    std::function<void()> before_solve;           // with matrix_prebuilt: join the setup, wait for it
+    // face values done (main) / hierarchy done (aux) / early matrix done (aux)
+    cudaEvent_t ov_ev[3] = {nullptr, nullptr, nullptr};
+    std::mutex prof_mu;                           // stage timers are recorded from both threads
+
     // solver state
     semo::Amg<double> amg64;
     semo::Amg<float> amg32;
@@ -247,18 +265,34 @@ inline cudaEvent_t take_event(semo_ctx* c) {
     return e;
 }
 
+// the stream the AMG setup launches on
+inline cudaStream_t setup_stream(const semo_ctx* c) { return c->setup_s ? c->setup_s : c->stream; }
+
+// the AMG setup stages run on setup_s
+inline bool is_setup_stage(int st) {
+    return st == ST_AMG_SETUP || st == ST_SETUP_AGG || st == ST_SETUP_PROLONG || st == ST_SETUP_GALERKIN ||
+           st == ST_SETUP_LEVEL || st == ST_SETUP_COARSE;
+}
+
 // RAII: times the enclosed launches of one stage when profiling is enabled.
 struct StageScope {
     semo_ctx* c;
     int stage;
+    cudaStream_t s;
     cudaEvent_t a = nullptr;
     StageScope(semo_ctx* ctx, int st) : c(ctx), stage(st) {
-        if (c->profiling) { a = take_event(c); cudaEventRecord(a, c->stream); }
+        s = is_setup_stage(st) ? setup_stream(c) : c->stream;
+        if (c->profiling) {
+            std::lock_guard<std::mutex> lk(c->prof_mu);
+            a = take_event(c);
+            cudaEventRecord(a, s);
+        }
     }
     ~StageScope() {
         if (a) {
+            std::lock_guard<std::mutex> lk(c->prof_mu);
             cudaEvent_t b = take_event(c);
-            cudaEventRecord(b, c->stream);
+            cudaEventRecord(b, s);
             c->pending.push_back({stage, a, b});
         }
     }
@@ -266,6 +300,7 @@ struct StageScope {
 
 // Accumulate finished stage timings (call after the stream is synchronized).
 inline void resolve_stage_timers(semo_ctx* c) {
+    std::lock_guard<std::mutex> lk(c->prof_mu);
     for (auto& p : c->pending) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
@@ -333,9 +368,18 @@ void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, con
 // exclusive scan of d[0..n) in place on the context's stream; returns the total
 int device_scan(cudaStream_t s, int* d, int n);
 
+// pressure matrix values only (A_val: off-diagonals and diagonal, the values
+// assemble_pressure writes) on stream s, after assemble_face_values
+void pressure_matrix(semo_ctx* c, cudaStream_t s);
+
 // cycle.cu
+// AMG hierarchy (and the FP64 outer operator) of the matrix, on c->setup_s;
 // may_reuse: the matrix is the context's own pressure system, so a hierarchy
-// built from bit-identical values may be kept (semo_params.reuse_hierarchy)
+// built from bit-identical values may be kept (semo_params.reuse_hierarchy).
+// Records the setup time in info->setup_ms.
+void pressure_setup(semo_ctx* c, const int* d_ptr, const int* d_col, const double* d_val, int n, int64_t nnz,
+                    bool may_reuse, semo_solve_info* info);
+// setup (unless c->matrix_prebuilt: the hierarchy is already there) and solve
 void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double* d_val, int n, int64_t nnz,
                   const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess, bool may_reuse = false);
 
@@ -346,8 +390,8 @@ semo_status solve_momentum(semo_ctx* c, semo_solve_info* info);
 // the volume-fraction system (c->Av_val, c->bvf) -> c->xvf; info[1]
 semo_status solve_vof(semo_ctx* c, semo_solve_info* info);
 
-// momentum.cu
-void assemble_momentum(semo_ctx* c);
+// momentum.cu (face_values_done: assemble_face_values(c, true) already ran)
+void assemble_momentum(semo_ctx* c, bool face_values_done = false);
 double momentum_update(semo_ctx* c);
 
 // vof.cu

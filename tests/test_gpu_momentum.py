@@ -145,3 +145,42 @@ def test_old_velocity_arguments(semo):
     p = u.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     assert ctx.L.semo_set_old_velocity(ctx.h, p, None, None, None, None, None) == 1
     assert ctx.L.semo_set_old_velocity(ctx.h, None, None, None, None, None, None) == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("reuse", [False, True])
+def test_overlapped_setup_is_bit_identical(semo, precision, reuse):
+    """The pressure hierarchy built on the second stream during the momentum
+    pass (semo_params.overlap_setup) gives the serial path's results bit for
+    bit, over several outer iterations (with and without hierarchy reuse)."""
+    from semo_mesh_gb300.cases import vof_case, with_history, with_fields
+    case = with_history(with_fields(vof_case(20, jitter=0.2), seed=31, p_scale=50.0), seed=32)
+    runs = []
+    for overlap in (True, False):
+        ctx = semo.Context(precision=precision, tol=1e-8, reuse_hierarchy=reuse, overlap_setup=overlap)
+        ctx.set_case(case)
+        norms, iters = [], []
+        for _ in range(3):
+            nm, info = ctx.outer_iteration()
+            norms.append(nm)
+            iters.append(info[3]["iterations"])
+        runs.append((norms, iters, ctx.fields(), ctx.system_rcm()))
+    (n1, i1, f1, s1), (n2, i2, f2, s2) = runs
+    assert n1 == n2 and i1 == i2
+    for k in ("P", "U", "V", "W"):
+        assert np.array_equal(f1[k], f2[k]), k
+    assert np.array_equal(s1["val"], s2["val"]) and np.array_equal(s1["b"], s2["b"])
+
+
+def test_overlapped_setup_with_profiling(semo):
+    """Stage timers recorded from both host threads (setup on the second stream)."""
+    from semo_mesh_gb300.cases import vof_case, with_history
+    case = with_history(vof_case(16), seed=33)
+    ctx = semo.Context(precision="mixed", reuse_hierarchy=False)
+    ctx.set_case(case)
+    ctx.set_profiling(True)
+    for _ in range(2):
+        ctx.outer_iteration()
+    st = ctx.stage_times()
+    assert st["amg_setup"][1] == 2 and st["amg_setup"][0] > 0.0
+    assert st["setup_galerkin"][1] > 0 and st["mface"][1] == 2
