@@ -112,20 +112,17 @@ __global__ void k_diag(int n, const int* __restrict__ ptr, const int* __restrict
                        V* __restrict__ dia, V* __restrict__ dinv, double* __restrict__ ratio, int* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    // in the value type: an FP32 hierarchy takes its reciprocals and the
-    // Gershgorin ratio (an estimate for the Chebyshev interval) in FP32, with
-    // no FP64 conversions or divisions (slow on this part) per row
-    V d = V(0), rs = V(0);
+    double d = 0.0, rs = 0.0;
     for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
-        const V v = val[k];
+        const double v = (double)val[k];
         if (col[k] == i) d = v;
         rs += fabs(v);
     }
-    if (!(d > V(0)) && !(d < V(0))) atomicExch(flag + 2, 1);   // zero diagonal
+    if (!(d > 0.0) && !(d < 0.0)) atomicExch(flag + 2, 1);   // zero diagonal
     if (!isfinite(d) || !isfinite(rs)) atomicExch(flag + 3, 1);
-    dia[i] = d;
-    dinv[i] = V(1) / d;
-    ratio[i] = (double)(rs / fabs(d));
+    dia[i] = (V)d;
+    dinv[i] = (V)(1.0 / d);
+    ratio[i] = rs / fabs(d);
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_max(int n, const double* __restrict__ a, double* __restrict__ part) {

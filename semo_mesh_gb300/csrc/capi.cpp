@@ -4,6 +4,7 @@
 // topology lists, the vertex stencil, RCM and the CSR pattern.  Everything per
 // outer iteration runs on the GPU.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -822,8 +823,12 @@ struct SideSetup {
         th = std::thread([this] {
             try {
                 SEMO_CUDA(cudaSetDevice(c->device));
+                const auto t0 = std::chrono::steady_clock::now();
                 semo::pressure_setup(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, true, nullptr);
                 SEMO_CUDA(cudaEventRecord(c->ov_ev[1], c->aux_stream));
+                SEMO_CUDA(cudaEventSynchronize(c->ov_ev[1]));
+                c->side_setup_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             } catch (...) {
                 err = std::current_exception();
             }

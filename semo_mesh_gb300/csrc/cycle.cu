@@ -1223,11 +1223,13 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
     }
     SEMO_CUDA(cudaEventRecord(c->ev[3], s));
     SEMO_CUDA(cudaEventSynchronize(c->ev[3]));
-    // the setup events may be on the other stream: their completion is
-    // observed explicitly before their elapsed time is read
-    SEMO_CUDA(cudaEventSynchronize(c->ev[1]));
     float t0 = 0, t1 = 0;
-    SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
+    if (c->matrix_prebuilt) {
+        t0 = (float)c->side_setup_ms;   // the setup shared the GPU with the momentum pass
+    } else {
+        SEMO_CUDA(cudaEventSynchronize(c->ev[1]));
+        SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
+    }
     SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[2], c->ev[3]));
     info->setup_ms = t0;
     info->solve_ms = t1;

@@ -228,6 +228,7 @@ struct semo_ctx {
     semo::DBuf<int> sflag;                        // setup error flags (16)
     semo::DBuf<double> pm_coef;                   // face coefficients of the early matrix (nf)
     bool matrix_prebuilt = false;
+    double side_setup_ms = 0.0;                   // host time of the setup on its thread
     std::function<void()> before_solve;           // with matrix_prebuilt: join the setup, wait for it
     // face values done (main) / hierarchy done (aux) / early matrix done (aux)
     cudaEvent_t ov_ev[3] = {nullptr, nullptr, nullptr};
