@@ -549,16 +549,32 @@ __global__ void __launch_bounds__(128) k_spgemm_small(int n, const int* __restri
 // Row-wise SpGEMM C = A * B, one warp per row, open-addressing hash table in
 // shared memory.  Pass 0 counts distinct columns (flagging rows that fill
 // more than 3/4 of the table); pass 1 fills.  Products are consumed in a fixed
-// order (A entries in row order, B entries in chunks of 32); lanes that hit
-// the same column are combined in lane order by the lowest lane, so every sum
-// has a fixed association.  Occupied slots are compacted and ranked by
-// column, so output rows are sorted.
+// order (A entries in row order, B entries in chunks of 32) and summed as
+// 64-bit fixed-point integers (integer addition is associative, so the sums
+// do not depend on the order the shared-memory atomics land in): with
+// S = sum_k |a_ik| sum_j |b_kj| >= the row's sum of |products|, each product
+// is scaled by 2^s, S 2^s < 2^62, and rounded to an integer -- an error of at
+// most 2^-63 S per product, below what FP64 accumulation of the same
+// products incurs (2^-53 S per addition).  Occupied slots are compacted and
+// ranked by column, so output rows are sorted.
 constexpr int kGemmWarps = 4;
+
+// babs[k] = sum_j |b_kj| (FP64)
+template <class V>
+__global__ void k_row_abs(int n, const int* __restrict__ ptr, const V* __restrict__ val, double* __restrict__ babs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) s += fabs((double)val[k]);
+    babs[i] = s;
+}
+
 template <class V, int HT>
 __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __restrict__ aptr,
                                                             const int* __restrict__ acol, const V* __restrict__ aval,
                                                             const int* __restrict__ bptr, const int* __restrict__ bcol,
-                                                            const V* __restrict__ bval, int pass,
+                                                            const V* __restrict__ bval,
+                                                            const double* __restrict__ babs, int pass,
                                                             int* __restrict__ cnt, const int* __restrict__ cptr,
                                                             int* __restrict__ ccol, V* __restrict__ cval,
                                                             int* __restrict__ overflow,
@@ -566,11 +582,12 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                                                             int* __restrict__ list, int* __restrict__ nlist) {
     extern __shared__ unsigned char smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // per warp: keys[HT] int, ckeys[HT] int, vals[HT] double, cvals[HT] double
+    // per warp: keys[HT] int, ckeys[HT] int, vals[HT] and cvals[HT] 64-bit fixed point
     int* keys = reinterpret_cast<int*>(smem) + wid * 2 * HT;
     int* ckeys = keys + HT;
-    double* vals = reinterpret_cast<double*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
-    double* cvals = vals + HT;
+    unsigned long long* vals =
+        reinterpret_cast<unsigned long long*>(smem + sizeof(int) * 2 * HT * kGemmWarps) + wid * 2 * HT;
+    unsigned long long* cvals = vals + HT;
     // rows: all of them, or (list given, defer 0) the ones a previous launch deferred
     const int nrows = (list && !defer) ? *nlist : n;
     for (int idx = blockIdx.x * kGemmWarps + wid; idx < nrows; idx += gridDim.x * kGemmWarps) {
@@ -594,7 +611,21 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
         int ht = 32;
         while (ht < need && ht < HT) ht <<= 1;
         const int hmask = ht - 1;
-        for (int t = lane; t < ht; t += 32) { keys[t] = -1; vals[t] = 0.0; }
+        for (int t = lane; t < ht; t += 32) { keys[t] = -1; vals[t] = 0ull; }
+        // the row's fixed-point scale 2^sc (a fixed reduction tree: deterministic)
+        double up_scale = 1.0, down_scale = 1.0;
+        if (pass != 0) {
+            double bound = 0.0;
+            for (int ka = aptr[row] + lane; ka < aptr[row + 1]; ka += 32)
+                bound += fabs((double)aval[ka]) * babs[acol[ka]];
+            for (int o = 16; o > 0; o >>= 1) bound += __shfl_xor_sync(0xffffffffu, bound, o);
+            // bound < 2^e with e from the biased exponent (subnormals: e = -1022)
+            const int be = (int)((__double_as_longlong(bound) >> 52) & 0x7ff);
+            const int e = be ? be - 1022 : -1022;
+            const int sc = max(-960, min(1000, 62 - e));
+            up_scale = __longlong_as_double((long long)(1023 + sc) << 52);     // 2^sc
+            down_scale = __longlong_as_double((long long)(1023 - sc) << 52);   // 2^-sc
+        }
         __syncwarp();
         int distinct = 0;
         bool full = false;
@@ -642,18 +673,9 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 }
                 distinct += __popc(__ballot_sync(0xffffffffu, fresh));
                 const bool lost = __any_sync(0xffffffffu, act && slot < 0);
-                if (pass != 0 && !lost) {
-                    // lanes that hit the same column are summed in lane order by the lowest one
-                    const double pv = act ? av * (double)bval[q] : 0.0;
-                    const unsigned grp = __match_any_sync(0xffffffffu, act ? slot : -1 - lane);
-                    double sum = 0.0;
-                    unsigned m = grp;
-                    while (m) {
-                        const int l = __ffs(m) - 1;
-                        sum += __shfl_sync(grp, pv, l);
-                        m &= m - 1;
-                    }
-                    if (act && lane == __ffs(grp) - 1) vals[slot] += sum;
+                if (pass != 0 && !lost && act) {
+                    const long long fx = __double2ll_rn((av * (double)bval[q]) * up_scale);
+                    atomicAdd(vals + slot, (unsigned long long)fx);   // two's complement: signed sum mod 2^64
                 }
                 __syncwarp();
                 if (lost || distinct > (ht * 3) / 4) { full = true; break; }
@@ -696,7 +718,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 int rank = 0;
                 for (int u = 0; u < base_c; ++u) rank += (ckeys[u] < ce);
                 ccol[out + rank] = ce;
-                cval[out + rank] = (V)cvals[e];
+                cval[out + rank] = (V)((double)(long long)cvals[e] * down_scale);
             }
         }
         __syncwarp();
@@ -775,7 +797,8 @@ int pick_vs(const DCsr<V>& A) {
 }
 
 template <class V>
-void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, DCsr<V>& C, int* cnt,
+void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<V>& B, const double* babs,
+                 DCsr<V>& C, int* cnt,
                  int* overflow, const int* small, const int* cptr, int* ccol, V* cval, int defer, int* list,
                  int* nlist) {
     const int n = A.n;
@@ -785,7 +808,8 @@ void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<
     case H:                                                                                                      \
         if (shm > 48 * 1024)                                                                                     \
             SEMO_CUDA(cudaFuncSetAttribute(k_spgemm<V, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm)); \
-        k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, pass, cnt,  \
+        k_spgemm<V, H><<<grid, 32 * kGemmWarps, shm, s>>>(n, A.ptr, A.col, A.val, B.ptr, B.col, B.val, babs, pass, \
+                                                           cnt,                                                  \
                                                            cptr, ccol, cval, overflow, small, defer, list, nlist); \
         break;
     switch (ht) {
@@ -843,10 +867,14 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
             nlist.alloc(1, s);
             nlist.zero();
         }
-        spgemm_pass(s, first, 2, A, B, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, ht > first ? 1 : 0, list.p,
-                    nlist.p);
+        DBuf<double> babs;   // per B row sum of |b|: the fixed-point scales
+        babs.alloc(std::max(B.n, 1), s);
+        k_row_abs<V><<<blocks(B.n, 256), 256, 0, s>>>(B.n, B.ptr, B.val, babs);
+        SEMO_CHECK_LAUNCH();
+        spgemm_pass(s, first, 2, A, B, babs.p, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, ht > first ? 1 : 0,
+                    list.p, nlist.p);
         if (ht > first)
-            spgemm_pass(s, ht, 2, A, B, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, 0, list.p, nlist.p);
+            spgemm_pass(s, ht, 2, A, B, babs.p, C, cnt.p, flags.p, cnt.p, up.p, tcol.p, tval.p, 0, list.p, nlist.p);
     }
     SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, cnt.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
     SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
