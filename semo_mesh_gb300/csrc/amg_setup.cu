@@ -72,31 +72,38 @@ __global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__
     if (i < n) out[i] += tile_off[i / kScanTile];
 }
 
-// exclusive scan of d[0..n) in place; returns the total (host sync)
-int scan_exclusive(cudaStream_t s, int* d, int n) {
-    if (n <= 0) return 0;
+// exclusive scan of d[0..n) in place, all on the stream; *total_dev (if
+// given) receives the total on the device
+void scan_async(cudaStream_t s, int* d, int n, int* total_dev) {
+    if (n <= 0) {
+        if (total_dev) SEMO_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int), s));
+        return;
+    }
     const int tiles = blocks(n, kScanTile);
     DBuf<int> ts;
     ts.alloc(tiles + 1, s);
     k_scan_tile<<<tiles, kScanT, 0, s>>>(n, d, d, ts.p);
     SEMO_CHECK_LAUNCH();
-    int total = 0;
     if (tiles > 1) {
         // scan the tile sums (recursively) and add them back
-        DBuf<int> tot;
-        tot.alloc(tiles + 1, s);
-        SEMO_CUDA(cudaMemcpyAsync(tot.p, ts.p, sizeof(int) * tiles, cudaMemcpyDeviceToDevice, s));
-        int last = 0;
-        SEMO_CUDA(cudaMemcpyAsync(&last, ts.p + tiles - 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-        int sum_before_last = scan_exclusive(s, tot.p, tiles);  // syncs
-        total = sum_before_last;
-        (void)last;
-        k_scan_add<<<blocks(n, 256), 256, 0, s>>>(n, d, tot.p);
+        scan_async(s, ts.p, tiles, total_dev);
+        k_scan_add<<<blocks(n, 256), 256, 0, s>>>(n, d, ts.p);
         SEMO_CHECK_LAUNCH();
-    } else {
-        SEMO_CUDA(cudaMemcpyAsync(&total, ts.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
+    } else if (total_dev) {
+        SEMO_CUDA(cudaMemcpyAsync(total_dev, ts.p, sizeof(int), cudaMemcpyDeviceToDevice, s));
     }
+}
+
+// exclusive scan of d[0..n) in place; returns the total (one host sync).
+// extra D2H copies enqueued before the call land by the time it returns.
+int scan_exclusive(cudaStream_t s, int* d, int n) {
+    if (n <= 0) return 0;
+    DBuf<int> tot;
+    tot.alloc(1, s);
+    scan_async(s, d, n, tot.p);
+    int total = 0;
+    SEMO_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
     return total;
 }
 
@@ -569,6 +576,36 @@ __global__ void k_row_abs(int n, const int* __restrict__ ptr, const V* __restric
     babs[i] = s;
 }
 
+// round(a b 2^sc) to the nearest integer (ties to even) for finite floats,
+// on the integer pipes: the 24-bit significands multiply exactly into 48
+// bits, so this equals __double2ll_rn(((double)a * b) * 2^sc) (the FP64
+// product of two floats is exact too) without touching the FP64 unit.
+// Requires |a b| 2^sc < 2^62.
+__device__ __forceinline__ long long fixed_product(float a, float b, int sc) {
+    const uint32_t ua = __float_as_uint(a), ub = __float_as_uint(b);
+    int ea = (int)((ua >> 23) & 0xff), eb = (int)((ub >> 23) & 0xff);
+    const uint32_t ma = (ua & 0x7fffffu) | (ea ? 0x800000u : 0u);
+    const uint32_t mb = (ub & 0x7fffffu) | (eb ? 0x800000u : 0u);
+    ea = ea ? ea : 1;
+    eb = eb ? eb : 1;
+    const unsigned long long m = (unsigned long long)ma * (unsigned long long)mb;   // exact
+    const int e = (ea - 150) + (eb - 150) + sc;                                     // |a b| 2^sc = m 2^e
+    unsigned long long q;
+    if (m == 0ull) {
+        q = 0ull;
+    } else if (e >= 0) {
+        q = (e < 64) ? (m << e) : 0ull;   // e <= 61 whenever the scale bound holds
+    } else if (e <= -64) {
+        q = 0ull;   // below half a unit (m < 2^48)
+    } else {
+        const int sh = -e;
+        q = m >> sh;
+        const unsigned long long rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+    }
+    return ((ua ^ ub) >> 31) ? -(long long)q : (long long)q;
+}
+
 template <class V, int HT>
 __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __restrict__ aptr,
                                                             const int* __restrict__ acol, const V* __restrict__ aval,
@@ -614,6 +651,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
         for (int t = lane; t < ht; t += 32) { keys[t] = -1; vals[t] = 0ull; }
         // the row's fixed-point scale 2^sc (a fixed reduction tree: deterministic)
         double up_scale = 1.0, down_scale = 1.0;
+        int sc = 0;
         if (pass != 0) {
             double bound = 0.0;
             for (int ka = aptr[row] + lane; ka < aptr[row + 1]; ka += 32)
@@ -622,7 +660,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
             // bound < 2^e with e from the biased exponent (subnormals: e = -1022)
             const int be = (int)((__double_as_longlong(bound) >> 52) & 0x7ff);
             const int e = be ? be - 1022 : -1022;
-            const int sc = max(-960, min(1000, 62 - e));
+            sc = max(-960, min(1000, 62 - e));
             up_scale = __longlong_as_double((long long)(1023 + sc) << 52);     // 2^sc
             down_scale = __longlong_as_double((long long)(1023 - sc) << 52);   // 2^-sc
         }
@@ -636,7 +674,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
             const int k = k0 + lane;
             const bool ka = k < ae;
             const int a = ka ? acol[k] : 0;
-            const double avk = ka ? (double)aval[k] : 0.0;
+            const V avk = ka ? aval[k] : V(0);
             const int bb = ka ? bptr[a] : 0;
             const int blen = ka ? bptr[a + 1] - bb : 0;
             int incl = blen;   // inclusive scan of the B row lengths over the lanes
@@ -658,7 +696,7 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                     if (e <= t) j += step;
                 }
                 const int q = __shfl_sync(0xffffffffu, bb, j) + (t - __shfl_sync(0xffffffffu, excl, j));
-                const double av = __shfl_sync(0xffffffffu, avk, j);
+                const V av = __shfl_sync(0xffffffffu, avk, j);
                 const int c = act ? bcol[q] : -1;
                 int slot = -1;
                 bool fresh = false;
@@ -674,7 +712,9 @@ __global__ void __launch_bounds__(32 * kGemmWarps) k_spgemm(int n, const int* __
                 distinct += __popc(__ballot_sync(0xffffffffu, fresh));
                 const bool lost = __any_sync(0xffffffffu, act && slot < 0);
                 if (pass != 0 && !lost && act) {
-                    const long long fx = __double2ll_rn((av * (double)bval[q]) * up_scale);
+                    long long fx;
+                    if constexpr (sizeof(V) == 4) fx = fixed_product(av, bval[q], sc);
+                    else fx = __double2ll_rn((av * bval[q]) * up_scale);
                     atomicAdd(vals + slot, (unsigned long long)fx);   // two's complement: signed sum mod 2^64
                 }
                 __syncwarp();
@@ -843,10 +883,10 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     SEMO_CUDA(cudaMemsetAsync(up.p + n, 0, sizeof(int), s));
     k_row_products<<<blocks(n, 256), 256, 0, s>>>(n, A.ptr, A.col, B.ptr, up.p, flags.p + 1);
     SEMO_CHECK_LAUNCH();
+    int* const hp = c->hpin_int;   // pinned: these copies land by the scan's sync
+    SEMO_CUDA(cudaMemcpyAsync(hp + 2, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     const int64_t total = scan_exclusive(s, up.p, n + 1);   // syncs
-    int maxprod = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&maxprod, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
+    const int maxprod = hp[2];
     DBuf<int> tcol;
     DBuf<V> tval;
     tcol.alloc(std::max<int64_t>(total, 1), s);
@@ -878,18 +918,15 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     }
     SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, cnt.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
     SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
+    SEMO_CUDA(cudaMemcpyAsync(hp + 3, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     const int nnz = scan_exclusive(s, C.ptr.p, n + 1);   // syncs
-    int of = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&of, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    if (of) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
+    if (hp[3]) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
     C.nnz = nnz;
     C.col.alloc(std::max(nnz, 1), s);
     C.val.alloc(std::max(nnz, 1), s);
     k_compact_rows<V><<<blocks(n, 256), 256, 0, s>>>(n, up.p, C.ptr.p, tcol.p, tval.p, C.col.p,
                                                                    C.val.p);
     SEMO_CHECK_LAUNCH();
-    (void)c;
 }
 
 template <class V>
@@ -909,7 +946,7 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
         k_col_count<<<blocks(A.nnz, 256), 256, 0, s>>>(A.nnz, A.col, T.ptr);
         SEMO_CHECK_LAUNCH();
     }
-    scan_exclusive(s, T.ptr.p, T.n + 1);
+    scan_async(s, T.ptr.p, T.n + 1, nullptr);   // the total is A.nnz
     DBuf<int> fill;
     fill.alloc(T.n + 1, s);
     SEMO_CUDA(cudaMemcpyAsync(fill.p, T.ptr.p, sizeof(int) * (T.n + 1), cudaMemcpyDeviceToDevice, s));
@@ -919,8 +956,18 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
     SEMO_CHECK_LAUNCH();
 }
 
+// max of kRedBlocks partial maxima into *out (one block, fixed order)
+__global__ void k_max_final(const double* __restrict__ part, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double m = 0.0;
+    for (int b = 0; b < kRedBlocks; ++b) m = fmax(m, part[b]);
+    *out = m;
+}
+
+// diagonal, its reciprocal and the Gershgorin bound of D^-1 A into *lam_dev
+// (read back with the setup's last host sync)
 template <class V>
-void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia) {
+void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia, double* lam_dev) {
     cudaStream_t s = setup_stream(c);
     const int n = L.A.n;
     L.dinv.alloc(n, s);
@@ -932,12 +979,8 @@ void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia) {
     SEMO_CHECK_LAUNCH();
     k_max<<<kRedBlocks, kRedThreads, 0, s>>>(n, ratio, part);
     SEMO_CHECK_LAUNCH();
-    std::vector<double> h(kRedBlocks);
-    SEMO_CUDA(cudaMemcpyAsync(h.data(), part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    double lam = 0.0;
-    for (double v : h) lam = std::max(lam, v);
-    L.lam_max = lam;
+    k_max_final<<<1, 32, 0, s>>>(part, lam_dev);
+    SEMO_CHECK_LAUNCH();
     L.x.alloc(n, s); L.b.alloc(n, s); L.r.alloc(n, s); L.t.alloc(n, s);
 }
 
@@ -946,6 +989,10 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     cudaStream_t s = setup_stream(c);
     c->sflag.alloc(16, s);
     SEMO_CUDA(cudaMemsetAsync(c->sflag.p, 0, 16 * sizeof(int), s));
+    if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
+    if (!c->hpin_setup) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_setup, 64 * sizeof(double)));
+    DBuf<double> lam_dev;   // per level Gershgorin bounds
+    lam_dev.alloc(64, s);
     h.clear();
     h.lev.reserve(c->prm.max_levels + 1);
     h.lev.emplace_back();
@@ -967,7 +1014,7 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
         DBuf<V> dia;
         {
             StageScope sc(c, ST_SETUP_LEVEL);
-            level_prepare(c, L, dia);
+            level_prepare(c, L, dia, lam_dev.p + l);
         }
         h.total_nnz += L.A.nnz;
         const int nl = L.A.n;
@@ -998,7 +1045,6 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
             need.alloc(nl, s);
             SEMO_CUDA(cudaMemsetAsync(need.p, 1, nl, s));
             undec.alloc(2, s);
-            if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
             for (auto& e : c->sync_ev)
                 if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             int* const hcnt = c->hpin_int;
@@ -1112,8 +1158,11 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     k_gauss_jordan<<<1, 1024, 0, s>>>(m, dense, h.cinv, c->sflag);
     SEMO_CHECK_LAUNCH();
     int hf[5] = {0, 0, 0, 0, 0};
+    const int nlev = (int)h.lev.size();
+    SEMO_CUDA(cudaMemcpyAsync(c->hpin_setup, lam_dev.p, sizeof(double) * nlev, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaMemcpyAsync(hf, c->sflag.p, sizeof(hf), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
+    for (int l = 0; l < nlev; ++l) h.lev[l].lam_max = c->hpin_setup[l];
     if (hf[2]) throw Error(SEMO_ERR_ARGUMENT, "matrix has a zero diagonal entry");
     if (hf[3]) throw Error(SEMO_ERR_NAN, "non-finite matrix entry");
     if (hf[4]) throw Error(SEMO_ERR_BREAKDOWN, "coarsest AMG matrix is singular");

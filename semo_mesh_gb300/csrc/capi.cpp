@@ -89,7 +89,7 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
     if (prm) c->prm = *prm; else semo_params_default(&c->prm);
     semo_physics_default(&c->phys);
     semo_status st = guarded(c, [&] {
-        need(c->prm.tol > 0.0 && c->prm.max_iter > 0 && c->prm.coarse_enough > 0 && c->prm.max_levels > 0 &&
+        need(c->prm.tol > 0.0 && c->prm.max_iter > 0 && c->prm.coarse_enough > 0 && c->prm.max_levels > 0 && c->prm.max_levels <= 64 &&
                  c->prm.cheb_degree > 0 && c->prm.cheb_degree <= 16 && c->prm.mom_tol > 0.0 &&
                  c->prm.mom_max_iter > 0 &&
                  (c->prm.precision == SEMO_PREC_FP64 || c->prm.precision == SEMO_PREC_MIXED),
@@ -144,6 +144,7 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     for (auto& e : c->sync_ev) if (e) cudaEventDestroy(e);
     if (c->hpin) cudaFreeHost(c->hpin);
     if (c->hpin_int) cudaFreeHost(c->hpin_int);
+    if (c->hpin_setup) cudaFreeHost(c->hpin_setup);
     cudaStream_t s = c->stream, aux = c->aux_stream;
     delete c;  // DBuf destructors enqueue frees on the (still valid) streams
     if (aux) { cudaStreamSynchronize(aux); cudaStreamDestroy(aux); }
@@ -813,6 +814,7 @@ struct SideSetup {
             if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         // host resources the setup creates on first use, made here on this thread
         if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
+        if (!c->hpin_setup) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_setup, 64 * sizeof(double)));
         for (auto& e : c->sync_ev)
             if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         SEMO_CUDA(cudaEventRecord(c->ov_ev[0], c->stream));   // face values (densities) are on the stream

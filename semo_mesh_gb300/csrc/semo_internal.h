@@ -241,6 +241,7 @@ struct semo_ctx {
     semo::DBuf<float> kz32, kr32;
     double* hpin = nullptr;                       // pinned host scalars for convergence checks
     int* hpin_int = nullptr;                      // pinned host counters read while setup kernels run
+    double* hpin_setup = nullptr;                 // pinned per-level scalars of the setup
     cudaEvent_t sync_ev[2] = {nullptr, nullptr};  // completion of those counter copies
     std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
 
