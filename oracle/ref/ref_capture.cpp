@@ -4,7 +4,7 @@
 // file) with -DsolveAMGCL=semo_ref_capture_solveAMGCL, so the calls at
 // src/solvers/eqPressure.cpp:677 and src/solvers/eqVolfrac.cpp:766 (scalar)
 // and src/solvers/eqMomentum.cpp:1017 (three right-hand sides) land here.  The assembled COO system is copied out
-// for the checker and then handed to the real solver, so the reference's pass
+// for the oracle tests and then handed to the real solver, so the reference's pass
 // continues exactly as it would.
 #include <string>
 #include <vector>

@@ -1,7 +1,7 @@
 /*
  * semo_oracle.c -- CPU restatement of SEMO's pressure-correction pass.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU path is compared
  * against (tests/, __graft_entry__.smoke) and the CPU baseline bench.py
  * times.  Nothing in the shipped library links or calls it.
  *
@@ -97,7 +97,7 @@ int orc_set(orc_ctx* c, const char* name, int type, long long n, const void* src
 /* :792-880 (volumes/centroids), :1206-1227 (distCells), :1297-1500 (weights) */
 /* ------------------------------------------------------------------------ */
 /* The reference takes sqrtl of a double (x87: root rounded to a 64-bit
-   significand, then to double).  Restated portably so the checker gives the
+   significand, then to double).  Restated portably so the oracle gives the
    same bits on hosts whose long double is not x87: IEEE sqrt, corrected when
    the root lies within 2^-12 ulp of a midpoint (exact residual via fma). */
 static double sqrt_ext_rounded(double x) {
