@@ -1051,7 +1051,11 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     const int nc = c->nc;
     CplSolver& S = solver_state(c);
     const bool mixed = c->prm.precision == SEMO_PREC_MIXED;
-    cudaEvent_t e0 = take_event(c), e1 = take_event(c), e2 = take_event(c);
+    cudaEvent_t e0, e1, e2;
+    {
+        std::lock_guard<std::mutex> lk(c->prof_mu);   // the event pool is shared with the stage timers
+        e0 = take_event(c); e1 = take_event(c); e2 = take_event(c);
+    }
     SEMO_CUDA(cudaEventRecord(e0, s));
     StageScope stage(c, ST_CSOLVE);
     S.part.alloc(2 * kRedBlocks, s);
@@ -1126,7 +1130,10 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     float t0 = 0.f, t1 = 0.f;
     cudaEventElapsedTime(&t0, e0, e1);
     cudaEventElapsedTime(&t1, e1, e2);
-    c->ev_pool.push_back(e0); c->ev_pool.push_back(e1); c->ev_pool.push_back(e2);
+    {
+        std::lock_guard<std::mutex> lk(c->prof_mu);
+        c->ev_pool.push_back(e0); c->ev_pool.push_back(e1); c->ev_pool.push_back(e2);
+    }
     if (info) {
         info->iterations = total;
         info->rel_residual = rel;
