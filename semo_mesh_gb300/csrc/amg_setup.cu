@@ -896,11 +896,14 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     SEMO_CHECK_LAUNCH();
     if (maxprod > kSmallMaxProducts) {
         // tables sized per row from its products (<= 3/4 load); most rows fit
-        // a 256-slot table, which keeps shared memory per block small; the
+        // a 128-slot table, which keeps shared memory per block small (12 KB:
+        // full occupancy, and room for the kernels of the other stream when
+        // the setup runs beside the momentum pass; 64 slots defer too many
+        // rows, 256 measured 1 ms slower per overlapped outer iteration); the
         // rest go to one more launch sized for the densest row
         int ht = 64;
         while (ht < 2048 && ht * 3 / 4 < maxprod + 2) ht <<= 1;
-        const int first = std::min(ht, 256);
+        const int first = std::min(ht, 128);
         DBuf<int> list, nlist;
         if (ht > first) {
             list.alloc(std::max(n, 1), s);
