@@ -959,12 +959,20 @@ void transpose(cudaStream_t s, const DCsr<V>& A, DCsr<V>& T) {
     SEMO_CHECK_LAUNCH();
 }
 
-// max of kRedBlocks partial maxima into *out (one block, fixed order)
+// max of kRedBlocks partial maxima into *out (one block; max is exact in
+// any order)
 __global__ void k_max_final(const double* __restrict__ part, double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    __shared__ double sh[32];
     double m = 0.0;
-    for (int b = 0; b < kRedBlocks; ++b) m = fmax(m, part[b]);
-    *out = m;
+    for (int b = threadIdx.x; b < kRedBlocks; b += blockDim.x) m = fmax(m, part[b]);
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
+        *out = r;
+    }
 }
 
 // diagonal, its reciprocal and the Gershgorin bound of D^-1 A into *lam_dev
@@ -982,7 +990,7 @@ void level_prepare(semo_ctx* c, AmgLevel<V>& L, DBuf<V>& dia, double* lam_dev) {
     SEMO_CHECK_LAUNCH();
     k_max<<<kRedBlocks, kRedThreads, 0, s>>>(n, ratio, part);
     SEMO_CHECK_LAUNCH();
-    k_max_final<<<1, 32, 0, s>>>(part, lam_dev);
+    k_max_final<<<1, 256, 0, s>>>(part, lam_dev);
     SEMO_CHECK_LAUNCH();
     L.x.alloc(n, s); L.b.alloc(n, s); L.r.alloc(n, s); L.t.alloc(n, s);
 }
