@@ -147,14 +147,16 @@ def test_old_velocity_arguments(semo):
     assert ctx.L.semo_set_old_velocity(ctx.h, None, None, None, None, None, None) == 0
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision,sigma", [("fp64", 0.0), ("mixed", 0.0), ("mixed", 0.05)])
 @pytest.mark.parametrize("reuse", [False, True])
-def test_overlapped_setup_is_bit_identical(semo, precision, reuse):
+def test_overlapped_setup_is_bit_identical(semo, precision, sigma, reuse):
     """The pressure hierarchy built on the second stream during the momentum
     pass (semo_params.overlap_setup) gives the serial path's results bit for
-    bit, over several outer iterations (with and without hierarchy reuse)."""
+    bit, over several outer iterations (with and without hierarchy reuse, and
+    with a surface tension)."""
     from semo_mesh_gb300.cases import vof_case, with_history, with_fields
     case = with_history(with_fields(vof_case(20, jitter=0.2), seed=31, p_scale=50.0), seed=32)
+    case.sigma = sigma
     runs = []
     for overlap in (True, False):
         ctx = semo.Context(precision=precision, tol=1e-8, reuse_hierarchy=reuse, overlap_setup=overlap)
