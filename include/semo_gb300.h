@@ -63,7 +63,7 @@ typedef struct {
     /* smoothed aggregation (AMGCL smoothed_aggregation semantics) */
     double eps_strong;           /* strength threshold, halved per level; default 0.03 (AMGCL: 0.08) */
     int coarse_enough;           /* direct solve at or below this size; default 64 */
-    int max_levels;              /* default 24 */
+    int max_levels;              /* default 24, at most 64 */
     int cheb_degree;             /* Chebyshev pre/post smoothing degree; default 2 */
     int reuse_hierarchy;         /* keep the pressure AMG hierarchy when the assembled matrix is bit-identical
                                     to the one it was built from (same hierarchy, same result); default 1 */
