@@ -110,19 +110,86 @@ def hbm_peak() -> tuple:
     return 6800.0, "fallback"
 
 
-def stencil_bytes(m: dict) -> float:
-    """Algorithmic bytes of one k_stencil launch (every array touched once).
+def stencil_algo_bytes(m: dict) -> float:
+    """Compulsory bytes of one full k_stencil launch, the survey's formula.
 
-    per cell: P,U,V,W,VF (40) + stencil row pointer (4) + M^-1 (48) read, 15
-    gradient components (120) + 8 min/max (64) written; per stencil entry:
-    cell index (4) + precomputed LSQ weight vector w*d (24); per boundary face:
-    weight vector (24) + 5 face values (40).
+    LSQ gradients of k = 5 fields: N (24 centroid + 48 M^-1 + 4 row pointer
+    + 8k phi + 24k grad phi) + 4 nnz_s = 236 B a cell + 4 B a stencil entry;
+    the stencil min/max of the same 5 fields reads nothing more and writes
+    10 planes (80 B a cell).
     """
-    return m["cells"] * (40 + 4 + 48 + 120 + 64) + m["stencil_nnz"] * (4 + 24) + m["boundary_faces"] * (24 + 40)
+    return m["cells"] * (236 + 80) + 4 * m["stencil_nnz"]
+
+
+def stencil_design_bytes(m: dict) -> float:
+    """Bytes this design's k_stencil moves when each array is touched once.
+
+    per cell: P,U,V,W,VF (40) + stencil row pointer (4) + M^-1 (48) + the
+    weight sums (24) read, 15 gradient components (120) + 10 min/max (80)
+    written; per stencil entry: cell index (4) + precomputed LSQ weight vector
+    w*d (24); per boundary face: weight vector (24) + 5 face values (40).
+    The weight vectors trade bytes for FP64 operations.
+    """
+    return (m["cells"] * (40 + 4 + 48 + 24 + 120 + 80) + m["stencil_nnz"] * (4 + 24)
+            + m["boundary_faces"] * (24 + 40))
+
+
+def stencil_fp64_flops(m: dict) -> float:
+    """FP64 flops of one full k_stencil launch (an FMA counts 2).
+
+    per stencil entry and per boundary face 15 FMAs (3 components x 5
+    fields); per cell 15 FMAs (phi_i times the weight sums) + 45 FMAs
+    (M^-1 applied to 5 vectors).
+    """
+    return 2.0 * (15 * (m["stencil_nnz"] + m["boundary_faces"]) + 60 * m["cells"])
+
+
+def spmv_algo_bytes(n: int, nnz: int, value_bytes: int) -> float:
+    """Compulsory bytes of y = A x, CSR (survey formula): FP64 12 nnz + 4(N+1)
+    + 16N; FP32 values and vectors 8 nnz + 4(N+1) + 8N."""
+    return (4 + value_bytes) * nnz + 4 * (n + 1) + 2 * value_bytes * n
+
+
+def pcg_iteration_bytes(levels: list) -> float:
+    """Compulsory bytes of one preconditioned CG iteration (V(2,2) cycle,
+    Chebyshev degree 2), each array counted once per kernel that touches it.
+
+    per level above the coarsest (values and vectors of `value_bytes` V):
+      4 operator sweeps (pre-smoothing, residual, two post-smoothing steps),
+      each as an SpMV, plus the D^-1 and b reads of the smoothing sweeps (3 x 2Vn);
+      restriction y = R r and prolongation x += P x_c as SpMVs (+ Vn for the
+      read-modify-write of x);
+    coarsest level: its dense FP64 inverse (8 n^2) and two vectors;
+    finest level, FP64: the outer SpMV (12 nnz + 4(N+1) + 16N), the update
+      of p (16N), the dot products' reads of r and q (16N) and the x, r update
+      (x and r read and written, p and q read: 48N) plus the FP32 copy of r (VN).
+    """
+    total = 0.0
+    for l, L in enumerate(levels):
+        n, V = L["rows"], L["value_bytes"]
+        if L["layout"] < 0:   # coarsest: dense inverse
+            total += 8.0 * n * n + 2 * V * n
+            continue
+        nc = levels[l + 1]["rows"]
+        total += 4 * spmv_algo_bytes(n, L["nnz_A"], V) + 3 * 2 * V * n
+        total += (4 + V) * L["nnz_R"] + 4 * (nc + 1) + V * n + V * nc
+        total += (4 + V) * L["nnz_P"] + 4 * (n + 1) + V * nc + 2 * V * n
+    L0 = levels[0]
+    N = L0["rows"]
+    total += spmv_algo_bytes(N, L0["nnz_A"], 8) + 16 * N + 16 * N + 48 * N + L0["value_bytes"] * N
+    return total
+
+
+def pface_algo_bytes(m: dict) -> float:
+    """Compulsory bytes of one k_pface launch, the survey's formula: per
+    internal face 136 B (owner/neighbour 8, 13 geometry doubles 104, two
+    off-diagonals 16, UnF 8), per cell 264 B (31 gathered doubles + diagonal
+    and right-hand side)."""
+    return m["internal_faces"] * 136 + m["cells"] * 264
 
 
 def pface_bytes(m: dict) -> float:
-    """Algorithmic bytes of one k_pface launch.
+    """Bytes this design's k_pface moves (each array touched once).
 
     per internal face: owner/neighbour (8), normal, e_PN, skew (72), alpha (8),
     4 face constants (32), 2 CSR slots (8) read; 2 off-diagonals (16) and coef,
@@ -133,7 +200,7 @@ def pface_bytes(m: dict) -> float:
 
 
 def mface_bytes(m: dict) -> float:
-    """Algorithmic bytes of one k_mface launch.
+    """Bytes this design's k_mface moves (each array touched once).
 
     per internal face: as k_pface's face reads (128) plus 8 face terms (64)
     and 2 off-diagonals (16) written; per cell, read once: 1/rho, rho, 1/mu,
@@ -142,11 +209,31 @@ def mface_bytes(m: dict) -> float:
     return m["internal_faces"] * (8 + 72 + 8 + 32 + 8 + 64 + 16) + m["cells"] * 264
 
 
-# stage -> (kernel, algorithmic bytes per launch); each of these stages is one
-# launch ("stencil" is the full five-field pass; the pressure pass of an outer
-# iteration runs the U,V,W-only variant, timed as "stencil_uvw")
-KERNEL_OF_STAGE = {"stencil": ("k_stencil", stencil_bytes), "pface": ("k_pface", pface_bytes),
-                   "mface": ("k_mface", mface_bytes)}
+# stage -> (kernel, algorithmic bytes, design bytes) per launch; each of these
+# stages is one launch ("stencil" is the full five-field pass; the pressure
+# pass of an outer iteration runs the U,V,W-only variant, timed as "stencil_uvw")
+KERNEL_OF_STAGE = {"stencil": ("k_stencil", stencil_algo_bytes, stencil_design_bytes),
+                   "pface": ("k_pface", pface_algo_bytes, pface_bytes),
+                   "mface": ("k_mface", mface_bytes, mface_bytes)}
+
+
+def fp64_peak_tflops(torch, dev) -> float:
+    """FP64 rate of this GPU: cuBLAS DGEMM 4096^3, best of 5 (CUDA events)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    c = a @ b
+    best = float("inf")
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 def oracle_outer_iteration(o) -> dict:
@@ -158,8 +245,9 @@ def oracle_outer_iteration(o) -> dict:
     return {"mom_iters": m["iters"], "iters": s["iters"]}
 
 
-def cpu_baseline(case, steps: int = 1) -> dict:
-    """The oracle (restated reference outer iteration) timed on this host's cores."""
+def cpu_baseline(case, steps: int = 1):
+    """The oracle (restated reference outer iteration) timed on this host's
+    cores; returns the baseline object and the oracle after its iteration."""
     from oracle.oracle import Oracle, build
     build()
     o = Oracle(case.mesh)
@@ -170,11 +258,91 @@ def cpu_baseline(case, steps: int = 1) -> dict:
         r = oracle_outer_iteration(o)
         t_total += time.perf_counter() - t0
     n = case.mesh.n_cells
-    return {"value": round(n * steps / t_total / 1e6, 4), "unit": UNIT, "cores": Oracle.threads(),
+    base = {"value": round(n * steps / t_total / 1e6, 4), "unit": UNIT, "cores": Oracle.threads(),
             "kind": "port", "seconds": round(t_total, 2),
-            "sample": f"{steps} outer iteration(s) of the same {n}-cell workload: serial assembly as in SEMO, "
-                      f"OpenMP Jacobi-BiCGStab momentum solves ({r['mom_iters']} iterations) and SA-AMG + CG "
-                      f"pressure solve ({r['iters']} iterations)"}
+            "sample": f"{steps} outer iteration of the same {n}-cell workload: serial assembly as in SEMO, "
+                      f"OpenMP Jacobi-BiCGStab momentum ({r['mom_iters']} iterations) and SA-AMG + CG "
+                      f"pressure ({r['iters']} iterations)"}
+    return base, o, r
+
+
+def _relmax(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    s = float(np.abs(b).max()) if b.size else 0.0
+    return float(np.abs(a - b).max() / (s if s > 0 else 1.0)) if a.size else 0.0
+
+
+def _rel_l2(a, b) -> float:
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / (nb if nb > 0 else 1.0))
+
+
+def error_vs_oracle(case, S, local, o_outer, oracle_iters) -> dict:
+    """The GPU path against the FP64 CPU oracle on the bench's own workload,
+    outside every timed region.
+
+    From the case's fields: the momentum system (CSR pattern in SEMO's layout,
+    coefficients, three right-hand sides) and its three solutions; the
+    pressure system (RCM CSR pattern, coefficients, right-hand side) and its
+    solution (the oracle solves to 1e-12; the GPU to the bench's 1e-8).  Then
+    P, U, V, W after one whole outer iteration against the timed oracle run.
+    Bars: pattern bit-exact, coefficients and right-hand sides 1e-12 relative
+    (max norm), solutions and fields 1e-7 relative L2.
+    """
+    from oracle.oracle import Oracle
+    n = case.mesh.n_cells
+    o = Oracle(case.mesh)
+    o.set_case(case)
+    ctx = S.Context(precision="mixed", tol=1e-8, device=local, reuse_hierarchy=False)
+    ctx.set_case(case)
+    # momentum: one matrix, three right-hand sides
+    ctx.assemble_momentum()
+    ms = ctx.momentum_system()
+    o.assemble_momentum()
+    B = o.get("mom_B").reshape(3, n)
+    mom = {"pattern_equal": bool(np.array_equal(ms["ptr"], o.get("mom_csr_ptr"))
+                                 and np.array_equal(ms["col"], o.get("mom_csr_col"))),
+           "coef_rel": _relmax(ms["val"], o.get("mom_csr_val")),
+           "rhs_rel": max(_relmax(ms["b"][j], B[j]) for j in range(3))}
+    xg, ig = ctx.solve_momentum()
+    xo = o.solve_momentum(1e-12)
+    mom["solution_rel_l2"] = max(_rel_l2(xg[j], xo["x"][j]) for j in range(3))
+    mom["iterations"] = {"gpu": [i["iterations"] for i in ig], "oracle": list(oracle_iters["mom_iters"])}
+    # pressure correction
+    ctx.assemble()
+    sysm = ctx.system_rcm()
+    o.assemble()
+    pre = {"pattern_equal": bool(np.array_equal(sysm["ptr"], o.get("rcm_csr_ptr"))
+                                 and np.array_equal(sysm["col"], o.get("rcm_csr_col"))),
+           "coef_rel": _relmax(sysm["val"], o.get("rcm_csr_val")),
+           "rhs_rel": _relmax(sysm["b"], o.get("rcm_B"))}
+    res = ctx.solve()
+    ref = o.solve(False, 1e-12)
+    pre["solution_rel_l2"] = _rel_l2(res.x, ref["x"])
+    pre["iterations"] = {"gpu": res.info["iterations"], "oracle": oracle_iters["iters"]}
+    pre["rel_residual_gpu"] = res.info["rel_residual"]
+    # one whole outer iteration
+    ctx.set_case(case)
+    ctx.outer_iteration()
+    f = ctx.fields()
+    outer = {k: _rel_l2(f[k], o_outer.get(k)) for k in ("P", "U", "V", "W")}
+    ctx.close()
+    ok = (mom["pattern_equal"] and pre["pattern_equal"] and max(mom["coef_rel"], mom["rhs_rel"], pre["coef_rel"],
+                                                                 pre["rhs_rel"]) <= 1e-12
+          and max(mom["solution_rel_l2"], pre["solution_rel_l2"], *outer.values()) <= 1e-7)
+    return {"pass": bool(ok), "momentum": mom, "pressure": pre, "outer_fields_rel_l2": outer,
+            "bars": "pattern bit-exact; coefficients, rhs 1e-12 rel (max); solutions, fields 1e-7 rel L2"}
+
+
+def workload_config(n: int, mesh, world: int) -> dict:
+    """The `config` both bench arms print."""
+    return {"workload": f"jittered hex {n}^3 two-phase VOF outer iteration: momentum (assembly + 3 BiCGStab "
+                        f"solves to 1e-9 + update) then pressure correction (assembly + SA-AMG setup + CG to "
+                        f"1e-8 + update)",
+            "cells": mesh.n_cells, "faces": mesh.n_faces, "nnz": mesh.n_cells + 2 * mesh.n_internal,
+            "parallelism": f"replicas x{world}" if world > 1 else "one device",
+            "l2": "inputs larger than L2 (mesh + fields several GB), no flush"}
 
 
 def bench_case(n: int):
@@ -255,6 +423,9 @@ def run_gpu_arm(args, rank, world, local) -> None:
     for _ in range(args.warmup):
         ctx.calc_pressure_eq()
     ms_pres, infos_p = timed(ctx, strm, args.steps, pressure)
+    # the apply kernels of the last pass's hierarchy, timed outside the CG graph
+    spmv_ms = (ctx.time_spmv(0, 50), ctx.time_spmv(1, 50))
+    levels = ctx.hierarchy_levels()
 
     # ---- one volume-fraction sub-iteration (MSTACS + calcVolfracEq) -------
     ctx.set_case(case)
@@ -365,11 +536,13 @@ def run_gpu_arm(args, rank, world, local) -> None:
 
     # ---- roofline for the dominant single-kernel stage ----------------------
     peak, peak_src = hbm_peak()
+    fp64_tf = fp64_peak_tflops(torch, torch.device(f"cuda:{local}"))
     single = {k: v for k, v in stages.items() if k in KERNEL_OF_STAGE and v[1] > 0}
     dom = max(single, key=lambda k: single[k][0])   # largest total device time per step
-    kname, fbytes = KERNEL_OF_STAGE[dom]
+    kname, falgo, fdesign = KERNEL_OF_STAGE[dom]
     per_launch_ms = single[dom][0] / single[dom][1]
-    algo = fbytes(minfo)
+    algo = falgo(minfo)
+    design = fdesign(minfo)
     achieved = algo / (per_launch_ms * 1e-3) / 1e9
     traffic = None
     fp64_pipe = None
@@ -386,65 +559,94 @@ def run_gpu_arm(args, rank, world, local) -> None:
             fp64_pipe = t["fp64_pipe_pct"] / 100.0
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "algorithmic_bytes": algo,
-                "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src,
-                "fp64_pipe_frac_ncu": fp64_pipe}
+                "design_bytes": design, "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src}
+    if kname == "k_stencil":
+        flops = stencil_fp64_flops(minfo)
+        roofline["fp64"] = {"tflops": round(flops / (per_launch_ms * 1e-3) / 1e12, 3),
+                            "peak_tflops": round(fp64_tf, 3), "frac": round(flops / (per_launch_ms * 1e-3) / 1e12
+                                                                           / fp64_tf, 3),
+                            "flops_per_launch": flops, "fp64_pipe_frac_ncu": fp64_pipe,
+                            "peak_source": "measured here: cuBLAS DGEMM 4096^3"}
+    # the solve: one SpMV of each operator, and a whole CG iteration inside its graph
+    L0 = levels[0]
+    b32 = spmv_algo_bytes(L0["rows"], L0["nnz_A"], L0["value_bytes"])
+    b64 = spmv_algo_bytes(L0["rows"], L0["nnz_A"], 8)
+    it_p = sum(i["iterations"] for i in infos_p)
+    ms_it = sum(i["solve_ms"] for i in infos_p) / max(it_p, 1)
+    pcg_b = pcg_iteration_bytes(levels)
+    roofline["spmv_level0"] = {"achieved": round(b32 / (spmv_ms[0] * 1e-3) / 1e9, 1),
+                               "frac": round(b32 / (spmv_ms[0] * 1e-3) / 1e9 / peak, 4),
+                               "ms_per_launch": round(spmv_ms[0], 4), "algorithmic_bytes": b32,
+                               "layout": {2: "SELL-32, 16-bit column offsets", 1: "SELL-32", 0: "CSR"}[L0["layout"]],
+                               "value_bytes": L0["value_bytes"]}
+    roofline["spmv_outer_fp64"] = {"achieved": round(b64 / (spmv_ms[1] * 1e-3) / 1e9, 1),
+                                   "frac": round(b64 / (spmv_ms[1] * 1e-3) / 1e9 / peak, 4),
+                                   "ms_per_launch": round(spmv_ms[1], 4), "algorithmic_bytes": b64}
+    roofline["pcg_iteration"] = {"achieved": round(pcg_b / (ms_it * 1e-3) / 1e9, 1),
+                                 "frac": round(pcg_b / (ms_it * 1e-3) / 1e9 / peak, 4), "ms": round(ms_it, 4),
+                                 "algorithmic_bytes": round(pcg_b), "levels": len(levels),
+                                 "note": "solve time / iterations of the pressure passes (the graph's iterations "
+                                         "plus the initial and final residuals)"}
 
     cells_all = nc * world
     value = cells_all / (ms_mixed * 1e-3) / 1e6
     clocks = clk.summary()
     mc = lambda ms: round(cells_all / (ms * 1e-3) / 1e6, 3)   # noqa: E731
+    # bulky detail first, the summaries last (a reader of the tail sees them)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_mixed, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 assembly + f32 AMG in f64 CG",
         "data": "synthetic (seeded jittered hex mesh, VOF fields, old velocities)",
-        "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF outer iteration: momentum (assembly + "
-                               f"3 BiCGStab solves to 1e-9 + update) then pressure correction (assembly + "
-                               f"SA-AMG setup + CG to 1e-8 + update)",
-                   "cells": nc, "faces": minfo["faces"], "nnz": minfo["nnz"],
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (mesh + fields several GB), no flush"},
-        "iterations": [i[3]["iterations"] for i in infos][:3],
-        "momentum_iterations": [i[0]["iterations"] for i in infos][:3],
-        "rel_residual": max(i[3]["rel_residual"] for i in infos),
+        "config": workload_config(args.n, mesh, world),
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1] > 0},
+        "memory": {"device_used_gb": round(used_gb, 2), "device_total_gb": round(total_b / 1e9, 1)},
         "amg_levels": infos[-1][3]["levels"], "operator_complexity": round(infos[-1][3]["operator_complexity"], 3),
-        "pressure_pass": {"value": mc(ms_pres), "ms_per_step": round(ms_pres, 3),
-                          "iterations": [i["iterations"] for i in infos_p][:3]},
         "vof_pass": {"value": mc(ms_vof), "ms_per_step": round(ms_vof, 3),
                      "iterations": [i["iterations"] for i in infos_v][:3],
                      "note": "one volume-fraction sub-iteration (SEMO runs nSpeciesEq of them per time step, "
                              "before its outer iterations)"},
-        "fp64": {"value": mc(ms_fp64), "ms_per_step": round(ms_fp64, 3),
-                 "iterations": infos64[-1][3]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3),
-                 "pressure_pass_ms": round(ms_fp64_p, 3),
-                 "pressure_pass_mixed_speedup": round(ms_fp64_p / ms_pres, 3)},
         "serial_setup": {"value": mc(ms_serial), "ms_per_step": round(ms_serial, 3),
                          "overlap_speedup": round(ms_serial / ms_mixed, 3),
-                         "note": "the same outer iteration with the pressure matrix and its hierarchy built "
-                                 "after the momentum pass on the one stream; the headline builds them on a "
-                                 "second stream while the momentum pass runs"},
+                         "note": "the pressure matrix and its hierarchy built after the momentum pass on the one "
+                                 "stream; the headline builds them on a second stream during the momentum pass"},
         "hierarchy_reuse": {"value": mc(ms_reuse), "ms_per_step": round(ms_reuse, 3),
                             "iterations": infos_r[-1][3]["iterations"],
                             "setup_ms_last_step": round(infos_r[-1][3]["setup_ms"], 3),
                             "note": "pressure AMG hierarchy kept while the assembled matrix stays bit-identical "
                                     "(outer iterations within a time step); the headline rebuilds it every step"},
-        "adjoint": {"ms_adjoint_solve": round(ms_adj, 3), "ms_forward_solve": round(ms_fwd, 3),
-                    "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
-                    "adj_over_fwd_pass": round(ms_adj / ms_pres, 3), "iterations": ainfo["iterations"]},
-        "stages_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stages.items() if v[1] > 0},
+    }
+    if coupled is not None:
+        line["coupled"] = coupled
+    line.update({
+        "roofline": roofline,
         "e2e": {"value": mc(ms_e2e), "unit": UNIT, "ms_per_step": round(ms_e2e, 3),
                 "host_buffers": "pinned, caller cell order; semo_set_fields + semo_set_old_velocity + "
                                 "semo_outer_iteration + semo_get_fields",
                 "h2d_bytes_per_step": 11 * 8 * nc, "d2h_bytes_per_step": 4 * 8 * nc},
-        "gpu_launches": int(launches),
-        "memory": {"device_used_gb": round(used_gb, 2), "device_total_gb": round(total_b / 1e9, 1)},
-        "roofline": roofline,
-        "clocks": clocks,
-    }
-    if coupled is not None:
-        line["coupled"] = coupled
+        "iterations": [i[3]["iterations"] for i in infos][:3],
+        "momentum_iterations": [i[0]["iterations"] for i in infos][:3],
+        "rel_residual": max(i[3]["rel_residual"] for i in infos),
+        "pressure_pass": {"value": mc(ms_pres), "ms_per_step": round(ms_pres, 3),
+                          "iterations": [i["iterations"] for i in infos_p][:3]},
+        "fp64": {"value": mc(ms_fp64), "ms_per_step": round(ms_fp64, 3),
+                 "iterations": infos64[-1][3]["iterations"], "mixed_speedup": round(ms_fp64 / ms_mixed, 3),
+                 "pressure_pass_ms": round(ms_fp64_p, 3),
+                 "pressure_pass_mixed_speedup": round(ms_fp64_p / ms_pres, 3)},
+        "adjoint": {"ms_adjoint_solve": round(ms_adj, 3), "ms_forward_solve": round(ms_fwd, 3),
+                    "adj_over_fwd_krylov": round(ainfo["solve_ms"] / fwd.info["solve_ms"], 3),
+                    "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
+                    "adj_over_fwd_pass": round(ms_adj / ms_pres, 3),
+                    "iterations": {"adjoint": ainfo["iterations"], "forward": fwd.info["iterations"]},
+                    "note": "krylov: both solves' Krylov time without setup; solve: the forward solve "
+                            "includes its AMG setup, the adjoint reuses the hierarchy"},
+    })
     if not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(case, steps=1)
+        base, o_outer, o_iters = cpu_baseline(case, steps=1)
+        line["error_vs_oracle"] = error_vs_oracle(case, S, local, o_outer, o_iters)
+        line["cpu_baseline"] = base
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -462,10 +664,8 @@ def coupled_bench(args, S, torch, local) -> dict:
     case = coupled_case(args.coupled_n)
     m = case.mesh
     steps = min(args.steps, 5)
-    out = {"workload": f"6 tetrahedra per hex of a jittered {args.coupled_n}^3 box, ideal gas (R = 287, gamma = 1.4), "
-                       "p = 1e5 + 1e3 smoothed N(0,1), T = 300 +- 5 K, U uniform[-50, 50] m/s, dt = 1e-5, walls; "
-                       "one calcCompCoupledEq: EOS, LSQ gradients, 5x5 block assembly, BiCGStab with AMG on a "
-                       "pressure equation + 5x5 block-Jacobi to 1e-8, update",
+    out = {"workload": f"6 tets per hex of a jittered {args.coupled_n}^3 box, ideal gas, config-2 fields, dt 1e-5; "
+                       "one calcCompCoupledEq to 1e-8",
            "cells": m.n_cells, "faces": m.n_faces, "block_slots": m.n_cells + 2 * m.n_internal, "steps": steps}
     for prec in ("fp64", "mixed"):
         ctx = S.Context(precision=prec, tol=1e-8, max_iter=3000, device=local)
@@ -532,9 +732,7 @@ def run_reference_arm(args, rank, world) -> None:
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded jittered hex mesh, VOF fields, old velocities)",
             "impl": "reference",
-            "config": {"workload": f"jittered hex {args.n}^3 two-phase VOF outer iteration: momentum (assembly + "
-                                   f"3 BiCGStab solves to 1e-9 + update) then pressure correction (assembly + "
-                                   f"SA-AMG setup + CG to 1e-8 + update)", "cells": nc},
+            "config": workload_config(args.n, case.mesh, world),
             "iterations": iters[:3],
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": Oracle.threads(), "kind": "port",
                              "sample": f"each step one full outer iteration over all {nc} cells on the host cores"},

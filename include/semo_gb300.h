@@ -312,6 +312,18 @@ semo_status semo_vjp_source(semo_ctx* ctx, const double* dJ_dx, double* lambda, 
 void semo_set_profiling(semo_ctx* ctx, int on);
 semo_status semo_stage_time(semo_ctx* ctx, const char* stage, double* total_ms, int64_t* calls);
 semo_status semo_reset_stats(semo_ctx* ctx);
+/* Device time of one y = A x launch on the last pressure hierarchy (after a
+   pressure solve), averaged over reps launches on the context's stream:
+   which 0 is the finest level's operator in the layout and precision the
+   V-cycle applies it, 1 the FP64 outer operator of the Krylov loop.  The
+   result vectors are the solver's scratch.  No reference counterpart. */
+semo_status semo_time_spmv(semo_ctx* ctx, int which, int reps, double* ms_per_launch);
+/* Sizes of the last pressure hierarchy: 6 values per level (rows, nnz of A,
+   nnz of the prolongator P, nnz of the restriction R, layout of A in the
+   V-cycle: 2 SELL-32 with 16-bit column offsets, 1 SELL-32, 0 CSR, -1 the
+   coarsest level's direct solve; bytes per value), at most max_levels
+   levels written; *levels gets the level count.  No reference counterpart. */
+semo_status semo_hierarchy_levels(semo_ctx* ctx, int64_t* out, int max_levels, int* levels);
 /* Kernel launches made by this library in this process so far. */
 int64_t semo_kernel_launches(void);
 /* Allocation-free relative residual ||b - A x|| / ||b|| of a CSR system
@@ -325,9 +337,14 @@ int64_t semo_kernel_launches(void);
    until the process exits.  Writes {||r||/||b||, ||r||, ||b||} to out3
    (device, 3 doubles) asynchronously on `stream` (a cudaStream_t, NULL for
    the default stream).  Rows above SEMO_STATIC_MAX_ROWS are rejected with
-   SEMO_ERR_ARGUMENT.  The first call on a device resolves the array's device
-   address; make it before any stream capture.  Every call shares the array:
-   calls that overlap on a GPU race. */
+   SEMO_ERR_ARGUMENT.  Each call made outside stream capture looks up the
+   array's device address again (so a re-created context is followed); a call
+   made during capture reuses the last address found on that device and gets
+   SEMO_ERR_STATE if there is none, so make the first call on each device
+   before any stream capture.  An error already pending from the caller's own
+   work is left pending and reported as SEMO_ERR_CUDA before any launch.
+   Every call shares the array: calls that overlap on a GPU race, so callers
+   serialise their calls on each GPU. */
 #define SEMO_STATIC_MAX_ROWS 2097152
 semo_status semo_residual_norm_static(const int32_t* ptr, const int32_t* col, const double* val, int n,
                                       const double* x, const double* b, double* out3, void* stream);

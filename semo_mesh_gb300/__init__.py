@@ -111,6 +111,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_reset_stats.argtypes = [vp]
     L.semo_kernel_launches.restype = C.c_int64
     L.semo_mesh_info.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.semo_time_spmv.argtypes = [vp, C.c_int, C.c_int, f64p]
+    L.semo_hierarchy_levels.argtypes = [vp, C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]
     L.semo_set_old_velocity.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p]
     L.semo_momentum_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_assemble_momentum.argtypes = [vp]
@@ -533,6 +535,22 @@ class Context:
         self._check(self.L.semo_mesh_info(self.h, out))
         keys = ("cells", "faces", "internal_faces", "boundary_faces", "stencil_nnz", "nnz")
         return {k: int(v) for k, v in zip(keys, out)}
+
+    def time_spmv(self, which: int, reps: int = 20) -> float:
+        """ms per y = A x launch on the last pressure hierarchy: which 0 the
+        finest V-cycle operator (its layout and precision), 1 the FP64 outer one."""
+        ms = C.c_double()
+        self._check(self.L.semo_time_spmv(self.h, int(which), int(reps), C.byref(ms)))
+        return ms.value
+
+    def hierarchy_levels(self) -> list:
+        """Per level of the last pressure hierarchy: rows, nnz of A, P and R,
+        the V-cycle layout of A and the value bytes."""
+        out = (C.c_int64 * (6 * 64))()
+        nl = C.c_int()
+        self._check(self.L.semo_hierarchy_levels(self.h, out, 64, C.byref(nl)))
+        keys = ("rows", "nnz_A", "nnz_P", "nnz_R", "layout", "value_bytes")
+        return [{k: int(out[6 * l + j]) for j, k in enumerate(keys)} for l in range(nl.value)]
 
     def vjp_source(self, dJ_dx) -> tuple:
         """lambda = A^-T dJ/dx and dJ/ds (s entering as b_i += s_i V_i)."""

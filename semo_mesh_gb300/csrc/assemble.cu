@@ -144,14 +144,19 @@ __global__ void k_grav_cell(int nc, int nf, const int* __restrict__ cfp, const i
 
 // One pass over each cell's vertex stencil: LSQ gradients of P,U,V,W,VF and
 // stencil min/max of U,V,W,VF,P (mm planes maxU,minU,maxV,minV,maxW,minW,
-// maxVF,minVF,maxP,minP).  Stencil weights w_k*d_k are precomputed.  With
-// kPVF false only the U,V,W parts are computed and the P and VF planes are
-// left as they are (they are still current: see assemble_gravity_stencil).
+// maxVF,minVF,maxP,minP).  Stencil weights w_k*d_k are precomputed, and so is
+// their per-cell sum S (stencil and boundary faces): the gradient's sum
+// sum_k w_k (phi_k - phi_i) is formed as sum_k w_k phi_k - phi_i S, three FMAs
+// an entry and field instead of a difference and three FMAs (FP64 issue bounds
+// this kernel on GB300).  With kPVF false only the U,V,W parts are computed
+// and the P and VF planes are left as they are (they are still current: see
+// assemble_gravity_stencil).
 template <bool kPVF>
 __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb, const int* __restrict__ stp,
                                                  const int* __restrict__ sti, const double* __restrict__ stw,
                                                  int64_t stn, const int* __restrict__ cfp,
                                                  const int* __restrict__ cfi, const double* __restrict__ bfw,
+                                                 const double* __restrict__ stws,
                                                  const double* __restrict__ minv, const double* __restrict__ P,
                                                  const double* __restrict__ U, const double* __restrict__ V,
                                                  const double* __restrict__ W, const double* __restrict__ VF,
@@ -169,18 +174,17 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
         const int j = __ldg(sti + k);
         const double wx = __ldg(stw + k), wy = __ldg(stw + stn + k), wz = __ldg(stw + 2 * stn + k);
         const double uj = __ldg(U + j), vj = __ldg(V + j), wj = __ldg(W + j);
-        double d;
         long long t;
         if constexpr (kPVF) {
             const double pj = __ldg(P + j), fj = __ldg(VF + j);
-            d = pj - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d;
-            d = fj - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d;
+            g[0][0] = fma(wx, pj, g[0][0]); g[0][1] = fma(wy, pj, g[0][1]); g[0][2] = fma(wz, pj, g[0][2]);
+            g[4][0] = fma(wx, fj, g[4][0]); g[4][1] = fma(wy, fj, g[4][1]); g[4][2] = fma(wz, fj, g[4][2]);
             t = okey(fj); kmaxf = (kmaxf < t) ? t : kmaxf; kminf = (t < kminf) ? t : kminf;
             t = okey(pj); kmaxp = (kmaxp < t) ? t : kmaxp; kminp = (t < kminp) ? t : kminp;
         }
-        d = uj - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
-        d = vj - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
-        d = wj - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
+        g[1][0] = fma(wx, uj, g[1][0]); g[1][1] = fma(wy, uj, g[1][1]); g[1][2] = fma(wz, uj, g[1][2]);
+        g[2][0] = fma(wx, vj, g[2][0]); g[2][1] = fma(wy, vj, g[2][1]); g[2][2] = fma(wz, vj, g[2][2]);
+        g[3][0] = fma(wx, wj, g[3][0]); g[3][1] = fma(wy, wj, g[3][1]); g[3][2] = fma(wz, wj, g[3][2]);
         t = okey(uj); kmaxu = (kmaxu < t) ? t : kmaxu; kminu = (t < kminu) ? t : kminu;
         t = okey(vj); kmaxv = (kmaxv < t) ? t : kmaxv; kminv = (t < kminv) ? t : kminv;
         t = okey(wj); kmaxw = (kmaxw < t) ? t : kmaxw; kminw = (t < kminw) ? t : kminw;
@@ -193,20 +197,25 @@ __global__ void __launch_bounds__(128) k_stencil(int nc, int nf, int ni, int nb,
             const int b = (cfi[k] & kFaceMask) - ni;
             const double wx = bfw[b], wy = bfw[nb + b], wz = bfw[2 * nb + b];
             double d;
-            if constexpr (kPVF) { d = bf[b] - pi; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d; }
-            d = bf[nb + b] - ui; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
-            d = bf[2 * nb + b] - vi; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
-            d = bf[3 * nb + b] - wi; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
-            if constexpr (kPVF) { d = bf[4 * nb + b] - fi; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d; }
+            if constexpr (kPVF) { d = bf[b]; g[0][0] += wx * d; g[0][1] += wy * d; g[0][2] += wz * d; }
+            d = bf[nb + b]; g[1][0] += wx * d; g[1][1] += wy * d; g[1][2] += wz * d;
+            d = bf[2 * nb + b]; g[2][0] += wx * d; g[2][1] += wy * d; g[2][2] += wz * d;
+            d = bf[3 * nb + b]; g[3][0] += wx * d; g[3][1] += wy * d; g[3][2] += wz * d;
+            if constexpr (kPVF) { d = bf[4 * nb + b]; g[4][0] += wx * d; g[4][1] += wy * d; g[4][2] += wz * d; }
         }
     }
+    const double sx = stws[i], sy = stws[nc + i], sz = stws[2 * nc + i];
+    const double phi_i[5] = {pi, ui, vi, wi, fi};
     const double m0 = minv[i], m1 = minv[nc + i], m2 = minv[2 * nc + i];
     const double m3 = minv[3 * nc + i], m4 = minv[4 * nc + i], m5 = minv[5 * nc + i];
 #pragma unroll
     for (int q = kPVF ? 0 : 1; q < (kPVF ? 5 : 4); ++q) {
-        double t0 = 0.0; t0 += m0 * g[q][0]; t0 += m1 * g[q][1]; t0 += m2 * g[q][2];
-        double t1 = 0.0; t1 += m1 * g[q][0]; t1 += m3 * g[q][1]; t1 += m4 * g[q][2];
-        double t2 = 0.0; t2 += m2 * g[q][0]; t2 += m4 * g[q][1]; t2 += m5 * g[q][2];
+        const double a0 = fma(-phi_i[q], sx, g[q][0]);
+        const double a1 = fma(-phi_i[q], sy, g[q][1]);
+        const double a2 = fma(-phi_i[q], sz, g[q][2]);
+        double t0 = 0.0; t0 += m0 * a0; t0 += m1 * a1; t0 += m2 * a2;
+        double t1 = 0.0; t1 += m1 * a0; t1 += m3 * a1; t1 += m4 * a2;
+        double t2 = 0.0; t2 += m2 * a0; t2 += m4 * a1; t2 += m5 * a2;
         grad[(3 * q + 0) * (size_t)nc + i] = t0;
         grad[(3 * q + 1) * (size_t)nc + i] = t1;
         grad[(3 * q + 2) * (size_t)nc + i] = t2;
@@ -532,7 +541,7 @@ void stencil_pass(semo_ctx* c, bool full) {
     StageScope sc(c, full ? ST_STENCIL : ST_STENCIL_UVW);
     auto launch = [&](auto kern) {
         kern<<<blocks(nc, 128), 128, 0, s>>>(nc, nf, ni, nb, c->st_ptr, c->st_idx, c->stw, c->st_nnz, c->cf_ptr,
-                                             c->cf_idx, c->bfw, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
+                                             c->cf_idx, c->bfw, c->stws, c->minv, c->P, c->U, c->V, c->W, c->VF, c->bface,
                                              c->grad, c->mm);
     };
     if (full) launch(k_stencil<true>);
@@ -544,7 +553,7 @@ void lsq_gradients5(semo_ctx* c, const double* f0, const double* f1, const doubl
                     const double* f4, const double* bf, double* grad, double* mm) {
     k_stencil<true><<<blocks(c->nc, 128), 128, 0, c->stream>>>(c->nc, c->nf, c->ni, c->nb, c->st_ptr, c->st_idx,
                                                                c->stw, c->st_nnz, c->cf_ptr, c->cf_idx, c->bfw,
-                                                               c->minv, f0, f1, f2, f3, f4, bf, grad, mm);
+                                                               c->stws, c->minv, f0, f1, f2, f3, f4, bf, grad, mm);
     SEMO_CHECK_LAUNCH();
 }
 

@@ -1090,6 +1090,22 @@ semo_status semo_reset_stats(semo_ctx* c) {
     });
 }
 
+semo_status semo_time_spmv(semo_ctx* c, int which, int reps, double* ms_per_launch) {
+    return guarded(c, [&] {
+        need(which == 0 || which == 1, SEMO_ERR_ARGUMENT, "which is 0 (finest V-cycle operator) or 1 (FP64 outer)");
+        need(reps > 0 && ms_per_launch != nullptr, SEMO_ERR_ARGUMENT, "bad reps or null output");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        *ms_per_launch = semo::time_pressure_spmv(c, which, reps);
+    });
+}
+
+semo_status semo_hierarchy_levels(semo_ctx* c, int64_t* out, int max_levels, int* levels) {
+    return guarded(c, [&] {
+        need(out != nullptr && levels != nullptr && max_levels > 0, SEMO_ERR_ARGUMENT, "bad output");
+        *levels = semo::pressure_levels(c, out, max_levels);
+    });
+}
+
 int64_t semo_kernel_launches(void) { return __atomic_load_n(&semo::g_kernel_launches, __ATOMIC_RELAXED); }
 
 semo_status semo_mesh_info(semo_ctx* c, int64_t* out6) {

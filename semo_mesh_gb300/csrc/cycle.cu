@@ -1413,6 +1413,87 @@ void solve_transpose_reuse(semo_ctx* c, const double* g, double* lam, semo_solve
     info->solve_ms = t1;
 }
 
+// ---- measurement hooks on the last pressure hierarchy ----------------------
+namespace {
+template <class V>
+Amg<V>& pressure_amg(semo_ctx* c);
+template <> Amg<float>& pressure_amg<float>(semo_ctx* c) { return c->amg32; }
+template <> Amg<double>& pressure_amg<double>(semo_ctx* c) { return c->amg64; }
+template <class V>
+Cycle<V>& pressure_cycle(ApplyState& st);
+template <> Cycle<float>& pressure_cycle<float>(ApplyState& st) { return st.cy32; }
+template <> Cycle<double>& pressure_cycle<double>(ApplyState& st) { return st.cy64; }
+
+// reps launches of y = A x with A the finest level's operator in the layout
+// the V-cycle uses (which = 0) or the FP64 outer operator (which = 1)
+template <class V>
+double time_spmv(semo_ctx* c, int which, int reps) {
+    ApplyState& st = apply_state(c);
+    Amg<V>& h = pressure_amg<V>(c);
+    if (!h.ready || h.lev.empty()) throw Error(SEMO_ERR_STATE, "no pressure hierarchy: run a pressure solve first");
+    cudaStream_t s = c->stream;
+    const int n = h.lev[0].A.n;
+    if (which == 0 && h.lev.size() < 2) throw Error(SEMO_ERR_STATE, "single-level hierarchy: no V-cycle operator");
+    if (which == 1 && (c->kp.n < (size_t)n || c->kq.n < (size_t)n)) throw Error(SEMO_ERR_STATE, "no Krylov vectors");
+    cudaEvent_t e0, e1;
+    SEMO_CUDA(cudaEventCreate(&e0));
+    SEMO_CUDA(cudaEventCreate(&e1));
+    float ms = 0.f;
+    try {
+        SEMO_CUDA(cudaEventRecord(e0, s));
+        for (int k = 0; k < reps; ++k) {
+            if (which == 0) {
+                AmgLevel<V>& L = h.lev[0];
+                with_A(pressure_cycle<V>(st).lev[0], L.A,
+                       [&](auto A) { k_mv<<<grid_for(A), 256, 0, s>>>(A, L.x.p, L.t.p); });
+            } else {
+                st.outer.with([&](auto A) { k_mv<<<grid_for(A), 256, 0, s>>>(A, c->kp.p, c->kq.p); });
+            }
+            SEMO_CHECK_LAUNCH();
+        }
+        SEMO_CUDA(cudaEventRecord(e1, s));
+        SEMO_CUDA(cudaEventSynchronize(e1));
+        SEMO_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
+}
+
+template <class V>
+int levels_of(semo_ctx* c, int64_t* out, int max_levels) {
+    ApplyState& st = apply_state(c);
+    Amg<V>& h = pressure_amg<V>(c);
+    if (!h.ready) throw Error(SEMO_ERR_STATE, "no pressure hierarchy: run a pressure solve first");
+    const int nl = (int)h.lev.size();
+    Cycle<V>& cy = pressure_cycle<V>(st);
+    for (int l = 0; l < nl && l < max_levels; ++l) {
+        const AmgLevel<V>& L = h.lev[l];
+        int64_t* o = out + 6 * l;
+        o[0] = L.A.n;
+        o[1] = L.A.nnz;
+        o[2] = L.P.nnz;
+        o[3] = L.R.nnz;
+        o[4] = (l + 1 < nl && l < (int)cy.lev.size()) ? (cy.lev[l].a16 ? 2 : (cy.lev[l].a ? 1 : 0)) : -1;
+        o[5] = (int64_t)sizeof(V);
+    }
+    return nl;
+}
+}  // namespace
+
+double time_pressure_spmv(semo_ctx* c, int which, int reps) {
+    return c->prm.precision == SEMO_PREC_MIXED ? time_spmv<float>(c, which, reps) : time_spmv<double>(c, which, reps);
+}
+
+int pressure_levels(semo_ctx* c, int64_t* out, int max_levels) {
+    return c->prm.precision == SEMO_PREC_MIXED ? levels_of<float>(c, out, max_levels)
+                                               : levels_of<double>(c, out, max_levels);
+}
+
 // ---- AMG on the pressure equation of the coupled system (first stage of its
 // two-stage preconditioner).  A hierarchy of its own, so the pressure
 // equation's hierarchy is left as it is.

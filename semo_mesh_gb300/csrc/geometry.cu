@@ -164,16 +164,21 @@ __global__ void k_face_weights(int nf, int ni, int nc, const int* __restrict__ o
 }
 
 // LSQ normal matrix over the vertex stencil then the cell's boundary faces,
-// its cofactor inverse, and the per-entry weight vectors w_k * d_k reused by
-// every gradient evaluation (w_k = 1/|d_k|^2).
+// its cofactor inverse, the per-entry weight vectors w_k * d_k reused by
+// every gradient evaluation (w_k = 1/|d_k|^2), and their per-cell sum over the
+// stencil and the boundary faces (3 planes of nc), with which a gradient sums
+// w_k phi_k and subtracts phi_i sum_k w_k once instead of forming every
+// difference phi_k - phi_i.
 __global__ void k_lsq_setup(int nc, int nf, int ni, const int* __restrict__ stp, const int* __restrict__ sti,
                             const int* __restrict__ cfp, const int* __restrict__ cfi, const double* __restrict__ cc,
                             const double* __restrict__ fc, int64_t stn, double* __restrict__ stw,
-                            double* __restrict__ bfw, double* __restrict__ minv, int* __restrict__ flag) {
+                            double* __restrict__ bfw, double* __restrict__ minv, double* __restrict__ stws,
+                            int* __restrict__ flag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     const double xi = cc[i], yi = cc[nc + i], zi = cc[2 * nc + i];
     double v0 = 0, v1 = 0, v2 = 0, v9 = 0, v10 = 0, v17 = 0;
+    double sx = 0, sy = 0, sz = 0;
     for (int k = stp[i]; k < stp[i + 1]; ++k) {
         const int j = sti[k];
         const double dx = cc[j] - xi, dy = cc[nc + j] - yi, dz = cc[2 * nc + j] - zi;
@@ -182,6 +187,7 @@ __global__ void k_lsq_setup(int nc, int nf, int ni, const int* __restrict__ stp,
         v0 += wx * dx; v1 += wx * dy; v2 += wx * dz;
         v9 += wy * dy; v10 += wy * dz; v17 += wz * dz;
         stw[k] = wx; stw[stn + k] = wy; stw[2 * stn + k] = wz;
+        sx += wx; sy += wy; sz += wz;
     }
     const int nb = nf - ni;
     for (int k = cfp[i]; k < cfp[i + 1]; ++k) {
@@ -194,7 +200,9 @@ __global__ void k_lsq_setup(int nc, int nf, int ni, const int* __restrict__ stp,
         v9 += wy * dy; v10 += wy * dz; v17 += wz * dz;
         const int b = f - ni;
         bfw[b] = wx; bfw[nb + b] = wy; bfw[2 * nb + b] = wz;
+        sx += wx; sy += wy; sz += wz;
     }
+    stws[i] = sx; stws[nc + i] = sy; stws[2 * nc + i] = sz;
     const double det = v0 * v9 * v17 + v1 * v10 * v2 + v2 * v1 * v10 - v0 * v10 * v10 - v2 * v9 * v2 - v1 * v1 * v17;
     if (det == 0.0) atomicExch(flag + 1, 1);
     minv[i] = (v9 * v17 - v10 * v10) / det;
@@ -233,6 +241,7 @@ void geometry_build(semo_ctx* c, const double* d_points, const int* d_fptr, cons
     c->vol.alloc(nc, s); c->cc.alloc(3 * (size_t)nc, s); c->minv.alloc(6 * (size_t)nc, s);
     c->stw.alloc(3 * (size_t)std::max<int64_t>(c->st_nnz, 1), s);
     c->bfw.alloc(3 * (size_t)std::max(nb, 1), s);
+    c->stws.alloc(3 * (size_t)nc, s);
     c->fk.alloc(4 * (size_t)std::max(ni, 1), s);
     DBuf<double> vsn3, cen;
     vsn3.alloc(nf, s);
@@ -247,7 +256,7 @@ void geometry_build(semo_ctx* c, const double* d_points, const int* d_fptr, cons
                                                 c->alf, c->epn, c->skew, c->pf, c->nfv);
     SEMO_CHECK_LAUNCH();
     k_lsq_setup<<<blocks(nc, T), T, 0, s>>>(nc, nf, ni, c->st_ptr, c->st_idx, c->cf_ptr, c->cf_idx, c->cc, c->fc,
-                                             c->st_nnz, c->stw, c->bfw, c->minv, c->flag);
+                                             c->st_nnz, c->stw, c->bfw, c->minv, c->stws, c->flag);
     SEMO_CHECK_LAUNCH();
     if (ni > 0) {
         k_face_consts<<<blocks(ni, T), T, 0, s>>>(ni, nf, c->fa, c->mpn, c->alf, c->wc, c->fk);

@@ -15,9 +15,19 @@
 // library holds its 1 MiB until the process exits, and every call shares it,
 // so calls whose kernels overlap on a GPU (two streams, two host threads)
 // race on it.  Each call overwrites every slot it reads, so nothing needs
-// clearing between calls.  Its device address is looked up once per device,
-// on the first call made with that device current; make that first call
-// before any stream capture.
+// clearing between calls.
+//
+// Its device address is looked up on every call made outside stream capture
+// (the lookup does not synchronise), so a primary context that was torn down
+// and created again (cudaDeviceReset) never sees a stale address.  Inside a
+// capture the address found by the last uncaptured call on that device is
+// used; a device with no uncaptured call yet gets SEMO_ERR_STATE, so make the
+// first call on each device before any stream capture.
+//
+// Launch errors: an error already pending in the caller's thread (from the
+// caller's own earlier work) is left in place and reported as SEMO_ERR_CUDA
+// before anything is launched; after the launches cudaGetLastError reads and
+// clears only the error of these two launches.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,7 +43,8 @@ static_assert(SEMO_STATIC_MAX_ROWS % kRowsPerBlock == 0, "row limit must be a wh
 
 __device__ __align__(256) double g_residual_scratch[2 * kMaxBlocks];
 
-// per device: address of g_residual_scratch, resolved once
+// per device: address of g_residual_scratch found by the last call made
+// outside stream capture
 std::mutex g_lock;
 double* g_addr[64] = {nullptr};
 
@@ -105,17 +116,23 @@ extern "C" semo_status semo_residual_norm_static(const int32_t* ptr, const int32
     if (n > SEMO_STATIC_MAX_ROWS) return SEMO_ERR_ARGUMENT;   // the static scratch holds 65536 blocks of 32 rows
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SEMO_ERR_NO_DEVICE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // an error left by the caller's own work stays the caller's: do not launch, do not clear it
+    if (cudaPeekAtLastError() != cudaSuccess) return SEMO_ERR_CUDA;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return SEMO_ERR_CUDA;
     double* scratch = nullptr;
     {
         std::lock_guard<std::mutex> g(g_lock);
-        if (!g_addr[dev]) {
+        if (cap == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_residual_scratch) != cudaSuccess || !p) return SEMO_ERR_CUDA;
             g_addr[dev] = static_cast<double*>(p);
+        } else if (!g_addr[dev]) {
+            return SEMO_ERR_STATE;   // no uncaptured call on this device yet: the address is unknown
         }
         scratch = g_addr[dev];
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nparts = (n + kRowsPerBlock - 1) / kRowsPerBlock;
     k_res_parts<<<nparts, kThreads, 0, s>>>(n, ptr, col, val, x, b, scratch, nparts);
     if (cudaGetLastError() != cudaSuccess) return SEMO_ERR_CUDA;

@@ -146,6 +146,7 @@ struct semo_ctx {
     semo::DBuf<double> vol, cc, minv;             // cc: 3 planes; minv: 6 planes
     semo::DBuf<double> stw;                       // 3 planes of st_nnz: w_k * d_k (LSQ weight vectors)
     semo::DBuf<double> bfw;                       // 3 planes of nb: boundary-face LSQ weight vectors
+    semo::DBuf<double> stws;                      // 3 planes of nc: per-cell sum of the stencil and boundary weights
     // derived per-face constants for the hot face kernel
     semo::DBuf<double> fk;                        // 4 planes of ni: kA = alpha*area/magPN, kP = alpha/magPN, area, wC
 
@@ -386,6 +387,13 @@ void solve_system(semo_ctx* c, const int* d_ptr, const int* d_col, const double*
                   const double* d_b, double* d_x, semo_solve_info* info, bool zero_guess, bool may_reuse = false);
 
 void solve_transpose_reuse(semo_ctx* c, const double* d_g, double* d_lam, semo_solve_info* info);
+// measurement: ms per launch of y = A x on the last pressure hierarchy's finest
+// operator in the V-cycle's layout (which 0) or the FP64 outer operator (which 1)
+double time_pressure_spmv(semo_ctx* c, int which, int reps);
+// per level of the last pressure hierarchy, 6 values: rows, nnz(A), nnz(P),
+// nnz(R), layout of A in the V-cycle (2 SELL-32 16-bit offsets, 1 SELL-32,
+// 0 CSR, -1 coarsest: direct solve), value bytes; returns the level count
+int pressure_levels(semo_ctx* c, int64_t* out, int max_levels);
 // three right-hand sides of the momentum system (c->Am_val, c->bm) -> c->xm; info[3]; returns the
 // worst status (SEMO_OK, SEMO_ERR_NOT_CONVERGED or SEMO_ERR_BREAKDOWN)
 semo_status solve_momentum(semo_ctx* c, semo_solve_info* info);
