@@ -25,6 +25,12 @@ needed between steps.
   adjoint        A^T lambda = dJ/dx on the forward hierarchy, time vs the forward solve
   coupled        calcCompCoupledEq (ideal gas, 5x5 blocks) on 6 x 96^3 tetrahedra,
                  FP64 and mixed
+  large          the 256^3 case: outer iterations, the adjoint transpose solve on
+                 the same hierarchy, per-kernel HBM fractions, device memory
+  roofline       the dominant single-launch kernel (HBM and FP64 fractions), the
+                 two SpMVs timed alone and a whole CG iteration
+  error_vs_oracle  the GPU path against the FP64 CPU oracle on this workload
+                 (systems, solutions, fields after one outer iteration)
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 128]
 """
@@ -234,6 +240,83 @@ def fp64_peak_tflops(torch, dev) -> float:
         best = min(best, e0.elapsed_time(e1))
     del a, b, c
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def kernel_rooflines(stages: dict, steps: int, minfo: dict, peak: float, spmv_ms: tuple, levels: list,
+                     solve_infos: list) -> dict:
+    """HBM fraction of each kernel of an outer iteration that has its own
+    stage timer (one launch each), of the two SpMVs timed alone, and of a
+    whole CG iteration, from device times and algorithmic bytes."""
+    out = {}
+    for st, (kname, falgo, _) in KERNEL_OF_STAGE.items():
+        ms, calls = stages.get(st, (0.0, 0))
+        if calls:
+            b = falgo(minfo)
+            out[kname] = {"ms": round(ms / calls, 4), "frac": round(b / (ms / calls * 1e-3) / 1e9 / peak, 4)}
+    L0 = levels[0]
+    b32 = spmv_algo_bytes(L0["rows"], L0["nnz_A"], L0["value_bytes"])
+    b64 = spmv_algo_bytes(L0["rows"], L0["nnz_A"], 8)
+    out["spmv_level0"] = {"ms": round(spmv_ms[0], 4), "frac": round(b32 / (spmv_ms[0] * 1e-3) / 1e9 / peak, 4)}
+    out["spmv_outer_fp64"] = {"ms": round(spmv_ms[1], 4), "frac": round(b64 / (spmv_ms[1] * 1e-3) / 1e9 / peak, 4)}
+    it = sum(i["iterations"] for i in solve_infos)
+    ms_it = sum(i["solve_ms"] for i in solve_infos) / max(it, 1)
+    out["pcg_iteration"] = {"ms": round(ms_it, 4),
+                            "frac": round(pcg_iteration_bytes(levels) / (ms_it * 1e-3) / 1e9 / peak, 4)}
+    return out
+
+
+def large_bench(args, S, torch, local) -> dict:
+    """The 256^3 jittered VOF case: outer iterations (mixed), then the adjoint
+    transpose solve on the same pressure hierarchy; per-kernel HBM fractions
+    and the device memory held, against a 180 GB budget."""
+    case = bench_case(args.large_n)
+    t0 = time.perf_counter()
+    ctx = S.Context(precision="mixed", tol=1e-8, device=local, reuse_hierarchy=False)
+    ctx.set_case(case)
+    t_upload = time.perf_counter() - t0
+    minfo = ctx.mesh_info()
+    strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
+    for _ in range(2):
+        ctx.outer_iteration()
+    steps = 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(strm)
+    infos = [ctx.outer_iteration()[1] for _ in range(steps)]
+    e1.record(strm)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    pinfos = [ctx.outer_iteration()[1] for _ in range(steps)]
+    stages = ctx.stage_times()
+    ctx.set_profiling(False)
+    spmv_ms = (ctx.time_spmv(0, 20), ctx.time_spmv(1, 20))
+    levels = ctx.hierarchy_levels()
+    free_b, total_b = torch.cuda.mem_get_info(local)
+    used = (total_b - free_b) / 1e9
+    # adjoint: J = sum of p'^2 over the z = 1 cells, on the forward hierarchy
+    zc = case.mesh.patch_cells("zmax")
+    ctx.set_case(case)
+    ctx.assemble()
+    fwd = ctx.solve()
+    g = np.zeros(case.mesh.n_cells)
+    np.add.at(g, zc, 2.0 * fwd.x[zc])
+    _, _, ainfo = ctx.vjp_source(g)
+    ctx.close()
+    nc = case.mesh.n_cells
+    return {"workload": f"jittered hex {args.large_n}^3 two-phase VOF outer iteration (mixed) + adjoint transpose "
+                        f"solve on the same hierarchy",
+            "cells": nc, "faces": minfo["faces"], "nnz": minfo["nnz"],
+            "value": round(nc / (ms * 1e-3) / 1e6, 3), "unit": UNIT, "ms_per_step": round(ms, 3), "steps": steps,
+            "iterations": [i[3]["iterations"] for i in infos], "rel_residual": max(i[3]["rel_residual"] for i in infos),
+            "adjoint": {"iterations": ainfo["iterations"], "rel_residual": ainfo["rel_residual"],
+                        "adj_over_fwd_krylov": round(ainfo["solve_ms"] / fwd.info["solve_ms"], 3),
+                        "ms_adjoint_krylov": round(ainfo["solve_ms"], 3)},
+            "device_used_gb": round(used, 2), "budget_gb": 180.0, "upload_s": round(t_upload, 1),
+            "amg_levels": len(levels), "level0_layout": levels[0]["layout"],
+            "kernels": kernel_rooflines(stages, steps, minfo, hbm_peak()[0], spmv_ms, levels,
+                                        [i[3] for i in pinfos])}
 
 
 def oracle_outer_iteration(o) -> dict:
@@ -521,6 +604,14 @@ def run_gpu_arm(args, rank, world, local) -> None:
     ms_fp64_p, infos64_p = timed(ctx64, strm64, args.steps, pressure)
     ctx64.close()
 
+    # ---- config 4: the 256^3 case, outer iteration and adjoint ---------------
+    large = None
+    if args.large_n > 0 and world == 1:
+        try:
+            large = large_bench(args, S, torch, local)
+        except S.SemoError as e:   # reported, never allowed to take the headline down
+            large = {"error": str(e)}
+
     # ---- compressible coupled 5x5 system (6 tetrahedra per hex) -------------
     coupled = None
     if args.coupled_n > 0:
@@ -546,6 +637,7 @@ def run_gpu_arm(args, rank, world, local) -> None:
     achieved = algo / (per_launch_ms * 1e-3) / 1e9
     traffic = None
     fp64_pipe = None
+    t = None
     if os.path.exists(TRAFFIC):
         with open(TRAFFIC) as f:
             tr = json.load(f)
@@ -560,8 +652,13 @@ def run_gpu_arm(args, rank, world, local) -> None:
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "algorithmic_bytes": algo,
                 "design_bytes": design, "ms_per_launch": round(per_launch_ms, 4), "peak_source": peak_src}
+    flops = None
     if kname == "k_stencil":
         flops = stencil_fp64_flops(minfo)
+    elif t and "dfma_per_launch" in t:
+        # the face kernels' FP64 operations (ncu, 64^3) scale with the faces
+        flops = (2 * t["dfma_per_launch"] + t["dadd_per_launch"] + t["dmul_per_launch"]) * minfo["faces"] / t["faces"]
+    if flops is not None:
         roofline["fp64"] = {"tflops": round(flops / (per_launch_ms * 1e-3) / 1e12, 3),
                             "peak_tflops": round(fp64_tf, 3), "frac": round(flops / (per_launch_ms * 1e-3) / 1e12
                                                                            / fp64_tf, 3),
@@ -620,6 +717,8 @@ def run_gpu_arm(args, rank, world, local) -> None:
     }
     if coupled is not None:
         line["coupled"] = coupled
+    if large is not None:
+        line["large"] = large
     line.update({
         "roofline": roofline,
         "e2e": {"value": mc(ms_e2e), "unit": UNIT, "ms_per_step": round(ms_e2e, 3),
@@ -750,6 +849,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--coupled-n", type=int, default=96,
                     help="hexes per edge of the tetrahedral coupled case (0 skips it)")
+    ap.add_argument("--large-n", type=int, default=256,
+                    help="hex cells per edge of the large VOF case (0 skips it)")
     ap.add_argument("--coupled-only", action="store_true",
                     help="run only the coupled case and print its object (profiling runs)")
     args = ap.parse_args()

@@ -292,6 +292,25 @@ semo_status semo_solve_pressure(semo_ctx* ctx, double* x, semo_solve_info* info)
 semo_status semo_solve_coo(semo_ctx* ctx, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,
                            const double* vals, const double* b, double* x, semo_solve_info* info);
 
+/* Solve a caller-supplied scalar system (B_n = 1, SEMO's COO triple) for
+   nrhs = 1, 2 or 3 right-hand sides b[j*n + i] by the momentum and volume-
+   fraction solver: Jacobi-preconditioned BiCGStab to params.mom_tol, batched
+   when nrhs = 3 (the matrix is read once per product for all three).  x is
+   nrhs*n, in/out: the initial guess in (zeros, as SEMO passes resiVar, or
+   any guess, from which the correction is solved), the solutions out.  Each
+   row needs a non-zero diagonal entry (the preconditioner reads the row's
+   first one).  info points to nrhs entries or NULL.  Replaces, with
+   BiCGStab instead of AMGCL's aggregation/ILU0 FGMRES:
+   SEMO_Solvers_Builder::solveAMGCL's three-right-hand-side overload
+   (src/solvers/build.h:233-239, src/solvers/solveAMGCL.cpp:1116-1271) that
+   calcMomentumEqs calls (src/solvers/eqMomentum.cpp:1017), with nrhs = 3;
+   solveAMGCL("volume_fraction", mesh, 1, ...) (src/solvers/solveAMGCL.cpp:
+   862-937) that calcVolfracEq calls (src/solvers/eqVolfrac.cpp:766), with
+   nrhs = 1 (a non-symmetric matrix, which semo_solve_coo's CG does not take). */
+semo_status semo_solve_coo_multi(semo_ctx* ctx, int nrhs, int n, int64_t nnz, const int32_t* rows,
+                                 const int32_t* cols, const double* vals, const double* b, double* x,
+                                 semo_solve_info* info);
+
 /* Optional per-cell source s (caller's order) added to the pressure RHS as
    b_i += s_i * V_i after assembly; NULL clears it.  No reference counterpart
    (used by the adjoint check of the pressure solve). */

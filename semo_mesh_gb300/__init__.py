@@ -104,6 +104,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_get_array.argtypes = [vp, C.c_char_p, f64p, C.c_int64]
     L.semo_solve_pressure.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_solve_coo.argtypes = [vp, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, f64p, C.POINTER(SolveInfo)]
+    L.semo_solve_coo_multi.argtypes = [vp, C.c_int, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, f64p,
+                                       C.POINTER(SolveInfo)]
     L.semo_set_source.argtypes = [vp, f64p]
     L.semo_vjp_source.argtypes = [vp, f64p, f64p, f64p, C.POINTER(SolveInfo)]
     L.semo_set_profiling.argtypes = [vp, C.c_int]
@@ -460,22 +462,51 @@ class Context:
                                     iperm.ctypes.data_as(C.POINTER(C.c_int32))))
         return perm, iperm
 
-    def solve_amgcl(self, equation: str, B_n: int, A_rows, A_cols, A_vals, B, resiVar=None) -> SolveResult:
-        """solveAMGCL(equation, mesh, B_n, A_rows, A_cols, A_vals, B, resiVar) for B_n == 1."""
+    def solve_amgcl(self, equation: str, B_n: int, A_rows, A_cols, A_vals, *args):
+        """solveAMGCL with SEMO's argument lists (src/solvers/build.h:225-239).
+
+        solve_amgcl("pressure", 1, rows, cols, vals, B[, resiVar]): AMG-CG
+        (semo_solve_coo); solve_amgcl("volume_fraction", 1, rows, cols, vals,
+        B[, resiVar]): BiCGStab (semo_solve_coo_multi, one right-hand side);
+        solve_amgcl("momentum", 1, rows, cols, vals, B0, B1, B2[, resiVar0,
+        resiVar1, resiVar2]): the three-right-hand-side overload, returns a
+        list of three SolveResult.  resiVar is the initial guess (zeros when
+        left out)."""
         if B_n != 1:
-            raise SemoError(1, "only scalar systems (B_n == 1) are supported")
-        if equation != "pressure":
-            raise SemoError(1, f"equation '{equation}' is not on this path (only 'pressure')")
-        n = len(B)
-        x = np.zeros(n) if resiVar is None else np.array(resiVar, dtype=np.float64)
+            raise SemoError(1, "only scalar systems (B_n == 1) have a live SEMO caller; the 5x5 coupled system "
+                               "goes through semo_solve_coupled")
         r, rp = _i32(A_rows)
         c, cp = _i32(A_cols)
         v, vp = _f64(A_vals)
-        b, bp = _f64(B)
-        info = SolveInfo()
-        self._check(self.L.semo_solve_coo(self.h, n, len(r), rp, cp, vp, bp,
-                                          x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
-        return SolveResult(x=x, info=info.as_dict())
+        if equation in ("pressure", "volume_fraction"):
+            if len(args) not in (1, 2):
+                raise SemoError(1, f"solveAMGCL('{equation}') takes B and optionally resiVar")
+            B = args[0]
+            n = len(B)
+            x = np.zeros(n) if len(args) == 1 or args[1] is None else np.array(args[1], dtype=np.float64)
+            b, bp = _f64(B)
+            if equation == "pressure":
+                info = SolveInfo()
+                self._check(self.L.semo_solve_coo(self.h, n, len(r), rp, cp, vp, bp,
+                                                  x.ctypes.data_as(C.POINTER(C.c_double)), C.byref(info)))
+                return SolveResult(x=x, info=info.as_dict())
+            info = (SolveInfo * 1)()
+            self._check(self.L.semo_solve_coo_multi(self.h, 1, n, len(r), rp, cp, vp, bp,
+                                                    x.ctypes.data_as(C.POINTER(C.c_double)), info))
+            return SolveResult(x=x, info=info[0].as_dict())
+        if equation == "momentum":
+            if len(args) not in (3, 6):
+                raise SemoError(1, "solveAMGCL('momentum') takes B0, B1, B2 and optionally three resiVar")
+            n = len(args[0])
+            b = np.ascontiguousarray(np.concatenate([np.asarray(a, dtype=np.float64) for a in args[:3]]))
+            x = (np.zeros(3 * n) if len(args) == 3
+                 else np.ascontiguousarray(np.concatenate([np.asarray(a, dtype=np.float64) for a in args[3:]])))
+            info = (SolveInfo * 3)()
+            self._check(self.L.semo_solve_coo_multi(self.h, 3, n, len(r), rp, cp, vp,
+                                                    b.ctypes.data_as(C.POINTER(C.c_double)),
+                                                    x.ctypes.data_as(C.POINTER(C.c_double)), info))
+            return [SolveResult(x=x[j * n:(j + 1) * n].copy(), info=info[j].as_dict()) for j in range(3)]
+        raise SemoError(1, f"equation '{equation}' is not on this path")
 
     # ---- pieces ----------------------------------------------------------
     def assemble(self) -> None:

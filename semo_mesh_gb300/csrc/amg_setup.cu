@@ -843,7 +843,11 @@ void spgemm_pass(cudaStream_t s, int ht, int pass, const DCsr<V>& A, const DCsr<
                  int* nlist) {
     const int n = A.n;
     const size_t shm = (size_t)kGemmWarps * ht * 2 * (sizeof(int) + sizeof(double));
-    const int grid = std::max(1, std::min(blocks(n, kGemmWarps), 152 * 32));
+    // grid-stride over the rows, 32 blocks a multiprocessor (the sums are exact
+    // integers, so the grid does not change the result)
+    int dev = 0;
+    SEMO_CUDA(cudaGetDevice(&dev));
+    const int grid = std::max(1, std::min(blocks(n, kGemmWarps), sm_count(dev) * 32));
 #define SEMO_GEMM_CASE(H)                                                                                        \
     case H:                                                                                                      \
         if (shm > 48 * 1024)                                                                                     \

@@ -117,6 +117,7 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
         int no_deps = 0;
         SEMO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no_deps));
         for (auto& e : c->ev) SEMO_CUDA(cudaEventCreate(&e));
+        for (auto& e : c->setup_ev) SEMO_CUDA(cudaEventCreate(&e));
         c->flag.alloc(16, c->stream);
         c->flag.zero();
     });
@@ -139,6 +140,7 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     c->amg64.clear();
     c->amg32.clear();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : c->setup_ev) if (e) cudaEventDestroy(e);
     semo::resolve_stage_timers(c);
     for (auto e : c->ev_pool) cudaEventDestroy(e);
     for (auto& e : c->sync_ev) if (e) cudaEventDestroy(e);
@@ -1060,6 +1062,59 @@ semo_status semo_solve_coo(semo_ctx* c, int n, int64_t nnz, const int32_t* rows,
         if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
     });
     if (st == SEMO_OK && conv != SEMO_OK) c->err = "Krylov solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
+semo_status semo_solve_coo_multi(semo_ctx* c, int nrhs, int n, int64_t nnz, const int32_t* rows, const int32_t* cols,
+                                 const double* vals, const double* b, double* x, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(nrhs >= 1 && nrhs <= 3, SEMO_ERR_ARGUMENT, "nrhs must be 1, 2 or 3");
+        need(n > 0 && nnz >= n && rows && cols && vals && b && x, SEMO_ERR_ARGUMENT, "bad COO system");
+        need(nnz < INT32_MAX, SEMO_ERR_ARGUMENT, "nnz too large");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        // COO -> CSR as solveAMGCL.cpp:1129-1172 (stable: in-row order = COO order)
+        std::vector<int> ptr(n + 1, 0), col(nnz), dig(n, -1);
+        std::vector<double> val(nnz);
+        for (int64_t k = 0; k < nnz; ++k) {
+            need(rows[k] >= 0 && rows[k] < n && cols[k] >= 0 && cols[k] < n, SEMO_ERR_ARGUMENT, "COO index out of range");
+            need(std::isfinite(vals[k]), SEMO_ERR_NAN, "non-finite matrix value");
+            ptr[rows[k]]++;
+        }
+        for (int i = 0, t = 0; i < n; ++i) { int u = ptr[i]; ptr[i] = t; t += u; }
+        ptr[n] = (int)nnz;
+        for (int64_t k = 0; k < nnz; ++k) {
+            const int d = ptr[rows[k]]++;
+            col[d] = cols[k];
+            val[d] = vals[k];
+            if (cols[k] == rows[k] && dig[rows[k]] < 0) dig[rows[k]] = d;   // each row's first diagonal entry
+        }
+        for (int i = 0, last = 0; i <= n; ++i) { int t = ptr[i]; ptr[i] = last; last = t; }
+        for (int i = 0; i < n; ++i) {
+            need(dig[i] >= 0, SEMO_ERR_ARGUMENT, "row " + std::to_string(i) + " has no diagonal entry");
+            need(val[dig[i]] != 0.0, SEMO_ERR_ARGUMENT, "row " + std::to_string(i) + " has a zero diagonal");
+        }
+        bool guess = false;
+        for (int64_t i = 0; i < (int64_t)nrhs * n; ++i) {
+            need(std::isfinite(b[i]) && std::isfinite(x[i]), SEMO_ERR_NAN, "non-finite rhs/guess");
+            guess |= x[i] != 0.0;
+        }
+        cudaStream_t s = c->stream;
+        semo::DBuf<int> dp, dc, dd;
+        semo::DBuf<double> dv, db, dx;
+        dp.upload(ptr.data(), n + 1, s);
+        dc.upload(col.data(), nnz, s);
+        dd.upload(dig.data(), n, s);
+        dv.upload(val.data(), nnz, s);
+        db.upload(b, (size_t)nrhs * n, s);
+        dx.upload(x, (size_t)nrhs * n, s);
+        semo_solve_info inf[3] = {};
+        conv = semo::solve_csr_multi(c, n, dp.p, dc.p, dd.p, dv.p, nrhs, db.p, dx.p, guess, inf);
+        SEMO_CUDA(cudaMemcpyAsync(x, dx.p, sizeof(double) * nrhs * n, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (info) for (int j = 0; j < nrhs; ++j) info[j] = inf[j];
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "a momentum-type solve did not reach the tolerance";
     return st != SEMO_OK ? st : conv;
 }
 

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -30,8 +31,11 @@ namespace semo {
 namespace {
 
 // Grid of the kernels that end in a reduction (dot products fused into the
-// SpMVs and vector updates): 4 blocks of 256 per SM on 152 SMs, grid-stride
-// (measured faster here than 16 a SM); fixed, so every sum has a fixed order.
+// SpMVs and vector updates), grid-stride: a fixed 608-way partition of the
+// rows, one partial sum per block, summed in a fixed order.  608 is 4 blocks
+// of 256 per multiprocessor on GB300's 152 (measured faster here than 16 a
+// multiprocessor); it is not taken from the device so that the partition,
+// and with it every sum's bits, is the same on any GPU.
 constexpr int kRedBlocks = 608;
 constexpr int kRedThreads = 256;
 inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
@@ -105,15 +109,26 @@ struct SellView {
     }
 };
 
-// SELL-32 with the column stored as a 16-bit offset from the row: an
-// RCM-ordered mesh matrix has a small bandwidth (|col - row| ~ 12k at 2.1M
-// cells), so 6 bytes an FP32 entry move instead of 8.  Padding entries point
-// at the row itself with value 0.
+// SELL-32 with 16-bit columns.  Each slice of 32 rows picks one of three
+// encodings (smode[s]), a choice that is uniform across the warp that walks it:
+//  0  a signed offset from the row (every |col - row| <= 32767: an RCM-ordered
+//     mesh matrix up to ~200^3 cells has all its slices so);
+//  1  an unsigned offset from a base column of its (slice, j) group,
+//     gbase[(sptr[s] >> 5) + j]: consecutive rows of an RCM order have their
+//     j-th entries next to one another (median spread 31 columns), so this
+//     holds at any bandwidth unless a group spans more than 65,535 columns;
+//  2  32-bit columns in wcol[wptr[s] ..] (values stay in val).
+// An FP32 entry moves 6 bytes instead of 8 in modes 0 and 1.  Padding entries
+// point at the row (mode 0) or at the group's base (1, 2) with value 0.
 template <class V>
 struct Sell16View {
     static constexpr int kVS = 1;
     const int* __restrict__ sptr;
-    const short* __restrict__ dcol;
+    const int* __restrict__ smode;
+    const int* __restrict__ gbase;
+    const int* __restrict__ wptr;
+    const unsigned short* __restrict__ dcol;
+    const int* __restrict__ wcol;
     const V* __restrict__ val;
     int n;
     template <class F>
@@ -122,15 +137,36 @@ struct Sell16View {
         if (row < n) {
             const int sl = row >> 5, l = row & 31;
             const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+            const int mode = smode[sl];
             int k = b + l;
             int j = 0;
-            for (; j + 1 < w; j += 2, k += 64) {
-                const int c0 = row + dcol[k], c1 = row + dcol[k + 32];
-                const V v0 = val[k], v1 = val[k + 32];
-                s += v0 * x(c0);
-                s += v1 * x(c1);
+            if (mode == 0) {
+                for (; j + 1 < w; j += 2, k += 64) {   // two independent loads in flight
+                    const int c0 = row + (short)dcol[k], c1 = row + (short)dcol[k + 32];
+                    const V v0 = val[k], v1 = val[k + 32];
+                    s += v0 * x(c0);
+                    s += v1 * x(c1);
+                }
+                if (j < w) s += val[k] * x(row + (short)dcol[k]);
+            } else if (mode == 1) {
+                const int* __restrict__ gb = gbase + (b >> 5);
+                for (; j + 1 < w; j += 2, k += 64) {
+                    const int c0 = __ldg(gb + j) + dcol[k], c1 = __ldg(gb + j + 1) + dcol[k + 32];
+                    const V v0 = val[k], v1 = val[k + 32];
+                    s += v0 * x(c0);
+                    s += v1 * x(c1);
+                }
+                if (j < w) s += val[k] * x(__ldg(gb + j) + dcol[k]);
+            } else {
+                const int* __restrict__ wc = wcol + wptr[sl] + l;
+                for (; j + 1 < w; j += 2, k += 64) {
+                    const int c0 = wc[32 * j], c1 = wc[32 * j + 32];
+                    const V v0 = val[k], v1 = val[k + 32];
+                    s += v0 * x(c0);
+                    s += v1 * x(c1);
+                }
+                if (j < w) s += val[k] * x(wc[32 * j]);
             }
-            if (j < w) s += val[k] * x(row + dcol[k]);
         }
         return s;
     }
@@ -459,62 +495,92 @@ void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, in
     SEMO_CHECK_LAUNCH();
 }
 
+// One warp per slice (blocks of whole warps): the slice's encoding, the base
+// column (smallest column) of every (slice, j) group and the slice's 32-bit
+// column count in wsz (0 unless its encoding is 2).
+__global__ void k_sell16_groups(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                const int* __restrict__ sptr, int* __restrict__ smode, int* __restrict__ gbase,
+                                int* __restrict__ wsz) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sl = row >> 5;
+    if (sl >= ((n + 31) >> 5)) return;   // whole warps: the test is uniform in a warp
+    const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+    const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
+    bool wide = false, near = true;
+    for (int j = 0; j < w; ++j) {
+        const int c = (j < len) ? col[rb + j] : -1;
+        const int mn = __reduce_min_sync(0xffffffffu, (c >= 0) ? c : INT_MAX);
+        const int mx = __reduce_max_sync(0xffffffffu, c);
+        wide |= (long long)mx - (long long)mn > 65535;
+        near &= (c < 0) || (c - row >= -32768 && c - row <= 32767);
+        if ((threadIdx.x & 31) == 0) gbase[(b >> 5) + j] = mn;
+    }
+    near = __all_sync(0xffffffffu, near);
+    const int mode = near ? 0 : (wide ? 2 : 1);
+    if ((threadIdx.x & 31) == 0) {
+        smode[sl] = mode;
+        wsz[sl] = (mode == 2) ? 32 * w : 0;
+    }
+}
+
 template <class V, class W>
 __global__ void k_sell16_fill(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                              const V* __restrict__ val, const int* __restrict__ sptr, short* __restrict__ dcol,
-                              W* __restrict__ sval, int* __restrict__ too_far) {
+                              const V* __restrict__ val, const int* __restrict__ sptr, const int* __restrict__ smode,
+                              const int* __restrict__ gbase, const int* __restrict__ wptr,
+                              unsigned short* __restrict__ dcol, int* __restrict__ wcol, W* __restrict__ sval) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= ((n + 31) & ~31)) return;
     const int sl = row >> 5, l = row & 31;
     const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+    const int mode = smode[sl];
     const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
-    bool far = false;
     for (int j = 0; j < w; ++j) {
         const int k = b + 32 * j + l;
-        if (j < len) {
-            const int d = col[rb + j] - row;
-            far |= (d < -32768 || d > 32767);
-            dcol[k] = (short)d;
-            sval[k] = (W)val[rb + j];
-        } else {
-            dcol[k] = 0;   // the row itself (exists for rows < n; rows past n are never read)
-            sval[k] = W(0);
-        }
+        const int base = (mode == 0) ? row : gbase[(b >> 5) + j];
+        const int c = (j < len) ? col[rb + j] : base;
+        dcol[k] = (mode == 2) ? (unsigned short)0 : (unsigned short)(c - base);
+        if (mode == 2) wcol[wptr[sl] + 32 * j + l] = c;
+        sval[k] = (j < len) ? (W)val[rb + j] : W(0);
     }
-    if (far) atomicExch(too_far, 1);
 }
 
 template <class V>
 struct Sell16 {
     int n = 0, nslices = 0;
-    DBuf<int> sptr;
-    DBuf<short> dcol;
+    DBuf<int> sptr, smode, gbase, wptr, wcol;
+    DBuf<unsigned short> dcol;
     DBuf<V> val;
-    Sell16View<V> view() const { return Sell16View<V>{sptr.p, dcol.p, val.p, n}; }
+    Sell16View<V> view() const {
+        return Sell16View<V>{sptr.p, smode.p, gbase.p, wptr.p, dcol.p, wcol.p, val.p, n};
+    }
 };
 
-// SELL-32 with 16-bit column offsets of a square CSR operator; false (and
-// nothing kept) if some column is 32768 or more away from its row
+// SELL-32 with 16-bit columns of a square CSR operator (always built: slices
+// that fit no 16-bit encoding keep 32-bit columns)
 template <class V, class W>
-bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int* flag) {
+bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int*) {
     S.n = n;
     S.nslices = (n + 31) / 32;
     S.sptr.alloc(S.nslices + 1, s);
+    S.wptr.alloc(S.nslices + 1, s);
+    S.smode.alloc(S.nslices, s);
     SEMO_CUDA(cudaMemsetAsync(S.sptr.p + S.nslices, 0, sizeof(int), s));
+    SEMO_CUDA(cudaMemsetAsync(S.wptr.p + S.nslices, 0, sizeof(int), s));
     const int rows_pad = S.nslices * 32;
     k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
     SEMO_CHECK_LAUNCH();
     const int total = device_scan(s, S.sptr.p, S.nslices + 1);
-    S.dcol.alloc(std::max(total, 1), s);
-    S.val.alloc(std::max(total, 1), s);
-    SEMO_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
-    k_sell16_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.dcol.p, S.val.p, flag);
+    S.gbase.alloc(std::max(total / 32, 1), s);
+    k_sell16_groups<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, S.sptr.p, S.smode.p, S.gbase.p, S.wptr.p);
     SEMO_CHECK_LAUNCH();
-    int far = 1;
-    SEMO_CUDA(cudaMemcpyAsync(&far, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    if (far) { S.sptr.release(); S.dcol.release(); S.val.release(); S.n = 0; }
-    return !far;
+    const int wide = device_scan(s, S.wptr.p, S.nslices + 1);
+    S.dcol.alloc(std::max(total, 1), s);
+    S.wcol.alloc(std::max(wide, 1), s);
+    S.val.alloc(std::max(total, 1), s);
+    k_sell16_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.smode.p, S.gbase.p,
+                                                               S.wptr.p, S.dcol.p, S.wcol.p, S.val.p);
+    SEMO_CHECK_LAUNCH();
+    return true;
 }
 
 // The FP64 outer operator: 16-bit column offsets when they fit, else SELL-32
@@ -1150,7 +1216,7 @@ void pressure_setup(semo_ctx* c, const int* ptr, const int* col, const double* v
     ApplyState& st = apply_state(c);
     c->sflag.alloc(16, s);
     SEMO_CUDA(cudaMemsetAsync(c->sflag.p, 0, 16 * sizeof(int), s));
-    SEMO_CUDA(cudaEventRecord(c->ev[0], s));
+    SEMO_CUDA(cudaEventRecord(c->setup_ev[0], s));
     {
         StageScope sc(c, ST_AMG_SETUP);
         // The hierarchy is a deterministic function of the matrix: when the
@@ -1193,7 +1259,7 @@ void pressure_setup(semo_ctx* c, const int* ptr, const int* col, const double* v
             }
         }
     }
-    SEMO_CUDA(cudaEventRecord(c->ev[1], s));   // setup_ms is read from ev[0..1] after the solve
+    SEMO_CUDA(cudaEventRecord(c->setup_ev[1], s));   // setup_ms is read from setup_ev after the solve
     (void)info;
 }
 
@@ -1227,8 +1293,8 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
     if (c->matrix_prebuilt) {
         t0 = (float)c->side_setup_ms;   // the setup shared the GPU with the momentum pass
     } else {
-        SEMO_CUDA(cudaEventSynchronize(c->ev[1]));
-        SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
+        SEMO_CUDA(cudaEventSynchronize(c->setup_ev[1]));
+        SEMO_CUDA(cudaEventElapsedTime(&t0, c->setup_ev[0], c->setup_ev[1]));
     }
     SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[2], c->ev[3]));
     info->setup_ms = t0;
@@ -1237,14 +1303,26 @@ void solve_system(semo_ctx* c, const int* ptr, const int* col, const double* val
 
 namespace {
 
+// The CSR pattern a batched BiCGStab solve runs on: the context's mesh
+// pattern (gen = the mesh generation, so its SELL layout is kept across
+// solves) or a caller's matrix (gen < 0: the layout is built for this solve).
+struct KrylovPattern {
+    int n;
+    const int* ptr;
+    const int* col;
+    const int* dig;   // position of each row's diagonal
+    int gen;
+};
+KrylovPattern mesh_pattern(semo_ctx* c) { return KrylovPattern{c->nc, c->A_ptr, c->A_col, c->A_dig, c->mesh_gen}; }
+
 // Jacobi-preconditioned BiCGStab on NR right-hand sides (planes of b, x) of
-// the matrix with values val on the context's CSR pattern.
+// the matrix with values val on the pattern pat, from x = 0.
 template <int NR>
-semo_status bicgstab_jacobi(semo_ctx* c, int stage, const double* val, const double* b, double* x,
-                            semo_solve_info* info) {
+semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, const double* val, const double* b,
+                            double* x, semo_solve_info* info) {
     StageScope scope(c, stage);
     cudaStream_t s = c->stream;
-    const int n = c->nc;
+    const int n = pat.n;
     const size_t N = n;
     MomState& st = mom_state(c);
     st.dinv.alloc(N, s);
@@ -1262,15 +1340,15 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const double* val, const dou
     // residual, checked at the end, lands under it
     const double tol2 = 0.25 * c->prm.mom_tol * c->prm.mom_tol;
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
-    if (st.gen != c->mesh_gen) {
-        build_sell<double, double>(s, c->A_ptr, c->A_col, val, n, st.A);
-        st.gen = c->mesh_gen;
+    if (pat.gen < 0 || st.gen != pat.gen) {
+        build_sell<double, double>(s, pat.ptr, pat.col, val, n, st.A);
+        st.gen = pat.gen;
     } else {   // same pattern (the mesh's): refill the values into the kept layout
         k_sell_fill<double, double><<<blocks((int64_t)st.A.nslices * 32, 256), 256, 0, s>>>(
-            n, c->A_ptr, c->A_col, val, st.A.sptr, st.A.col, st.A.val);
+            n, pat.ptr, pat.col, val, st.A.sptr, st.A.col, st.A.val);
         SEMO_CHECK_LAUNCH();
     }
-    k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, c->A_dig, val, st.dinv);
+    k_dinv_dig<<<blocks(n, 256), 256, 0, s>>>(n, pat.dig, val, st.dinv);
     SEMO_CHECK_LAUNCH();
     SEMO_CUDA(cudaEventRecord(c->ev[1], s));
     const SellView<double> A = st.A.view();
@@ -1382,12 +1460,50 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const double* val, const dou
 
 semo_status solve_momentum(semo_ctx* c, semo_solve_info* info) {
     c->xm.alloc(3 * (size_t)c->nc, c->stream);
-    return bicgstab_jacobi<3>(c, ST_MSOLVE, c->Am_val, c->bm, c->xm, info);
+    return bicgstab_jacobi<3>(c, ST_MSOLVE, mesh_pattern(c), c->Am_val, c->bm, c->xm, info);
 }
 
 semo_status solve_vof(semo_ctx* c, semo_solve_info* info) {
     c->xvf.alloc((size_t)c->nc, c->stream);
-    return bicgstab_jacobi<1>(c, ST_VSOLVE, c->Av_val, c->bvf, c->xvf, info);
+    return bicgstab_jacobi<1>(c, ST_VSOLVE, mesh_pattern(c), c->Av_val, c->bvf, c->xvf, info);
+}
+
+semo_status solve_csr_multi(semo_ctx* c, int n, const int* ptr, const int* col, const int* dig, const double* val,
+                            int nrhs, const double* b, double* x, bool guess, semo_solve_info* info) {
+    cudaStream_t s = c->stream;
+    const size_t N = n;
+    const KrylovPattern pat{n, ptr, col, dig, -1};
+    // with an initial guess x0: solve A d = b - A x0 from d = 0, then x = x0 + d
+    DBuf<double> rb, d;
+    const double* rhs = b;
+    double* sol = x;
+    if (guess) {
+        rb.alloc(N * nrhs, s);
+        d.alloc(N * nrhs, s);
+        const CsrView<double, 8> A8{ptr, col, val, n};
+        for (int j = 0; j < nrhs; ++j) {
+            k_res64<<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(A8, x + j * N, b + j * N, rb.p + j * N);
+            SEMO_CHECK_LAUNCH();
+        }
+        rhs = rb.p;
+        sol = d.p;
+    }
+    semo_status worst = SEMO_OK;
+    auto merge = [&](semo_status st) {
+        if (st == SEMO_ERR_BREAKDOWN || (st != SEMO_OK && worst == SEMO_OK)) worst = st;
+    };
+    if (nrhs == 3) {
+        merge(bicgstab_jacobi<3>(c, ST_MSOLVE, pat, val, rhs, sol, info));
+    } else {
+        for (int j = 0; j < nrhs; ++j)
+            merge(bicgstab_jacobi<1>(c, ST_MSOLVE, pat, val, rhs + j * N, sol + j * N, info ? info + j : nullptr));
+    }
+    if (guess) {
+        k_axpy1<double><<<blocks((int64_t)N * nrhs, 256), 256, 0, s>>>((int)(N * nrhs), d.p, x);
+        SEMO_CHECK_LAUNCH();
+    }
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    return worst;
 }
 
 // Adjoint solve on the hierarchy of the last forward solve (the pressure

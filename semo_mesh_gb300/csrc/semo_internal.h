@@ -249,6 +249,9 @@ struct semo_ctx {
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
     int mesh_gen = 0;                             // bumped by every mesh upload (cached layouts check it)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // the pressure setup's own timing pair: the setup may run on the second
+    // host thread while the momentum solve records ev[] on the main one
+    cudaEvent_t setup_ev[2] = {nullptr, nullptr};
 
     // profiling: per-stage device time from event pairs, resolved after each call
     bool profiling = false;
@@ -399,6 +402,12 @@ int pressure_levels(semo_ctx* c, int64_t* out, int max_levels);
 semo_status solve_momentum(semo_ctx* c, semo_solve_info* info);
 // the volume-fraction system (c->Av_val, c->bvf) -> c->xvf; info[1]
 semo_status solve_vof(semo_ctx* c, semo_solve_info* info);
+// nrhs (1..3) right-hand sides (planes of n) of a caller's CSR matrix (device
+// arrays; dig = position of each row's diagonal) by the momentum solver
+// (Jacobi BiCGStab, batched for three); x in/out (the initial guess is used
+// when guess); info[nrhs]; returns the worst status as solve_momentum does
+semo_status solve_csr_multi(semo_ctx* c, int n, const int* ptr, const int* col, const int* dig, const double* val,
+                            int nrhs, const double* b, double* x, bool guess, semo_solve_info* info);
 
 // momentum.cu (face_values_done: assemble_face_values(c, true) already ran)
 void assemble_momentum(semo_ctx* c, bool face_values_done = false);
