@@ -571,6 +571,13 @@ def run_gpu_arm(args, rank, world, local) -> None:
     e1.record(strm)
     e1.synchronize()
     ms_adj = e0.elapsed_time(e1)
+    # the whole field gradient: transpose solve + transposed face-flux kernels
+    ctx.vjp_fields(g)
+    e0.record(strm)
+    _, _, finfo = ctx.vjp_fields(g)
+    e1.record(strm)
+    e1.synchronize()
+    ms_vjpf = e0.elapsed_time(e1)
     ctx.close()
 
     # ---- hierarchy kept across outer iterations (bit-identical pressure matrix) --
@@ -739,8 +746,11 @@ def run_gpu_arm(args, rank, world, local) -> None:
                     "adj_over_fwd_solve": round(ms_adj / ms_fwd, 3),
                     "adj_over_fwd_pass": round(ms_adj / ms_pres, 3),
                     "iterations": {"adjoint": ainfo["iterations"], "forward": fwd.info["iterations"]},
+                    "ms_vjp_fields": round(ms_vjpf, 3), "vjp_fields_over_pressure_pass": round(ms_vjpf / ms_pres, 3),
                     "note": "krylov: both solves' Krylov time without setup; solve: the forward solve "
-                            "includes its AMG setup, the adjoint reuses the hierarchy"},
+                            "includes its AMG setup, the adjoint reuses the hierarchy; vjp_fields: dJ/d(U,V,W,P) "
+                            "(transpose solve + transposed face-flux kernels + host copies) against one "
+                            "calcPressureEq"},
     })
     if not args.no_cpu_baseline and world == 1:
         base, o_outer, o_iters = cpu_baseline(case, steps=1)

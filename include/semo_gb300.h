@@ -323,6 +323,25 @@ semo_status semo_set_source(semo_ctx* ctx, const double* s);
 semo_status semo_vjp_source(semo_ctx* ctx, const double* dJ_dx, double* lambda, double* dJ_ds,
                             semo_solve_info* info);
 
+/* Discrete adjoint of the pressure-correction equation with respect to the
+   cell fields: given dJ/dx for the solution x of the assembled pressure
+   system (caller's order), solves A^T lambda = dJ/dx on the forward solve's
+   AMG hierarchy and returns the vector-Jacobian products
+   dJ/dphi = lambda^T db/dphi for phi = U, V, W, P, where b is the face-flux
+   right-hand side of calcPressureEq (src/solvers/eqPressure.cpp:246-673:
+   the skew-corrected, stencil-limited face velocity and the Rhie-Chow
+   pressure terms of src/solvers/surfaceNormalVelocity.cpp:100-187, the
+   boundary-face rules) at the context's current fields; the matrix depends
+   only on geometry, dt and the densities, so this is the whole gradient of
+   J through the solve.  At a clamped face reconstruction the derivative
+   goes to the stencil cell holding the limit.  The face gradients are
+   recomputed from the cell fields, not kept from the forward pass.  Needs a
+   forward solve (semo_pressure_pass, or semo_assemble_pressure and
+   semo_solve_pressure).  Any output pointer may be NULL.  No reference
+   counterpart (SEMO has no adjoint). */
+semo_status semo_vjp_fields(semo_ctx* ctx, const double* dJ_dx, double* lambda, double* dJ_dU, double* dJ_dV,
+                            double* dJ_dW, double* dJ_dP, semo_solve_info* info);
+
 /* Measurement hooks (no reference counterpart).  With profiling on, the
    named stages are bracketed by CUDA events on the context's stream:
    "face_values","gravity","stencil","pface","pbface","pcell","amg_setup",

@@ -108,6 +108,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
                                        C.POINTER(SolveInfo)]
     L.semo_set_source.argtypes = [vp, f64p]
     L.semo_vjp_source.argtypes = [vp, f64p, f64p, f64p, C.POINTER(SolveInfo)]
+    L.semo_vjp_fields.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p, C.POINTER(SolveInfo)]
     L.semo_set_profiling.argtypes = [vp, C.c_int]
     L.semo_stage_time.argtypes = [vp, C.c_char_p, f64p, C.POINTER(C.c_int64)]
     L.semo_reset_stats.argtypes = [vp]
@@ -582,6 +583,17 @@ class Context:
         self._check(self.L.semo_hierarchy_levels(self.h, out, 64, C.byref(nl)))
         keys = ("rows", "nnz_A", "nnz_P", "nnz_R", "layout", "value_bytes")
         return [{k: int(out[6 * l + j]) for j, k in enumerate(keys)} for l in range(nl.value)]
+
+    def vjp_fields(self, dJ_dx) -> tuple:
+        """lambda = A^-T dJ/dx and dJ/d(U, V, W, P) through the pressure
+        equation's face-flux right-hand side (a dict of four arrays)."""
+        g, gp = _f64(dJ_dx)
+        out = {k: np.empty(self.n_cells) for k in ("lambda", "U", "V", "W", "P")}
+        ptr = [out[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("lambda", "U", "V", "W", "P")]
+        info = SolveInfo()
+        self._check(self.L.semo_vjp_fields(self.h, gp, *ptr, C.byref(info)))
+        lam = out.pop("lambda")
+        return lam, out, info.as_dict()
 
     def vjp_source(self, dJ_dx) -> tuple:
         """lambda = A^-T dJ/dx and dJ/ds (s entering as b_i += s_i V_i)."""

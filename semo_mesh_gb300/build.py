@@ -29,6 +29,7 @@ UNITS = [
     ("surftens.cu", []),
     ("amg_setup.cu", []),
     ("cycle.cu", []),
+    ("adjoint.cu", []),
     ("noalloc.cu", []),
     ("capi.cpp", []),
     ("foam.cpp", []),

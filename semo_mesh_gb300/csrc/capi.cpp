@@ -1223,6 +1223,40 @@ semo_status semo_vjp_source(semo_ctx* c, const double* dJ_dx, double* lambda, do
     return st != SEMO_OK ? st : conv;
 }
 
+semo_status semo_vjp_fields(semo_ctx* c, const double* dJ_dx, double* lambda, double* dJ_dU, double* dJ_dV,
+                            double* dJ_dW, double* dJ_dP, semo_solve_info* info) {
+    semo_status conv = SEMO_OK;
+    semo_status st = guarded(c, [&] {
+        need(c->assembled, SEMO_ERR_STATE, "no assembled system: run a forward pass first");
+        need(dJ_dx != nullptr, SEMO_ERR_ARGUMENT, "null dJ/dx");
+        SEMO_CUDA(cudaSetDevice(c->device));
+        const size_t n = (size_t)c->nc;
+        cudaStream_t s = c->stream;
+        semo::DBuf<double> g, lam, grads;
+        g.alloc(n, s);
+        lam.alloc(n, s);
+        grads.alloc(4 * n, s);
+        c->stage.alloc(5 * n, s);
+        SEMO_CUDA(cudaMemcpyAsync(c->stage.p, dJ_dx, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        double* gdst[1] = {g.p};
+        if (!semo::fields_from_caller_order(c, c->stage.p, gdst, 1)) throw Error(SEMO_ERR_NAN, "non-finite dJ/dx");
+        semo_solve_info inf{};
+        semo::solve_transpose_reuse(c, g.p, lam.p, &inf);
+        if (info) *info = inf;
+        semo::vjp_fields(c, lam.p, grads.p);
+        const double* src[5] = {lam.p, grads.p, grads.p + n, grads.p + 2 * n, grads.p + 3 * n};
+        semo::fields_to_caller_order(c, src, c->stage.p, 5);
+        double* dst[5] = {lambda, dJ_dU, dJ_dV, dJ_dW, dJ_dP};
+        for (int q = 0; q < 5; ++q)
+            if (dst[q]) SEMO_CUDA(cudaMemcpyAsync(dst[q], c->stage.p + q * n, sizeof(double) * n,
+                                                  cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (!(inf.rel_residual <= c->prm.tol)) conv = std::isfinite(inf.rel_residual) ? SEMO_ERR_NOT_CONVERGED : SEMO_ERR_NAN;
+    });
+    if (st == SEMO_OK && conv != SEMO_OK) c->err = "adjoint solve did not reach the tolerance";
+    return st != SEMO_OK ? st : conv;
+}
+
 // ---------------------------------------------------------------------------
 // compressible coupled system
 // ---------------------------------------------------------------------------

@@ -147,6 +147,8 @@ struct semo_ctx {
     semo::DBuf<double> stw;                       // 3 planes of st_nnz: w_k * d_k (LSQ weight vectors)
     semo::DBuf<double> bfw;                       // 3 planes of nb: boundary-face LSQ weight vectors
     semo::DBuf<double> stws;                      // 3 planes of nc: per-cell sum of the stencil and boundary weights
+    semo::DBuf<int> st_tpos;                      // per stencil entry (j, i): the entry's position in i's row (adjoint)
+    int st_tpos_gen = -1;                         // mesh generation st_tpos was built for
     // derived per-face constants for the hot face kernel
     semo::DBuf<double> fk;                        // 4 planes of ni: kA = alpha*area/magPN, kP = alpha/magPN, area, wC
 
@@ -412,6 +414,11 @@ semo_status solve_csr_multi(semo_ctx* c, int n, const int* ptr, const int* col, 
 // momentum.cu (face_values_done: assemble_face_values(c, true) already ran)
 void assemble_momentum(semo_ctx* c, bool face_values_done = false);
 double momentum_update(semo_ctx* c);
+
+// adjoint.cu: lambda^T db/d(U, V, W, P) of the pressure equation's right-hand
+// side at the current fields (lambda device, RCM order) -> out, 4 planes
+// (dJ/dU, dJ/dV, dJ/dW, dJ/dP), RCM order
+void vjp_fields(semo_ctx* c, const double* lam, double* out);
 
 // vof.cu
 void assemble_vof(semo_ctx* c);
