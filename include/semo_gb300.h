@@ -73,6 +73,10 @@ typedef struct {
     int overlap_setup;           /* semo_outer_iteration assembles the pressure matrix (which depends only on
                                     geometry, dt and the densities) and builds its hierarchy on a second stream
                                     while the momentum pass runs; same results bit for bit; default 1 */
+    int smoother;                /* AMG smoother: 0 Chebyshev (degree cheb_degree, default), 1 multicolour
+                                    Gauss-Seidel (a forward sweep before the coarse correction, a backward one
+                                    after; colours from a deterministic Jones-Plassmann colouring of each
+                                    level; AMGCL's relaxation/gauss_seidel.hpp family) */
 } semo_params;
 
 /* Physics of one outer iteration (calcMomentumEqs / calcPressureEq inputs). */

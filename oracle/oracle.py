@@ -60,6 +60,7 @@ def lib():
         L.orc_update_vof.restype = C.c_double
         L.orc_update_vof.argtypes = [vp, vp]
         L.orc_num_threads.restype = C.c_int
+        L.orc_set_smoother.argtypes = [C.c_int]
         L.orc_set_coupled.argtypes = [vp, vp, vp, vp]
         L.orc_curvature.argtypes = [vp]
         L.orc_surface_tension.argtypes = [vp, C.c_double]
@@ -143,9 +144,16 @@ class Oracle:
         lib().orc_coo_to_csr(self.h)
         lib().orc_permute_csr(self.h)
 
-    def solve(self, use_rcm: bool = False, tol: float = 1e-8, maxiter: int = 500) -> dict:
+    def solve(self, use_rcm: bool = False, tol: float = 1e-8, maxiter: int = 500,
+              smoother: str = "chebyshev") -> dict:
+        """SA-AMG CG on the assembled system; smoother "chebyshev" or
+        "gauss_seidel" (multicolour, the GPU's colouring and sweep order)."""
         info = np.zeros(16)
-        it = lib().orc_solve(self.h, 1 if use_rcm else 0, tol, maxiter, _p(info))
+        lib().orc_set_smoother(1 if smoother == "gauss_seidel" else 0)
+        try:
+            it = lib().orc_solve(self.h, 1 if use_rcm else 0, tol, maxiter, _p(info))
+        finally:
+            lib().orc_set_smoother(0)
         if it < 0:
             raise RuntimeError("oracle AMG setup failed")
         x = self.get("rcm_x_orc" if use_rcm else "x_orc")

@@ -829,14 +829,21 @@ typedef struct {
     double *dinv, lam_max;
     double *r, *x, *b, *t1, *t2;   /* work vectors */
     int nagg;
+    int ncolors; int *cptr, *crow;  /* Gauss-Seidel: rows grouped by colour */
 } level_t;
 typedef struct {
     int nlev;
     level_t lev[32];
     int nc; double* chol;  /* coarsest dense Cholesky factor (lower, row-major) */
     int cheb_degree;
+    int smoother;          /* 0 Chebyshev, 1 multicolour Gauss-Seidel */
     long long total_nnz;
 } amg_t;
+
+/* Smoother of the oracle's AMG (orc_set_smoother): 0 Chebyshev, 1 multicolour
+   Gauss-Seidel, restating the GPU's (its colouring and its sweep order). */
+static int g_smoother = 0;
+void orc_set_smoother(int s) { g_smoother = s; }
 
 static void csr_free(csr_t* a) { free(a->ptr); free(a->col); free(a->val); memset(a, 0, sizeof *a); }
 
@@ -966,12 +973,84 @@ static void spmv(const csr_t* A, const double* x, double* y) {
 
 typedef struct { double eps_strong; int coarse_enough; int max_levels; int cheb_degree; } amg_prm;
 
+/* Jones-Plassmann colouring in synchronous rounds (the GPU's k_color_round):
+   an uncoloured row whose (hash, index) key exceeds every uncoloured
+   neighbour's takes the smallest colour that no neighbour coloured in an
+   earlier round holds.  Fills L->cptr / L->crow (rows grouped by colour,
+   ascending row order inside a colour); returns -1 beyond 128 colours. */
+static int color_level(level_t* L) {
+    const csr_t* A = &L->A;
+    int n = A->n;
+    int* cold = (int*)malloc(sizeof(int) * n);
+    int* cnew = (int*)malloc(sizeof(int) * n);
+    for (int i = 0; i < n; ++i) cold[i] = -1;
+    int left = n, bad = 0;
+    while (left > 0 && !bad) {
+        memcpy(cnew, cold, sizeof(int) * n);
+        left = 0;
+        for (int i = 0; i < n; ++i) {
+            if (cold[i] >= 0) continue;
+            uint64_t ki = (((uint64_t)hash_u32((uint32_t)i)) << 32) | (uint64_t)(uint32_t)i;
+            uint64_t used0 = 0, used1 = 0;
+            int top = 1;
+            for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+                int j = A->col[k];
+                if (j == i) continue;
+                int cj = cold[j];
+                if (cj < 0) {
+                    uint64_t kj = (((uint64_t)hash_u32((uint32_t)j)) << 32) | (uint64_t)(uint32_t)j;
+                    if (kj > ki) { top = 0; break; }
+                } else if (cj < 64) used0 |= 1ull << cj;
+                else if (cj < 128) used1 |= 1ull << (cj - 64);
+            }
+            if (!top) { left++; continue; }
+            int c = -1;
+            for (int b = 0; b < 64 && c < 0; ++b) if (!(used0 >> b & 1)) c = b;
+            for (int b = 0; b < 64 && c < 0; ++b) if (!(used1 >> b & 1)) c = 64 + b;
+            if (c < 0) { bad = 1; break; }
+            cnew[i] = c;
+        }
+        int* t = cold; cold = cnew; cnew = t;
+    }
+    int nc = 0;
+    for (int i = 0; i < n && !bad; ++i) if (cold[i] + 1 > nc) nc = cold[i] + 1;
+    if (!bad) {
+        L->ncolors = nc;
+        L->cptr = (int*)calloc(nc + 1, sizeof(int));
+        L->crow = (int*)malloc(sizeof(int) * (n + 1));
+        for (int i = 0; i < n; ++i) L->cptr[cold[i] + 1]++;
+        for (int k = 0; k < nc; ++k) L->cptr[k + 1] += L->cptr[k];
+        int* fill = (int*)malloc(sizeof(int) * (nc + 1));
+        memcpy(fill, L->cptr, sizeof(int) * (nc + 1));
+        for (int i = 0; i < n; ++i) L->crow[fill[cold[i]]++] = i;
+        free(fill);
+    }
+    free(cold); free(cnew);
+    return bad ? -1 : nc;
+}
+
+/* one Gauss-Seidel sweep, colours ascending (forward) or descending */
+static void gs_sweep(const level_t* L, const double* b, double* x, int backward) {
+    const csr_t* A = &L->A;
+    for (int q = 0; q < L->ncolors; ++q) {
+        int k = backward ? L->ncolors - 1 - q : q;
+#pragma omp parallel for schedule(static)
+        for (int t = L->cptr[k]; t < L->cptr[k + 1]; ++t) {
+            int i = L->crow[t];
+            double s = 0.0;
+            for (int e = A->ptr[i]; e < A->ptr[i + 1]; ++e) s += A->val[e] * x[A->col[e]];
+            x[i] += L->dinv[i] * (b[i] - s);
+        }
+    }
+}
+
 static void amg_free(amg_t* h) {
     for (int l = 0; l < h->nlev; ++l) {
         level_t* L = &h->lev[l];
         if (l > 0) csr_free(&L->A);
         csr_free(&L->P); csr_free(&L->R);
         free(L->dinv); free(L->r); free(L->x); free(L->b); free(L->t1); free(L->t2);
+        free(L->cptr); free(L->crow);
     }
     free(h->chol);
     memset(h, 0, sizeof *h);
@@ -996,6 +1075,7 @@ static int dense_cholesky(int n, double* a) {
 static int amg_setup(amg_t* h, const csr_t* A0, const amg_prm* prm) {
     memset(h, 0, sizeof *h);
     h->cheb_degree = prm->cheb_degree;
+    h->smoother = g_smoother;
     float eps = (float)prm->eps_strong;
     h->lev[0].A = *A0;
     int l = 0;
@@ -1077,6 +1157,8 @@ static int amg_setup(amg_t* h, const csr_t* A0, const amg_prm* prm) {
         h->lev[l].A = Ac;
     }
     h->nlev = l + 1;
+    /* the finest level above 16384 rows (the GPU keeps Chebyshev elsewhere) */
+    if (h->smoother == 1 && h->nlev > 1 && h->lev[0].A.n > 16384 && color_level(&h->lev[0]) < 0) return -3;
     /* coarsest: dense Cholesky */
     csr_t* Ac = &h->lev[l].A;
     h->nc = Ac->n;
@@ -1118,7 +1200,8 @@ static void vcycle(amg_t* h, int l, const double* b, double* x) {
         return;
     }
     for (int i = 0; i < n; ++i) x[i] = 0.0;
-    cheb_smooth(L, b, x, h->cheb_degree);
+    if (L->ncolors > 0) gs_sweep(L, b, x, 0);
+    else cheb_smooth(L, b, x, h->cheb_degree);
     spmv(&L->A, x, L->r);
     for (int i = 0; i < n; ++i) L->r[i] = b[i] - L->r[i];
     level_t* C = &h->lev[l + 1];
@@ -1129,7 +1212,8 @@ static void vcycle(amg_t* h, int l, const double* b, double* x) {
         for (int k = L->P.ptr[i]; k < L->P.ptr[i + 1]; ++k) s += L->P.val[k] * C->x[L->P.col[k]];
         x[i] += s;
     }
-    cheb_smooth(L, b, x, h->cheb_degree);
+    if (L->ncolors > 0) gs_sweep(L, b, x, 1);
+    else cheb_smooth(L, b, x, h->cheb_degree);
 }
 
 static double dot(const double* a, const double* b, int n) {

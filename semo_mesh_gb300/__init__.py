@@ -44,7 +44,7 @@ class Params(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int),
                 ("eps_strong", C.c_double), ("coarse_enough", C.c_int), ("max_levels", C.c_int),
                 ("cheb_degree", C.c_int), ("reuse_hierarchy", C.c_int), ("mom_tol", C.c_double),
-                ("mom_max_iter", C.c_int), ("overlap_setup", C.c_int)]
+                ("mom_max_iter", C.c_int), ("overlap_setup", C.c_int), ("smoother", C.c_int)]
 
 
 class Physics(C.Structure):
@@ -166,7 +166,7 @@ class Context:
     def __init__(self, precision: str = "mixed", tol: float = 1e-8, max_iter: int = 500, device: int = 0,
                  eps_strong: float = 0.03, coarse_enough: int = 64, cheb_degree: int = 2, max_levels: int = 24,
                  mom_tol: float = 1e-9, mom_max_iter: int = 1000, reuse_hierarchy: bool = True,
-                 overlap_setup: bool = True):
+                 overlap_setup: bool = True, smoother: str = "chebyshev"):
         self.L = load_library()
         p = Params()
         self.L.semo_params_default(C.byref(p))
@@ -182,6 +182,9 @@ class Context:
         p.mom_tol = mom_tol
         p.mom_max_iter = mom_max_iter
         p.overlap_setup = 1 if overlap_setup else 0
+        if smoother not in ("chebyshev", "gauss_seidel"):
+            raise SemoError(1, f"unknown smoother '{smoother}' (chebyshev or gauss_seidel)")
+        p.smoother = 1 if smoother == "gauss_seidel" else 0
         h = C.c_void_p()
         st = self.L.semo_ctx_create(C.byref(h), C.byref(p))
         if st != SEMO_OK:

@@ -65,6 +65,7 @@ void semo_params_default(semo_params* p) {
     p->mom_tol = 1e-9;
     p->mom_max_iter = 1000;
     p->overlap_setup = 1;
+    p->smoother = 0;
 }
 
 void semo_physics_default(semo_physics* p) {
@@ -91,6 +92,7 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
     semo_status st = guarded(c, [&] {
         need(c->prm.tol > 0.0 && c->prm.max_iter > 0 && c->prm.coarse_enough > 0 && c->prm.max_levels > 0 && c->prm.max_levels <= 64 &&
                  c->prm.cheb_degree > 0 && c->prm.cheb_degree <= 16 && c->prm.mom_tol > 0.0 &&
+                 (c->prm.smoother == 0 || c->prm.smoother == 1) &&
                  c->prm.mom_max_iter > 0 &&
                  (c->prm.precision == SEMO_PREC_FP64 || c->prm.precision == SEMO_PREC_MIXED),
              SEMO_ERR_ARGUMENT, "invalid semo_params");

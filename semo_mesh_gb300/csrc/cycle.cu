@@ -626,6 +626,11 @@ struct LevelMats {
     Sell<V> A, P, R;
     Sell16<V> A16;
     bool a = false, p = false, r = false, a16 = false;
+    // multicolour Gauss-Seidel (semo_params.smoother == 1): the level's rows
+    // grouped by colour, colour k at crow[cptr[k] .. cptr[k + 1])
+    bool gs = false;
+    DBuf<int> crow;
+    std::vector<int> cptr;
 };
 template <class V>
 struct Cycle {
@@ -643,6 +648,131 @@ template <class V, class F>
 void with_A(const LevelMats<V>& M, const DCsr<V>& A, F&& f) {
     if (M.a16) f(M.A16.view());
     else with_op(M.A, M.a, A, f);
+}
+
+// ---------------------------------------------- multicolour Gauss-Seidel
+__device__ __forceinline__ uint32_t color_hash(uint32_t x) {
+    // integer avalanche mixer (public-domain "lowbias32" constants), as the MIS uses
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+// One synchronous Jones-Plassmann round on the pattern of A: an uncoloured row
+// whose (hash, index) key is larger than every uncoloured neighbour's takes
+// the smallest colour no neighbour coloured in an earlier round holds (the
+// rows coloured in one round are independent, so they never clash).  Reads
+// cold, writes cnew (a copy of cold); counts the rows still uncoloured and
+// flags a row that would need a colour beyond 127.
+__global__ void k_color_round(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                              const int* __restrict__ cold, int* __restrict__ cnew, int* __restrict__ left,
+                              int* __restrict__ overflow) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || cold[i] >= 0) return;
+    const unsigned long long ki = ((unsigned long long)color_hash((uint32_t)i) << 32) | (unsigned)i;
+    unsigned long long used0 = 0, used1 = 0;
+    bool top = true;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+        const int j = col[k];
+        if (j == i) continue;
+        const int cj = cold[j];
+        if (cj < 0) {
+            const unsigned long long kj = ((unsigned long long)color_hash((uint32_t)j) << 32) | (unsigned)j;
+            if (kj > ki) { top = false; break; }
+        } else if (cj < 64) {
+            used0 |= 1ull << cj;
+        } else if (cj < 128) {
+            used1 |= 1ull << (cj - 64);
+        }
+    }
+    if (!top) { atomicAdd(left, 1); return; }
+    int c = -1;
+    if (~used0) c = __ffsll((long long)~used0) - 1;
+    else if (~used1) c = 64 + __ffsll((long long)~used1) - 1;
+    if (c < 0) { atomicExch(overflow, 1); c = 127; }
+    cnew[i] = c;
+}
+
+// One colour of a Gauss-Seidel sweep: x_i += (b_i - (A x)_i) / a_ii for the
+// rows of that colour (no two of them are coupled, so the order is free)
+template <class M, class V>
+__global__ void __launch_bounds__(256) k_gs_color(M A, const int* __restrict__ rows, int nrows,
+                                                  const V* __restrict__ dinv, const V* __restrict__ b,
+                                                  V* __restrict__ x) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = g / M::kVS, lane = g % M::kVS;
+    const int row = (t < nrows) ? rows[t] : A.n;   // rows past the list: an empty dot
+    const V s = A.dot(row, lane, Vec<V, V>{x});
+    if (t < nrows && lane == 0) x[row] += dinv[row] * (b[row] - s);
+}
+// Under the Gauss-Seidel option only the finest level, when it has more than
+// this many rows, is swept by colours; the coarser levels keep Chebyshev.
+// A sweep is one launch per colour: the finest mesh graph needs a handful of
+// colours, a coarse level (denser rows) 20-40, each colour a launch of a few
+// thousand rows, and there the sweeps cost launch latency, not bandwidth
+// (measured at 128^3: 50 extra launches per V-cycle, twice the solve time).
+constexpr int kGsMinRows = 16384;
+
+template <class V>
+void color_level(semo_ctx* c, cudaStream_t s, const DCsr<V>& A, LevelMats<V>& M) {
+    const int n = A.n;
+    DBuf<int> c0, c1, cnt;
+    c0.alloc(n, s);
+    c1.alloc(n, s);
+    cnt.alloc(2, s);
+    SEMO_CUDA(cudaMemsetAsync(c0.p, 0xff, sizeof(int) * n, s));   // -1: uncoloured
+    int h[2] = {1, 0};
+    int* cold = c0.p;
+    int* cnew = c1.p;
+    // rounds in batches of 4 between host checks (a round over a fully
+    // coloured graph changes nothing)
+    for (int batch = 0; h[0] > 0; ++batch) {
+        if (batch > 1024) throw Error(SEMO_ERR_CUDA, "graph colouring did not finish");
+        for (int r = 0; r < 4; ++r) {
+            SEMO_CUDA(cudaMemcpyAsync(cnew, cold, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+            SEMO_CUDA(cudaMemsetAsync(cnt.p, 0, 2 * sizeof(int), s));
+            k_color_round<<<blocks(n, 256), 256, 0, s>>>(n, A.ptr, A.col, cold, cnew, cnt.p, cnt.p + 1);
+            SEMO_CHECK_LAUNCH();
+            std::swap(cold, cnew);
+        }
+        SEMO_CUDA(cudaMemcpyAsync(h, cnt.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+        if (h[1]) throw Error(SEMO_ERR_CUDA, "graph colouring needs more than 128 colours");
+    }
+    // rows grouped by colour (counting sort on the host; the order inside a colour is free)
+    std::vector<int> hc(n);
+    SEMO_CUDA(cudaMemcpyAsync(hc.data(), cold, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaStreamSynchronize(s));
+    int ncol = 0;
+    for (int v : hc) ncol = std::max(ncol, v + 1);
+    M.cptr.assign(ncol + 1, 0);
+    for (int v : hc) M.cptr[v + 1]++;
+    for (int k = 0; k < ncol; ++k) M.cptr[k + 1] += M.cptr[k];
+    std::vector<int> fill(M.cptr.begin(), M.cptr.end() - 1), rows(n);
+    for (int i = 0; i < n; ++i) rows[fill[hc[i]]++] = i;
+    M.crow.upload(rows.data(), n, s);
+    SEMO_CUDA(cudaStreamSynchronize(s));   // the host vector above is freed on return
+    M.gs = true;
+}
+
+// one Gauss-Seidel sweep of level L (forward: colours ascending)
+template <class V>
+void gs_sweep(cudaStream_t s, AmgLevel<V>& L, const LevelMats<V>& M, bool backward, bool zero_start) {
+    const int n = L.A.n;
+    const int ncol = (int)M.cptr.size() - 1;
+    if (zero_start) {
+        k_zero<V><<<blocks(n, 256), 256, 0, s>>>(n, L.x.p);
+        SEMO_CHECK_LAUNCH();
+    }
+    for (int q = 0; q < ncol; ++q) {
+        const int k = backward ? ncol - 1 - q : q;
+        const int nr = M.cptr[k + 1] - M.cptr[k];
+        if (nr == 0) continue;
+        with_csr(L.A, [&](auto A) {
+            using MV = decltype(A);
+            k_gs_color<<<blocks((int64_t)nr * MV::kVS, 256), 256, 0, s>>>(A, M.crow.p + M.cptr[k], nr, L.dinv.p,
+                                                                          L.b.p, L.x.p);
+        });
+        SEMO_CHECK_LAUNCH();
+    }
 }
 
 template <class V>
@@ -691,7 +821,9 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     const LevelMats<V>& M = cy.lev[l];
     const int degree = c->prm.cheb_degree;
     const ChebCoef cc = cheb2(L.lam_max);
-    if (degree == 2) {
+    if (M.gs) {
+        gs_sweep(s, L, M, false, true);   // forward sweep from x = 0
+    } else if (degree == 2) {
         with_A(M, L.A, [&](auto A) {
             k_pre2<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
         });
@@ -707,7 +839,9 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     vcycle_from(c, h, cy, l + 1);
     with_op(M.P, M.p, L.P, [&](auto P) { k_prolong_add<<<grid_for(P), 256, 0, s>>>(P, C.x.p, L.x.p); });
     SEMO_CHECK_LAUNCH();
-    if (degree == 2) {
+    if (M.gs) {
+        gs_sweep(s, L, M, true, false);   // backward sweep: the cycle stays symmetric
+    } else if (degree == 2) {
         with_A(M, L.A, [&](auto A) {
             k_post0<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
         });
@@ -749,7 +883,7 @@ void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, do
         SEMO_CHECK_LAUNCH();
         k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L.x.p, r, q, R.part);
         SEMO_CHECK_LAUNCH();
-    } else if (degree == 2) {
+    } else if (degree == 2 && !cy.lev[0].gs) {
         const ChebCoef cc = cheb2(L.lam_max);
         vcycle_from(c, h, cy, 0);   // everything but the last smoothing step of the finest level
         // z lands in L.x; z.r and z.q folded in
@@ -942,6 +1076,8 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
         if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
         if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
         if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R);
+        M.gs = false;
+        if (c->prm.smoother == 1 && l == 0 && L.A.n > kGsMinRows) color_level(c, s, L.A, M);
     }
 }
 
@@ -1648,7 +1784,7 @@ void cpr_vcycle(semo_ctx* c, const V* b, V* x) {
     const int n = L.A.n;
     SEMO_CUDA(cudaMemcpyAsync(L.b.p, b, sizeof(V) * n, cudaMemcpyDeviceToDevice, s));
     vcycle_from(c, h, cy, 0);
-    if (h.lev.size() > 1 && c->prm.cheb_degree == 2) {
+    if (h.lev.size() > 1 && c->prm.cheb_degree == 2 && !cy.lev[0].gs) {
         // the last step vcycle_from leaves to the fused CG kernels on the finest level
         const ChebCoef cc = cheb2(L.lam_max);
         with_A(cy.lev[0], L.A, [&](auto A) {
