@@ -665,9 +665,11 @@ def run_gpu_arm(args, rank, world, local) -> None:
     traffic = None
     fp64_pipe = None
     t = None
+    t_all = None
     if os.path.exists(TRAFFIC):
         with open(TRAFFIC) as f:
             tr = json.load(f)
+        t_all = tr
         t = tr.get(kname)
         if t and "dram_bytes_per_cell" in t:
             traffic = t["dram_bytes_per_cell"] * nc
@@ -706,6 +708,12 @@ def run_gpu_arm(args, rank, world, local) -> None:
     roofline["spmv_outer_fp64"] = {"achieved": round(b64 / (spmv_ms[1] * 1e-3) / 1e9, 1),
                                    "frac": round(b64 / (spmv_ms[1] * 1e-3) / 1e9 / peak, 4),
                                    "ms_per_launch": round(spmv_ms[1], 4), "algorithmic_bytes": b64}
+    # DRAM traffic of the two SpMVs (ncu at 128^3), scaled by the nonzeros
+    for key, tk in (("spmv_level0", "k_mv_sell16_f32"), ("spmv_outer_fp64", "k_mv_sell16_f64")):
+        if t_all and tk in t_all:
+            tb = t_all[tk]["dram_bytes_per_launch"] * L0["nnz_A"] / t_all[tk]["nnz"]
+            roofline[key]["traffic"] = round(tb)
+            roofline[key]["dram_frac"] = round(tb / (roofline[key]["ms_per_launch"] * 1e-3) / 1e9 / peak, 4)
     roofline["pcg_iteration"] = {"achieved": round(pcg_b / (ms_it * 1e-3) / 1e9, 1),
                                  "frac": round(pcg_b / (ms_it * 1e-3) / 1e9 / peak, 4), "ms": round(ms_it, 4),
                                  "algorithmic_bytes": round(pcg_b), "levels": len(levels),
