@@ -53,6 +53,13 @@ typedef enum {
     SEMO_BC_SLIP = 3             /* velocity only */
 } semo_bc;
 
+typedef enum {
+    SEMO_EQ_PRESSURE = 0,        /* calcPressureEq's system */
+    SEMO_EQ_MOMENTUM = 1,        /* calcMomentumEqs' matrix with its three right-hand sides */
+    SEMO_EQ_VOF = 2,             /* calcVolfracEq's system */
+    SEMO_EQ_COUPLED = 3          /* calcCompCoupledEq's 5x5 block system */
+} semo_eq;
+
 typedef struct semo_ctx semo_ctx;
 
 typedef struct {
@@ -275,6 +282,18 @@ semo_status semo_assemble_pressure(semo_ctx* ctx);
    b (n_cells).  In-row order is SEMO's (diagonal first, then faces in face
    order, src/solvers/solveAMGCL.cpp:206-251).  nnz = n_cells + 2*n_internal. */
 semo_status semo_get_system_rcm(semo_ctx* ctx, int32_t* ptr, int32_t* col, double* val, double* b);
+
+/* Any assembled system in RCM order on the mesh's CSR pattern (the pattern
+   semo_get_system_rcm gives, nnz = n_cells + 2*n_internal entries, diagonal
+   first in each row, then faces in face order): eq is a semo_eq; val holds
+   nnz values (25 per entry, row-major 5x5 blocks, for SEMO_EQ_COUPLED) with
+   0.0 where SEMO leaves an entry out of the momentum or volume-fraction
+   matrix; b holds 1 plane of n_cells (pressure, volume fraction), 3
+   (momentum x, y, z) or 5 (coupled p, u, v, w, T).  Any output may be NULL.
+   Replaces: the (A_rows, A_cols, A_vals, B) each calc*Eq hands solveAMGCL
+   (src/solvers/eqPressure.cpp:677, eqMomentum.cpp:1017, eqVolfrac.cpp:766),
+   reordered by lib_RCM. */
+semo_status semo_get_system_rcm_eq(semo_ctx* ctx, int eq, int32_t* ptr, int32_t* col, double* val, double* b);
 
 /* Intermediates of the last assembly, in the caller's cell order, for
    checking: name is one of "grad_P","grad_U","grad_V","grad_W","grad_VF"

@@ -101,6 +101,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.semo_pressure_pass.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_assemble_pressure.argtypes = [vp]
     L.semo_get_system_rcm.argtypes = [vp, i32p, i32p, f64p, f64p]
+    L.semo_get_system_rcm_eq.argtypes = [vp, C.c_int, i32p, i32p, f64p, f64p]
     L.semo_get_array.argtypes = [vp, C.c_char_p, f64p, C.c_int64]
     L.semo_solve_pressure.argtypes = [vp, f64p, C.POINTER(SolveInfo)]
     L.semo_solve_coo.argtypes = [vp, C.c_int, C.c_int64, i32p, i32p, f64p, f64p, f64p, C.POINTER(SolveInfo)]
@@ -528,6 +529,26 @@ class Context:
                                                val.ctypes.data_as(C.POINTER(C.c_double)),
                                                b.ctypes.data_as(C.POINTER(C.c_double))))
         return {"ptr": ptr, "col": col, "val": val, "b": b}
+
+    EQUATIONS = {"pressure": 0, "momentum": 1, "volume_fraction": 2, "coupled": 3}
+
+    def system_rcm_eq(self, equation: str) -> dict:
+        """An assembled system in RCM order on the mesh's CSR pattern (dropped
+        momentum / volume-fraction entries as 0.0; 5x5 blocks for "coupled")."""
+        eq = self.EQUATIONS[equation]
+        n = self.n_cells
+        nnz = n + 2 * self.mesh.n_internal
+        per, planes = (25, 5) if eq == 3 else (1, 3 if eq == 1 else 1)
+        ptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz, dtype=np.int32)
+        val = np.empty(per * nnz)
+        b = np.empty(planes * n)
+        self._check(self.L.semo_get_system_rcm_eq(self.h, eq, ptr.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  col.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  val.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  b.ctypes.data_as(C.POINTER(C.c_double))))
+        return {"ptr": ptr, "col": col, "val": val.reshape(-1, 5, 5) if eq == 3 else val,
+                "b": b.reshape(planes, n) if planes > 1 else b}
 
     def solve(self) -> SolveResult:
         x = np.empty(self.n_cells)

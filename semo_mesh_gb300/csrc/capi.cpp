@@ -589,6 +589,39 @@ semo_status semo_get_system_rcm(semo_ctx* c, int32_t* ptr, int32_t* col, double*
     });
 }
 
+semo_status semo_get_system_rcm_eq(semo_ctx* c, int eq, int32_t* ptr, int32_t* col, double* val, double* b) {
+    return guarded(c, [&] {
+        need(eq >= SEMO_EQ_PRESSURE && eq <= SEMO_EQ_COUPLED, SEMO_ERR_ARGUMENT, "unknown equation");
+        const double* v = nullptr;
+        const double* rhs = nullptr;
+        size_t vper = 1, planes = 1;
+        switch (eq) {
+            case SEMO_EQ_PRESSURE:
+                need(c->assembled, SEMO_ERR_STATE, "pressure system not assembled");
+                v = c->A_val.p; rhs = c->b.p;
+                break;
+            case SEMO_EQ_MOMENTUM:
+                need(c->mom_assembled, SEMO_ERR_STATE, "momentum system not assembled");
+                v = c->Am_val.p; rhs = c->bm.p; planes = 3;
+                break;
+            case SEMO_EQ_VOF:
+                need(c->vof_assembled, SEMO_ERR_STATE, "volume-fraction system not assembled");
+                v = c->Av_val.p; rhs = c->bvf.p;
+                break;
+            default:
+                need(c->cpl_assembled, SEMO_ERR_STATE, "coupled system not assembled");
+                v = c->cpl_val.p; rhs = c->cpl_b.p; vper = 25; planes = 5;
+                break;
+        }
+        cudaStream_t s = c->stream;
+        if (ptr) SEMO_CUDA(cudaMemcpyAsync(ptr, c->A_ptr.p, sizeof(int) * (c->nc + 1), cudaMemcpyDeviceToHost, s));
+        if (col) SEMO_CUDA(cudaMemcpyAsync(col, c->A_col.p, sizeof(int) * c->nnz, cudaMemcpyDeviceToHost, s));
+        if (val) SEMO_CUDA(cudaMemcpyAsync(val, v, sizeof(double) * vper * c->nnz, cudaMemcpyDeviceToHost, s));
+        if (b) SEMO_CUDA(cudaMemcpyAsync(b, rhs, sizeof(double) * planes * c->nc, cudaMemcpyDeviceToHost, s));
+        SEMO_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
 semo_status semo_get_array(semo_ctx* c, const char* name, double* out, int64_t count) {
     return guarded(c, [&] {
         need(c->mesh_ready, SEMO_ERR_STATE, "no mesh uploaded");
