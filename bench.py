@@ -61,7 +61,13 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region.
+
+    Started before the warm-up (its start-up initialises NVML, which must not
+    fall inside the timed loop); `wait_first()` blocks until it has sampled
+    once, `mark(t0, t1)` records the timed window, and `summary()` keeps the
+    samples taken inside it (all of them if the window was shorter than the
+    sampling period)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -71,6 +77,7 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
+        self.window = None
 
     def __enter__(self):
         try:
@@ -84,7 +91,15 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append([time.monotonic()] + [x.strip() for x in line.split(",")])
+
+    def wait_first(self, timeout: float = 10.0) -> None:
+        t_end = time.monotonic() + timeout
+        while self.proc and not self.rows and time.monotonic() < t_end:
+            time.sleep(0.02)
+
+    def mark(self, t0: float, t1: float) -> None:
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -100,13 +115,18 @@ class ClockSampler:
                 return float(x)
             except ValueError:
                 return None
-        sm = [v for v in (num(r[1]) for r in self.rows if len(r) > 2) if v is not None]
-        mx = [v for v in (num(r[2]) for r in self.rows if len(r) > 2) if v is not None]
+        rows = self.rows
+        if self.window:
+            inside = [r for r in rows if self.window[0] <= r[0] <= self.window[1]]
+            rows = inside if inside else rows
+        rows = [r[1:] for r in rows]
+        sm = [v for v in (num(r[1]) for r in rows if len(r) > 2) if v is not None]
+        mx = [v for v in (num(r[2]) for r in rows if len(r) > 2) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({nm for r in self.rows for k, nm in enumerate(names)
+        reasons = sorted({nm for r in rows for k, nm in enumerate(names)
                           if len(r) > 5 + k and r[5 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
 
 
 def hbm_peak() -> tuple:
@@ -477,14 +497,18 @@ def run_gpu_arm(args, rank, world, local) -> None:
     strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
 
     # ---- mixed precision, inputs resident in HBM (the headline value) ------
-    for _ in range(args.warmup):
-        ctx.outer_iteration()
-    l0 = ctx.kernel_launches()
-    barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        clk.wait_first()
+        for _ in range(args.warmup):
+            ctx.outer_iteration()
+        l0 = ctx.kernel_launches()
+        barrier()
+        torch.cuda.synchronize()
+        tw0 = time.monotonic()
         ms_mixed, infos = timed(ctx, strm, args.steps, outer)
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        clk.mark(tw0, time.monotonic())
+        time.sleep(0.25)   # one more sample after the window
     barrier()
     launches = ctx.kernel_launches() - l0
     # per-stage device times from a second, untimed run of the same steps
