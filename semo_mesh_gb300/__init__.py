@@ -566,7 +566,7 @@ class Context:
               "gauss_green", "update", "vcycle", "setup_aggregate", "setup_prolong", "setup_galerkin",
               "setup_level", "setup_coarse", "mface", "mcell", "msolve", "mupdate", "mstacs", "vface",
               "vsolve", "vupdate", "stencil_uvw", "mbface", "cgrad", "cface", "ccell", "csolve", "cupdate",
-              "surface_tension")
+              "surface_tension", "setup_cycle")
 
     def set_profiling(self, on: bool) -> None:
         self.L.semo_set_profiling(self.h, 1 if on else 0)

@@ -253,10 +253,10 @@ void vjp_fields(semo_ctx* c, const double* lam, double* out) {
         SEMO_CUDA(cudaMemsetAsync(c->flag.p + 13, 0, sizeof(int), s));
         k_stencil_tpos<<<nblocks(nc, 128), 128, 0, s>>>(nc, c->st_ptr, c->st_idx, c->st_tpos, c->flag.p + 13);
         SEMO_CHECK_LAUNCH();
-        int bad = 0;
-        SEMO_CUDA(cudaMemcpyAsync(&bad, c->flag.p + 13, sizeof(int), cudaMemcpyDeviceToHost, s));
+        int* const bad = c->hpin_scan + 2;
+        SEMO_CUDA(cudaMemcpyAsync(bad, c->flag.p + 13, sizeof(int), cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
-        if (bad) throw Error(SEMO_ERR_MESH, "vertex stencil is not symmetric");
+        if (*bad) throw Error(SEMO_ERR_MESH, "vertex stencil is not symmetric");
         c->st_tpos_gen = c->mesh_gen;
     }
     // checkpointed recomputation: face values, gradients, limits and their

@@ -94,17 +94,17 @@ void scan_async(cudaStream_t s, int* d, int n, int* total_dev) {
     }
 }
 
-// exclusive scan of d[0..n) in place; returns the total (one host sync).
-// extra D2H copies enqueued before the call land by the time it returns.
-int scan_exclusive(cudaStream_t s, int* d, int n) {
+// exclusive scan of d[0..n) in place; returns the total, read back through
+// the pinned int *hpin (one host sync).  Extra D2H copies enqueued before the
+// call land by the time it returns.
+int scan_exclusive(cudaStream_t s, int* d, int n, int* hpin) {
     if (n <= 0) return 0;
     DBuf<int> tot;
     tot.alloc(1, s);
     scan_async(s, d, n, tot.p);
-    int total = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hpin, tot.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
-    return total;
+    return *hpin;
 }
 
 template <class A, class B>
@@ -889,7 +889,7 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     SEMO_CHECK_LAUNCH();
     int* const hp = c->hpin_int;   // pinned: these copies land by the scan's sync
     SEMO_CUDA(cudaMemcpyAsync(hp + 2, flags.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-    const int64_t total = scan_exclusive(s, up.p, n + 1);   // syncs
+    const int64_t total = scan_exclusive(s, up.p, n + 1, hp + 4);   // syncs
     const int maxprod = hp[2];
     DBuf<int> tcol;
     DBuf<V> tval;
@@ -926,7 +926,7 @@ void spgemm(cudaStream_t s, semo_ctx* c, const DCsr<V>& A, const DCsr<V>& B, DCs
     SEMO_CUDA(cudaMemcpyAsync(C.ptr.p, cnt.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
     SEMO_CUDA(cudaMemsetAsync(C.ptr.p + n, 0, sizeof(int), s));
     SEMO_CUDA(cudaMemcpyAsync(hp + 3, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    const int nnz = scan_exclusive(s, C.ptr.p, n + 1);   // syncs
+    const int nnz = scan_exclusive(s, C.ptr.p, n + 1, hp + 4);   // syncs
     if (hp[3]) throw Error(SEMO_ERR_CUDA, "SpGEMM row has more than 1536 distinct columns");
     C.nnz = nnz;
     C.col.alloc(std::max(nnz, 1), s);
@@ -1004,8 +1004,6 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     cudaStream_t s = setup_stream(c);
     c->sflag.alloc(16, s);
     SEMO_CUDA(cudaMemsetAsync(c->sflag.p, 0, 16 * sizeof(int), s));
-    if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
-    if (!c->hpin_setup) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_setup, 64 * sizeof(double)));
     DBuf<double> lam_dev;   // per level Gershgorin bounds
     lam_dev.alloc(64, s);
     h.clear();
@@ -1091,7 +1089,7 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
             if (hu) throw Error(SEMO_ERR_CUDA, "MIS(2) aggregation did not terminate");
             k_root_flags<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2);
             SEMO_CHECK_LAUNCH();
-            nagg = scan_exclusive(s, agg2.p, nl);
+            nagg = scan_exclusive(s, agg2.p, nl, c->hpin_int + 4);
             if (nagg > 0 && nagg < nl) {
                 k_root_ids<<<blocks(nl, 256), 256, 0, s>>>(nl, state, agg2, agg);
                 SEMO_CHECK_LAUNCH();
@@ -1131,7 +1129,7 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
             });
         }
         SEMO_CHECK_LAUNCH();
-        L.P.nnz = scan_exclusive(s, L.P.ptr.p, nl + 1);
+        L.P.nnz = scan_exclusive(s, L.P.ptr.p, nl + 1, c->hpin_int + 4);
         L.P.col.alloc(std::max<int64_t>(L.P.nnz, 1), s);
         L.P.val.alloc(std::max<int64_t>(L.P.nnz, 1), s);
         // filling: the lane version rescans the row per output entry, which
@@ -1172,10 +1170,10 @@ void amg_setup(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const dou
     SEMO_CHECK_LAUNCH();
     k_gauss_jordan<<<1, 1024, 0, s>>>(m, dense, h.cinv, c->sflag);
     SEMO_CHECK_LAUNCH();
-    int hf[5] = {0, 0, 0, 0, 0};
+    int* const hf = c->hpin_int + 8;   // sflag[0..5)
     const int nlev = (int)h.lev.size();
     SEMO_CUDA(cudaMemcpyAsync(c->hpin_setup, lam_dev.p, sizeof(double) * nlev, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaMemcpyAsync(hf, c->sflag.p, sizeof(hf), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(hf, c->sflag.p, 5 * sizeof(int), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
     for (int l = 0; l < nlev; ++l) h.lev[l].lam_max = c->hpin_setup[l];
     if (hf[2]) throw Error(SEMO_ERR_ARGUMENT, "matrix has a zero diagonal entry");
@@ -1194,6 +1192,6 @@ void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, con
 template void build_hierarchy<float>(semo_ctx*, Amg<float>&, const int*, const int*, const double*, int, int64_t);
 template void build_hierarchy<double>(semo_ctx*, Amg<double>&, const int*, const int*, const double*, int, int64_t);
 
-int device_scan(cudaStream_t s, int* d, int n) { return scan_exclusive(s, d, n); }
+int device_scan(cudaStream_t s, int* d, int n, int* hpin) { return scan_exclusive(s, d, n, hpin); }
 
 }  // namespace semo

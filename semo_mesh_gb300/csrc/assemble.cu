@@ -477,10 +477,10 @@ bool fields_from_caller_order(semo_ctx* c, const double* src, double* const* dst
     SEMO_CUDA(cudaMemsetAsync(c->flag.p + 8, 0, sizeof(int), c->stream));
     k_from_caller<<<blocks(c->nc, 256), 256, 0, c->stream>>>(c->nc, planes, c->dperm, src, d, c->flag.p + 8);
     SEMO_CHECK_LAUNCH();
-    int bad = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&bad, c->flag.p + 8, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int* const bad = c->hpin_scan + 1;
+    SEMO_CUDA(cudaMemcpyAsync(bad, c->flag.p + 8, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SEMO_CUDA(cudaStreamSynchronize(c->stream));
-    return bad == 0;
+    return *bad == 0;
 }
 
 void cellwise_product(semo_ctx* c, const double* a, const double* b, double* out) {
@@ -639,8 +639,8 @@ double pressure_update(semo_ctx* c) {
     SEMO_CHECK_LAUNCH();
     k_finish2<<<1, 256, 0, s>>>(c->red, c->red.p + 2 * kRedBlocks);
     SEMO_CHECK_LAUNCH();
-    double h[2];
-    SEMO_CUDA(cudaMemcpyAsync(h, c->red.p + 2 * kRedBlocks, sizeof(h), cudaMemcpyDeviceToHost, s));
+    double* const h = c->hpin;
+    SEMO_CUDA(cudaMemcpyAsync(h, c->red.p + 2 * kRedBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
     return std::sqrt(h[0]) / std::sqrt(h[1]);
 }

@@ -120,6 +120,10 @@ semo_status semo_ctx_create(semo_ctx** out, const semo_params* prm) {
         SEMO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no_deps));
         for (auto& e : c->ev) SEMO_CUDA(cudaEventCreate(&e));
         for (auto& e : c->setup_ev) SEMO_CUDA(cudaEventCreate(&e));
+        SEMO_CUDA(cudaMallocHost((void**)&c->hpin, semo::kHostScalars * sizeof(double)));
+        SEMO_CUDA(cudaMallocHost((void**)&c->hpin_setup, semo::kHostScalars * sizeof(double)));
+        SEMO_CUDA(cudaMallocHost((void**)&c->hpin_scan, semo::kHostInts * sizeof(int)));
+        SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, semo::kHostInts * sizeof(int)));
         c->flag.alloc(16, c->stream);
         c->flag.zero();
     });
@@ -149,6 +153,7 @@ semo_status semo_ctx_destroy(semo_ctx* c) {
     if (c->hpin) cudaFreeHost(c->hpin);
     if (c->hpin_int) cudaFreeHost(c->hpin_int);
     if (c->hpin_setup) cudaFreeHost(c->hpin_setup);
+    if (c->hpin_scan) cudaFreeHost(c->hpin_scan);
     cudaStream_t s = c->stream, aux = c->aux_stream;
     delete c;  // DBuf destructors enqueue frees on the (still valid) streams
     if (aux) { cudaStreamSynchronize(aux); cudaStreamDestroy(aux); }
@@ -850,8 +855,6 @@ struct SideSetup {
         for (auto& e : c->ov_ev)
             if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         // host resources the setup creates on first use, made here on this thread
-        if (!c->hpin_int) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_int, 8 * sizeof(int)));
-        if (!c->hpin_setup) SEMO_CUDA(cudaMallocHost((void**)&c->hpin_setup, 64 * sizeof(double)));
         for (auto& e : c->sync_ev)
             if (!e) SEMO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         SEMO_CUDA(cudaEventRecord(c->ov_ev[0], c->stream));   // face values (densities) are on the stream

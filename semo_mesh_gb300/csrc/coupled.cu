@@ -979,7 +979,6 @@ int bicgstab_inner(semo_ctx* c, CplSolver& S, const M* val, const M* minv, P* cp
     double *y = vec + 6 * n5, *z = vec + 7 * n5;
     double* part = S.part;
     double* sc = S.sc;
-    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* h = c->hpin;
     // y = M^-1 in
     auto precond = [&](const double* in) {
@@ -1154,7 +1153,7 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
         SEMO_CHECK_LAUNCH();
         SEMO_CUDA(cudaMemcpyAsync(S.off32.p, S.width.p, sizeof(int) * S.nch, cudaMemcpyDeviceToDevice, s));
         SEMO_CUDA(cudaMemsetAsync(S.off32.p + S.nch, 0, sizeof(int), s));
-        S.rows32 = device_scan(s, S.off32.p, S.nch + 1);
+        S.rows32 = device_scan(s, S.off32.p, S.nch + 1, c->hpin_scan);
         S.col.alloc(32 * (size_t)S.rows32, s);
         S.gen = c->mesh_gen;
         S.val32.release(); S.val64.release();
@@ -1164,10 +1163,10 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     if (mixed) prepare_blocks<float, float>(c, S, S.val32, S.minv32, S.cp32, kScaleMixed);
     else prepare_blocks<double, double>(c, S, S.val64, S.minv64, S.cp64, false);
     SEMO_CUDA(cudaEventRecord(e1, s));
-    int singular = 0;
-    SEMO_CUDA(cudaMemcpyAsync(&singular, c->flag.p + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int* const singular = c->hpin_scan + 3;
+    SEMO_CUDA(cudaMemcpyAsync(singular, c->flag.p + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
-    if (singular) throw Error(SEMO_ERR_BREAKDOWN, "singular 5x5 diagonal block");
+    if (*singular) throw Error(SEMO_ERR_BREAKDOWN, "singular 5x5 diagonal block");
     // defect correction: x = 0; r = b - A x; inner solve of A z = r; x += z
     c->cpl_x.alloc(n5, s);
     S.r64.alloc(n5, s);
@@ -1175,7 +1174,6 @@ semo_status coupled_solve(semo_ctx* c, semo_solve_info* info) {
     c->cpl_x.zero();
     const double tol = c->prm.tol;
     const int maxit = c->prm.max_iter > 0 ? c->prm.max_iter : 1000;
-    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* h = c->hpin;
     auto residual = [&]() {
         k_bsr_res<<<kRedBlocks, kT, 0, s>>>(nc, c->A_ptr, c->A_col, c->cpl_val, c->cpl_x, c->cpl_b, S.r64, S.part);

@@ -158,6 +158,17 @@ struct Sell16View {
                 for (int q = 0; q < 8; ++q)
                     if (q < w) s += vj[q] * xj[q];
             } else if (mode == 0) {
+                if (sizeof(V) == 4)   // longer FP32 rows (coarse levels): four entries in flight
+                    for (; j + 3 < w; j += 4, k += 128) {
+                        const int c0 = row + (short)dcol[k], c1 = row + (short)dcol[k + 32];
+                        const int c2 = row + (short)dcol[k + 64], c3 = row + (short)dcol[k + 96];
+                        const V v0 = val[k], v1 = val[k + 32], v2 = val[k + 64], v3 = val[k + 96];
+                        const V x0 = x(c0), x1 = x(c1), x2 = x(c2), x3 = x(c3);
+                        s += v0 * x0;
+                        s += v1 * x1;
+                        s += v2 * x2;
+                        s += v3 * x3;
+                    }
                 for (; j + 1 < w; j += 2, k += 64) {   // two independent loads in flight
                     const int c0 = row + (short)dcol[k], c1 = row + (short)dcol[k + 32];
                     const V v0 = val[k], v1 = val[k + 32];
@@ -495,9 +506,10 @@ void with_csr(const DCsr<V>& A, F&& f) {
 template <class M>
 int grid_for(const M& A) { return blocks((int64_t)A.n * M::kVS, 256); }
 
-// SELL-32 copy of a CSR matrix's structure and values (value type W)
+// SELL-32 copy of a CSR matrix's structure and values (value type W); hpin:
+// a pinned int of the calling thread for the slice scan's total
 template <class V, class W>
-void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell<W>& S) {
+void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell<W>& S, int* hpin) {
     S.n = n;
     S.nslices = (n + 31) / 32;
     S.sptr.alloc(S.nslices + 1, s);
@@ -505,7 +517,7 @@ void build_sell(cudaStream_t s, const int* ptr, const int* col, const V* val, in
     const int rows_pad = S.nslices * 32;
     k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
     SEMO_CHECK_LAUNCH();
-    const int total = device_scan(s, S.sptr.p, S.nslices + 1);
+    const int total = device_scan(s, S.sptr.p, S.nslices + 1, hpin);
     S.col.alloc(std::max(total, 1), s);
     S.val.alloc(std::max(total, 1), s);
     k_sell_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.col.p, S.val.p);
@@ -575,7 +587,7 @@ struct Sell16 {
 // SELL-32 with 16-bit columns of a square CSR operator (always built: slices
 // that fit no 16-bit encoding keep 32-bit columns)
 template <class V, class W>
-bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int*) {
+bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int* hpin) {
     S.n = n;
     S.nslices = (n + 31) / 32;
     S.sptr.alloc(S.nslices + 1, s);
@@ -586,11 +598,11 @@ bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, 
     const int rows_pad = S.nslices * 32;
     k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
     SEMO_CHECK_LAUNCH();
-    const int total = device_scan(s, S.sptr.p, S.nslices + 1);
+    const int total = device_scan(s, S.sptr.p, S.nslices + 1, hpin);
     S.gbase.alloc(std::max(total / 32, 1), s);
     k_sell16_groups<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, S.sptr.p, S.smode.p, S.gbase.p, S.wptr.p);
     SEMO_CHECK_LAUNCH();
-    const int wide = device_scan(s, S.wptr.p, S.nslices + 1);
+    const int wide = device_scan(s, S.wptr.p, S.nslices + 1, hpin);
     S.dcol.alloc(std::max(total, 1), s);
     S.wcol.alloc(std::max(wide, 1), s);
     S.val.alloc(std::max(total, 1), s);
@@ -958,7 +970,6 @@ void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, const int* 
     cudaStream_t s = c->stream;
     Red R = red_area(c);
     c->kr.alloc(n, s); c->kp.alloc(n, s); c->kq.alloc(n, s);
-    if (!c->hpin) SEMO_CUDA(cudaMallocHost((void**)&c->hpin, 16 * sizeof(double)));
     double* h2 = c->hpin;
     double* r = c->kr.p;
     const CsrView<double, 8> A8{ptr, col, val, n};
@@ -1088,11 +1099,12 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
         M.a = sell_pays(L.A);
         M.p = sell_pays(L.P);
         M.r = sell_pays(L.R);
-        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, c->sflag.p + 11);
+        int* const hp = c->hpin_int + 4;
+        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, hp);
         if (M.a16) M.a = false;
-        if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A);
-        if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P);
-        if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R);
+        if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A, hp);
+        if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P, hp);
+        if (M.r) build_sell<V, V>(s, L.R.ptr, L.R.col, L.R.val, L.R.n, M.R, hp);
         M.gs = false;
         if (c->prm.smoother == 1 && l == 0 && L.A.n > kGsMinRows) color_level(c, s, L.A, M);
     }
@@ -1385,23 +1397,26 @@ void pressure_setup(semo_ctx* c, const int* ptr, const int* col, const double* v
             st.src_nnz == nnz) {
             k_differs<<<kRedBlocks, kRedThreads, 0, s>>>(nnz, val, st.src_val, c->sflag.p + 10);
             SEMO_CHECK_LAUNCH();
-            int differs = 1;
-            SEMO_CUDA(cudaMemcpyAsync(&differs, c->sflag.p + 10, sizeof(int), cudaMemcpyDeviceToHost, s));
+            int* const differs = c->hpin_int + 13;
+            SEMO_CUDA(cudaMemcpyAsync(differs, c->sflag.p + 10, sizeof(int), cudaMemcpyDeviceToHost, s));
             SEMO_CUDA(cudaStreamSynchronize(s));
-            reuse = differs == 0;
+            reuse = *differs == 0;
         }
         if (!reuse) {
             if (c->prm.precision == SEMO_PREC_MIXED) {
                 c->amg64.clear();
                 build_hierarchy<float>(c, c->amg32, ptr, col, val, n, nnz);
-                prepare_cycle(c, c->amg32, st.cy32);
             } else {
                 c->amg32.clear();
                 build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
-                prepare_cycle(c, c->amg64, st.cy64);
             }
-            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->sflag.p + 11);
-            if (!st.outer.use16) build_sell<double, double>(s, ptr, col, val, n, st.outer.s32);
+            StageScope scy(c, ST_SETUP_CYCLE);
+            if (c->prm.precision == SEMO_PREC_MIXED)
+                prepare_cycle(c, c->amg32, st.cy32);
+            else
+                prepare_cycle(c, c->amg64, st.cy64);
+            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->hpin_int + 4);
+            if (!st.outer.use16) build_sell<double, double>(s, ptr, col, val, n, st.outer.s32, c->hpin_int + 4);
             st.src_prec = -1;
             if (may_reuse && c->prm.reuse_hierarchy) {
                 st.src_val.alloc(nnz, s);
@@ -1494,7 +1509,7 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
     const double tol2 = 0.25 * c->prm.mom_tol * c->prm.mom_tol;
     SEMO_CUDA(cudaEventRecord(c->ev[0], s));
     if (pat.gen < 0 || st.gen != pat.gen) {
-        build_sell<double, double>(s, pat.ptr, pat.col, val, n, st.A);
+        build_sell<double, double>(s, pat.ptr, pat.col, val, n, st.A, c->hpin_scan);
         st.gen = pat.gen;
     } else {   // same pattern (the mesh's): refill the values into the kept layout
         k_sell_fill<double, double><<<blocks((int64_t)st.A.nslices * 32, 256), 256, 0, s>>>(
@@ -1509,7 +1524,8 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
     SEMO_CHECK_LAUNCH();
     k_bi_fin0<NR><<<1, 256, 0, s>>>(st.part, st.scal, tol2);
     SEMO_CHECK_LAUNCH();
-    double hs[3 * kMomScal];
+    // pinned: hs = hpin[0, 48), the loop's scalars hpin[48, 112), residuals hpin[112, 115)
+    double* const hs = c->hpin;
     SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(double) * NR * kMomScal, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
     int iters[NR] = {};
@@ -1565,8 +1581,8 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
         __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
         SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
         SEMO_CUDA(cudaGraphLaunch(gg.e, s));
-        double hit[4 * kMomScal];
-        SEMO_CUDA(cudaMemcpyAsync(hit, st.scal.p, sizeof(hit), cudaMemcpyDeviceToHost, s));
+        double* const hit = c->hpin + 3 * kMomScal;
+        SEMO_CUDA(cudaMemcpyAsync(hit, st.scal.p, sizeof(double) * 4 * kMomScal, cudaMemcpyDeviceToHost, s));
         SEMO_CUDA(cudaStreamSynchronize(s));
         const int it = (int)hit[3 * kMomScal];
         __atomic_add_fetch(&g_kernel_launches, 9LL * it, __ATOMIC_RELAXED);
@@ -1582,7 +1598,7 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
     SEMO_CHECK_LAUNCH();
     k_bi_fin_res<NR><<<1, 256, 0, s>>>(st.part, st.scal.p + 3 * kMomScal - 3);
     SEMO_CHECK_LAUNCH();
-    double tr[3];
+    double* const tr = c->hpin + 7 * kMomScal;
     SEMO_CUDA(cudaMemcpyAsync(tr, st.scal.p + 3 * kMomScal - 3, sizeof(double) * NR, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaEventRecord(c->ev[2], s));
     SEMO_CUDA(cudaEventSynchronize(c->ev[2]));

@@ -272,8 +272,8 @@ double momentum_update(semo_ctx* c) {
     SEMO_CHECK_LAUNCH();
     face::k_finish2<<<1, 256, 0, s>>>(c->red, c->red.p + 2 * kRedBlocks);
     SEMO_CHECK_LAUNCH();
-    double h[2];
-    SEMO_CUDA(cudaMemcpyAsync(h, c->red.p + 2 * kRedBlocks, sizeof(h), cudaMemcpyDeviceToHost, s));
+    double* const h = c->hpin;
+    SEMO_CUDA(cudaMemcpyAsync(h, c->red.p + 2 * kRedBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
     return std::sqrt(h[0]) / std::sqrt(h[1]);
 }

@@ -41,13 +41,14 @@ extern long long g_kernel_launches;
 enum Stage { ST_FACE_VALUES, ST_GRAVITY, ST_STENCIL, ST_PFACE, ST_PBFACE, ST_PCELL, ST_AMG_SETUP, ST_PCG,
              ST_GG, ST_UPDATE, ST_VCYCLE, ST_SETUP_AGG, ST_SETUP_PROLONG, ST_SETUP_GALERKIN, ST_SETUP_LEVEL,
              ST_SETUP_COARSE, ST_MFACE, ST_MCELL, ST_MSOLVE, ST_MUPDATE, ST_MSTACS, ST_VFACE, ST_VSOLVE, ST_VUPDATE,
-             ST_STENCIL_UVW, ST_MBFACE, ST_CGRAD, ST_CFACE, ST_CCELL, ST_CSOLVE, ST_CUPDATE, ST_SFT, ST_COUNT };
+             ST_STENCIL_UVW, ST_MBFACE, ST_CGRAD, ST_CFACE, ST_CCELL, ST_CSOLVE, ST_CUPDATE, ST_SFT, ST_SETUP_CYCLE, ST_COUNT };
 static const char* const kStageNames[ST_COUNT] = {"face_values", "gravity", "stencil", "pface", "pbface", "pcell",
                                                   "amg_setup", "pcg", "gauss_green", "update", "vcycle",
                                                   "setup_aggregate", "setup_prolong", "setup_galerkin",
                                                   "setup_level", "setup_coarse", "mface", "mcell", "msolve",
                                                   "mupdate", "mstacs", "vface", "vsolve", "vupdate", "stencil_uvw", "mbface",
-                                                  "cgrad", "cface", "ccell", "csolve", "cupdate", "surface_tension"};
+                                                  "cgrad", "cface", "ccell", "csolve", "cupdate", "surface_tension",
+                                                  "setup_cycle"};
 
 // Device buffer, stream-ordered allocation (memory pool keeps freed blocks).
 template <class T>
@@ -115,6 +116,9 @@ struct Amg {
 struct Timer {
     cudaEvent_t a = nullptr, b = nullptr;
 };
+
+constexpr int kHostScalars = 128;   // doubles in semo_ctx::hpin and ::hpin_setup
+constexpr int kHostInts = 16;       // ints in semo_ctx::hpin_scan and ::hpin_int
 
 }  // namespace semo
 
@@ -242,9 +246,15 @@ struct semo_ctx {
     semo::Amg<float> amg32;
     semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
     semo::DBuf<float> kz32, kr32;
-    double* hpin = nullptr;                       // pinned host scalars for convergence checks
-    int* hpin_int = nullptr;                      // pinned host counters read while setup kernels run
-    double* hpin_setup = nullptr;                 // pinned per-level scalars of the setup
+    // Pinned host scalars, one set per host thread that reads results back:
+    // a device-to-host copy into pageable memory waits inside the driver for
+    // its stream, and while it waits the other thread's CUDA calls queue
+    // behind it (the hierarchy built beside the momentum pass stalled for the
+    // momentum assembly's duration on such a read).  Allocated with the context.
+    double* hpin = nullptr;                       // context's stream: convergence checks, norms (kHostScalars)
+    int* hpin_scan = nullptr;                     // context's stream: scan totals and flags (kHostInts)
+    int* hpin_int = nullptr;                      // setup: counters and scan totals (kHostInts)
+    double* hpin_setup = nullptr;                 // setup: per-level scalars (kHostScalars)
     cudaEvent_t sync_ev[2] = {nullptr, nullptr};  // completion of those counter copies
     std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
 
@@ -279,7 +289,7 @@ inline cudaStream_t setup_stream(const semo_ctx* c) { return c->setup_s ? c->set
 // the AMG setup stages run on setup_s
 inline bool is_setup_stage(int st) {
     return st == ST_AMG_SETUP || st == ST_SETUP_AGG || st == ST_SETUP_PROLONG || st == ST_SETUP_GALERKIN ||
-           st == ST_SETUP_LEVEL || st == ST_SETUP_COARSE;
+           st == ST_SETUP_LEVEL || st == ST_SETUP_COARSE || st == ST_SETUP_CYCLE;
 }
 
 // RAII: times the enclosed launches of one stage when profiling is enabled.
@@ -374,7 +384,9 @@ template <class V>
 void build_hierarchy(semo_ctx* c, Amg<V>& h, const int* ptr, const int* col, const double* val, int n,
                      int64_t nnz);
 // exclusive scan of d[0..n) in place on the context's stream; returns the total
-int device_scan(cudaStream_t s, int* d, int n);
+// exclusive scan of d[0..n) on the stream; returns the total, read through
+// the pinned int *hpin (one host sync)
+int device_scan(cudaStream_t s, int* d, int n, int* hpin);
 
 // pressure matrix values only (A_val: off-diagonals and diagonal, the values
 // assemble_pressure writes) on stream s, after assemble_face_values
