@@ -949,11 +949,27 @@ struct GraphGuard {
     }
 };
 
+// The loop's stopping threshold on r.r: (tol |b|)^2, |b| = 1 for b = 0
+// (scal[11] = b.b)
+__device__ __forceinline__ double cg_stop_rr(const double* scal, double tol) {
+    const double bn = sqrt(scal[11]);
+    const double bnorm = (bn > 0.0) ? bn : 1.0;
+    return (tol * bnorm) * (tol * bnorm);
+}
+// Before the loop: iterate at all? (no when r0 already meets the tolerance,
+// or b or r0 is not finite -- the host reports that after the graph)
+__global__ void k_cg_begin(cudaGraphConditionalHandle h, const double* __restrict__ scal, double tol, int max_iter) {
+    const double bn = sqrt(scal[11]), rn = sqrt(scal[12]);
+    const double bnorm = (bn > 0.0) ? bn : 1.0;
+    const bool go = isfinite(bn) && isfinite(rn) && rn > tol * bnorm && max_iter > 0;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
 // End of one CG iteration on the device: count it and decide whether the
 // loop goes on (scal[13] iterations, scal[14] status: 1 NaN/Inf, 2 p.q <= 0).
 // The loop is a conditional WHILE node, so no iteration waits for the host;
 // max_iter bounds it.
-__global__ void k_cg_check(cudaGraphConditionalHandle h, double* __restrict__ scal, double stop_rr, int max_iter) {
+__global__ void k_cg_check(cudaGraphConditionalHandle h, double* __restrict__ scal, double tol, int max_iter) {
+    const double stop_rr = cg_stop_rr(scal, tol);
     const double it = scal[13] + 1.0;
     scal[13] = it;
     const double pq = scal[2], rr = scal[3];
@@ -993,67 +1009,68 @@ void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, const int* 
     SEMO_CHECK_LAUNCH();
     k_fin_rr<<<1, 256, 0, s>>>(R.part + kRedBlocks, R.scal + 9);   // ||r0||^2 -> scal[12]
     SEMO_CHECK_LAUNCH();
-    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 11, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    const double bn = std::sqrt(h2[0]);
-    double rn = std::sqrt(h2[1]);
-    if (!std::isfinite(bn) || !std::isfinite(rn)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
-    const double bnorm = (bn > 0.0) ? bn : 1.0;
-    int it = 0;
-    // The whole iteration loop is one graph: a conditional WHILE node whose
-    // body is one CG iteration (~30 kernels) plus k_cg_check, which decides
-    // on the device whether to go on.  The host waits once, at the end.
-    if (rn > c->prm.tol * bnorm && c->prm.max_iter > 0) {
-        GraphGuard gg;
-        SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
-        cudaGraphConditionalHandle handle;
-        SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, gg.g, 1, cudaGraphCondAssignDefault));
-        cudaGraphNodeParams cp = {};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = handle;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        cudaGraphNode_t loop;
-        SEMO_CUDA(cudaGraphAddNode(&loop, gg.g, nullptr, nullptr, 0, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        const double stop_rr = (c->prm.tol * bnorm) * (c->prm.tol * bnorm);
-        const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        try {
-            cg_iteration(c, h, cy, outer, x, R);
-            k_cg_check<<<1, 1, 0, s>>>(handle, R.scal, stop_rr, c->prm.max_iter);
-            SEMO_CHECK_LAUNCH();
-        } catch (...) {
-            cudaGraph_t junk = nullptr;
-            cudaStreamEndCapture(s, &junk);
-            throw;
-        }
-        cudaGraph_t captured = nullptr;
-        SEMO_CUDA(cudaStreamEndCapture(s, &captured));
-        size_t body_nodes = 0;
-        SEMO_CUDA(cudaGraphGetNodes(body, nullptr, &body_nodes));
-        __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
-        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
-        SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        it = (int)h2[13];
-        __atomic_add_fetch(&g_kernel_launches, (long long)body_nodes * it, __ATOMIC_RELAXED);
-        if (h2[14] == 1.0) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
-        if (h2[14] == 2.0) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
-        rn = std::sqrt(h2[3]);
+    // The loop is one graph: k_cg_begin, then a conditional WHILE node whose
+    // body is one CG iteration (~30 kernels) plus k_cg_check, which decides on
+    // the device whether to go on.  It is captured and instantiated while the
+    // kernels above run, and the host waits once, after the true residual.
+    GraphGuard gg;
+    SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
+    cudaGraphConditionalHandle handle;
+    SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, gg.g, 0, cudaGraphCondAssignDefault));
+    cudaKernelNodeParams kb = {};
+    const double tol = c->prm.tol;
+    const int max_iter = c->prm.max_iter;
+    const double* scal_c = R.scal;
+    void* kb_args[] = {(void*)&handle, (void*)&scal_c, (void*)&tol, (void*)&max_iter};
+    kb.func = (void*)k_cg_begin;
+    kb.gridDim = dim3(1);
+    kb.blockDim = dim3(1);
+    kb.kernelParams = kb_args;
+    cudaGraphNode_t begin;
+    SEMO_CUDA(cudaGraphAddKernelNode(&begin, gg.g, nullptr, 0, &kb));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    SEMO_CUDA(cudaGraphAddNode(&loop, gg.g, &begin, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+    SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    try {
+        cg_iteration(c, h, cy, outer, x, R);
+        k_cg_check<<<1, 1, 0, s>>>(handle, R.scal, tol, max_iter);
+        SEMO_CHECK_LAUNCH();
+    } catch (...) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(s, &junk);
+        throw;
     }
-    // true FP64 residual of the returned solution
+    cudaGraph_t captured = nullptr;
+    SEMO_CUDA(cudaStreamEndCapture(s, &captured));
+    size_t body_nodes = 0;
+    SEMO_CUDA(cudaGraphGetNodes(body, nullptr, &body_nodes));
+    __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
+    SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
+    SEMO_CUDA(cudaGraphLaunch(gg.e, s));
+    // true FP64 residual of the returned solution -> scal[16]
     k_res64<<<blocks((int64_t)n * 8, 256), 256, 0, s>>>(A8, x, b, r);
     SEMO_CHECK_LAUNCH();
     k_dot<<<kRedBlocks, kRedThreads, 0, s>>>(n, r, r, R.part);
     SEMO_CHECK_LAUNCH();
-    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal + 8);
+    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal + 13);
     SEMO_CHECK_LAUNCH();
-    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal + 11, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SEMO_CUDA(cudaMemcpyAsync(h2, R.scal, sizeof(double) * 17, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaStreamSynchronize(s));
+    const double bn = std::sqrt(h2[11]), rn0 = std::sqrt(h2[12]);
+    if (!std::isfinite(bn) || !std::isfinite(rn0)) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
+    const int it = (int)h2[13];
+    __atomic_add_fetch(&g_kernel_launches, 1LL + (long long)body_nodes * it, __ATOMIC_RELAXED);
+    if (h2[14] == 1.0) throw Error(SEMO_ERR_NAN, "NaN/Inf in the Krylov residual");
+    if (h2[14] == 2.0) throw Error(SEMO_ERR_BREAKDOWN, "CG breakdown: p.Ap <= 0 (matrix not SPD?)");
     info->iterations = it;
-    info->rel_residual = (bn > 0.0) ? std::sqrt(h2[0]) / bn : 0.0;
+    info->rel_residual = (bn > 0.0) ? std::sqrt(h2[16]) / bn : 0.0;
 }
 
 template <class V>
@@ -1352,10 +1369,42 @@ __global__ void k_dinv_dig(int n, const int* __restrict__ dig, const double* __r
     if (i < n) dinv[i] = 1.0 / val[dig[i]];
 }
 
+// The instantiated iteration graph of a batched BiCGStab, kept while every
+// pointer and scalar baked into its kernels stays the same (the buffers below
+// are reused from call to call, so the momentum and volume-fraction solves of
+// successive outer iterations launch it without capturing it again).
+struct BiGraphKey {
+    int nr = 0, n = 0, max_iter = 0;
+    double tol2 = 0.0;
+    const void* ptrs[8] = {};
+    bool operator==(const BiGraphKey& o) const {
+        if (nr != o.nr || n != o.n || max_iter != o.max_iter || tol2 != o.tol2) return false;
+        for (int k = 0; k < 8; ++k)
+            if (ptrs[k] != o.ptrs[k]) return false;
+        return true;
+    }
+};
+struct BiGraph {
+    BiGraphKey key;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    void reset() {
+        if (e) cudaGraphExecDestroy(e);
+        if (g) cudaGraphDestroy(g);
+        e = nullptr;
+        g = nullptr;
+        key = BiGraphKey{};
+    }
+    BiGraph() = default;
+    BiGraph(const BiGraph&) = delete;
+    BiGraph& operator=(const BiGraph&) = delete;
+    ~BiGraph() { reset(); }
+};
 struct MomState {
     Sell<double> A;
     int gen = -1;                 // mesh generation the SELL layout was built for
     DBuf<double> dinv, vec, part, scal;
+    BiGraph graph[2];             // NR = 1, NR = 3
 };
 
 // end of one batched BiCGStab iteration on the device: go on while a system
@@ -1524,32 +1573,32 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
     SEMO_CHECK_LAUNCH();
     k_bi_fin0<NR><<<1, 256, 0, s>>>(st.part, st.scal, tol2);
     SEMO_CHECK_LAUNCH();
-    // pinned: hs = hpin[0, 48), the loop's scalars hpin[48, 112), residuals hpin[112, 115)
-    double* const hs = c->hpin;
-    SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(double) * NR * kMomScal, cudaMemcpyDeviceToHost, s));
-    SEMO_CUDA(cudaStreamSynchronize(s));
-    int iters[NR] = {};
-    bool any = false;
-    for (int j = 0; j < NR; ++j) {
-        if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
-        any |= hs[kMomScal * j + 9] != 0.0;
-    }
-    // the iterations run as one graph: a conditional WHILE node around one
-    // iteration (8 kernels + k_bi_check); the host waits once
-    if (any && c->prm.mom_max_iter > 0) {
-        GraphGuard gg;
-        SEMO_CUDA(cudaGraphCreate(&gg.g, 0));
+    // The iterations run as one graph: a conditional WHILE node around one
+    // iteration (8 kernels + k_bi_check), launched without a host round trip
+    // first: systems whose right-hand side is zero, already converged or not
+    // finite start inactive (k_bi_fin0), every kernel skips them, and the
+    // host reads the outcome once, after the true residuals.
+    BiGraph& G = st.graph[NR == 1 ? 0 : 1];
+    BiGraphKey key;
+    key.nr = NR;
+    key.n = n;
+    key.max_iter = c->prm.mom_max_iter;
+    key.tol2 = tol2;
+    const void* kp[8] = {A.sptr, A.col, A.val, st.dinv.p, st.vec.p, st.part.p, st.scal.p, x};
+    std::copy(kp, kp + 8, key.ptrs);
+    if (!G.e || !(G.key == key)) {
+        G.reset();
+        SEMO_CUDA(cudaGraphCreate(&G.g, 0));
         cudaGraphConditionalHandle handle;
-        SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, gg.g, 1, cudaGraphCondAssignDefault));
+        SEMO_CUDA(cudaGraphConditionalHandleCreate(&handle, G.g, 1, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = handle;
         cp.conditional.type = cudaGraphCondTypeWhile;
         cp.conditional.size = 1;
         cudaGraphNode_t loop;
-        SEMO_CUDA(cudaGraphAddNode(&loop, gg.g, nullptr, nullptr, 0, &cp));
+        SEMO_CUDA(cudaGraphAddNode(&loop, G.g, nullptr, nullptr, 0, &cp));
         cudaGraph_t body = cp.conditional.phGraph_out[0];
-        SEMO_CUDA(cudaMemsetAsync(st.scal.p + 3 * kMomScal, 0, sizeof(double) * kMomScal, s));
         const long long before = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
         SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
@@ -1574,34 +1623,39 @@ semo_status bicgstab_jacobi(semo_ctx* c, int stage, const KrylovPattern& pat, co
         } catch (...) {
             cudaGraph_t junk = nullptr;
             cudaStreamEndCapture(s, &junk);
+            G.reset();
             throw;
         }
         cudaGraph_t captured = nullptr;
         SEMO_CUDA(cudaStreamEndCapture(s, &captured));
         __atomic_store_n(&g_kernel_launches, before, __ATOMIC_RELAXED);
-        SEMO_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
-        SEMO_CUDA(cudaGraphLaunch(gg.e, s));
-        double* const hit = c->hpin + 3 * kMomScal;
-        SEMO_CUDA(cudaMemcpyAsync(hit, st.scal.p, sizeof(double) * 4 * kMomScal, cudaMemcpyDeviceToHost, s));
-        SEMO_CUDA(cudaStreamSynchronize(s));
-        const int it = (int)hit[3 * kMomScal];
-        __atomic_add_fetch(&g_kernel_launches, 9LL * it, __ATOMIC_RELAXED);
-        std::copy(hit, hit + 3 * kMomScal, hs);
-        for (int j = 0; j < NR; ++j) {
-            if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the BiCGStab residual");
-            // systems converge one after another; each counts the iterations it was active
-            iters[j] = (int)hs[kMomScal * j + 11];
-        }
+        SEMO_CUDA(cudaGraphInstantiate(&G.e, G.g, 0));
+        G.key = key;
     }
+    SEMO_CUDA(cudaMemsetAsync(st.scal.p + 3 * kMomScal, 0, sizeof(double) * kMomScal, s));
+    SEMO_CUDA(cudaGraphLaunch(G.e, s));
     // true FP64 residuals of the returned solutions
     k_bi_res<NR><<<kRedBlocks, kRedThreads, 0, s>>>(A, x, b, st.part);
     SEMO_CHECK_LAUNCH();
     k_bi_fin_res<NR><<<1, 256, 0, s>>>(st.part, st.scal.p + 3 * kMomScal - 3);
     SEMO_CHECK_LAUNCH();
-    double* const tr = c->hpin + 7 * kMomScal;
+    // pinned: the systems' scalars and the iteration count hpin[0, 64), the
+    // true residuals hpin[64, 64 + NR)
+    double* const hs = c->hpin;
+    double* const tr = c->hpin + 4 * kMomScal;
+    SEMO_CUDA(cudaMemcpyAsync(hs, st.scal.p, sizeof(double) * 4 * kMomScal, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaMemcpyAsync(tr, st.scal.p + 3 * kMomScal - 3, sizeof(double) * NR, cudaMemcpyDeviceToHost, s));
     SEMO_CUDA(cudaEventRecord(c->ev[2], s));
     SEMO_CUDA(cudaEventSynchronize(c->ev[2]));
+    const int it = (int)hs[3 * kMomScal];
+    __atomic_add_fetch(&g_kernel_launches, 9LL * it, __ATOMIC_RELAXED);
+    int iters[NR] = {};
+    for (int j = 0; j < NR; ++j) {
+        if (!std::isfinite(hs[kMomScal * j + 8])) throw Error(SEMO_ERR_NAN, "non-finite right-hand side");
+        if (!std::isfinite(hs[kMomScal * j + 7])) throw Error(SEMO_ERR_NAN, "NaN/Inf in the BiCGStab residual");
+        // systems converge one after another; each counts the iterations it was active
+        iters[j] = (int)hs[kMomScal * j + 11];
+    }
     float t0 = 0, t1 = 0;
     SEMO_CUDA(cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]));
     SEMO_CUDA(cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]));
