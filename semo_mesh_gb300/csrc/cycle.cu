@@ -214,11 +214,43 @@ struct FirstIterate {
     __device__ __forceinline__ V operator()(int j) const { return __ldg(dinv + j) * __ldg(b + j) * inv_theta; }
 };
 
+// ------------------------------------------- programmatic dependent launch
+// The ~30 kernels of a CG iteration each depend on the one before and are
+// short, so the gap between one kernel's last block and the next one's first
+// is a real share of an iteration.  They are launched with programmatic
+// stream serialisation: a kernel's launch is processed while its predecessor
+// drains (the predecessor's blocks signal it implicitly as they exit), and
+// the kernel waits at pdl_enter() -- its first statement: nothing is read
+// before it -- until the predecessor has finished and its writes are
+// visible.  Measured at 128^3: 0.42 -> 0.40 ms a CG iteration.  Signalling
+// early instead (griddepcontrol.launch_dependents after the wait) put the
+// waiting successor's blocks on the multiprocessors beside the running
+// kernel and made the iteration 8 % slower than plain launches.  Without a
+// programmatic predecessor the wait returns at once, so the kernels stay
+// correct under plain launches.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <class... P, class... A>
+void launch_pdl(void (*k)(P...), int grid, int block, cudaStream_t s, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SEMO_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...));
+    SEMO_CHECK_LAUNCH();
+}
+
 // ------------------------------------------------------- V-cycle kernels
 // pre-smoothing, degree 2 from x = 0:  x = d0 + c1 d0 + c2 D^-1 (b - A d0),  d0 = D^-1 b / theta
 template <class M, class V>
 __global__ void __launch_bounds__(256) k_pre2(M A, const V* __restrict__ dinv, const V* __restrict__ b,
                                               V inv_theta, V c1, V c2, V* __restrict__ x) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = A.dot(row, lane, FirstIterate<V>{dinv, b, inv_theta});
@@ -232,6 +264,7 @@ __global__ void __launch_bounds__(256) k_pre2(M A, const V* __restrict__ dinv, c
 template <class M, class V>
 __global__ void __launch_bounds__(256) k_res(M A, const V* __restrict__ x, const V* __restrict__ b,
                                              V* __restrict__ r) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = A.dot(row, lane, Vec<V, V>{x});
@@ -240,6 +273,7 @@ __global__ void __launch_bounds__(256) k_res(M A, const V* __restrict__ x, const
 // y = A x (restriction with R, or any plain product)
 template <class M, class V>
 __global__ void __launch_bounds__(256) k_mv(M A, const V* __restrict__ x, V* __restrict__ y) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = A.dot(row, lane, Vec<V, V>{x});
@@ -248,6 +282,7 @@ __global__ void __launch_bounds__(256) k_mv(M A, const V* __restrict__ x, V* __r
 // x += P xc
 template <class M, class V>
 __global__ void __launch_bounds__(256) k_prolong_add(M P, const V* __restrict__ xc, V* __restrict__ x) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = P.dot(row, lane, Vec<V, V>{xc});
@@ -258,6 +293,7 @@ template <class M, class V>
 __global__ void __launch_bounds__(256) k_post0(M A, const V* __restrict__ dinv, const V* __restrict__ b,
                                                V inv_theta, const V* __restrict__ x, V* __restrict__ d,
                                                V* __restrict__ y) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = A.dot(row, lane, Vec<V, V>{x});
@@ -272,6 +308,7 @@ template <class M, class V>
 __global__ void __launch_bounds__(256) k_post1(M A, const V* __restrict__ dinv, const V* __restrict__ b, V c1, V c2,
                                                const V* __restrict__ y, const V* __restrict__ d,
                                                V* __restrict__ x) {
+    pdl_enter();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int row = g / M::kVS, lane = g % M::kVS;
     const V s = A.dot(row, lane, Vec<V, V>{y});
@@ -286,6 +323,7 @@ __global__ void __launch_bounds__(kRedThreads) k_post1_dots(M A, const V* __rest
                                                             V* __restrict__ z, const double* __restrict__ r,
                                                             const double* __restrict__ q,
                                                             double* __restrict__ part) {
+    pdl_enter();
     __shared__ double sh[32];
     double zr = 0.0, zq = 0.0;
     const int per_block = blockDim.x / M::kVS, lane = threadIdx.x % M::kVS;
@@ -332,6 +370,7 @@ __global__ void k_copy_t(int n, const V* __restrict__ a, V* __restrict__ b) {
 // coarsest level: x = A^-1 b with the explicit FP64 inverse, one block
 template <class V>
 __global__ void k_coarse_solve(int n, const double* __restrict__ inv, const V* __restrict__ b, V* __restrict__ x) {
+    pdl_enter();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double s = 0.0;
         for (int k = 0; k < n; ++k) s += inv[(size_t)i * n + k] * (double)b[k];
@@ -348,6 +387,7 @@ __device__ __forceinline__ double sum_parts(const double* part, double* sh) {
     return block_sum(s, sh);
 }
 __global__ void k_fin_beta(const double* __restrict__ part, double* __restrict__ scal) {
+    pdl_enter();
     __shared__ double sh[32];
     const double rz = sum_parts(part, sh);
     const double zq = sum_parts(part + kRedBlocks, sh);
@@ -366,6 +406,7 @@ __global__ void __launch_bounds__(kRedThreads) k_outer_mv(M A, const Z* __restri
                                                           double* __restrict__ p, double* __restrict__ q,
                                                           const double* __restrict__ scal,
                                                           double* __restrict__ part) {
+    pdl_enter();
     __shared__ double sh[32];
     const double beta = scal[5];
     double pq = 0.0;
@@ -382,6 +423,7 @@ __global__ void __launch_bounds__(kRedThreads) k_outer_mv(M A, const Z* __restri
     if (threadIdx.x == 0) part[blockIdx.x] = pq;
 }
 __global__ void k_fin_alpha(const double* __restrict__ part, double* __restrict__ scal) {
+    pdl_enter();
     __shared__ double sh[32];
     const double pq = sum_parts(part, sh);
     if (threadIdx.x == 0) {
@@ -396,6 +438,7 @@ __global__ void __launch_bounds__(kRedThreads) k_xr(int n, double* __restrict__ 
                                                     V* __restrict__ rv, const double* __restrict__ p,
                                                     const double* __restrict__ q, const double* __restrict__ scal,
                                                     double* __restrict__ part) {
+    pdl_enter();
     __shared__ double sh[32];
     const double alpha = scal[6];
     double s = 0.0;
@@ -410,6 +453,7 @@ __global__ void __launch_bounds__(kRedThreads) k_xr(int n, double* __restrict__ 
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 __global__ void k_fin_rr(const double* __restrict__ part, double* __restrict__ scal) {
+    pdl_enter();
     __shared__ double sh[32];
     const double rr = sum_parts(part, sh);
     if (threadIdx.x == 0) scal[3] = rr;
@@ -843,8 +887,7 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
     cudaStream_t s = c->stream;
     AmgLevel<V>& L = h.lev[l];
     if (l == (int)h.lev.size() - 1) {
-        k_coarse_solve<V><<<1, 256, 0, s>>>(h.coarse_n, h.cinv, L.b, L.x);
-        SEMO_CHECK_LAUNCH();
+        launch_pdl(k_coarse_solve<V>, 1, 256, s, h.coarse_n, h.cinv.p, L.b.p, L.x.p);
         return;
     }
     const LevelMats<V>& M = cy.lev[l];
@@ -854,32 +897,30 @@ void vcycle_from(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, int l) {
         gs_sweep(s, L, M, false, true);   // forward sweep from x = 0
     } else if (degree == 2) {
         with_A(M, L.A, [&](auto A) {
-            k_pre2<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1, (V)cc.c2, L.x.p);
+            launch_pdl(k_pre2<decltype(A), V>, grid_for(A), 256, s, A, L.dinv.p, L.b.p, (V)cc.inv_theta, (V)cc.c1,
+                       (V)cc.c2, L.x.p);
         });
-        SEMO_CHECK_LAUNCH();
     } else {
         chebyshev_generic(s, L, degree, true);
     }
-    with_A(M, L.A, [&](auto A) { k_res<<<grid_for(A), 256, 0, s>>>(A, L.x.p, L.b.p, L.r.p); });
-    SEMO_CHECK_LAUNCH();
+    with_A(M, L.A, [&](auto A) { launch_pdl(k_res<decltype(A), V>, grid_for(A), 256, s, A, L.x.p, L.b.p, L.r.p); });
     AmgLevel<V>& C = h.lev[l + 1];
-    with_op(M.R, M.r, L.R, [&](auto R) { k_mv<<<grid_for(R), 256, 0, s>>>(R, L.r.p, C.b.p); });
-    SEMO_CHECK_LAUNCH();
+    with_op(M.R, M.r, L.R, [&](auto R) { launch_pdl(k_mv<decltype(R), V>, grid_for(R), 256, s, R, L.r.p, C.b.p); });
     vcycle_from(c, h, cy, l + 1);
-    with_op(M.P, M.p, L.P, [&](auto P) { k_prolong_add<<<grid_for(P), 256, 0, s>>>(P, C.x.p, L.x.p); });
-    SEMO_CHECK_LAUNCH();
+    with_op(M.P, M.p, L.P,
+            [&](auto P) { launch_pdl(k_prolong_add<decltype(P), V>, grid_for(P), 256, s, P, C.x.p, L.x.p); });
     if (M.gs) {
         gs_sweep(s, L, M, true, false);   // backward sweep: the cycle stays symmetric
     } else if (degree == 2) {
         with_A(M, L.A, [&](auto A) {
-            k_post0<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p, L.t.p, L.r.p);
+            launch_pdl(k_post0<decltype(A), V>, grid_for(A), 256, s, A, L.dinv.p, L.b.p, (V)cc.inv_theta, L.x.p,
+                       L.t.p, L.r.p);
         });
-        SEMO_CHECK_LAUNCH();
         if (l > 0) {
             with_A(M, L.A, [&](auto A) {
-                k_post1<<<grid_for(A), 256, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p, L.x.p);
+                launch_pdl(k_post1<decltype(A), V>, grid_for(A), 256, s, A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2,
+                           L.r.p, L.t.p, L.x.p);
             });
-            SEMO_CHECK_LAUNCH();
         }
         // on the finest level the last step is fused with the CG dot products (cg_iteration)
     } else {
@@ -917,27 +958,21 @@ void cg_iteration(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, do
         vcycle_from(c, h, cy, 0);   // everything but the last smoothing step of the finest level
         // z lands in L.x; z.r and z.q folded in
         with_A(cy.lev[0], L.A, [&](auto A) {
-            k_post1_dots<<<kRedBlocks, kRedThreads, 0, s>>>(A, L.dinv.p, L.b.p, (V)cc.c1, (V)cc.c2, L.r.p, L.t.p,
-                                                            L.x.p, r, q, R.part);
+            launch_pdl(k_post1_dots<decltype(A), V>, kRedBlocks, kRedThreads, s, A, L.dinv.p, L.b.p, (V)cc.c1,
+                       (V)cc.c2, L.r.p, L.t.p, L.x.p, r, q, R.part);
         });
-        SEMO_CHECK_LAUNCH();
     } else {
         vcycle_from(c, h, cy, 0);
         k_dot2<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, L.x.p, r, q, R.part);
         SEMO_CHECK_LAUNCH();
     }
-    k_fin_beta<<<1, 256, 0, s>>>(R.part, R.scal);
-    SEMO_CHECK_LAUNCH();
+    launch_pdl(k_fin_beta, 1, 256, s, R.part, R.scal);
     outer.with([&](auto A) {
-        k_outer_mv<<<kRedBlocks, kRedThreads, 0, s>>>(A, L.x.p, p, q, R.scal, R.part);
+        launch_pdl(k_outer_mv<decltype(A), V>, kRedBlocks, kRedThreads, s, A, L.x.p, p, q, R.scal, R.part);
     });
-    SEMO_CHECK_LAUNCH();
-    k_fin_alpha<<<1, 256, 0, s>>>(R.part, R.scal);
-    SEMO_CHECK_LAUNCH();
-    k_xr<V><<<kRedBlocks, kRedThreads, 0, s>>>(n, x, r, L.b.p, p, q, R.scal, R.part);
-    SEMO_CHECK_LAUNCH();
-    k_fin_rr<<<1, 256, 0, s>>>(R.part, R.scal);
-    SEMO_CHECK_LAUNCH();
+    launch_pdl(k_fin_alpha, 1, 256, s, R.part, R.scal);
+    launch_pdl(k_xr<V>, kRedBlocks, kRedThreads, s, n, x, r, L.b.p, p, q, R.scal, R.part);
+    launch_pdl(k_fin_rr, 1, 256, s, R.part, R.scal);
 }
 
 struct GraphGuard {
@@ -969,6 +1004,7 @@ __global__ void k_cg_begin(cudaGraphConditionalHandle h, const double* __restric
 // The loop is a conditional WHILE node, so no iteration waits for the host;
 // max_iter bounds it.
 __global__ void k_cg_check(cudaGraphConditionalHandle h, double* __restrict__ scal, double tol, int max_iter) {
+    pdl_enter();
     const double stop_rr = cg_stop_rr(scal, tol);
     const double it = scal[13] + 1.0;
     scal[13] = it;
@@ -1040,8 +1076,7 @@ void pcg(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const OuterOp& outer, const int* 
     SEMO_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     try {
         cg_iteration(c, h, cy, outer, x, R);
-        k_cg_check<<<1, 1, 0, s>>>(handle, R.scal, tol, max_iter);
-        SEMO_CHECK_LAUNCH();
+        launch_pdl(k_cg_check, 1, 1, s, handle, R.scal, tol, max_iter);
     } catch (...) {
         cudaGraph_t junk = nullptr;
         cudaStreamEndCapture(s, &junk);
