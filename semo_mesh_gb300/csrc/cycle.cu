@@ -1180,6 +1180,26 @@ __device__ __forceinline__ void sell_mv(const SellView<double>& A, int row, cons
     for (int j = 0; j < NR; ++j) y[j] = 0.0;
     const int sl = row >> 5, l = row & 31;
     const int b = A.sptr[sl], w = (A.sptr[sl + 1] - b) >> 5;
+    if (NR == 1 && w <= 8) {
+        // one right-hand side, short rows (the mesh's): every entry load
+        // first, then the gathers, so a row costs about two memory round
+        // trips instead of one per entry; the products are summed in entry
+        // order as below (0.85 -> 0.73 ms for the volume-fraction solve at
+        // 128^3; with three right-hand sides the batch's registers cost more
+        // than it gains: 1.63 -> 1.67 ms for the momentum solve)
+        int cj[8];
+        double vj[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < w) { cj[q] = A.col[b + l + 32 * q]; vj[q] = A.val[b + l + 32 * q]; }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < w) {
+#pragma unroll
+                for (int j = 0; j < NR; ++j) y[j] += vj[q] * __ldg(x + j * N + cj[q]);
+            }
+        return;
+    }
     for (int e = 0, k = b + l; e < w; ++e, k += 32) {
         const int c = A.col[k];
         const double v = A.val[k];
