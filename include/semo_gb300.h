@@ -366,10 +366,17 @@ semo_status semo_vjp_fields(semo_ctx* ctx, const double* dJ_dx, double* lambda, 
                             double* dJ_dW, double* dJ_dP, semo_solve_info* info);
 
 /* Measurement hooks (no reference counterpart).  With profiling on, the
-   named stages are bracketed by CUDA events on the context's stream:
-   "face_values","gravity","stencil","pface","pbface","pcell","amg_setup",
-   "pcg","gauss_green","update","vcycle".  semo_stage_time returns the summed
-   device time and number of timed calls since the last semo_reset_stats. */
+   named stages are bracketed by CUDA events on the stream that runs them
+   (the pressure setup's on its own stream when it is built beside the
+   momentum pass): assembly "face_values","gravity","stencil" (LSQ gradients
+   and limits of all five fields),"stencil_uvw" (their U, V, W part, when P
+   and VF are unchanged since the last full pass),"surface_tension";
+   pressure "pface","pbface","pcell","amg_setup" (with "setup_aggregate",
+   "setup_prolong","setup_galerkin","setup_level","setup_coarse",
+   "setup_cycle"),"pcg","vcycle","gauss_green","update"; momentum "mface",
+   "mbface","mcell","msolve","mupdate"; volume fraction "mstacs","vface",
+   "vsolve","vupdate"; coupled "cgrad","cface","ccell","csolve","cupdate".  semo_stage_time returns the summed device time and
+   number of timed calls since the last semo_reset_stats. */
 void semo_set_profiling(semo_ctx* ctx, int on);
 semo_status semo_stage_time(semo_ctx* ctx, const char* stage, double* total_ms, int64_t* calls);
 semo_status semo_reset_stats(semo_ctx* ctx);
