@@ -37,6 +37,7 @@ needed between steps.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import subprocess
@@ -78,16 +79,32 @@ class ClockSampler:
         self.rows = []
         self.proc = None
         self.window = None
+        self.t_start = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
+            atexit.register(self.stop)
         except OSError:
             self.proc = None
+        self.t_start = time.monotonic()
         return self
+
+    def __enter__(self):
+        return self.start()
+
+    def settle(self, seconds: float = 3.0) -> None:
+        """Wait until `seconds` after the sampler started.  Measured on a GB300:
+        an outer iteration that ran 1-1.3 s after nvidia-smi started took
+        75 ms instead of 22 ms (once; later ones were unaffected), so the
+        sampler starts before the case is built and the timing waits for this."""
+        if self.t_start is not None:
+            rest = self.t_start + seconds - time.monotonic()
+            if rest > 0:
+                time.sleep(rest)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -101,13 +118,17 @@ class ClockSampler:
     def mark(self, t0: float, t1: float) -> None:
         self.window = (t0, t1)
 
-    def __exit__(self, *exc):
+    def stop(self) -> None:
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.proc = None
+
+    def __exit__(self, *exc):
+        self.stop()
 
     def summary(self) -> dict:
         def num(x):
@@ -477,6 +498,8 @@ def run_gpu_arm(args, rank, world, local) -> None:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    # the clock sampler starts before the case is built (ClockSampler.settle)
+    clk = ClockSampler(local).start()
     case = bench_case(args.n)
     mesh = case.mesh
     nc = mesh.n_cells
@@ -511,18 +534,19 @@ def run_gpu_arm(args, rank, world, local) -> None:
     strm = torch.cuda.ExternalStream(ctx.stream, device=torch.device(f"cuda:{local}"))
 
     # ---- mixed precision, inputs resident in HBM (the headline value) ------
-    with ClockSampler(local) as clk:
-        clk.wait_first()
-        for _ in range(args.warmup):
-            ctx.outer_iteration()
-        l0 = ctx.kernel_launches()
-        barrier()
-        torch.cuda.synchronize()
-        tw0 = time.monotonic()
-        ms_mixed, infos = timed(ctx, strm, args.steps, outer)
-        torch.cuda.synchronize()
-        clk.mark(tw0, time.monotonic())
-        time.sleep(0.25)   # one more sample after the window
+    clk.settle(3.0)
+    clk.wait_first()
+    for _ in range(args.warmup):
+        ctx.outer_iteration()
+    l0 = ctx.kernel_launches()
+    barrier()
+    torch.cuda.synchronize()
+    tw0 = time.monotonic()
+    ms_mixed, infos = timed(ctx, strm, args.steps, outer)
+    torch.cuda.synchronize()
+    clk.mark(tw0, time.monotonic())
+    time.sleep(0.25)   # one more sample after the window
+    clk.stop()
     barrier()
     launches = ctx.kernel_launches() - l0
     # per-stage device times from a second, untimed run of the same steps
