@@ -6,8 +6,11 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <exception>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <numeric>
 #include <string>
@@ -831,6 +834,77 @@ semo_status semo_solve_momentum(semo_ctx* c, double* x, semo_solve_info* info) {
 }
 
 namespace {
+// The host thread that builds the pressure hierarchy beside the momentum pass,
+// kept for the context's lifetime: the setup is the overlapped outer
+// iteration's critical path, and a thread started for each outer iteration
+// put its creation and its first CUDA call at the head of it.  One job at a
+// time; a job's exception is handed to the waiter.
+struct SetupWorker {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::function<void()> job;
+    bool pending = false, busy = false, quit = false;
+    std::exception_ptr err;
+    std::thread th;
+    explicit SetupWorker(int device) {
+        th = std::thread([this, device] { run(device); });
+    }
+    ~SetupWorker() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            quit = true;
+        }
+        cv.notify_all();
+        th.join();
+    }
+    void run(int device) {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv.wait(lk, [this] { return pending || quit; });
+            if (!pending) return;   // quit with nothing left to do
+            std::function<void()> f = std::move(job);
+            pending = false;
+            busy = true;
+            lk.unlock();
+            std::exception_ptr e;
+            try {
+                f();
+            } catch (...) {
+                e = std::current_exception();
+            }
+            lk.lock();
+            err = e;
+            busy = false;
+            cv.notify_all();
+        }
+    }
+    void post(std::function<void()> f) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            job = std::move(f);
+            err = nullptr;
+            pending = true;
+        }
+        cv.notify_all();
+    }
+    // wait for the posted job; rethrow its exception
+    void wait() {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [this] { return !pending && !busy; });
+        if (err) {
+            std::exception_ptr e = err;
+            err = nullptr;
+            std::rethrow_exception(e);
+        }
+    }
+};
+
+SetupWorker& setup_worker(semo_ctx* c) {
+    if (!c->setup_worker) c->setup_worker = std::make_shared<SetupWorker>(c->device);
+    return *static_cast<SetupWorker*>(c->setup_worker.get());
+}
+
 // The pressure matrix and its AMG hierarchy built on the second stream, the
 // hierarchy from a second host thread, while this thread runs the momentum
 // pass and the pressure assembly on the context's stream.  The pressure
@@ -841,8 +915,7 @@ namespace {
 // throws) and puts the setup back on the context's stream.
 struct SideSetup {
     semo_ctx* c;
-    std::thread th;
-    std::exception_ptr err;
+    bool waiting = false;   // a job is posted and not yet waited for
     explicit SideSetup(semo_ctx* ctx) : c(ctx) {
         if (!c->aux_stream) {
             // high priority: the setup is a chain of short dependent launches and
@@ -862,29 +935,38 @@ struct SideSetup {
         semo::pressure_matrix(c, c->aux_stream);
         SEMO_CUDA(cudaEventRecord(c->ov_ev[2], c->aux_stream));   // the face values may be rewritten after this
         c->setup_s = c->aux_stream;
-        th = std::thread([this] {
-            try {
-                SEMO_CUDA(cudaSetDevice(c->device));
-                const auto t0 = std::chrono::steady_clock::now();
-                semo::pressure_setup(c, c->A_ptr.p, c->A_col.p, c->A_val.p, c->nc, c->nnz, true, nullptr);
-                SEMO_CUDA(cudaEventRecord(c->ov_ev[1], c->aux_stream));
-                SEMO_CUDA(cudaEventSynchronize(c->ov_ev[1]));
-                c->side_setup_ms =
-                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-            } catch (...) {
-                err = std::current_exception();
-            }
+        SetupWorker& w = setup_worker(c);
+        semo_ctx* const cc = c;
+        w.post([cc] {
+            SEMO_CUDA(cudaSetDevice(cc->device));
+            const auto t0 = std::chrono::steady_clock::now();
+            semo::pressure_setup(cc, cc->A_ptr.p, cc->A_col.p, cc->A_val.p, cc->nc, cc->nnz, true, nullptr);
+            SEMO_CUDA(cudaEventRecord(cc->ov_ev[1], cc->aux_stream));
+            SEMO_CUDA(cudaEventSynchronize(cc->ov_ev[1]));
+            cc->side_setup_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         });
+        waiting = true;
     }
-    // join; rethrow a setup failure; the context's stream then waits for the hierarchy
+    // wait for the setup; rethrow its failure; the context's stream then waits for the hierarchy
     void finish() {
-        th.join();
+        waiting = false;
+        try {
+            setup_worker(c).wait();
+        } catch (...) {
+            c->setup_s = c->stream;
+            throw;
+        }
         c->setup_s = c->stream;
-        if (err) std::rethrow_exception(err);
         SEMO_CUDA(cudaStreamWaitEvent(c->stream, c->ov_ev[1], 0));
     }
     ~SideSetup() {
-        if (th.joinable()) th.join();
+        if (waiting) {
+            try {
+                setup_worker(c).wait();
+            } catch (...) {
+            }
+        }
         c->setup_s = c->stream;
     }
 };

@@ -596,11 +596,10 @@ __global__ void k_sell16_groups(int n, const int* __restrict__ ptr, const int* _
     }
 }
 
-template <class V, class W>
-__global__ void k_sell16_fill(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                              const V* __restrict__ val, const int* __restrict__ sptr, const int* __restrict__ smode,
+__global__ void k_sell16_cols(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                              const int* __restrict__ sptr, const int* __restrict__ smode,
                               const int* __restrict__ gbase, const int* __restrict__ wptr,
-                              unsigned short* __restrict__ dcol, int* __restrict__ wcol, W* __restrict__ sval) {
+                              unsigned short* __restrict__ dcol, int* __restrict__ wcol) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= ((n + 31) & ~31)) return;
     const int sl = row >> 5, l = row & 31;
@@ -613,46 +612,82 @@ __global__ void k_sell16_fill(int n, const int* __restrict__ ptr, const int* __r
         const int c = (j < len) ? col[rb + j] : base;
         dcol[k] = (mode == 2) ? (unsigned short)0 : (unsigned short)(c - base);
         if (mode == 2) wcol[wptr[sl] + 32 * j + l] = c;
-        sval[k] = (j < len) ? (W)val[rb + j] : W(0);
     }
 }
+// the values into a layout's slots (padding slots 0)
+template <class V, class W>
+__global__ void k_sell16_vals(int n, const int* __restrict__ ptr, const V* __restrict__ val,
+                              const int* __restrict__ sptr, W* __restrict__ sval) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= ((n + 31) & ~31)) return;
+    const int sl = row >> 5, l = row & 31;
+    const int b = sptr[sl], w = (sptr[sl + 1] - b) >> 5;
+    const int rb = (row < n) ? ptr[row] : 0, len = (row < n) ? ptr[row + 1] - rb : 0;
+    for (int j = 0; j < w; ++j) sval[b + 32 * j + l] = (j < len) ? (W)val[rb + j] : W(0);
+}
 
-template <class V>
-struct Sell16 {
+// The structure of a SELL-32 layout with 16-bit columns (slice pointers,
+// per-slice encodings, group bases, 16- and 32-bit columns).  It depends on
+// the pattern only, so the FP64 outer operator and the finest level of the
+// pressure hierarchy, both on the mesh's pattern, share one, built once per
+// mesh; a setup then only writes the two value arrays.
+struct Sell16Struct {
     int n = 0, nslices = 0;
+    int slots = 0;   // padded entries (sptr[nslices])
     DBuf<int> sptr, smode, gbase, wptr, wcol;
     DBuf<unsigned short> dcol;
+};
+template <class V>
+struct Sell16 {
+    std::shared_ptr<Sell16Struct> st;
     DBuf<V> val;
     Sell16View<V> view() const {
-        return Sell16View<V>{sptr.p, smode.p, gbase.p, wptr.p, dcol.p, wcol.p, val.p, n};
+        return Sell16View<V>{st->sptr.p, st->smode.p, st->gbase.p, st->wptr.p, st->dcol.p, st->wcol.p, val.p,
+                             st->n};
     }
 };
 
-// SELL-32 with 16-bit columns of a square CSR operator (always built: slices
-// that fit no 16-bit encoding keep 32-bit columns)
+// SELL-32 structure with 16-bit columns of a square CSR pattern (slices that
+// fit no 16-bit encoding keep 32-bit columns)
+std::shared_ptr<Sell16Struct> build_sell16_struct(cudaStream_t s, const int* ptr, const int* col, int n,
+                                                  int* hpin) {
+    auto S = std::make_shared<Sell16Struct>();
+    S->n = n;
+    S->nslices = (n + 31) / 32;
+    S->sptr.alloc(S->nslices + 1, s);
+    S->wptr.alloc(S->nslices + 1, s);
+    S->smode.alloc(S->nslices, s);
+    SEMO_CUDA(cudaMemsetAsync(S->sptr.p + S->nslices, 0, sizeof(int), s));
+    SEMO_CUDA(cudaMemsetAsync(S->wptr.p + S->nslices, 0, sizeof(int), s));
+    const int rows_pad = S->nslices * 32;
+    k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S->sptr.p);
+    SEMO_CHECK_LAUNCH();
+    S->slots = device_scan(s, S->sptr.p, S->nslices + 1, hpin);
+    S->gbase.alloc(std::max(S->slots / 32, 1), s);
+    k_sell16_groups<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, S->sptr.p, S->smode.p, S->gbase.p,
+                                                          S->wptr.p);
+    SEMO_CHECK_LAUNCH();
+    const int wide = device_scan(s, S->wptr.p, S->nslices + 1, hpin);
+    S->dcol.alloc(std::max(S->slots, 1), s);
+    S->wcol.alloc(std::max(wide, 1), s);
+    k_sell16_cols<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, S->sptr.p, S->smode.p, S->gbase.p, S->wptr.p,
+                                                         S->dcol.p, S->wcol.p);
+    SEMO_CHECK_LAUNCH();
+    return S;
+}
+// the values of a CSR operator on the structure's pattern into S (type W)
+template <class V, class W>
+void fill_sell16(cudaStream_t s, const int* ptr, const V* val, const std::shared_ptr<Sell16Struct>& st,
+                 Sell16<W>& S) {
+    S.st = st;
+    S.val.alloc(std::max(st->slots, 1), s);
+    k_sell16_vals<V, W><<<blocks((int64_t)st->nslices * 32, 256), 256, 0, s>>>(st->n, ptr, val, st->sptr.p,
+                                                                              S.val.p);
+    SEMO_CHECK_LAUNCH();
+}
 template <class V, class W>
 bool build_sell16(cudaStream_t s, const int* ptr, const int* col, const V* val, int n, Sell16<W>& S, int* hpin) {
-    S.n = n;
-    S.nslices = (n + 31) / 32;
-    S.sptr.alloc(S.nslices + 1, s);
-    S.wptr.alloc(S.nslices + 1, s);
-    S.smode.alloc(S.nslices, s);
-    SEMO_CUDA(cudaMemsetAsync(S.sptr.p + S.nslices, 0, sizeof(int), s));
-    SEMO_CUDA(cudaMemsetAsync(S.wptr.p + S.nslices, 0, sizeof(int), s));
-    const int rows_pad = S.nslices * 32;
-    k_sell_width<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, S.sptr.p);
-    SEMO_CHECK_LAUNCH();
-    const int total = device_scan(s, S.sptr.p, S.nslices + 1, hpin);
-    S.gbase.alloc(std::max(total / 32, 1), s);
-    k_sell16_groups<<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, S.sptr.p, S.smode.p, S.gbase.p, S.wptr.p);
-    SEMO_CHECK_LAUNCH();
-    const int wide = device_scan(s, S.wptr.p, S.nslices + 1, hpin);
-    S.dcol.alloc(std::max(total, 1), s);
-    S.wcol.alloc(std::max(wide, 1), s);
-    S.val.alloc(std::max(total, 1), s);
-    k_sell16_fill<V, W><<<blocks(rows_pad, 256), 256, 0, s>>>(n, ptr, col, val, S.sptr.p, S.smode.p, S.gbase.p,
-                                                               S.wptr.p, S.dcol.p, S.wcol.p, S.val.p);
-    SEMO_CHECK_LAUNCH();
+    fill_sell16<V, W>(s, ptr, val, build_sell16_struct(s, ptr, col, n, hpin), S);
     return true;
 }
 
@@ -1120,6 +1155,10 @@ struct ApplyState {
     Cycle<float> cy32;
     Cycle<double> cy64;
     OuterOp outer;
+    // the SELL-32/16-bit structure of the context's mesh pattern (A_ptr, A_col)
+    // and the mesh generation it was built for
+    std::shared_ptr<Sell16Struct> pat16;
+    int pat16_gen = 0;
     // the matrix values the current hierarchy was built from (pressure path only)
     DBuf<double> src_val;
     int src_n = 0;
@@ -1141,7 +1180,7 @@ ApplyState& apply_state(semo_ctx* c) {
 }
 
 template <class V>
-void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
+void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy, const std::shared_ptr<Sell16Struct>& lev0 = nullptr) {
     cudaStream_t s = setup_stream(c);
     const int nl = (int)h.lev.size();
     cy.lev.resize(std::max(nl - 1, 0));
@@ -1152,7 +1191,12 @@ void prepare_cycle(semo_ctx* c, Amg<V>& h, Cycle<V>& cy) {
         M.p = sell_pays(L.P);
         M.r = sell_pays(L.R);
         int* const hp = c->hpin_int + 4;
-        M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, hp);
+        if (l == 0 && M.a && lev0 && lev0->n == L.A.n) {   // the mesh pattern's structure, shared
+            fill_sell16<V, V>(s, L.A.ptr, L.A.val, lev0, M.A16);
+            M.a16 = true;
+        } else {
+            M.a16 = M.a && build_sell16<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A16, hp);
+        }
         if (M.a16) M.a = false;
         if (M.a) build_sell<V, V>(s, L.A.ptr, L.A.col, L.A.val, L.A.n, M.A, hp);
         if (M.p) build_sell<V, V>(s, L.P.ptr, L.P.col, L.P.val, L.P.n, M.P, hp);
@@ -1515,12 +1559,22 @@ void pressure_setup(semo_ctx* c, const int* ptr, const int* col, const double* v
                 build_hierarchy<double>(c, c->amg64, ptr, col, val, n, nnz);
             }
             StageScope scy(c, ST_SETUP_CYCLE);
+            // on the mesh's own pattern the layout structure is built once per mesh
+            std::shared_ptr<Sell16Struct> pat;
+            if (ptr == c->A_ptr.p && col == c->A_col.p) {
+                if (!st.pat16 || st.pat16_gen != c->mesh_gen || st.pat16->n != n)
+                    st.pat16 = build_sell16_struct(s, ptr, col, n, c->hpin_int + 4);
+                st.pat16_gen = c->mesh_gen;
+                pat = st.pat16;
+            } else {
+                pat = build_sell16_struct(s, ptr, col, n, c->hpin_int + 4);
+            }
             if (c->prm.precision == SEMO_PREC_MIXED)
-                prepare_cycle(c, c->amg32, st.cy32);
+                prepare_cycle(c, c->amg32, st.cy32, pat);
             else
-                prepare_cycle(c, c->amg64, st.cy64);
-            st.outer.use16 = build_sell16<double, double>(s, ptr, col, val, n, st.outer.s16, c->hpin_int + 4);
-            if (!st.outer.use16) build_sell<double, double>(s, ptr, col, val, n, st.outer.s32, c->hpin_int + 4);
+                prepare_cycle(c, c->amg64, st.cy64, pat);
+            fill_sell16<double, double>(s, ptr, val, pat, st.outer.s16);
+            st.outer.use16 = true;
             st.src_prec = -1;
             if (may_reuse && c->prm.reuse_hierarchy) {
                 st.src_val.alloc(nnz, s);

@@ -257,6 +257,7 @@ struct semo_ctx {
     double* hpin_setup = nullptr;                 // setup: per-level scalars (kHostScalars)
     cudaEvent_t sync_ev[2] = {nullptr, nullptr};  // completion of those counter copies
     std::shared_ptr<void> apply;                  // V-cycle/Krylov apply state (cycle.cu)
+    std::shared_ptr<void> setup_worker;           // host thread of the overlapped pressure setup (capi.cpp)
 
     bool mesh_ready = false, phys_ready = false, fields_ready = false, assembled = false;
     int mesh_gen = 0;                             // bumped by every mesh upload (cached layouts check it)
