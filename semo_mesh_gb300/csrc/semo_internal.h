@@ -247,7 +247,7 @@ struct semo_ctx {
     semo::DBuf<double> kr, kz, kp, kq;            // Krylov vectors (FP64)
     semo::DBuf<float> kz32, kr32;
     // Pinned host scalars, one set per host thread that reads results back:
-    // a device-to-host copy into pageable memory waits inside the driver for
+    // a device-to-host copy into pageable memory waits inside the CUDA runtime for
     // its stream, and while it waits the other thread's CUDA calls queue
     // behind it (the hierarchy built beside the momentum pass stalled for the
     // momentum assembly's duration on such a read).  Allocated with the context.
